@@ -1,0 +1,315 @@
+/*
+ * libdftgpu -- GB300 (sm_103a) implementation of libdft's per-time-step hot
+ * path: the Orsay-Trento (OT) potential and energy density and the
+ * split-operator wave-function step, behind the call signatures libdft and
+ * libgrid expose for that path.
+ *
+ * Grids live in GPU memory.  A grid's values are FP64 or FP32 ("bulk"
+ * precision, chosen with dftgpu_set_precision() before allocation);
+ * reductions (norm, energies) accumulate in FP64 and the k-space convolution
+ * kernels are generated in FP64.  Host data moves only through the explicit
+ * *_to_host / *_from_host copies (libgrid's CUDA mode has the same rule:
+ * *_host_lock, libdft src/spectroscopy1a.c:53).
+ *
+ * Reference citations are paths inside jmeloranta/libdft.  libgrid functions
+ * (grid_wf_*, rgrid_*, cgrid_*) are not in that tree; their citations are the
+ * libdft call sites that define how they are used.
+ *
+ * Error convention: the drop-in entry points keep libdft's void / pointer
+ * returns; a failure sets a code readable with dftgpu_last_error() (and
+ * allocation returns NULL, as src/ot.c:82-85 does).  The dftgpu_* entry points
+ * return the code directly.  The library never calls exit().
+ */
+#ifndef DFTGPU_H
+#define DFTGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#ifndef REAL
+#define REAL double
+#endif
+#ifndef INT
+#define INT long
+#endif
+
+/* ---------------------------------------------------------------- status */
+#define DFTGPU_OK               0
+#define DFTGPU_ERR_ARG          1   /* invalid argument / grid mismatch */
+#define DFTGPU_ERR_SIZE         2   /* unsupported grid size */
+#define DFTGPU_ERR_NOMEM        3   /* device allocation failed */
+#define DFTGPU_ERR_CUDA         4   /* CUDA runtime error */
+#define DFTGPU_ERR_NONFINITE    5   /* NaN / Inf detected by an FP64 reduction */
+#define DFTGPU_ERR_UNSUPPORTED  6   /* model / boundary / propagator not provided */
+#define DFTGPU_ERR_NODEVICE     7   /* no CUDA device */
+
+/* precision of newly allocated grids */
+#define DFTGPU_FP64 0
+#define DFTGPU_FP32 1
+
+/* -------------------------------------------------------- OT model flags
+ * Same values as libdft src/ot.h:37-60.  Provided: DFT_OT_PLAIN, DFT_OT_KC,
+ * DFT_OT_BACKFLOW and their combinations; the others are rejected with
+ * DFTGPU_ERR_UNSUPPORTED. */
+#define DFT_OT_PLAIN    0
+#define DFT_OT_KC       1
+#define DFT_OT_HD       2
+#define DFT_OT_HD2      4
+#define DFT_OT_BACKFLOW 8
+#define DFT_OT_T0MK    16
+#define DFT_GP         524288
+#define DFT_DR         1048576
+#define DFT_ZERO       2097152
+#define DFT_GP2        4194304
+
+/* wave-function options (libgrid; used at examples/imag_time/imag_time.c:197) */
+#define WF_DIRICHLET_BOUNDARY  1
+#define WF_NEUMANN_BOUNDARY    2
+#define WF_PERIODIC_BOUNDARY   3
+#define WF_2ND_ORDER_FFT       1
+#define WF_4TH_ORDER_FFT       2
+#define WF_2ND_ORDER_CN        3
+
+#define DFT_MIN_SUBSTEPS 4      /* src/ot.h:140 */
+#define DFT_MAX_SUBSTEPS 32     /* src/ot.h:141 */
+#define DFT_EPS 1E-4            /* src/ot.h:147 */
+
+/* atomic units (libgrid au.h, restated from CODATA 2018) */
+#define GRID_AUTOANG   0.529177210903
+#define GRID_AUTOK     3.1577502480407E5
+#define GRID_AUTOFS    0.024188843265857
+#define GRID_AUTOAMU   (1.0 / 1822.888486209)
+#define GRID_AUTOMPS   2.18769126364E6
+#define GRID_AUTOBAR   2.9421015697E8
+#define DFT_HELIUM_MASS (4.002602 / GRID_AUTOAMU)   /* src/ot.h:137 */
+
+/* ----------------------------------------------------------------- types */
+typedef struct rgrid_struct rgrid;
+typedef struct cgrid_struct cgrid;
+
+/* Real grid.  value is a DEVICE pointer to nx*ny*nz values in [x][y][z]
+ * order (FP32 or FP64 per prec).  Coordinates: x_i = (i - nx/2) step - x0. */
+struct rgrid_struct {
+  void *value;
+  INT nx, ny, nz;
+  REAL step;
+  REAL x0, y0, z0;
+  int prec;
+  char id[32];
+};
+
+/* Complex grid, same layout with interleaved (re, im). */
+struct cgrid_struct {
+  void *value;
+  INT nx, ny, nz;
+  REAL step;
+  REAL x0, y0, z0;
+  REAL kx0, ky0, kz0;
+  int prec;
+  char id[32];
+};
+
+/* Wave function (libgrid wf: grid, mass, norm, boundary, propagator). */
+typedef struct wf_struct {
+  cgrid *grid;
+  REAL mass;
+  REAL norm;          /* target particle number for grid_wf_normalize() */
+  char boundary;
+  char propagator;
+  void *priv;
+} wf;
+
+typedef struct {      /* src/dft.h:23-28 */
+  REAL h, sigma, epsilon, cval;
+} dft_common_lj;
+
+typedef struct {      /* src/ot.h:69-71 */
+  REAL g11, g12, g21, g22, a1, a2;
+} dft_ot_bf;
+
+/* OT functional; public fields as in src/ot.h:159-202.  The kernel and
+ * workspace fields of libdft are replaced by the opaque priv state (device
+ * kernel spectra and work buffers); density is kept (device grid). */
+typedef struct dft_ot_functional_struct {
+  INT model;
+  REAL b, c2, c2_exp, c3, c3_exp, c4;
+  REAL rho_0s, alpha_s, l_g, mass, rho0, temp;
+  dft_common_lj lj_params;
+  dft_ot_bf bf_params;
+  REAL beta, rhom, C, mu0, xi, rhobf;
+  REAL div_epsilon, max_veloc, max_bfpot, c_bfpot;
+  rgrid *density;
+  void *priv;
+} dft_ot_functional;
+
+typedef REAL (*rgrid_outside_fn)(rgrid *grid, INT i, INT j, INT k);
+typedef REAL (*rgrid_map_fn)(void *arg, REAL x, REAL y, REAL z);
+typedef void (*cgrid_map_fn)(void *arg, REAL x, REAL y, REAL z, REAL *re, REAL *im);
+
+/* periodic boundary sentinel (libgrid RGRID_PERIODIC_BOUNDARY, src/ot.c:95) */
+REAL rgrid_value_outside_periodic(rgrid *grid, INT i, INT j, INT k);
+#define RGRID_PERIODIC_BOUNDARY rgrid_value_outside_periodic
+
+/* ------------------------------------------------------- runtime control */
+/* Select the GPU.  libgrid: cuda_enable(1, NGPUS, gpus)
+ * (examples/imag_time/imag_time.c:185-189).  One GPU only: ngpus must be 1. */
+void cuda_enable(char value, INT ngpus, int *gpus);
+int dftgpu_init(int device);
+/* Precision for grids allocated from now on (DFTGPU_FP64 / DFTGPU_FP32). */
+int dftgpu_set_precision(int prec);
+int dftgpu_get_precision(void);
+/* Last error code of this thread (0 = none) and its message; clears it. */
+int dftgpu_last_error(void);
+const char *dftgpu_last_error_message(void);
+int dftgpu_synchronize(void);
+/* CUDA stream (cudaStream_t) all work is issued on; NULL = legacy default. */
+int dftgpu_set_stream(void *stream);
+void *dftgpu_get_stream(void);
+
+/* ------------------------------------------------------------ real grids
+ * libgrid rgrid API as used by libdft (src/ot.c:95-244, ot-energy.c:59-72,
+ * examples/imag_time/imag_time.c:213-253). */
+rgrid *rgrid_alloc(INT nx, INT ny, INT nz, REAL step, rgrid_outside_fn value_outside, void *outside_params_ptr, char *id);
+void rgrid_free(rgrid *grid);
+rgrid *rgrid_clone(rgrid *grid, char *id);
+void rgrid_set_origin(rgrid *grid, REAL x0, REAL y0, REAL z0);
+void rgrid_zero(rgrid *grid);
+void rgrid_constant(rgrid *grid, REAL c);
+void rgrid_copy(rgrid *dst, rgrid *src);
+void rgrid_add(rgrid *grid, REAL c);
+void rgrid_multiply(rgrid *grid, REAL c);
+void rgrid_sum(rgrid *dst, rgrid *a, rgrid *b);
+void rgrid_product(rgrid *dst, rgrid *a, rgrid *b);
+void rgrid_add_scaled(rgrid *dst, REAL c, rgrid *src);
+void rgrid_add_scaled_product(rgrid *dst, REAL c, rgrid *a, rgrid *b);
+REAL rgrid_integral(rgrid *grid);
+/* Host callback evaluated in FP64 on the host at every grid point, then copied
+ * to the device (setup only; examples/imag_time/imag_time.c:218). */
+void rgrid_map(rgrid *grid, rgrid_map_fn func, void *farg);
+REAL rgrid_value_at_index(rgrid *grid, INT i, INT j, INT k);
+/* Host copies: buffers are FP64, nx*ny*nz values in [x][y][z] order. */
+int rgrid_copy_to_host(rgrid *grid, double *host);
+int rgrid_copy_from_host(rgrid *grid, const double *host);
+/* Raw copies in the grid's own precision (4 or 8 bytes per value). */
+int rgrid_copy_to_host_raw(rgrid *grid, void *host);
+int rgrid_copy_from_host_raw(rgrid *grid, const void *host);
+
+/* --------------------------------------------------------- complex grids */
+cgrid *cgrid_alloc(INT nx, INT ny, INT nz, REAL step, void *value_outside, void *outside_params_ptr, char *id);
+void cgrid_free(cgrid *grid);
+cgrid *cgrid_clone(cgrid *grid, char *id);
+void cgrid_zero(cgrid *grid);                             /* src/helium-ot-bulk.c:335 */
+void cgrid_constant_re_im(cgrid *grid, REAL re, REAL im);
+void cgrid_add_re_im(cgrid *grid, REAL re, REAL im);      /* cgrid_add(P, -mu0), imag_time.c:233 */
+void cgrid_multiply_re_im(cgrid *grid, REAL re, REAL im); /* cgrid_multiply(P, 0.5), imag_time.c:238 */
+void cgrid_copy(cgrid *dst, cgrid *src);
+void cgrid_map_re_im(cgrid *grid, cgrid_map_fn func, void *farg);
+int cgrid_copy_to_host(cgrid *grid, double *host);        /* interleaved re, im */
+int cgrid_copy_from_host(cgrid *grid, const double *host);
+int cgrid_copy_to_host_raw(cgrid *grid, void *host);
+int cgrid_copy_from_host_raw(cgrid *grid, const void *host);
+
+/* grid_real_to_complex_re / grid_add_real_to_complex_re / _im
+ * (imag_time.c:231,235; src/ot.c:530,990) */
+void grid_real_to_complex_re(cgrid *dst, rgrid *src);
+void grid_add_real_to_complex_re(cgrid *dst, rgrid *src);
+void grid_add_real_to_complex_im(cgrid *dst, rgrid *src);
+
+/* -------------------------------------------------------- wave functions
+ * libgrid wf API as called by libdft and its examples. */
+/* grid_wf_alloc (imag_time.c:197): periodic boundary + WF_2ND_ORDER_FFT only. */
+wf *grid_wf_alloc(INT nx, INT ny, INT nz, REAL step, REAL mass, char boundary, char propagator, char *id);
+wf *grid_wf_clone(wf *gwf, char *id);                     /* imag_time.c:201 */
+void grid_wf_free(wf *gwf);
+void grid_wf_constant_re_im(wf *gwf, REAL re, REAL im);   /* grid_wf_constant, imag_time.c:221 */
+void grid_wf_density(wf *gwf, rgrid *density);            /* src/ot.c:320 */
+REAL grid_wf_norm(wf *gwf);                               /* imag_time.c:254 */
+REAL grid_wf_normalize(wf *gwf);                          /* examples/imag_time_rot/imag_time.c:208 */
+REAL grid_wf_energy(wf *gwf, rgrid *potential);           /* kinetic (+ <V>), imag_time.c:253 */
+REAL grid_wf_kinetic_energy(wf *gwf);
+void grid_wf_velocity(wf *gwf, rgrid *vx, rgrid *vy, rgrid *vz, REAL eps);  /* src/ot.c:390 */
+/* propagation with complex time step split into (re, im)
+ * (grid_wf_propagate / _predict / _correct: imag_time.c:234,239,
+ * src/helium-ot-bulk.c:340-347); the REAL complex forms are below. */
+int dftgpu_wf_propagate(wf *gwf, cgrid *potential, double dt_re, double dt_im);
+int dftgpu_wf_propagate_predict(wf *gwf, wf *gwfp, cgrid *potential, double dt_re, double dt_im);
+int dftgpu_wf_propagate_correct(wf *gwf, cgrid *potential, double dt_re, double dt_im);
+
+/* ---------------------------------------------------------- OT functional */
+dft_ot_functional *dft_ot_alloc(INT model, wf *gwf, INT min_substeps, INT max_substeps);   /* src/ot.c:66 */
+void dft_ot_free(dft_ot_functional *otf);                                                   /* src/ot.c:268 */
+void dft_ot_potential(dft_ot_functional *otf, cgrid *potential, wf *gwf);                    /* src/ot.c:314 */
+void dft_ot_energy_density(dft_ot_functional *otf, rgrid *energy_density, wf *gwf);         /* src/ot-energy.c:38 */
+void dft_ot_init_params(dft_ot_functional *otf, INT model);                                 /* src/ot.c:1002 */
+/* Regenerate the k-space kernels after changing otf parameters such as l_g
+ * (src/ot.c:138-217 run again); libdft has no separate entry for this. */
+int dft_ot_update_kernels(dft_ot_functional *otf, INT min_substeps, INT max_substeps);
+
+/* Inspection: the k-space kernel `which` (0 LJ, 1 spherical average, 2 F,
+ * 3-5 dF/dx,dy,dz, 6 V_j) as stored: the non-negative octant
+ * [kz][kx][ky] (extents nz/2+1, nx/2+1, ny/2+1) of its spectrum (real part;
+ * imaginary part for dF), times (-1)^(kx+ky+kz) step^3/N (LJ and the
+ * spherical average additionally rescaled to integrals b and 1, src/ot.c:160,181).
+ * host receives FP64 values.  No libdft counterpart (libdft keeps the full
+ * spectra in otf->lennard_jones etc., src/ot.h:174-180). */
+int dftgpu_ot_kernel(dft_ot_functional *otf, int which, double *host);
+/* Inspection: unnormalised forward r2c 3-D FFT of a real grid, written to
+ * host as nx*ny*(nz/2+1) complex values in [x][y][kz] order (libgrid
+ * rgrid_fft, src/ot.c:527, but out of place). */
+int dftgpu_rgrid_spectrum(rgrid *grid, double *host);
+
+/* bulk liquid relations, host-only (src/helium-ot-bulk.c:21-434) */
+REAL dft_ot_bulk_energy(dft_ot_functional *otf, REAL rho);
+REAL dft_ot_bulk_dEdRho(dft_ot_functional *otf, REAL rho);
+REAL dft_ot_bulk_pressure(dft_ot_functional *otf, REAL rho);
+REAL dft_ot_bulk_dPdRho(dft_ot_functional *otf, REAL rho);
+REAL dft_ot_bulk_density_pressurized(dft_ot_functional *otf, REAL pressure);
+REAL dft_ot_bulk_chempot_pressurized(dft_ot_functional *otf, REAL pressure);
+REAL dft_ot_bulk_density(dft_ot_functional *otf);
+REAL dft_ot_bulk_chempot(dft_ot_functional *otf);
+REAL dft_ot_bulk_chempot2(dft_ot_functional *otf);
+REAL dft_ot_bulk_compressibility(dft_ot_functional *otf, REAL rho);
+REAL dft_ot_bulk_sound_speed(dft_ot_functional *otf, REAL rho);
+REAL dft_ot_bulk_dispersion(dft_ot_functional *otf, REAL *k, REAL rho0);
+
+/* ----------------------------------------------- fused step and reports */
+/* One predict-correct step exactly as the libdft dynamics examples write it
+ * (examples/imag_time/imag_time.c:231-239):
+ *   P = Vext; P += V_OT[psi]; P -= mu0; psi_p = S(P,dt) psi;
+ *   P += Vext; P += V_OT[psi_p]; P -= mu0; P *= 1/2; psi = S(P,dt) psi.
+ * vext may be NULL (zero).  P is left holding the averaged potential. */
+int dftgpu_pc_step(dft_ot_functional *otf, wf *gwf, wf *gwfp, cgrid *potential, rgrid *vext,
+                   double mu0, double dt_re, double dt_im);
+/* nsteps predict-correct steps; if renorm != 0, grid_wf_normalize(gwf) after
+ * each (examples/imag_time_rot/imag_time.c:208).  The loop is captured once
+ * in a CUDA graph and replayed. */
+int dftgpu_run(dft_ot_functional *otf, wf *gwf, wf *gwfp, cgrid *potential, rgrid *vext,
+               double mu0, double dt_re, double dt_im, INT nsteps, int renorm);
+/* E = <T> + int eps[psi] + int rho Vext, N = int |psi|^2 and the chemical
+ * potential mu = (<T> + int rho (V_OT + Vext)) / N, all FP64
+ * (examples/imag_time/imag_time.c:251-257).  vext may be NULL. */
+int dftgpu_energy_report(dft_ot_functional *otf, wf *gwf, rgrid *vext, double *energy,
+                         double *natoms, double *mu);
+
+#ifndef __cplusplus
+#include <complex.h>
+/* REAL complex forms of the libgrid / libdft entry points (C only). */
+void grid_wf_propagate(wf *gwf, cgrid *potential, REAL complex time);
+void grid_wf_propagate_predict(wf *gwf, wf *gwfp, cgrid *potential, REAL complex time);
+void grid_wf_propagate_correct(wf *gwf, cgrid *potential, REAL complex time);
+void grid_wf_constant(wf *gwf, REAL complex c);
+void cgrid_add(cgrid *grid, REAL complex c);
+void cgrid_multiply(cgrid *grid, REAL complex c);
+void cgrid_constant(cgrid *grid, REAL complex c);
+void cgrid_map(cgrid *grid, REAL complex (*func)(void *arg, REAL x, REAL y, REAL z), void *farg);
+void grid_wf_map(wf *gwf, REAL complex (*func)(void *arg, REAL x, REAL y, REAL z), void *farg);  /* src/helium-ot-bulk.c:331 */
+#endif
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,625 @@
+// extern "C" entry points of libdftgpu (declared in include/dftgpu.h).
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <vector>
+
+#include "grid_internal.cuh"
+#include "ot_internal.cuh"
+
+using namespace dftgpu;
+
+namespace {
+
+rgrid *rgrid_new(INT nx, INT ny, INT nz, REAL step, int prec, const char *id) {
+  if (ensure_device() != DFTGPU_OK) return nullptr;
+  if (check_dims(nx, ny, nz) != DFTGPU_OK) return nullptr;
+  rgrid *g = (rgrid *) calloc(1, sizeof(rgrid));
+  g->nx = nx; g->ny = ny; g->nz = nz; g->step = step; g->prec = prec;
+  if (id) strncpy(g->id, id, sizeof(g->id) - 1);
+  g->value = dev_alloc(gsize(g) * elem_size(prec));
+  if (!g->value) { free(g); return nullptr; }
+  if (cudaMemsetAsync(g->value, 0, gsize(g) * elem_size(prec), rt().stream) != cudaSuccess) {
+    dev_free(g->value); free(g); set_error(DFTGPU_ERR_CUDA, "memset"); return nullptr;
+  }
+  return g;
+}
+
+cgrid *cgrid_new(INT nx, INT ny, INT nz, REAL step, int prec, const char *id) {
+  if (ensure_device() != DFTGPU_OK) return nullptr;
+  if (check_dims(nx, ny, nz) != DFTGPU_OK) return nullptr;
+  cgrid *g = (cgrid *) calloc(1, sizeof(cgrid));
+  g->nx = nx; g->ny = ny; g->nz = nz; g->step = step; g->prec = prec;
+  if (id) strncpy(g->id, id, sizeof(g->id) - 1);
+  g->value = dev_alloc(gsize(g) * 2 * elem_size(prec));
+  if (!g->value) { free(g); return nullptr; }
+  if (cudaMemsetAsync(g->value, 0, gsize(g) * 2 * elem_size(prec), rt().stream) != cudaSuccess) {
+    dev_free(g->value); free(g); set_error(DFTGPU_ERR_CUDA, "memset"); return nullptr;
+  }
+  return g;
+}
+
+template <class G> bool same_shape(const G *a, const G *b) {
+  return a && b && a->nx == b->nx && a->ny == b->ny && a->nz == b->nz && a->prec == b->prec;
+}
+
+bool rc_shape(const cgrid *c, const rgrid *r) {
+  return c && r && c->nx == r->nx && c->ny == r->ny && c->nz == r->nz && c->prec == r->prec;
+}
+
+int bad_arg(const char *what) { set_error(DFTGPU_ERR_ARG, "%s", what); return DFTGPU_ERR_ARG; }
+
+}  // namespace
+
+extern "C" {
+
+// ------------------------------------------------------------------ runtime
+int dftgpu_init(int device) {
+  Runtime &R = rt();
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    set_error(DFTGPU_ERR_NODEVICE, "no CUDA device available");
+    return DFTGPU_ERR_NODEVICE;
+  }
+  if (device < 0 || device >= n) return bad_arg("dftgpu_init: device index out of range");
+  DFT_CUDA(cudaSetDevice(device));
+  cudaDeviceProp p;
+  DFT_CUDA(cudaGetDeviceProperties(&p, device));
+  R.device = device;
+  R.num_sms = p.multiProcessorCount;
+  R.max_smem_optin = p.sharedMemPerBlockOptin;
+  return DFTGPU_OK;
+}
+
+void cuda_enable(char value, INT ngpus, int *gpus) {
+  if (!value) return;
+  if (ngpus != 1) set_error(DFTGPU_ERR_UNSUPPORTED, "cuda_enable: one GPU per process (got %ld); using the first", (long) ngpus);
+  dftgpu_init(gpus ? gpus[0] : 0);
+}
+
+int dftgpu_set_precision(int prec) {
+  if (prec != DFTGPU_FP32 && prec != DFTGPU_FP64) return bad_arg("dftgpu_set_precision: FP32 or FP64");
+  rt().precision = prec;
+  return DFTGPU_OK;
+}
+int dftgpu_get_precision(void) { return rt().precision; }
+
+int dftgpu_last_error(void) { int e = g_last_error; g_last_error = 0; return e; }
+const char *dftgpu_last_error_message(void);
+
+int dftgpu_synchronize(void) {
+  if (ensure_device() != DFTGPU_OK) return DFTGPU_ERR_NODEVICE;
+  DFT_CUDA(cudaStreamSynchronize(rt().stream));
+  return DFTGPU_OK;
+}
+int dftgpu_set_stream(void *stream) { rt().stream = (cudaStream_t) stream; return DFTGPU_OK; }
+void *dftgpu_get_stream(void) { return (void *) rt().stream; }
+
+REAL rgrid_value_outside_periodic(rgrid *grid, INT i, INT j, INT k) {
+  (void) grid; (void) i; (void) j; (void) k;
+  return 0.0;   // sentinel only: the library evaluates periodic boundaries itself
+}
+
+// ------------------------------------------------------------------ rgrid
+rgrid *rgrid_alloc(INT nx, INT ny, INT nz, REAL step, rgrid_outside_fn value_outside, void *outside_params_ptr, char *id) {
+  (void) outside_params_ptr;
+  if (value_outside && value_outside != rgrid_value_outside_periodic) {
+    set_error(DFTGPU_ERR_UNSUPPORTED, "rgrid_alloc: only periodic boundaries");
+    return nullptr;
+  }
+  return rgrid_new(nx, ny, nz, step, rt().precision, id);
+}
+
+void rgrid_free(rgrid *g) { if (g) { dev_free(g->value); free(g); } }
+
+rgrid *rgrid_clone(rgrid *g, char *id) {
+  if (!g) return nullptr;
+  rgrid *c = rgrid_new(g->nx, g->ny, g->nz, g->step, g->prec, id);
+  if (c) { c->x0 = g->x0; c->y0 = g->y0; c->z0 = g->z0; }
+  return c;
+}
+
+void rgrid_set_origin(rgrid *g, REAL x0, REAL y0, REAL z0) { g->x0 = x0; g->y0 = y0; g->z0 = z0; }
+void rgrid_zero(rgrid *g) { rfill(g, 0.0); }
+void rgrid_constant(rgrid *g, REAL c) { rfill(g, c); }
+void rgrid_copy(rgrid *d, rgrid *s) {
+  if (!same_shape(d, s)) { bad_arg("rgrid_copy: shape mismatch"); return; }
+  if (cudaMemcpyAsync(d->value, s->value, gsize(s) * elem_size(s->prec), cudaMemcpyDeviceToDevice, rt().stream) != cudaSuccess)
+    set_error(DFTGPU_ERR_CUDA, "rgrid_copy");
+}
+void rgrid_add(rgrid *g, REAL c) { raxpb(g, 1.0, c); }
+void rgrid_multiply(rgrid *g, REAL c) { raxpb(g, c, 0.0); }
+void rgrid_sum(rgrid *d, rgrid *a, rgrid *b) {
+  if (!same_shape(d, a) || !same_shape(d, b)) { bad_arg("rgrid_sum: shape mismatch"); return; }
+  rbinary(d, a, b, 0.0, 0);
+}
+void rgrid_product(rgrid *d, rgrid *a, rgrid *b) {
+  if (!same_shape(d, a) || !same_shape(d, b)) { bad_arg("rgrid_product: shape mismatch"); return; }
+  rbinary(d, a, b, 0.0, 1);
+}
+void rgrid_add_scaled(rgrid *d, REAL c, rgrid *s) {
+  if (!same_shape(d, s)) { bad_arg("rgrid_add_scaled: shape mismatch"); return; }
+  rbinary(d, s, nullptr, c, 2);
+}
+void rgrid_add_scaled_product(rgrid *d, REAL c, rgrid *a, rgrid *b) {
+  if (!same_shape(d, a) || !same_shape(d, b)) { bad_arg("rgrid_add_scaled_product: shape mismatch"); return; }
+  rbinary(d, a, b, c, 3);
+}
+REAL rgrid_integral(rgrid *g) {
+  double v = NAN;
+  rintegral(g, &v);
+  return v;
+}
+
+void rgrid_map(rgrid *g, rgrid_map_fn func, void *farg) {
+  const INT nx = g->nx, ny = g->ny, nz = g->nz;
+  std::vector<double> h(gsize(g));
+  for (INT i = 0; i < nx; i++) {
+    const REAL x = (REAL) (i - nx / 2) * g->step - g->x0;
+    for (INT j = 0; j < ny; j++) {
+      const REAL y = (REAL) (j - ny / 2) * g->step - g->y0;
+      for (INT k = 0; k < nz; k++) {
+        const REAL z = (REAL) (k - nz / 2) * g->step - g->z0;
+        h[(i * ny + j) * nz + k] = func(farg, x, y, z);
+      }
+    }
+  }
+  copy_values_in(g->prec, g->value, h.data(), h.size());
+}
+
+REAL rgrid_value_at_index(rgrid *g, INT i, INT j, INT k) {
+  i = ((i % g->nx) + g->nx) % g->nx; j = ((j % g->ny) + g->ny) % g->ny; k = ((k % g->nz) + g->nz) % g->nz;
+  const size_t idx = ((size_t) i * g->ny + j) * g->nz + k;
+  double v = NAN;
+  if (g->prec == DFTGPU_FP32) {
+    float f;
+    if (cudaMemcpy(&f, (float *) g->value + idx, 4, cudaMemcpyDeviceToHost) == cudaSuccess) v = f;
+  } else cudaMemcpy(&v, (double *) g->value + idx, 8, cudaMemcpyDeviceToHost);
+  return v;
+}
+
+int rgrid_copy_to_host(rgrid *g, double *host) { return copy_values_out(g->prec, g->value, host, gsize(g)); }
+int rgrid_copy_from_host(rgrid *g, const double *host) { return copy_values_in(g->prec, g->value, host, gsize(g)); }
+int rgrid_copy_to_host_raw(rgrid *g, void *host) {
+  DFT_CUDA(cudaMemcpyAsync(host, g->value, gsize(g) * elem_size(g->prec), cudaMemcpyDeviceToHost, rt().stream));
+  DFT_CUDA(cudaStreamSynchronize(rt().stream));
+  return DFTGPU_OK;
+}
+int rgrid_copy_from_host_raw(rgrid *g, const void *host) {
+  DFT_CUDA(cudaMemcpyAsync(g->value, host, gsize(g) * elem_size(g->prec), cudaMemcpyHostToDevice, rt().stream));
+  return DFTGPU_OK;
+}
+
+// ------------------------------------------------------------------ cgrid
+cgrid *cgrid_alloc(INT nx, INT ny, INT nz, REAL step, void *value_outside, void *outside_params_ptr, char *id) {
+  (void) value_outside; (void) outside_params_ptr;
+  return cgrid_new(nx, ny, nz, step, rt().precision, id);
+}
+void cgrid_free(cgrid *g) { if (g) { dev_free(g->value); free(g); } }
+cgrid *cgrid_clone(cgrid *g, char *id) {
+  if (!g) return nullptr;
+  cgrid *c = cgrid_new(g->nx, g->ny, g->nz, g->step, g->prec, id);
+  if (c) { c->x0 = g->x0; c->y0 = g->y0; c->z0 = g->z0; }
+  return c;
+}
+void cgrid_zero(cgrid *g) { cfill(g, 0.0, 0.0); }
+void cgrid_constant_re_im(cgrid *g, REAL re, REAL im) { cfill(g, re, im); }
+void cgrid_add_re_im(cgrid *g, REAL re, REAL im) { cmuladd(g, 1.0, 0.0, re, im); }
+void cgrid_multiply_re_im(cgrid *g, REAL re, REAL im) { cmuladd(g, re, im, 0.0, 0.0); }
+void cgrid_copy(cgrid *d, cgrid *s) {
+  if (!same_shape(d, s)) { bad_arg("cgrid_copy: shape mismatch"); return; }
+  if (cudaMemcpyAsync(d->value, s->value, gsize(s) * 2 * elem_size(s->prec), cudaMemcpyDeviceToDevice, rt().stream) != cudaSuccess)
+    set_error(DFTGPU_ERR_CUDA, "cgrid_copy");
+}
+void cgrid_map_re_im(cgrid *g, cgrid_map_fn func, void *farg) {
+  const INT nx = g->nx, ny = g->ny, nz = g->nz;
+  std::vector<double> h(2 * gsize(g));
+  for (INT i = 0; i < nx; i++) {
+    const REAL x = (REAL) (i - nx / 2) * g->step - g->x0;
+    for (INT j = 0; j < ny; j++) {
+      const REAL y = (REAL) (j - ny / 2) * g->step - g->y0;
+      for (INT k = 0; k < nz; k++) {
+        const REAL z = (REAL) (k - nz / 2) * g->step - g->z0;
+        const size_t idx = (size_t) ((i * ny + j) * nz + k);
+        func(farg, x, y, z, &h[2 * idx], &h[2 * idx + 1]);
+      }
+    }
+  }
+  copy_values_in(g->prec, g->value, h.data(), h.size());
+}
+int cgrid_copy_to_host(cgrid *g, double *host) { return copy_values_out(g->prec, g->value, host, 2 * gsize(g)); }
+int cgrid_copy_from_host(cgrid *g, const double *host) { return copy_values_in(g->prec, g->value, host, 2 * gsize(g)); }
+int cgrid_copy_to_host_raw(cgrid *g, void *host) {
+  DFT_CUDA(cudaMemcpyAsync(host, g->value, gsize(g) * 2 * elem_size(g->prec), cudaMemcpyDeviceToHost, rt().stream));
+  DFT_CUDA(cudaStreamSynchronize(rt().stream));
+  return DFTGPU_OK;
+}
+int cgrid_copy_from_host_raw(cgrid *g, const void *host) {
+  DFT_CUDA(cudaMemcpyAsync(g->value, host, gsize(g) * 2 * elem_size(g->prec), cudaMemcpyHostToDevice, rt().stream));
+  return DFTGPU_OK;
+}
+
+void grid_real_to_complex_re(cgrid *d, rgrid *s) { if (!rc_shape(d, s)) { bad_arg("grid_real_to_complex_re"); return; } real_to_complex(d, s, 0); }
+void grid_add_real_to_complex_re(cgrid *d, rgrid *s) { if (!rc_shape(d, s)) { bad_arg("grid_add_real_to_complex_re"); return; } real_to_complex(d, s, 1); }
+void grid_add_real_to_complex_im(cgrid *d, rgrid *s) { if (!rc_shape(d, s)) { bad_arg("grid_add_real_to_complex_im"); return; } real_to_complex(d, s, 2); }
+
+// ------------------------------------------------------------------ wave functions
+wf *grid_wf_alloc(INT nx, INT ny, INT nz, REAL step, REAL mass, char boundary, char propagator, char *id) {
+  if (boundary != WF_PERIODIC_BOUNDARY || propagator != WF_2ND_ORDER_FFT) {
+    set_error(DFTGPU_ERR_UNSUPPORTED, "grid_wf_alloc: periodic boundary with WF_2ND_ORDER_FFT only");
+    return nullptr;
+  }
+  cgrid *c = cgrid_new(nx, ny, nz, step, rt().precision, id);
+  if (!c) return nullptr;
+  wf *w = (wf *) calloc(1, sizeof(wf));
+  w->grid = c;
+  w->mass = mass;
+  w->norm = 1.0;
+  w->boundary = boundary;
+  w->propagator = propagator;
+  w->priv = new WfPriv();
+  return w;
+}
+
+wf *grid_wf_clone(wf *g, char *id) {
+  if (!g) return nullptr;
+  int save = rt().precision;
+  rt().precision = g->grid->prec;
+  wf *w = grid_wf_alloc(g->grid->nx, g->grid->ny, g->grid->nz, g->grid->step, g->mass, g->boundary, g->propagator, id);
+  rt().precision = save;
+  if (w) {
+    w->norm = g->norm;
+    w->grid->x0 = g->grid->x0; w->grid->y0 = g->grid->y0; w->grid->z0 = g->grid->z0;
+  }
+  return w;
+}
+
+void grid_wf_free(wf *g) {
+  if (!g) return;
+  WfPriv *p = (WfPriv *) g->priv;
+  if (p) { dev_free(p->spec); delete p; }
+  cgrid_free(g->grid);
+  free(g);
+}
+
+void grid_wf_constant_re_im(wf *g, REAL re, REAL im) { cfill(g->grid, re, im); }
+
+void grid_wf_density(wf *g, rgrid *d) {
+  if (!rc_shape(g->grid, d)) { bad_arg("grid_wf_density: shape mismatch"); return; }
+  density(g->grid, d);
+}
+
+REAL grid_wf_norm(wf *g) {
+  double v = NAN;
+  double *slot = reduce_slots();
+  if (norm_dev(g->grid, slot + 1) != DFTGPU_OK) return NAN;
+  if (cudaMemcpyAsync(&v, slot + 1, sizeof(double), cudaMemcpyDeviceToHost, rt().stream) != cudaSuccess ||
+      cudaStreamSynchronize(rt().stream) != cudaSuccess) { set_error(DFTGPU_ERR_CUDA, "grid_wf_norm"); return NAN; }
+  if (!isfinite(v)) set_error(DFTGPU_ERR_NONFINITE, "grid_wf_norm: non-finite norm");
+  return v;
+}
+
+REAL grid_wf_normalize(wf *g) {
+  double *slot = reduce_slots();
+  if (norm_dev(g->grid, slot + 2) != DFTGPU_OK) return NAN;
+  if (scale_by_norm(g->grid, slot + 2, g->norm) != DFTGPU_OK) return NAN;
+  double v = NAN;
+  if (cudaMemcpyAsync(&v, slot + 2, sizeof(double), cudaMemcpyDeviceToHost, rt().stream) != cudaSuccess ||
+      cudaStreamSynchronize(rt().stream) != cudaSuccess) { set_error(DFTGPU_ERR_CUDA, "grid_wf_normalize"); return NAN; }
+  if (!isfinite(v) || v <= 0.0) set_error(DFTGPU_ERR_NONFINITE, "grid_wf_normalize: norm %g", v);
+  return sqrt(g->norm / v);
+}
+
+REAL grid_wf_kinetic_energy(wf *g) {
+  double v = NAN;
+  kinetic_energy(g, &v);
+  return v;
+}
+
+REAL grid_wf_energy(wf *g, rgrid *pot) {
+  double e = grid_wf_kinetic_energy(g);
+  if (pot) {
+    rgrid *d = rgrid_new(g->grid->nx, g->grid->ny, g->grid->nz, g->grid->step, g->grid->prec, "tmp");
+    if (!d) return NAN;
+    density(g->grid, d);
+    rbinary(d, d, pot, 0.0, 1);
+    double v = NAN;
+    rintegral(d, &v);
+    rgrid_free(d);
+    e += v;
+  }
+  return e;
+}
+
+void grid_wf_velocity(wf *g, rgrid *vx, rgrid *vy, rgrid *vz, REAL eps) {
+  if (!rc_shape(g->grid, vx) || !rc_shape(g->grid, vy) || !rc_shape(g->grid, vz)) { bad_arg("grid_wf_velocity"); return; }
+  velocity(g, vx, vy, vz, eps);
+}
+
+int dftgpu_wf_propagate(wf *g, cgrid *pot, double dr, double di) { return propagate(g, g->grid, g->grid, pot, dr, di); }
+int dftgpu_wf_propagate_predict(wf *g, wf *gp, cgrid *pot, double dr, double di) {
+  if (!gp || !same_shape(g->grid, gp->grid)) return bad_arg("propagate_predict: wave function mismatch");
+  return propagate(g, gp->grid, g->grid, pot, dr, di);
+}
+int dftgpu_wf_propagate_correct(wf *g, cgrid *pot, double dr, double di) { return propagate(g, g->grid, g->grid, pot, dr, di); }
+
+// ------------------------------------------------------------------ OT functional
+// 0 K OT parameters and unit conversions (src/ot.c:1026-1036, 1234-1270)
+void dft_ot_init_params(dft_ot_functional *otf, INT model) {
+  const double a3 = GRID_AUTOANG * GRID_AUTOANG * GRID_AUTOANG;
+  otf->model = model;
+  otf->beta = otf->rhom = otf->C = 0.0;
+  otf->b = -718.99;
+  otf->c2 = -2.411857E4;
+  otf->c2_exp = 2.0;
+  otf->c3 = 1.858496E6;
+  otf->c3_exp = 3.0;
+  otf->c4 = 0.0;
+  otf->temp = 0.0;
+  otf->rho0 = 0.0218360;
+  otf->lj_params.h = 2.1903;
+  otf->mu0 = 0.0;
+  otf->xi = 1E4 / a3;
+  otf->rhobf = 0.033 * a3;
+  otf->b /= GRID_AUTOK * a3;
+  otf->c2 /= GRID_AUTOK * pow(GRID_AUTOANG, 3.0 * otf->c2_exp);
+  otf->c3 /= GRID_AUTOK * pow(GRID_AUTOANG, 3.0 * otf->c3_exp);
+  otf->rho0 *= a3;
+  otf->lj_params.h /= GRID_AUTOANG;
+  otf->lj_params.sigma = 2.556 / GRID_AUTOANG;
+  otf->lj_params.epsilon = 10.22 / GRID_AUTOK;
+  otf->lj_params.cval = 0.0;
+  otf->rho_0s = 0.04 * a3;
+  otf->alpha_s = 54.31 / a3;
+  otf->l_g = 1.0 / GRID_AUTOANG;
+  otf->mass = 4.0026 / GRID_AUTOAMU;
+  otf->bf_params.g11 = -19.7544;
+  otf->bf_params.g12 = 12.5616 * GRID_AUTOANG * GRID_AUTOANG;
+  otf->bf_params.a1 = 1.023 * GRID_AUTOANG * GRID_AUTOANG;
+  otf->bf_params.g21 = -0.2395;
+  otf->bf_params.g22 = 0.0312 * GRID_AUTOANG * GRID_AUTOANG;
+  otf->bf_params.a2 = 0.14912 * GRID_AUTOANG * GRID_AUTOANG;
+  otf->div_epsilon = DFT_EPS;
+  otf->max_veloc = 999.0 / GRID_AUTOMPS;
+  otf->max_bfpot = 10000.0 / GRID_AUTOK;
+  otf->c_bfpot = 1.0;
+}
+
+dft_ot_functional *dft_ot_alloc(INT model, wf *gwf, INT min_substeps, INT max_substeps) {
+  if (!gwf) { bad_arg("dft_ot_alloc: NULL wave function"); return nullptr; }
+  if (model & ~((INT) (DFT_OT_KC | DFT_OT_BACKFLOW))) {
+    set_error(DFTGPU_ERR_UNSUPPORTED, "dft_ot_alloc: model %ld outside {PLAIN, KC, BACKFLOW}", (long) model);
+    return nullptr;
+  }
+  cgrid *c = gwf->grid;
+  dft_ot_functional *otf = (dft_ot_functional *) calloc(1, sizeof(dft_ot_functional));
+  if (!otf) return nullptr;
+  dft_ot_init_params(otf, model);
+  OtPriv *P = new OtPriv();
+  P->prec = c->prec;
+  P->nx = (int) c->nx; P->ny = (int) c->ny; P->nz = (int) c->nz;
+  P->step = c->step; P->x0 = c->x0; P->y0 = c->y0; P->z0 = c->z0;
+  P->oct_n = (size_t) (P->nz / 2 + 1) * (P->nx / 2 + 1) * (P->ny / 2 + 1);
+  otf->priv = P;
+  otf->density = rgrid_new(c->nx, c->ny, c->nz, c->step, c->prec, "OT density");
+  if (!otf->density || ot_generate_kernels(otf, (int) min_substeps, (int) max_substeps) != DFTGPU_OK) {
+    dft_ot_free(otf);
+    return nullptr;
+  }
+  return otf;
+}
+
+int dft_ot_update_kernels(dft_ot_functional *otf, INT min_substeps, INT max_substeps) {
+  if (!otf) return bad_arg("dft_ot_update_kernels: NULL");
+  return ot_generate_kernels(otf, (int) min_substeps, (int) max_substeps);
+}
+
+void dft_ot_free(dft_ot_functional *otf) {
+  if (!otf) return;
+  OtPriv *P = (OtPriv *) otf->priv;
+  if (P) {
+    for (int i = 0; i < OT_NKER; i++) dev_free(P->ker[i]);
+    for (int i = 0; i < OT_MAX_REAL; i++) dev_free(P->real[i]);
+    for (int i = 0; i < OT_MAX_SPEC; i++) dev_free(P->spec[i]);
+    cgrid_free(P->pot_tmp);
+    rgrid_free(P->ed_tmp);
+    delete P;
+  }
+  rgrid_free(otf->density);
+  free(otf);
+}
+
+static bool ot_matches(dft_ot_functional *otf, const cgrid *c) {
+  OtPriv *P = (OtPriv *) otf->priv;
+  return c && P && c->nx == P->nx && c->ny == P->ny && c->nz == P->nz && c->prec == P->prec;
+}
+
+void dft_ot_potential(dft_ot_functional *otf, cgrid *potential, wf *gwf) {
+  if (!otf || !gwf || !ot_matches(otf, potential) || !ot_matches(otf, gwf->grid)) { bad_arg("dft_ot_potential: grid mismatch"); return; }
+  ot_potential(otf, potential, gwf);
+}
+
+void dft_ot_energy_density(dft_ot_functional *otf, rgrid *ed, wf *gwf) {
+  OtPriv *P = otf ? (OtPriv *) otf->priv : nullptr;
+  if (!P || !gwf || !ot_matches(otf, gwf->grid) || !ed || ed->nx != P->nx || ed->ny != P->ny || ed->nz != P->nz || ed->prec != P->prec) {
+    bad_arg("dft_ot_energy_density: grid mismatch");
+    return;
+  }
+  ot_energy_density(otf, ed, gwf);
+}
+
+int dftgpu_rgrid_spectrum(rgrid *g, double *host) {
+  if (!g || !host) return bad_arg("dftgpu_rgrid_spectrum: NULL");
+  return rspectrum(g, host);
+}
+
+int dftgpu_ot_kernel(dft_ot_functional *otf, int which, double *host) {
+  if (!otf || !host || which < 0 || which >= OT_NKER) return bad_arg("dftgpu_ot_kernel: argument");
+  OtPriv *P = (OtPriv *) otf->priv;
+  if (which >= OT_F && which <= OT_FZ && !(otf->model & DFT_OT_KC)) return bad_arg("dftgpu_ot_kernel: no KC kernels");
+  if (which == OT_VJ && !(otf->model & DFT_OT_BACKFLOW)) return bad_arg("dftgpu_ot_kernel: no backflow kernel");
+  return copy_values_out(P->prec, P->ker[which], host, P->oct_n);
+}
+
+// ------------------------------------------------------------------ bulk (host)
+// src/helium-ot-bulk.c:21-33, 45-57, 143-172, 185-258, 376-434
+REAL dft_ot_bulk_energy(dft_ot_functional *o, REAL rho) {
+  return 0.5 * o->b * rho * rho + 0.5 * o->c2 * rho * rho * rho + (1.0 / 3.0) * o->c3 * rho * rho * rho * rho;
+}
+REAL dft_ot_bulk_dEdRho(dft_ot_functional *o, REAL rho) {
+  return o->b * rho + 1.5 * o->c2 * rho * rho + (4.0 / 3.0) * o->c3 * rho * rho * rho;
+}
+REAL dft_ot_bulk_pressure(dft_ot_functional *o, REAL rho) { return rho * dft_ot_bulk_dEdRho(o, rho) - dft_ot_bulk_energy(o, rho); }
+REAL dft_ot_bulk_dPdRho(dft_ot_functional *o, REAL rho) {
+  const double h = 1E-7;
+  return (dft_ot_bulk_pressure(o, rho + h) - dft_ot_bulk_pressure(o, rho - h)) / (2.0 * h);
+}
+REAL dft_ot_bulk_density_pressurized(dft_ot_functional *o, REAL pressure) {
+  double rho = 1.0, miss = dft_ot_bulk_pressure(o, rho) - pressure;
+  for (int it = 0; it < 1000; it++) {
+    if (fabs(miss) < 1.0E-12) return rho;
+    rho -= miss / dft_ot_bulk_dPdRho(o, rho);
+    miss = dft_ot_bulk_pressure(o, rho) - pressure;
+  }
+  set_error(DFTGPU_ERR_NONFINITE, "bulk density: Newton iteration did not converge");
+  return NAN;
+}
+REAL dft_ot_bulk_chempot_pressurized(dft_ot_functional *o, REAL p) { return dft_ot_bulk_dEdRho(o, dft_ot_bulk_density_pressurized(o, p)); }
+REAL dft_ot_bulk_density(dft_ot_functional *o) { return dft_ot_bulk_density_pressurized(o, 0.0); }
+REAL dft_ot_bulk_chempot(dft_ot_functional *o) { return dft_ot_bulk_dEdRho(o, dft_ot_bulk_density(o)); }
+REAL dft_ot_bulk_chempot2(dft_ot_functional *o) { return dft_ot_bulk_dEdRho(o, o->rho0); }
+REAL dft_ot_bulk_compressibility(dft_ot_functional *o, REAL rho) { return 1.0 / (rho * dft_ot_bulk_dPdRho(o, rho)); }
+REAL dft_ot_bulk_sound_speed(dft_ot_functional *o, REAL rho) { return 1.0 / sqrt(o->mass * rho * dft_ot_bulk_compressibility(o, rho)); }
+
+REAL dft_ot_bulk_dispersion(dft_ot_functional *o, REAL *kp, REAL rho0) {
+  const double k = *kp;
+  if (rho0 < 0.0 || k < 1E-3) return 0.0;
+  const double sg = o->lj_params.sigma, ks = k * sg;
+  double lj = 0.0;
+  for (double x = o->lj_params.h / sg; x < 1E3; x += 1.0E-2) lj += sin(ks * x) * (pow(x, -11.0) - pow(x, -5.0));
+  lj *= 1.0E-2 * 16.0 * M_PI * o->lj_params.epsilon * sg * sg * sg / ks;
+  const double kh = k * o->lj_params.h, pi = (3.0 / (kh * kh * kh)) * (sin(kh) - kh * cos(kh));
+  const double t = k * k / o->mass;
+  double chi = t / 4.0 + rho0 * lj + o->c2 * (2.0 * pi + pi * pi) * rho0 * rho0 + 2.0 * o->c3 * (pi + pi * pi) * rho0 * rho0 * rho0;
+  if (o->model & DFT_OT_KC) {
+    const double f = 1.0 - rho0 / o->rho_0s;
+    chi += -(t / 2.0) * o->alpha_s * rho0 * f * f * exp(-k * k * o->l_g * o->l_g / 4.0);
+  }
+  if (o->model & DFT_OT_BACKFLOW) {
+    const dft_ot_bf &p = o->bf_params;
+    auto vj = [&](double q) {
+      const double q2 = q * q, pi32 = pow(M_PI, 1.5);
+      return (p.g11 * pow(M_PI / p.a1, 1.5) + p.g12 * (6.0 * p.a1 - q2) * pi32 / (4.0 * pow(p.a1, 3.5))) * exp(-q2 / (4.0 * p.a1)) +
+             (p.g21 * pow(M_PI / p.a2, 1.5) + p.g22 * (6.0 * p.a2 - q2) * pi32 / (4.0 * pow(p.a2, 3.5))) * exp(-q2 / (4.0 * p.a2));
+    };
+    return sqrt(t * chi * (1.0 - rho0 * (vj(0.0) - vj(k))));
+  }
+  return sqrt(t * chi);
+}
+
+// ------------------------------------------------------------------ fused step
+static int pc_step_impl(dft_ot_functional *otf, wf *gwf, wf *gwfp, cgrid *P, rgrid *vext, double mu0, double dr, double di) {
+  if (vext) DFT_TRY(real_to_complex(P, vext, 0)); else DFT_TRY(cfill(P, 0.0, 0.0));
+  DFT_TRY(ot_potential(otf, P, gwf));
+  DFT_TRY(cmuladd(P, 1.0, 0.0, -mu0, 0.0));
+  DFT_TRY(propagate(gwf, gwfp->grid, gwf->grid, P, dr, di));
+  if (vext) DFT_TRY(real_to_complex(P, vext, 1));
+  DFT_TRY(ot_potential(otf, P, gwfp));
+  DFT_TRY(cmuladd(P, 0.5, 0.0, -0.5 * mu0, 0.0));     // (P - mu0) / 2, bit-identical
+  return propagate(gwf, gwf->grid, gwf->grid, P, dr, di);
+}
+
+static int check_step_args(dft_ot_functional *otf, wf *gwf, wf *gwfp, cgrid *P, rgrid *vext) {
+  if (!otf || !gwf || !gwfp || !P) return bad_arg("pc step: NULL argument");
+  if (!ot_matches(otf, gwf->grid) || !ot_matches(otf, gwfp->grid) || !ot_matches(otf, P)) return bad_arg("pc step: grid mismatch");
+  if (vext && !rc_shape(P, vext)) return bad_arg("pc step: vext mismatch");
+  return DFTGPU_OK;
+}
+
+int dftgpu_pc_step(dft_ot_functional *otf, wf *gwf, wf *gwfp, cgrid *P, rgrid *vext, double mu0, double dr, double di) {
+  DFT_TRY(check_step_args(otf, gwf, gwfp, P, vext));
+  return pc_step_impl(otf, gwf, gwfp, P, vext, mu0, dr, di);
+}
+
+static int step_with_renorm(dft_ot_functional *otf, wf *gwf, wf *gwfp, cgrid *P, rgrid *vext, double mu0, double dr, double di, int renorm) {
+  DFT_TRY(pc_step_impl(otf, gwf, gwfp, P, vext, mu0, dr, di));
+  if (renorm) {
+    double *slot = reduce_slots();
+    DFT_TRY(norm_dev(gwf->grid, slot + 3));
+    DFT_TRY(scale_by_norm(gwf->grid, slot + 3, gwf->norm));
+  }
+  return DFTGPU_OK;
+}
+
+int dftgpu_run(dft_ot_functional *otf, wf *gwf, wf *gwfp, cgrid *P, rgrid *vext, double mu0, double dr, double di,
+               INT nsteps, int renorm) {
+  DFT_TRY(check_step_args(otf, gwf, gwfp, P, vext));
+  if (nsteps <= 0) return DFTGPU_OK;
+  // first step eagerly: allocates work buffers and FFT tables outside capture
+  DFT_TRY(step_with_renorm(otf, gwf, gwfp, P, vext, mu0, dr, di, renorm));
+  if (nsteps == 1) return DFTGPU_OK;
+  const bool use_graph = !getenv("DFTGPU_NO_GRAPH");
+  if (!use_graph) {
+    for (INT s = 1; s < nsteps; s++) DFT_TRY(step_with_renorm(otf, gwf, gwfp, P, vext, mu0, dr, di, renorm));
+    return DFTGPU_OK;
+  }
+  cudaStream_t user = rt().stream, cap;
+  DFT_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+  cudaEvent_t ev;
+  DFT_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  DFT_CUDA(cudaEventRecord(ev, user));
+  DFT_CUDA(cudaStreamWaitEvent(cap, ev, 0));
+  rt().stream = cap;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int rc = DFTGPU_OK;
+  if (cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess) rc = DFTGPU_ERR_CUDA;
+  if (!rc) {
+    rc = step_with_renorm(otf, gwf, gwfp, P, vext, mu0, dr, di, renorm);
+    cudaError_t e = cudaStreamEndCapture(cap, &graph);
+    if (!rc && e != cudaSuccess) { rc = DFTGPU_ERR_CUDA; set_error(rc, "graph capture: %s", cudaGetErrorString(e)); }
+  }
+  if (!rc && cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) { rc = DFTGPU_ERR_CUDA; set_error(rc, "graph instantiate"); }
+  for (INT s = 1; !rc && s < nsteps; s++)
+    if (cudaGraphLaunch(exec, cap) != cudaSuccess) { rc = DFTGPU_ERR_CUDA; set_error(rc, "graph launch"); }
+  cudaEventRecord(ev, cap);
+  cudaStreamWaitEvent(user, ev, 0);
+  rt().stream = user;
+  if (exec) cudaGraphExecDestroy(exec);
+  if (graph) cudaGraphDestroy(graph);
+  cudaEventDestroy(ev);
+  cudaStreamDestroy(cap);
+  return rc;
+}
+
+int dftgpu_energy_report(dft_ot_functional *otf, wf *gwf, rgrid *vext, double *energy, double *natoms, double *mu) {
+  if (!otf || !gwf || !ot_matches(otf, gwf->grid)) return bad_arg("energy report: grid mismatch");
+  OtPriv *Pv = (OtPriv *) otf->priv;
+  cgrid *c = gwf->grid;
+  if (!Pv->ed_tmp) Pv->ed_tmp = rgrid_new(c->nx, c->ny, c->nz, c->step, c->prec, "ed");
+  if (!Pv->pot_tmp) Pv->pot_tmp = cgrid_new(c->nx, c->ny, c->nz, c->step, c->prec, "pot");
+  if (!Pv->ed_tmp || !Pv->pot_tmp) return DFTGPU_ERR_NOMEM;
+  double ekin = 0, eint = 0, evx = 0, n = 0, epot = 0;
+  DFT_TRY(kinetic_energy(gwf, &ekin));
+  DFT_TRY(ot_energy_density(otf, Pv->ed_tmp, gwf));
+  DFT_TRY(rintegral(Pv->ed_tmp, &eint));
+  if (vext) {   // density is current after ot_energy_density
+    DFT_TRY(rbinary(Pv->ed_tmp, otf->density, vext, 0.0, 1));
+    DFT_TRY(rintegral(Pv->ed_tmp, &evx));
+  }
+  n = grid_wf_norm(gwf);
+  DFT_TRY(cfill(Pv->pot_tmp, 0.0, 0.0));
+  DFT_TRY(ot_potential(otf, Pv->pot_tmp, gwf));          // also refreshes otf->density
+  double e_rho_v = 0.0;
+  DFT_TRY(rho_dot_re(otf->density, Pv->pot_tmp, &e_rho_v));
+  epot = e_rho_v;
+  if (energy) *energy = ekin + eint + evx;
+  if (natoms) *natoms = n;
+  if (mu) *mu = (ekin + epot + evx) / n;
+  if (!isfinite(ekin + eint + evx) || !isfinite(n)) { set_error(DFTGPU_ERR_NONFINITE, "energy report: non-finite"); return DFTGPU_ERR_NONFINITE; }
+  return DFTGPU_OK;
+}
+
+}  // extern "C"

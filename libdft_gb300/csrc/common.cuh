@@ -1,0 +1,97 @@
+// Shared definitions for the GB300 OT-DFT library (sm_103a).
+//
+// Precision model: a grid stores either FP32 or FP64 values (the "bulk"
+// precision).  Reductions (norms, energies, chemical potential) always
+// accumulate in FP64; the k-space convolution kernels are generated in FP64
+// and stored in the bulk precision.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#include "dftgpu.h"
+
+namespace dftgpu {
+
+// ------------------------------------------------------------------ complex
+template <typename T> struct cplx_t;
+template <> struct cplx_t<float> { typedef float2 type; };
+template <> struct cplx_t<double> { typedef double2 type; };
+
+template <typename T> __host__ __device__ __forceinline__ typename cplx_t<T>::type mk(T re, T im) {
+  typename cplx_t<T>::type r; r.x = re; r.y = im; return r;
+}
+__host__ __device__ __forceinline__ float2 operator+(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__host__ __device__ __forceinline__ float2 operator-(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__host__ __device__ __forceinline__ float2 operator*(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+__host__ __device__ __forceinline__ double2 operator+(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__host__ __device__ __forceinline__ double2 operator-(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__host__ __device__ __forceinline__ double2 operator*(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
+
+template <typename C> __host__ __device__ __forceinline__ C cmul(C a, C b) {
+  C r; r.x = a.x * b.x - a.y * b.y; r.y = a.x * b.y + a.y * b.x; return r;
+}
+// a * conj(b)
+template <typename C> __host__ __device__ __forceinline__ C cmulc(C a, C b) {
+  C r; r.x = a.x * b.x + a.y * b.y; r.y = a.y * b.x - a.x * b.y; return r;
+}
+// multiply by +i (s = +1) or -i (s = -1)
+template <typename C, typename T> __host__ __device__ __forceinline__ C imul(C a, T s) {
+  C r; r.x = -s * a.y; r.y = s * a.x; return r;
+}
+template <typename C> __host__ __device__ __forceinline__ C conjc(C a) { C r; r.x = a.x; r.y = -a.y; return r; }
+
+// exp(z) for complex z, in the precision of C
+__device__ __forceinline__ float2 cexp_dev(float2 z) {
+  float e = expf(z.x), s, c; sincosf(z.y, &s, &c); return make_float2(e * c, e * s);
+}
+__device__ __forceinline__ double2 cexp_dev(double2 z) {
+  double e = exp(z.x), s, c; sincos(z.y, &s, &c); return make_double2(e * c, e * s);
+}
+
+// ------------------------------------------------------------------ errors
+extern thread_local int g_last_error;
+void set_error(int code, const char *fmt, ...);
+
+#define DFT_CUDA(call)                                                         \
+  do {                                                                         \
+    cudaError_t _e = (call);                                                   \
+    if (_e != cudaSuccess) {                                                   \
+      ::dftgpu::set_error(DFTGPU_ERR_CUDA, "%s:%d %s: %s", __FILE__, __LINE__, \
+                          #call, cudaGetErrorString(_e));                      \
+      return DFTGPU_ERR_CUDA;                                                  \
+    }                                                                          \
+  } while (0)
+
+#define DFT_CHECK_LAUNCH()                                                     \
+  do {                                                                         \
+    cudaError_t _e = cudaGetLastError();                                       \
+    if (_e != cudaSuccess) {                                                   \
+      ::dftgpu::set_error(DFTGPU_ERR_CUDA, "%s:%d launch: %s", __FILE__,       \
+                          __LINE__, cudaGetErrorString(_e));                   \
+      return DFTGPU_ERR_CUDA;                                                  \
+    }                                                                          \
+  } while (0)
+
+#define DFT_TRY(expr)                                                          \
+  do { int _r = (expr); if (_r != DFTGPU_OK) return _r; } while (0)
+
+// ------------------------------------------------------------------ runtime
+struct Runtime {
+  int device = -1;
+  int num_sms = 0;
+  int precision = DFTGPU_FP64;
+  cudaStream_t stream = 0;
+  size_t max_smem_optin = 0;
+};
+Runtime &rt();
+int ensure_device();
+
+// Device-resident FP64 accumulator slots used by reductions.
+double *reduce_slots();
+int reduce_partials(double **buf, size_t *n);
+
+inline size_t elem_size(int prec) { return prec == DFTGPU_FP32 ? 4 : 8; }
+
+}  // namespace dftgpu

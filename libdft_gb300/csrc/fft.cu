@@ -1,0 +1,136 @@
+// FFT plans, twiddle tables and launchers for the x-pencil kernels.
+#include <math.h>
+#include <map>
+#include <mutex>
+#include <utility>
+
+#include "fft.cuh"
+
+namespace dftgpu {
+
+namespace {
+struct PlanEntry {
+  int nst;
+  int radix[FFT_MAX_STAGES];
+  void *tw;
+};
+std::map<std::pair<int, int>, PlanEntry> g_plans;   // (n, sizeof(T)) -> plan
+std::mutex g_plan_mu;
+
+int factorize(int n, int *radix, int *nst) {
+  int m = n, k = 0;
+  while (m % 8 == 0 && m > 8) { radix[k++] = 8; m /= 8; }
+  // finish the power-of-two part with one 8, 4 or 2
+  if (m % 8 == 0) { radix[k++] = 8; m /= 8; }
+  if (m % 4 == 0) { radix[k++] = 4; m /= 4; }
+  if (m % 2 == 0) { radix[k++] = 2; m /= 2; }
+  while (m % 3 == 0) { radix[k++] = 3; m /= 3; }
+  while (m % 5 == 0) { radix[k++] = 5; m /= 5; }
+  if (m != 1 || k > FFT_MAX_STAGES) return DFTGPU_ERR_SIZE;
+  *nst = k;
+  return DFTGPU_OK;
+}
+}  // namespace
+
+template <typename T> int get_plan(int n, FftPlan<T> *plan) {
+  typedef typename cplx_t<T>::type C;
+  if (n < 1 || n > 2 * FFT_MAX_N) {
+    set_error(DFTGPU_ERR_SIZE, "FFT length %d outside [1, %d]", n, 2 * FFT_MAX_N);
+    return DFTGPU_ERR_SIZE;
+  }
+  std::lock_guard<std::mutex> lock(g_plan_mu);
+  auto key = std::make_pair(n, (int) sizeof(T));
+  auto it = g_plans.find(key);
+  if (it == g_plans.end()) {
+    PlanEntry e;
+    if (n == 1) { e.nst = 0; }
+    else if (factorize(n, e.radix, &e.nst) != DFTGPU_OK) {
+      set_error(DFTGPU_ERR_SIZE, "FFT length %d is not of the form 2^a 3^b 5^c", n);
+      return DFTGPU_ERR_SIZE;
+    }
+    C *h = (C *) malloc(sizeof(C) * (size_t) n);
+    for (int t = 0; t < n; t++) {
+      // reduce the angle to [-pi, pi] and evaluate in long double, round once
+      long tt = (t <= n / 2) ? t : (long) t - n;
+      long double ang = -2.0L * 3.14159265358979323846264338327950288L * (long double) tt / (long double) n;
+      h[t].x = (T) cosl(ang);
+      h[t].y = (T) sinl(ang);
+    }
+    void *d = nullptr;
+    cudaError_t err = cudaMalloc(&d, sizeof(C) * (size_t) n);
+    if (err == cudaSuccess) err = cudaMemcpy(d, h, sizeof(C) * (size_t) n, cudaMemcpyHostToDevice);
+    free(h);
+    if (err != cudaSuccess) {
+      set_error(DFTGPU_ERR_CUDA, "twiddle table: %s", cudaGetErrorString(err));
+      return DFTGPU_ERR_CUDA;
+    }
+    e.tw = d;
+    it = g_plans.emplace(key, e).first;
+  }
+  plan->n = n;
+  plan->nst = it->second.nst;
+  for (int i = 0; i < it->second.nst; i++) plan->radix[i] = it->second.radix[i];
+  plan->tw = (const C *) it->second.tw;
+  return DFTGPU_OK;
+}
+
+template int get_plan<float>(int, FftPlan<float> *);
+template int get_plan<double>(int, FftPlan<double> *);
+
+int choose_tile(int n, int nb, size_t cplx_bytes, int nbufs, int *B, size_t *smem) {
+  const size_t budget = 113 * 1024, hard = 225 * 1024;
+  const int cand[5] = { 16, 8, 4, 2, 1 };
+  for (int pass = 0; pass < 2; pass++) {
+    for (int c = 0; c < 5; c++) {
+      int b = cand[c];
+      if (nb % b) continue;
+      size_t s = (size_t) nbufs * (size_t) n * (size_t) (b + 1) * cplx_bytes;
+      if (s <= (pass == 0 ? budget : hard)) { *B = b; *smem = s; return DFTGPU_OK; }
+    }
+  }
+  set_error(DFTGPU_ERR_SIZE, "FFT tile for n=%d does not fit in shared memory", n);
+  return DFTGPU_ERR_SIZE;
+}
+
+template <typename T> int launch_xconv(XConvArgs<T> &A) {
+  typedef typename cplx_t<T>::type C;
+  DFT_TRY(get_plan<T>(A.nx, &A.plan));
+  int B; size_t smem;
+  DFT_TRY(choose_tile(A.nx, A.ny, sizeof(C), A.nin + 2, &B, &smem));
+  A.B = B;
+  A.kxh = A.nx / 2 + 1;
+  A.kyh = A.ny / 2 + 1;
+  static bool attr = false;
+  if (!attr) {
+    DFT_CUDA(cudaFuncSetAttribute(xconv_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+    attr = true;
+  }
+  dim3 grid(A.ny / B, A.nkz);
+  xconv_kernel<T><<<grid, FFT_THREADS, smem, rt().stream>>>(A);
+  DFT_CHECK_LAUNCH();
+  return DFTGPU_OK;
+}
+
+template <typename T> int launch_xkinetic(KinArgs<T> &A) {
+  typedef typename cplx_t<T>::type C;
+  DFT_TRY(get_plan<T>(A.nx, &A.plan));
+  int B; size_t smem;
+  DFT_TRY(choose_tile(A.nx, A.ny, sizeof(C), 2, &B, &smem));
+  A.B = B;
+  static bool attr = false;
+  if (!attr) {
+    DFT_CUDA(cudaFuncSetAttribute(xkinetic_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+    attr = true;
+  }
+  dim3 grid(A.ny / B, A.nz);
+  xkinetic_kernel<T><<<grid, FFT_THREADS, smem, rt().stream>>>(A);
+  DFT_CHECK_LAUNCH();
+  return DFTGPU_OK;
+}
+
+template int launch_xconv<float>(XConvArgs<float> &);
+template int launch_xconv<double>(XConvArgs<double> &);
+template int launch_xkinetic<float>(KinArgs<float> &);
+template int launch_xkinetic<double>(KinArgs<double> &);
+
+}  // namespace dftgpu

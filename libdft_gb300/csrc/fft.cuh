@@ -1,0 +1,420 @@
+// 3-D FFT building blocks for sm_103a (header-only templates).
+//
+// A 3-D transform of an [nx][ny][nz] grid runs as three line passes:
+//   z pass  rows (x,y) are contiguous in real space; the output is written
+//           transposed into the spectral layout [kz][x][y]
+//   y pass  lines along y are contiguous in [kz][x][y]
+//   x pass  pencils along x (stride ny); B consecutive y per CTA, so every
+//           global access is a contiguous run of B complex values.
+// Real fields use the half spectrum (kz = 0..nz/2) produced by packing a real
+// row of length nz into nz/2 complex values (even + i odd), one FFT of length
+// nz/2 and a twiddle post-processing step; the inverse does the reverse.
+//
+// Every line pass stages a tile of B lines in shared memory as [n][B+1]
+// (element-major, padded), runs a Stockham autosort FFT with radices
+// {8,4,2,3,5} (ping-pong buffers) and streams the tile back.  Loads and
+// stores go through functors, which is where pointwise producers (|psi|^2,
+// products of fields, phase factors) and consumers (accumulate into the
+// potential) are fused.  Twiddles come from per-length tables computed in
+// FP64 on the host and rounded once to the bulk precision.
+#pragma once
+
+#include "common.cuh"
+
+namespace dftgpu {
+
+constexpr int FFT_THREADS = 256;
+constexpr int FFT_MAX_STAGES = 16;
+constexpr int FFT_MAX_N = 1024;
+
+template <typename T> struct FftPlan {
+  int n;                       // transform length
+  int nst;                     // number of stages
+  int radix[FFT_MAX_STAGES];
+  const typename cplx_t<T>::type *tw;   // tw[t] = exp(-2 pi i t / n), t < n
+};
+
+// Host: build (and cache) the plan for length n in precision T.
+template <typename T> int get_plan(int n, FftPlan<T> *plan);
+
+// ------------------------------------------------------------ butterflies
+template <typename C, typename T>
+__device__ __forceinline__ void dft2(C &a, C &b) { C t = a; a = t + b; b = t - b; }
+
+template <int R, typename C, typename T>
+__device__ __forceinline__ void small_dft(C *u, T s) {
+  // s = -1 forward, +1 inverse
+  if constexpr (R == 2) {
+    dft2<C, T>(u[0], u[1]);
+  } else if constexpr (R == 3) {
+    const T s3 = (T) 0.86602540378443864676;
+    C a = u[0], b = u[1], c = u[2];
+    C m = a - (b + c) * (T) 0.5;
+    C d = (b - c) * s3;
+    u[0] = a + b + c;
+    u[1] = m + imul<C, T>(d, s);
+    u[2] = m - imul<C, T>(d, s);
+  } else if constexpr (R == 4) {
+    C t0 = u[0] + u[2], t1 = u[0] - u[2], t2 = u[1] + u[3], t3 = u[1] - u[3];
+    u[0] = t0 + t2;
+    u[2] = t0 - t2;
+    u[1] = t1 + imul<C, T>(t3, s);
+    u[3] = t1 - imul<C, T>(t3, s);
+  } else if constexpr (R == 5) {
+    const T c1 = (T) 0.30901699437494742410, c2 = (T) -0.80901699437494742410;
+    const T s1 = (T) 0.95105651629515357212, s2 = (T) 0.58778525229247312917;
+    C a = u[0];
+    C t1 = u[1] + u[4], t2 = u[2] + u[3], t3 = u[1] - u[4], t4 = u[2] - u[3];
+    C m1 = a + t1 * c1 + t2 * c2;
+    C m2 = a + t1 * c2 + t2 * c1;
+    C n1 = t3 * s1 + t4 * s2;
+    C n2 = t3 * s2 - t4 * s1;
+    u[0] = a + t1 + t2;
+    u[1] = m1 + imul<C, T>(n1, s);
+    u[4] = m1 - imul<C, T>(n1, s);
+    u[2] = m2 + imul<C, T>(n2, s);
+    u[3] = m2 - imul<C, T>(n2, s);
+  } else if constexpr (R == 8) {
+    const T h = (T) 0.70710678118654752440;
+    // radix-2 over stride 4, then two radix-4 with the W8 twiddles
+    C a0 = u[0] + u[4], a1 = u[0] - u[4];
+    C b0 = u[2] + u[6], b1 = u[2] - u[6];
+    C c0 = u[1] + u[5], c1 = u[1] - u[5];
+    C d0 = u[3] + u[7], d1 = u[3] - u[7];
+    // even outputs: 4-point DFT of (a0, c0, b0, d0)
+    C e0 = a0 + b0, e1 = a0 - b0, f0 = c0 + d0, f1 = c0 - d0;
+    u[0] = e0 + f0;
+    u[4] = e0 - f0;
+    u[2] = e1 + imul<C, T>(f1, s);
+    u[6] = e1 - imul<C, T>(f1, s);
+    // odd outputs: 4-point DFT of (a1, W c1, W^2 b1, W^3 d1), W = exp(s i pi/4)
+    C b1w = imul<C, T>(b1, s);                       // W^2 b1
+    C c1w, d1w;
+    c1w.x = h * (c1.x - s * c1.y); c1w.y = h * (c1.y + s * c1.x);      // W c1
+    d1w.x = h * (-d1.x - s * d1.y); d1w.y = h * (-d1.y + s * d1.x);    // W^3 d1
+    C g0 = a1 + b1w, g1 = a1 - b1w, k0 = c1w + d1w, k1 = c1w - d1w;
+    u[1] = g0 + k0;
+    u[5] = g0 - k0;
+    u[3] = g1 + imul<C, T>(k1, s);
+    u[7] = g1 - imul<C, T>(k1, s);
+  }
+}
+
+// One radix-R Stockham stage over a tile of B lines in [n][ldb] layout.
+template <int R, typename T>
+__device__ __forceinline__ void stockham_stage(const typename cplx_t<T>::type *__restrict__ in,
+                                               typename cplx_t<T>::type *__restrict__ out,
+                                               int n, int B, int ldb, int p,
+                                               const typename cplx_t<T>::type *__restrict__ tw, T s) {
+  typedef typename cplx_t<T>::type C;
+  const int nR = n / R, twstep = n / (p * R);
+  for (int idx = threadIdx.x; idx < nR * B; idx += blockDim.x) {
+    const int l = idx % B, i = idx / B, k = i % p;
+    C u[R];
+#pragma unroll
+    for (int q = 0; q < R; q++) {
+      C v = in[(i + q * nR) * ldb + l];
+      if (q > 0 && k > 0) {
+        C w = __ldg(&tw[(q * k * twstep) % n]);
+        w.y *= -s;   // tw holds exp(-i...); inverse (s=+1) uses the conjugate
+        v = cmul(v, w);
+      }
+      u[q] = v;
+    }
+    small_dft<R, C, T>(u, s);
+    const int j = (i - k) * R + k;
+#pragma unroll
+    for (int q = 0; q < R; q++) out[(j + q * p) * ldb + l] = u[q];
+  }
+}
+
+// Runs all stages; returns the buffer holding the result (a or b).
+template <typename T>
+__device__ __forceinline__ typename cplx_t<T>::type *tile_fft(typename cplx_t<T>::type *a,
+                                                              typename cplx_t<T>::type *b,
+                                                              const FftPlan<T> &pl, int B, int ldb, T s) {
+  typedef typename cplx_t<T>::type C;
+  C *in = a, *out = b;
+  int p = 1;
+  for (int st = 0; st < pl.nst; st++) {
+    const int R = pl.radix[st];
+    switch (R) {
+      case 8: stockham_stage<8, T>(in, out, pl.n, B, ldb, p, pl.tw, s); break;
+      case 4: stockham_stage<4, T>(in, out, pl.n, B, ldb, p, pl.tw, s); break;
+      case 2: stockham_stage<2, T>(in, out, pl.n, B, ldb, p, pl.tw, s); break;
+      case 3: stockham_stage<3, T>(in, out, pl.n, B, ldb, p, pl.tw, s); break;
+      default: stockham_stage<5, T>(in, out, pl.n, B, ldb, p, pl.tw, s); break;
+    }
+    __syncthreads();
+    p *= R;
+    C *t = in; in = out; out = t;
+  }
+  return in;
+}
+
+// ------------------------------------------------------------ line pass
+enum { LINE_C2C = 0, LINE_R2C = 1, LINE_C2R = 2 };
+
+template <typename T> struct LineArgs {
+  FftPlan<T> plan;       // length of the complex FFT actually run
+  int B;                 // lines per CTA (divides nb)
+  int nb;                // extent of the fast line index b
+  T sign;                // -1 forward, +1 inverse
+  const typename cplx_t<T>::type *tw2;  // R2C/C2R: table of length 2n
+  int e_fast;            // 1: the load functor's fast address index is the element
+  int e_fast_store;      // 1: the store functor's fast address index is the element
+};
+
+// Line (a, b) = (blockIdx.y, blockIdx.x * B + l), element e.
+//   LINE_C2C: X = FFT(ld(a,b,e)), st(a,b,e,X[e]) for e < n
+//   LINE_R2C: z = ld(a,b,e) (packed even/odd reals), st(a,b,k,X[k]) for k <= n
+//   LINE_C2R: X[k] = ld(a,b,k) for k <= n, st(a,b,e, (x[2e], x[2e+1]))
+template <typename T, int MODE, class Ld, class St>
+__global__ void __launch_bounds__(FFT_THREADS) line_fft_kernel(const LineArgs<T> args, const Ld ld, const St st) {
+  typedef typename cplx_t<T>::type C;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int n = args.plan.n, B = args.B, ldb = B + 1;
+  C *buf0 = reinterpret_cast<C *>(smem_raw);
+  C *buf1 = buf0 + n * ldb;
+  const int a = blockIdx.y, b0 = blockIdx.x * B;
+
+  // ---- load
+  if (MODE == LINE_C2R) {
+    // Z[k] = (X[k] + X*[n-k]) + i w^{-k} (X[k] - X*[n-k]),  w = exp(-2 pi i / 2n)
+    for (int idx = threadIdx.x; idx < n * B; idx += blockDim.x) {
+      int k, l;
+      if (args.e_fast) { k = idx % n; l = idx / n; } else { l = idx % B; k = idx / B; }
+      C xk = ld(a, b0 + l, k), xm = ld(a, b0 + l, n - k);
+      if (k == 0) { xk.y = (T) 0; xm.y = (T) 0; }   // DC / Nyquist are real
+      C sum = xk + conjc(xm), dif = xk - conjc(xm);
+      C w = __ldg(&args.tw2[k]);
+      w.y = -w.y;                                    // w^{-k}
+      C t = cmul(dif, w);
+      C z; z.x = sum.x - t.y; z.y = sum.y + t.x;     // sum + i t
+      buf0[k * ldb + l] = z;
+    }
+  } else {
+    for (int idx = threadIdx.x; idx < n * B; idx += blockDim.x) {
+      int e, l;
+      if (args.e_fast) { e = idx % n; l = idx / n; } else { l = idx % B; e = idx / B; }
+      buf0[e * ldb + l] = ld(a, b0 + l, e);
+    }
+  }
+  __syncthreads();
+
+  C *res = tile_fft<T>(buf0, buf1, args.plan, B, ldb, args.sign);
+
+  // ---- store
+  if (MODE == LINE_R2C) {
+    // X[k] = (Z[k] + Z*[n-k]) / 2 - (i/2) w^k (Z[k] - Z*[n-k]),  k = 0..n
+    const int cnt = (n + 1) * B;
+    for (int idx = threadIdx.x; idx < cnt; idx += blockDim.x) {
+      int k, l;
+      if (args.e_fast_store) { k = idx % (n + 1); l = idx / (n + 1); } else { l = idx % B; k = idx / B; }
+      C zk = res[(k == n ? 0 : k) * ldb + l];
+      C zm = res[(k == 0 ? 0 : n - k) * ldb + l];
+      C sum = zk + conjc(zm), dif = zk - conjc(zm);
+      C w = __ldg(&args.tw2[k == n ? 0 : k]);
+      if (k == n) { w.x = (T) -1; w.y = (T) 0; }
+      C t = cmul(dif, w);
+      C x; x.x = (T) 0.5 * (sum.x + t.y); x.y = (T) 0.5 * (sum.y - t.x);   // (sum - i t)/2
+      st(a, b0 + l, k, x);
+    }
+  } else {
+    for (int idx = threadIdx.x; idx < n * B; idx += blockDim.x) {
+      int e, l;
+      if (args.e_fast_store) { e = idx % n; l = idx / n; } else { l = idx % B; e = idx / B; }
+      st(a, b0 + l, e, res[e * ldb + l]);
+    }
+  }
+}
+
+// ------------------------------------------------------------ x-pencil convolution
+// Kernel spectra are stored for the non-negative octant only, in layout
+// [kz][kx][ky] with extents (nz/2+1, nx/2+1, ny/2+1), already multiplied by the
+// centring phase (-1)^(kx+ky+kz) and the convolution normalisation step^3/N.
+enum { KER_EVEN = 0, KER_ODD_X = 1, KER_ODD_Y = 2, KER_ODD_Z = 3, KER_UNIT = 4 };
+
+constexpr int XC_MAX_IN = 4;
+constexpr int XC_MAX_OUT = 8;
+constexpr int XC_MAX_TERMS = 16;
+
+template <typename T> struct XTerm {
+  const T *ker;   // octant spectrum (real part for KER_EVEN, imaginary part for KER_ODD_*)
+  int kind;
+  int in;         // input index
+  T coef;
+};
+
+template <typename T> struct XOut {
+  typename cplx_t<T>::type *dst;   // spectral buffer [kz][x][y]
+  int t0, nt;                      // terms [t0, t0+nt)
+  int accumulate;                  // 1: dst += result
+};
+
+template <typename T> struct XConvArgs {
+  FftPlan<T> plan;                 // length nx
+  int B, nx, ny, nkz;              // tile width, grid dims, number of kz planes
+  int kxh, kyh;                    // octant extents nx/2+1, ny/2+1
+  int nin, nout;
+  const typename cplx_t<T>::type *src[XC_MAX_IN];
+  XOut<T> out[XC_MAX_OUT];
+  XTerm<T> term[XC_MAX_TERMS];
+};
+
+template <typename T>
+__device__ __forceinline__ typename cplx_t<T>::type apply_kernel(const XTerm<T> &t, typename cplx_t<T>::type v,
+                                                                 int kx, int ky, int kz, const XConvArgs<T> &A) {
+  typedef typename cplx_t<T>::type C;
+  if (t.kind == KER_UNIT) return v * t.coef;
+  const int ix = kx <= A.nx / 2 ? kx : A.nx - kx;
+  const int iy = ky <= A.ny / 2 ? ky : A.ny - ky;
+  const T kv = __ldg(&t.ker[((size_t) kz * A.kxh + ix) * A.kyh + iy]) * t.coef;
+  if (t.kind == KER_EVEN) return v * kv;
+  T sgn = (T) 1;
+  if (t.kind == KER_ODD_X && kx > A.nx / 2) sgn = (T) -1;
+  if (t.kind == KER_ODD_Y && ky > A.ny / 2) sgn = (T) -1;
+  C r; r.x = -sgn * kv * v.y; r.y = sgn * kv * v.x;   // (i sgn kv) v
+  return r;
+}
+
+// grid (ny / B, nkz); one CTA = B consecutive y pencils of one kz plane.
+template <typename T>
+__global__ void __launch_bounds__(FFT_THREADS) xconv_kernel(const XConvArgs<T> A) {
+  typedef typename cplx_t<T>::type C;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int n = A.plan.n, B = A.B, ldb = B + 1, tile = n * ldb;
+  C *bufs = reinterpret_cast<C *>(smem_raw);
+  C *scr0 = bufs + A.nin * tile, *scr1 = scr0 + tile;
+  const int kz = blockIdx.y, y0 = blockIdx.x * B;
+  const size_t plane = (size_t) A.nx * A.ny;
+
+  for (int in = 0; in < A.nin; in++) {
+    const C *src = A.src[in] + kz * plane + y0;
+    for (int idx = threadIdx.x; idx < n * B; idx += blockDim.x) {
+      const int l = idx % B, e = idx / B;
+      scr0[e * ldb + l] = src[(size_t) e * A.ny + l];
+    }
+    __syncthreads();
+    C *r = tile_fft<T>(scr0, scr1, A.plan, B, ldb, (T) -1);
+    C *dst = bufs + in * tile;
+    for (int idx = threadIdx.x; idx < tile; idx += blockDim.x) dst[idx] = r[idx];
+    __syncthreads();
+  }
+
+  for (int o = 0; o < A.nout; o++) {
+    const XOut<T> &out = A.out[o];
+    for (int idx = threadIdx.x; idx < n * B; idx += blockDim.x) {
+      const int l = idx % B, e = idx / B;
+      C acc = mk<T>((T) 0, (T) 0);
+      for (int t = out.t0; t < out.t0 + out.nt; t++) {
+        const XTerm<T> &tm = A.term[t];
+        acc = acc + apply_kernel<T>(tm, bufs[tm.in * tile + e * ldb + l], e, y0 + l, kz, A);
+      }
+      scr0[e * ldb + l] = acc;
+    }
+    __syncthreads();
+    C *r = tile_fft<T>(scr0, scr1, A.plan, B, ldb, (T) 1);
+    C *dst = out.dst + kz * plane + y0;
+    for (int idx = threadIdx.x; idx < n * B; idx += blockDim.x) {
+      const int l = idx % B, e = idx / B;
+      C v = r[e * ldb + l];
+      if (out.accumulate) v = v + dst[(size_t) e * A.ny + l];
+      dst[(size_t) e * A.ny + l] = v;
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------ kinetic x pass
+// psi(k) *= exp(-i hbar k^2 dt / 2m) / N in the middle of an x-pencil FFT pair.
+template <typename T> struct KinArgs {
+  FftPlan<T> plan;
+  int B, nx, ny, nz;
+  double2 cdt;          // -i dt / (2 m) * (2 pi)^2 folded: factor = exp(cdt * kk)
+  double inv_n;
+  double dkx, dky, dkz; // 2 pi / (n step)
+  typename cplx_t<T>::type *data;
+};
+
+__device__ __forceinline__ double kfreq(int i, int n, double dk) {
+  return (double) (i < (n + 1) / 2 ? i : i - n) * dk;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(FFT_THREADS) xkinetic_kernel(const KinArgs<T> A) {
+  typedef typename cplx_t<T>::type C;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int n = A.plan.n, B = A.B, ldb = B + 1, tile = n * ldb;
+  C *s0 = reinterpret_cast<C *>(smem_raw), *s1 = s0 + tile;
+  const int kz = blockIdx.y, y0 = blockIdx.x * B;
+  const size_t plane = (size_t) A.nx * A.ny;
+  C *base = A.data + kz * plane + y0;
+  for (int idx = threadIdx.x; idx < n * B; idx += blockDim.x) {
+    const int l = idx % B, e = idx / B;
+    s0[e * ldb + l] = base[(size_t) e * A.ny + l];
+  }
+  __syncthreads();
+  C *r = tile_fft<T>(s0, s1, A.plan, B, ldb, (T) -1);
+  const double kzv = kfreq(kz, A.nz, A.dkz);
+  for (int idx = threadIdx.x; idx < n * B; idx += blockDim.x) {
+    const int l = idx % B, e = idx / B;
+    const double kxv = kfreq(e, A.nx, A.dkx), kyv = kfreq(y0 + l, A.ny, A.dky);
+    const double k2 = kxv * kxv + kyv * kyv + kzv * kzv;
+    C f;
+    if (sizeof(T) == 4) {
+      float2 z = make_float2((float) (A.cdt.x * k2), (float) (A.cdt.y * k2));
+      float2 ex = cexp_dev(z);
+      f.x = (T) (ex.x * A.inv_n); f.y = (T) (ex.y * A.inv_n);
+    } else {
+      double2 ex = cexp_dev(make_double2(A.cdt.x * k2, A.cdt.y * k2));
+      f.x = (T) (ex.x * A.inv_n); f.y = (T) (ex.y * A.inv_n);
+    }
+    r[e * ldb + l] = cmul(r[e * ldb + l], f);
+  }
+  __syncthreads();
+  C *other = (r == s0) ? s1 : s0;
+  C *r2 = tile_fft<T>(r, other, A.plan, B, ldb, (T) 1);
+  for (int idx = threadIdx.x; idx < n * B; idx += blockDim.x) {
+    const int l = idx % B, e = idx / B;
+    base[(size_t) e * A.ny + l] = r2[e * ldb + l];
+  }
+}
+
+// ------------------------------------------------------------ launch helpers
+int choose_tile(int n, int nb, size_t cplx_bytes, int nbufs, int *B, size_t *smem);
+
+template <typename T, int MODE, class Ld, class St>
+int launch_lines(int n_fft, int na, int nb, T sign, int e_fast, int e_fast_store, const Ld &ld, const St &st) {
+  typedef typename cplx_t<T>::type C;
+  LineArgs<T> args;
+  DFT_TRY(get_plan<T>(n_fft, &args.plan));
+  args.sign = sign;
+  args.nb = nb;
+  args.e_fast = e_fast;
+  args.e_fast_store = e_fast_store;
+  args.tw2 = nullptr;
+  if (MODE != LINE_C2C) {
+    FftPlan<T> p2;
+    DFT_TRY(get_plan<T>(2 * n_fft, &p2));
+    args.tw2 = p2.tw;
+  }
+  int B; size_t smem;
+  DFT_TRY(choose_tile(n_fft + 1, nb, sizeof(C), 2, &B, &smem));
+  args.B = B;
+  auto kfn = line_fft_kernel<T, MODE, Ld, St>;
+  static thread_local bool attr_done = false;  // per instantiation
+  if (!attr_done) {
+    DFT_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+    attr_done = true;
+  }
+  dim3 grid(nb / B, na);
+  kfn<<<grid, FFT_THREADS, smem, rt().stream>>>(args, ld, st);
+  DFT_CHECK_LAUNCH();
+  return DFTGPU_OK;
+}
+
+template <typename T> int launch_xconv(XConvArgs<T> &A);
+template <typename T> int launch_xkinetic(KinArgs<T> &A);
+
+}  // namespace dftgpu

@@ -1,0 +1,423 @@
+// Runtime control, grid objects, elementwise operations, FP64 reductions and
+// the split-operator wave-function propagator.
+//
+// The libgrid functions restated here have no source in the reference tree;
+// their meaning follows their libdft call sites (cited per entry point in
+// include/dftgpu.h) and the conventions below:
+//   x_i = (i - nx/2) step - x0;  k_i = 2 pi (i or i - n) / (n step)
+//   S(V, dt) = exp(-i V dt/2) F^-1 exp(-i hbar k^2 dt / 2m) F exp(-i V dt/2)
+//   v = (hbar/m) Im(psi^* D psi) / max(|psi|^2, eps), D = central difference.
+#include <math.h>
+#include <stdarg.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <vector>
+
+#include "ops.cuh"
+#include "grid_internal.cuh"
+
+namespace dftgpu {
+
+thread_local int g_last_error = 0;
+static thread_local char g_last_msg[512] = "";
+
+void set_error(int code, const char *fmt, ...) {
+  g_last_error = code;
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_last_msg, sizeof(g_last_msg), fmt, ap);
+  va_end(ap);
+  if (getenv("DFTGPU_VERBOSE")) fprintf(stderr, "libdftgpu: error %d: %s\n", code, g_last_msg);
+}
+
+}  // namespace dftgpu
+
+extern "C" const char *dftgpu_last_error_message(void) { return dftgpu::g_last_msg; }
+
+namespace dftgpu {
+
+Runtime &rt() {
+  static Runtime r;
+  return r;
+}
+
+int ensure_device() {
+  Runtime &R = rt();
+  if (R.device >= 0) return DFTGPU_OK;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    set_error(DFTGPU_ERR_NODEVICE, "no CUDA device available");
+    return DFTGPU_ERR_NODEVICE;
+  }
+  DFT_CUDA(cudaSetDevice(0));
+  R.device = 0;
+  cudaDeviceProp p;
+  DFT_CUDA(cudaGetDeviceProperties(&p, 0));
+  R.num_sms = p.multiProcessorCount;
+  R.max_smem_optin = p.sharedMemPerBlockOptin;
+  return DFTGPU_OK;
+}
+
+static double *g_slots = nullptr;
+static double *g_partials = nullptr;
+
+double *reduce_slots() {
+  if (!g_slots) {
+    if (cudaMalloc(&g_slots, 64 * sizeof(double)) != cudaSuccess) return nullptr;
+    cudaMemset(g_slots, 0, 64 * sizeof(double));
+  }
+  return g_slots;
+}
+
+int reduce_partials(double **buf, size_t *n) {
+  if (!g_partials) DFT_CUDA(cudaMalloc(&g_partials, 8 * RED_BLOCKS * sizeof(double)));
+  if (!reduce_slots()) { set_error(DFTGPU_ERR_NOMEM, "reduction slots"); return DFTGPU_ERR_NOMEM; }
+  *buf = g_partials;
+  *n = 8 * RED_BLOCKS;
+  return DFTGPU_OK;
+}
+
+// ------------------------------------------------------------------ buffers
+void *dev_alloc(size_t bytes) {
+  void *p = nullptr;
+  if (ensure_device() != DFTGPU_OK) return nullptr;
+  if (cudaMalloc(&p, bytes ? bytes : 16) != cudaSuccess) {
+    cudaGetLastError();
+    set_error(DFTGPU_ERR_NOMEM, "cudaMalloc(%zu) failed", bytes);
+    return nullptr;
+  }
+  return p;
+}
+
+void dev_free(void *p) { if (p) cudaFree(p); }
+
+int check_dims(INT nx, INT ny, INT nz) {
+  INT d[3] = { nx, ny, nz };
+  for (int i = 0; i < 3; i++) {
+    INT m = d[i];
+    if (m < 2 || m > FFT_MAX_N || (m & 1)) {
+      set_error(DFTGPU_ERR_SIZE, "grid dimension %ld must be even and in [2, %d]", (long) m, FFT_MAX_N);
+      return DFTGPU_ERR_SIZE;
+    }
+    while (m % 2 == 0) m /= 2;
+    while (m % 3 == 0) m /= 3;
+    while (m % 5 == 0) m /= 5;
+    if (m != 1) {
+      set_error(DFTGPU_ERR_SIZE, "grid dimension %ld is not of the form 2^a 3^b 5^c", (long) d[i]);
+      return DFTGPU_ERR_SIZE;
+    }
+  }
+  return DFTGPU_OK;
+}
+
+// ------------------------------------------------------------------ elementwise
+template <typename T> int k_fill(T *p, size_t n, T v) {
+  return launch_each(n, [=] __device__(size_t i) { p[i] = v; });
+}
+template <typename T> int k_axpb(T *p, size_t n, T a, T b) {   // p = a p + b
+  return launch_each(n, [=] __device__(size_t i) { p[i] = a * p[i] + b; });
+}
+
+// ------------------------------------------------------------------ propagation
+template <typename T> struct PhaseLoad {   // psi * exp(-i V dt / 2)
+  typedef typename cplx_t<T>::type C;
+  const C *psi; const C *V; int ny, nz; T hr, hi;   // (hr, hi) = dt / 2
+  __device__ C operator()(int x, int y, int e) const {
+    const size_t i = ((size_t) x * ny + y) * nz + e;
+    C v = V[i];
+    // -i V dt/2 = (Im(V dt/2), -Re(V dt/2))
+    C z = mk<T>(v.x * hi + v.y * hr, -(v.x * hr - v.y * hi));
+    return cmul(psi[i], cexp_dev(z));
+  }
+};
+template <typename T> struct PhaseStore {
+  typedef typename cplx_t<T>::type C;
+  C *psi; const C *V; int ny, nz; T hr, hi;
+  __device__ void operator()(int x, int y, int e, C val) const {
+    const size_t i = ((size_t) x * ny + y) * nz + e;
+    C v = V[i];
+    C z = mk<T>(v.x * hi + v.y * hr, -(v.x * hr - v.y * hi));
+    psi[i] = cmul(val, cexp_dev(z));
+  }
+};
+
+// dst = S(V, dt) src, through the wave function's spectral scratch buffer
+template <typename T> int strang(wf *g, cgrid *dst, cgrid *src, cgrid *V, double dr, double di) {
+  typedef typename cplx_t<T>::type C;
+  const int nx = (int) src->nx, ny = (int) src->ny, nz = (int) src->nz;
+  C *spec = (C *) wf_spec(g);
+  if (!spec) return DFTGPU_ERR_NOMEM;
+  const T hr = (T) (0.5 * dr), hi = (T) (0.5 * di);
+  PhaseLoad<T> ld{(const C *) src->value, (const C *) V->value, ny, nz, hr, hi};
+  SpecStoreZ<T> sz{spec, nx, ny};
+  DFT_TRY((launch_lines<T, LINE_C2C>(nz, nx, ny, (T) -1, 1, 0, ld, sz)));
+  DFT_TRY(ypass<T>(spec, nx, ny, nz, (T) -1));
+  KinArgs<T> K;
+  K.nx = nx; K.ny = ny; K.nz = nz;
+  K.data = spec;
+  const double m = g->mass;
+  K.cdt = make_double2(di / (2.0 * m), -dr / (2.0 * m));   // -i dt / 2m
+  K.inv_n = 1.0 / ((double) nx * ny * nz);
+  K.dkx = 2.0 * M_PI / (nx * src->step);
+  K.dky = 2.0 * M_PI / (ny * src->step);
+  K.dkz = 2.0 * M_PI / (nz * src->step);
+  DFT_TRY(launch_xkinetic<T>(K));
+  DFT_TRY(ypass<T>(spec, nx, ny, nz, (T) 1));
+  SpecLoadZ<T> lz{spec, nx, ny};
+  PhaseStore<T> st{(C *) dst->value, (const C *) V->value, ny, nz, hr, hi};
+  return launch_lines<T, LINE_C2C>(nz, nx, ny, (T) 1, 0, 1, lz, st);
+}
+
+int propagate(wf *g, cgrid *dst, cgrid *src, cgrid *V, double dr, double di) {
+  if (!g || !dst || !src || !V) { set_error(DFTGPU_ERR_ARG, "propagate: NULL argument"); return DFTGPU_ERR_ARG; }
+  if (V->prec != src->prec || dst->prec != src->prec || V->nx != src->nx || V->ny != src->ny || V->nz != src->nz) {
+    set_error(DFTGPU_ERR_ARG, "propagate: potential / wave function mismatch");
+    return DFTGPU_ERR_ARG;
+  }
+  return src->prec == DFTGPU_FP32 ? strang<float>(g, dst, src, V, dr, di) : strang<double>(g, dst, src, V, dr, di);
+}
+
+// ------------------------------------------------------------------ spectra of psi
+template <typename T> int cfft3_forward(cgrid *src, typename cplx_t<T>::type *spec) {
+  const int nx = (int) src->nx, ny = (int) src->ny, nz = (int) src->nz;
+  CplxLoad<T> ld{(const typename cplx_t<T>::type *) src->value, ny, nz};
+  SpecStoreZ<T> sz{spec, nx, ny};
+  DFT_TRY((launch_lines<T, LINE_C2C>(nz, nx, ny, (T) -1, 1, 0, ld, sz)));
+  DFT_TRY(ypass<T>(spec, nx, ny, nz, (T) -1));
+  SpecLineXT<T> io{spec, nx, ny};
+  return launch_lines<T, LINE_C2C>(nx, nz, ny, (T) -1, 0, 0, io, io);
+}
+
+template <typename T> int kinetic_energy_t(wf *g, double *out) {
+  typedef typename cplx_t<T>::type C;
+  cgrid *c = g->grid;
+  C *spec = (C *) wf_spec(g);
+  if (!spec) return DFTGPU_ERR_NOMEM;
+  DFT_TRY(cfft3_forward<T>(c, spec));
+  const int nx = (int) c->nx, ny = (int) c->ny, nz = (int) c->nz;
+  const double dkx = 2.0 * M_PI / (nx * c->step), dky = 2.0 * M_PI / (ny * c->step), dkz = 2.0 * M_PI / (nz * c->step);
+  const double dv = c->step * c->step * c->step;
+  const double scale = 1.0 / (2.0 * g->mass) * dv / ((double) nx * ny * nz);
+  const size_t n = (size_t) nx * ny * nz;
+  // spectral layout [kz][kx][ky]
+  return reduce_host<1>(n, [=] __device__(size_t i, double *v) {
+    const int ky = (int) (i % ny), kx = (int) ((i / ny) % nx), kz = (int) (i / ((size_t) nx * ny));
+    const double a = kfreq(kx, nx, dkx), b = kfreq(ky, ny, dky), cc = kfreq(kz, nz, dkz);
+    const C s = spec[i];
+    v[0] = (a * a + b * b + cc * cc) * ((double) s.x * s.x + (double) s.y * s.y);
+  }, out, scale);
+}
+
+int kinetic_energy(wf *g, double *out) {
+  return g->grid->prec == DFTGPU_FP32 ? kinetic_energy_t<float>(g, out) : kinetic_energy_t<double>(g, out);
+}
+
+template <typename T> int norm_dev_t(cgrid *c, double *slot) {
+  typedef typename cplx_t<T>::type C;
+  const C *p = (const C *) c->value;
+  const double dv = c->step * c->step * c->step;
+  return reduce_dev<1>(gsize(c), [=] __device__(size_t i, double *v) {
+    const C z = p[i];
+    v[0] = (double) z.x * z.x + (double) z.y * z.y;
+  }, slot, dv);
+}
+
+int norm_dev(cgrid *c, double *slot) {
+  return c->prec == DFTGPU_FP32 ? norm_dev_t<float>(c, slot) : norm_dev_t<double>(c, slot);
+}
+
+// psi *= sqrt(target / norm) with norm read from the device slot
+template <typename T> int scale_by_norm_t(cgrid *c, const double *slot, double target) {
+  typedef typename cplx_t<T>::type C;
+  C *p = (C *) c->value;
+  return launch_each(gsize(c), [=] __device__(size_t i) {
+    const T f = (T) sqrt(target / slot[0]);
+    C z = p[i];
+    z.x *= f; z.y *= f;
+    p[i] = z;
+  });
+}
+
+int scale_by_norm(cgrid *c, const double *slot, double target) {
+  return c->prec == DFTGPU_FP32 ? scale_by_norm_t<float>(c, slot, target) : scale_by_norm_t<double>(c, slot, target);
+}
+
+template <typename T> int velocity_t(wf *g, rgrid *vx, rgrid *vy, rgrid *vz, double eps) {
+  typedef typename cplx_t<T>::type C;
+  cgrid *c = g->grid;
+  const C *p = (const C *) c->value;
+  T *out[3] = { (T *) vx->value, (T *) vy->value, (T *) vz->value };
+  T *ox = out[0], *oy = out[1], *oz = out[2];
+  const int nx = (int) c->nx, ny = (int) c->ny, nz = (int) c->nz;
+  const double f = 1.0 / (g->mass * 2.0 * c->step);
+  return launch_each(gsize(c), [=] __device__(size_t i) {
+    const int k = (int) (i % nz), j = (int) ((i / nz) % ny), x = (int) (i / ((size_t) ny * nz));
+    const C z = p[i];
+    double rho = (double) z.x * z.x + (double) z.y * z.y;
+    if (rho < eps) rho = eps;
+    const double g0 = f / rho;
+    const size_t ixp = ((size_t) ((x + 1) % nx) * ny + j) * nz + k, ixm = ((size_t) ((x - 1 + nx) % nx) * ny + j) * nz + k;
+    const size_t iyp = ((size_t) x * ny + (j + 1) % ny) * nz + k, iym = ((size_t) x * ny + (j - 1 + ny) % ny) * nz + k;
+    const size_t izp = ((size_t) x * ny + j) * nz + (k + 1) % nz, izm = ((size_t) x * ny + j) * nz + (k - 1 + nz) % nz;
+    C d;
+    d = p[ixp] - p[ixm]; ox[i] = (T) (g0 * ((double) z.x * d.y - (double) z.y * d.x));
+    d = p[iyp] - p[iym]; oy[i] = (T) (g0 * ((double) z.x * d.y - (double) z.y * d.x));
+    d = p[izp] - p[izm]; oz[i] = (T) (g0 * ((double) z.x * d.y - (double) z.y * d.x));
+  });
+}
+
+// forward r2c of a real grid to the host, in the oracle's [x][y][kz] order
+template <typename T> static int rspectrum_t(rgrid *g, double *host) {
+  typedef typename cplx_t<T>::type C;
+  const int nx = (int) g->nx, ny = (int) g->ny, nz = (int) g->nz, nzh = nz / 2 + 1;
+  const size_t ns = (size_t) nzh * nx * ny;
+  C *spec = (C *) dev_alloc(ns * sizeof(C));
+  if (!spec) return DFTGPU_ERR_NOMEM;
+  RealPairLoad<T> ld{(const T *) g->value, ny, nz};
+  int rc = rfft_zy<T>(ld, spec, nx, ny, nz);
+  SpecLineXT<T> io{spec, nx, ny};
+  if (!rc) rc = launch_lines<T, LINE_C2C>(nx, nzh, ny, (T) -1, 0, 0, io, io);
+  std::vector<C> h(ns);
+  if (!rc && (cudaMemcpyAsync(h.data(), spec, ns * sizeof(C), cudaMemcpyDeviceToHost, rt().stream) != cudaSuccess ||
+              cudaStreamSynchronize(rt().stream) != cudaSuccess)) rc = DFTGPU_ERR_CUDA;
+  dev_free(spec);
+  if (rc) return rc;
+  for (int kz = 0; kz < nzh; kz++)
+    for (int x = 0; x < nx; x++)
+      for (int y = 0; y < ny; y++) {
+        const C v = h[((size_t) kz * nx + x) * ny + y];
+        const size_t o = ((size_t) x * ny + y) * nzh + kz;
+        host[2 * o] = v.x; host[2 * o + 1] = v.y;
+      }
+  return DFTGPU_OK;
+}
+
+int rspectrum(rgrid *g, double *host) {
+  return g->prec == DFTGPU_FP32 ? rspectrum_t<float>(g, host) : rspectrum_t<double>(g, host);
+}
+
+int velocity(wf *g, rgrid *vx, rgrid *vy, rgrid *vz, double eps) {
+  return g->grid->prec == DFTGPU_FP32 ? velocity_t<float>(g, vx, vy, vz, eps) : velocity_t<double>(g, vx, vy, vz, eps);
+}
+
+// ------------------------------------------------------------------ host copies
+template <typename T> static int copy_out(const void *dev, double *host, size_t n) {
+  if (sizeof(T) == 8) { DFT_CUDA(cudaMemcpyAsync(host, dev, n * 8, cudaMemcpyDeviceToHost, rt().stream)); }
+  else {
+    std::vector<float> tmp(n);
+    DFT_CUDA(cudaMemcpyAsync(tmp.data(), dev, n * 4, cudaMemcpyDeviceToHost, rt().stream));
+    DFT_CUDA(cudaStreamSynchronize(rt().stream));
+    for (size_t i = 0; i < n; i++) host[i] = tmp[i];
+  }
+  DFT_CUDA(cudaStreamSynchronize(rt().stream));
+  return DFTGPU_OK;
+}
+
+template <typename T> static int copy_in(void *dev, const double *host, size_t n) {
+  if (sizeof(T) == 8) { DFT_CUDA(cudaMemcpyAsync(dev, host, n * 8, cudaMemcpyHostToDevice, rt().stream)); }
+  else {
+    std::vector<float> tmp(n);
+    for (size_t i = 0; i < n; i++) tmp[i] = (float) host[i];
+    DFT_CUDA(cudaMemcpyAsync(dev, tmp.data(), n * 4, cudaMemcpyHostToDevice, rt().stream));
+  }
+  DFT_CUDA(cudaStreamSynchronize(rt().stream));
+  return DFTGPU_OK;
+}
+
+int copy_values_out(int prec, const void *dev, double *host, size_t n) {
+  return prec == DFTGPU_FP32 ? copy_out<float>(dev, host, n) : copy_out<double>(dev, host, n);
+}
+int copy_values_in(int prec, void *dev, const double *host, size_t n) {
+  return prec == DFTGPU_FP32 ? copy_in<float>(dev, host, n) : copy_in<double>(dev, host, n);
+}
+
+// ------------------------------------------------------------------ generic real ops
+int rfill(rgrid *g, double v) {
+  return g->prec == DFTGPU_FP32 ? k_fill<float>((float *) g->value, gsize(g), (float) v) : k_fill<double>((double *) g->value, gsize(g), v);
+}
+int raxpb(rgrid *g, double a, double b) {
+  return g->prec == DFTGPU_FP32 ? k_axpb<float>((float *) g->value, gsize(g), (float) a, (float) b)
+                                : k_axpb<double>((double *) g->value, gsize(g), a, b);
+}
+int cfill(cgrid *g, double re, double im) {
+  if (g->prec == DFTGPU_FP32) { float2 v = make_float2((float) re, (float) im); float2 *p = (float2 *) g->value;
+    return launch_each(gsize(g), [=] __device__(size_t i) { p[i] = v; }); }
+  double2 v = make_double2(re, im); double2 *p = (double2 *) g->value;
+  return launch_each(gsize(g), [=] __device__(size_t i) { p[i] = v; });
+}
+template <typename T> static int cmuladd_t(cgrid *g, double mr, double mi, double ar, double ai) {
+  typedef typename cplx_t<T>::type C;
+  C *p = (C *) g->value;
+  const C m = mk<T>((T) mr, (T) mi), a = mk<T>((T) ar, (T) ai);
+  return launch_each(gsize(g), [=] __device__(size_t i) { p[i] = cmul(p[i], m) + a; });
+}
+int cmuladd(cgrid *g, double mr, double mi, double ar, double ai) {
+  return g->prec == DFTGPU_FP32 ? cmuladd_t<float>(g, mr, mi, ar, ai) : cmuladd_t<double>(g, mr, mi, ar, ai);
+}
+
+// mode 0: dst.re = src (im = 0); 1: dst.re += src; 2: dst.im += src
+template <typename T> static int r2c_t(cgrid *d, rgrid *s, int mode) {
+  typedef typename cplx_t<T>::type C;
+  C *p = (C *) d->value;
+  const T *q = (const T *) s->value;
+  return launch_each(gsize(d), [=] __device__(size_t i) {
+    C v = p[i];
+    if (mode == 0) { v.x = q[i]; v.y = (T) 0; }
+    else if (mode == 1) v.x += q[i];
+    else v.y += q[i];
+    p[i] = v;
+  });
+}
+int real_to_complex(cgrid *d, rgrid *s, int mode) {
+  return d->prec == DFTGPU_FP32 ? r2c_t<float>(d, s, mode) : r2c_t<double>(d, s, mode);
+}
+
+// op 0: d = a + b; 1: d = a * b; 2: d += c a; 3: d += c a b
+template <typename T> static int rbin_t(rgrid *d, rgrid *a, rgrid *b, double c, int op) {
+  T *pd = (T *) d->value;
+  const T *pa = (const T *) a->value, *pb = b ? (const T *) b->value : nullptr;
+  const T cc = (T) c;
+  return launch_each(gsize(d), [=] __device__(size_t i) {
+    if (op == 0) pd[i] = pa[i] + pb[i];
+    else if (op == 1) pd[i] = pa[i] * pb[i];
+    else if (op == 2) pd[i] += cc * pa[i];
+    else pd[i] += cc * pa[i] * pb[i];
+  });
+}
+int rbinary(rgrid *d, rgrid *a, rgrid *b, double c, int op) {
+  return d->prec == DFTGPU_FP32 ? rbin_t<float>(d, a, b, c, op) : rbin_t<double>(d, a, b, c, op);
+}
+
+template <typename T> static int rsum_t(rgrid *g, double *out) {
+  const T *p = (const T *) g->value;
+  const double dv = g->step * g->step * g->step;
+  return reduce_host<1>(gsize(g), [=] __device__(size_t i, double *v) { v[0] = (double) p[i]; }, out, dv);
+}
+int rintegral(rgrid *g, double *out) {
+  return g->prec == DFTGPU_FP32 ? rsum_t<float>(g, out) : rsum_t<double>(g, out);
+}
+
+template <typename T> static int density_t(cgrid *c, rgrid *d) {
+  typedef typename cplx_t<T>::type C;
+  const C *p = (const C *) c->value;
+  T *q = (T *) d->value;
+  return launch_each(gsize(c), [=] __device__(size_t i) { const C z = p[i]; q[i] = z.x * z.x + z.y * z.y; });
+}
+int density(cgrid *c, rgrid *d) {
+  return c->prec == DFTGPU_FP32 ? density_t<float>(c, d) : density_t<double>(c, d);
+}
+
+template <typename T> static int rho_dot_re_t(rgrid *r, cgrid *P, double *out) {
+  typedef typename cplx_t<T>::type C;
+  const T *a = (const T *) r->value;
+  const C *b = (const C *) P->value;
+  const double dv = r->step * r->step * r->step;
+  return reduce_host<1>(gsize(r), [=] __device__(size_t i, double *v) { v[0] = (double) a[i] * (double) b[i].x; }, out, dv);
+}
+int rho_dot_re(rgrid *r, cgrid *P, double *out) {
+  return r->prec == DFTGPU_FP32 ? rho_dot_re_t<float>(r, P, out) : rho_dot_re_t<double>(r, P, out);
+}
+
+}  // namespace dftgpu

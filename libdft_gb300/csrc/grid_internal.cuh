@@ -1,0 +1,54 @@
+// Internal grid helpers shared by grid.cu, ot.cu and api.cu.
+#pragma once
+
+#include "common.cuh"
+
+namespace dftgpu {
+
+inline size_t gsize(const rgrid *g) { return (size_t) g->nx * g->ny * g->nz; }
+inline size_t gsize(const cgrid *g) { return (size_t) g->nx * g->ny * g->nz; }
+
+struct WfPriv {
+  void *spec = nullptr;        // nx*ny*nz complex spectral scratch
+};
+
+void *dev_alloc(size_t bytes);
+void dev_free(void *p);
+int check_dims(INT nx, INT ny, INT nz);
+
+inline void *wf_spec(wf *g) {
+  WfPriv *p = (WfPriv *) g->priv;
+  if (!p->spec) p->spec = dev_alloc(gsize(g->grid) * 2 * elem_size(g->grid->prec));
+  return p->spec;
+}
+
+// x pencils of a spectral buffer [kz][x][y] as plain lines: line (kz, y), element x
+template <typename T> struct SpecLineXT {
+  typename cplx_t<T>::type *spec; int nx, ny;
+  __device__ typename cplx_t<T>::type operator()(int kz, int y, int x) const {
+    return spec[((size_t) kz * nx + x) * ny + y];
+  }
+  __device__ void operator()(int kz, int y, int x, typename cplx_t<T>::type v) const {
+    spec[((size_t) kz * nx + x) * ny + y] = v;
+  }
+};
+
+int propagate(wf *g, cgrid *dst, cgrid *src, cgrid *V, double dr, double di);
+int kinetic_energy(wf *g, double *out);
+int norm_dev(cgrid *c, double *slot);
+int scale_by_norm(cgrid *c, const double *slot, double target);
+int velocity(wf *g, rgrid *vx, rgrid *vy, rgrid *vz, double eps);
+int copy_values_out(int prec, const void *dev, double *host, size_t n);
+int copy_values_in(int prec, void *dev, const double *host, size_t n);
+int rfill(rgrid *g, double v);
+int raxpb(rgrid *g, double a, double b);
+int cfill(cgrid *g, double re, double im);
+int cmuladd(cgrid *g, double mr, double mi, double ar, double ai);
+int real_to_complex(cgrid *d, rgrid *s, int mode);
+int rbinary(rgrid *d, rgrid *a, rgrid *b, double c, int op);
+int rintegral(rgrid *g, double *out);
+int density(cgrid *c, rgrid *d);
+int rspectrum(rgrid *g, double *host);
+int rho_dot_re(rgrid *rho, cgrid *P, double *out);   // sum rho Re(P) dV
+
+}  // namespace dftgpu

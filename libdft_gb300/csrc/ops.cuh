@@ -1,0 +1,158 @@
+// Elementwise launch, FP64 reductions and 3-D transform sequences shared by
+// the grid and OT translation units.
+#pragma once
+
+#include "fft.cuh"
+
+namespace dftgpu {
+
+// grid-stride elementwise launch of a device lambda f(i), i < n
+template <class F> __global__ void each_kernel(size_t n, F f) {
+  for (size_t i = (size_t) blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t) gridDim.x * blockDim.x) f(i);
+}
+
+template <class F> int launch_each(size_t n, F f) {
+  if (n == 0) return DFTGPU_OK;
+  int blocks = (int) ((n + 255) / 256);
+  int cap = rt().num_sms * 8;
+  if (blocks > cap) blocks = cap;
+  each_kernel<<<blocks, 256, 0, rt().stream>>>(n, f);
+  DFT_CHECK_LAUNCH();
+  return DFTGPU_OK;
+}
+
+// ---------------------------------------------------------------- reductions
+// Deterministic FP64 sum of f(i) over i < n: a fixed grid of RED_BLOCKS
+// blocks each sums a fixed strided subset, block partials are combined by a
+// single block in a fixed order.  Result left in *slot (device).
+constexpr int RED_BLOCKS = 1024;
+constexpr int RED_THREADS = 256;
+
+__device__ __forceinline__ double block_sum(double v) {
+  __shared__ double sh[RED_THREADS / 32];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    v = (l < (int) (blockDim.x >> 5)) ? sh[l] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  }
+  __syncthreads();
+  return v;
+}
+
+template <int NV, class F> __global__ void reduce_partial_kernel(size_t n, F f, double *partial) {
+  double acc[NV];
+#pragma unroll
+  for (int j = 0; j < NV; j++) acc[j] = 0.0;
+  for (size_t i = (size_t) blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t) gridDim.x * blockDim.x) {
+    double v[NV];
+    f(i, v);
+#pragma unroll
+    for (int j = 0; j < NV; j++) acc[j] += v[j];
+  }
+#pragma unroll
+  for (int j = 0; j < NV; j++) {
+    double s = block_sum(acc[j]);
+    if (threadIdx.x == 0) partial[j * RED_BLOCKS + blockIdx.x] = s;
+  }
+}
+
+template <int NV> __global__ void reduce_final_kernel(const double *partial, double *slot, double scale) {
+#pragma unroll
+  for (int j = 0; j < NV; j++) {
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < RED_BLOCKS; i += blockDim.x) acc += partial[j * RED_BLOCKS + i];
+    double s = block_sum(acc);
+    if (threadIdx.x == 0) slot[j] = s * scale;
+  }
+}
+
+// f(i, double v[NV]); results (times scale) to slot[0..NV) on the device.
+template <int NV, class F> int reduce_dev(size_t n, F f, double *slot, double scale) {
+  double *part; size_t np;
+  DFT_TRY(reduce_partials(&part, &np));
+  reduce_partial_kernel<NV><<<RED_BLOCKS, RED_THREADS, 0, rt().stream>>>(n, f, part);
+  DFT_CHECK_LAUNCH();
+  reduce_final_kernel<NV><<<1, RED_THREADS, 0, rt().stream>>>(part, slot, scale);
+  DFT_CHECK_LAUNCH();
+  return DFTGPU_OK;
+}
+
+// Same, result copied to the host (synchronises the stream).
+template <int NV, class F> int reduce_host(size_t n, F f, double *out, double scale) {
+  double *slot = reduce_slots();
+  DFT_TRY(reduce_dev<NV>(n, f, slot, scale));
+  DFT_CUDA(cudaMemcpyAsync(out, slot, sizeof(double) * NV, cudaMemcpyDeviceToHost, rt().stream));
+  DFT_CUDA(cudaStreamSynchronize(rt().stream));
+  return DFTGPU_OK;
+}
+
+// ---------------------------------------------------------------- functors
+// Spectral layout [kz][x][y]; real / complex grids [x][y][z].
+template <typename T> struct SpecStoreZ {           // z pass output
+  typename cplx_t<T>::type *spec; int nx, ny;
+  __device__ void operator()(int x, int y, int k, typename cplx_t<T>::type v) const {
+    spec[((size_t) k * nx + x) * ny + y] = v;
+  }
+};
+template <typename T> struct SpecLoadZ {            // z pass input (inverse)
+  const typename cplx_t<T>::type *spec; int nx, ny;
+  __device__ typename cplx_t<T>::type operator()(int x, int y, int k) const {
+    return spec[((size_t) k * nx + x) * ny + y];
+  }
+};
+template <typename T> struct SpecLineY {            // y pass in place: line (kz, x), element y
+  typename cplx_t<T>::type *spec; int nx, ny;
+  __device__ typename cplx_t<T>::type operator()(int kz, int x, int y) const {
+    return spec[((size_t) kz * nx + x) * ny + y];
+  }
+  __device__ void operator()(int kz, int x, int y, typename cplx_t<T>::type v) const {
+    spec[((size_t) kz * nx + x) * ny + y] = v;
+  }
+};
+template <typename T> struct RealPairLoad {         // packed (f[2e], f[2e+1]) of a real row
+  const T *f; int ny, nz;
+  __device__ typename cplx_t<T>::type operator()(int x, int y, int e) const {
+    const T *row = f + ((size_t) x * ny + y) * nz;
+    return mk<T>(row[2 * e], row[2 * e + 1]);
+  }
+};
+template <typename T> struct RealPairStore {        // real row <- scale * (re, im)
+  T *f; int ny, nz; T scale;
+  __device__ void operator()(int x, int y, int e, typename cplx_t<T>::type v) const {
+    T *row = f + ((size_t) x * ny + y) * nz;
+    row[2 * e] = v.x * scale;
+    row[2 * e + 1] = v.y * scale;
+  }
+};
+template <typename T> struct CplxLoad {
+  const typename cplx_t<T>::type *f; int ny, nz;
+  __device__ typename cplx_t<T>::type operator()(int x, int y, int e) const {
+    return f[((size_t) x * ny + y) * nz + e];
+  }
+};
+
+// y passes over nkz planes of a spectral buffer
+template <typename T> int ypass(typename cplx_t<T>::type *spec, int nx, int ny, int nkz, T sign) {
+  SpecLineY<T> io{spec, nx, ny};
+  return launch_lines<T, LINE_C2C>(ny, nkz, nx, sign, 1, 1, io, io);
+}
+
+// forward r2c of a real field through its z and y passes, with a custom
+// packed-pair loader (fused producer); spec is [nz/2+1][nx][ny]
+template <typename T, class Ld> int rfft_zy(const Ld &ld, typename cplx_t<T>::type *spec, int nx, int ny, int nz) {
+  SpecStoreZ<T> st{spec, nx, ny};
+  DFT_TRY((launch_lines<T, LINE_R2C>(nz / 2, nx, ny, (T) -1, 1, 0, ld, st)));
+  return ypass<T>(spec, nx, ny, nz / 2 + 1, (T) -1);
+}
+
+// inverse: y passes then c2r z pass into a custom consumer st(x, y, e, (v[2e], v[2e+1]))
+template <typename T, class St> int irfft_yz(typename cplx_t<T>::type *spec, const St &st, int nx, int ny, int nz) {
+  DFT_TRY(ypass<T>(spec, nx, ny, nz / 2 + 1, (T) 1));
+  SpecLoadZ<T> ld{spec, nx, ny};
+  return launch_lines<T, LINE_C2R>(nz / 2, nx, ny, (T) 1, 0, 1, ld, st);
+}
+
+}  // namespace dftgpu

@@ -1,0 +1,588 @@
+// Orsay-Trento functional on the GPU: kernel generation, potential and
+// energy density (libdft src/ot.c:66-991, src/ot-energy.c:38-288).
+//
+// Potential dataflow (full model), one forward r2c per produced field and
+// one inverse c2r per needed real field; linearity merges the reference's
+// per-axis KC transforms:
+//   rho = |psi|^2 ;  rho^ = F rho
+//   x pass 1 (one input, up to 7 outputs): V_LJ rho^, w rho^, F rho^,
+//             dF_a rho^ (a = x,y,z), V_j rho^
+//   pointwise 1: P.re += u_LJ + c2/2 rb^2 + c3/3 rb^3 ; q = (c2 rb + c3 rb^2) rho
+//             KC: rho_st, s_a = (d_a rho) rho_st ;  BF: v, rho|v|^2, rho v_a
+//   x pass 2: w q^ ; sum_a dF_a s_a^ ; F s_a^ (-> J_a) ; V_j (rho|v|^2)^, V_j (rho v_a)^
+//   pointwise 2: P.re += w*q + c rho_st sum_a(dF_a*s_a) - c sum_a J_a (dF_a*rho)
+//             KC: h = sum_a (d_a rho) J_a ;  BF real part, w_a = v_a A - B_a
+//   x pass 3 (KC): F h^ ;  pointwise 3: P.re += c F*h ; BF imaginary part.
+// KC count: 1 + 3 + 1 forward, 4 + 4 + 1 inverse instead of src/ot.c's 19.
+#include <math.h>
+#include <string.h>
+
+#include "ops.cuh"
+#include "grid_internal.cuh"
+#include "ot_internal.cuh"
+
+namespace dftgpu {
+
+// ------------------------------------------------------------------ shapes
+// (src/common.c:31-66, 131-138, 193-200; src/ot-private.h:10-21)
+struct ShapeLJ {
+  double h, sig, eps, cval;
+  __device__ double operator()(double x, double y, double z) const {
+    const double r2 = x * x + y * y + z * z;
+    if (r2 <= h * h) return cval;
+    const double s2 = sig * sig / r2, s6 = s2 * s2 * s2;
+    return 4.0 * eps * s6 * (s6 - 1.0);
+  }
+};
+struct ShapeSA {
+  double h;
+  __device__ double operator()(double x, double y, double z) const {
+    return (x * x + y * y + z * z <= h * h) ? 3.0 / (4.0 * M_PI * h * h * h) : 0.0;
+  }
+};
+struct ShapeGauss {
+  double iw;
+  __device__ double operator()(double x, double y, double z) const {
+    const double nrm = iw / sqrt(M_PI);
+    return nrm * nrm * nrm * exp(-(x * x + y * y + z * z) * iw * iw);
+  }
+};
+struct ShapeBF {
+  double g11, g12, g21, g22, a1, a2;
+  __device__ double operator()(double x, double y, double z) const {
+    const double r2 = x * x + y * y + z * z;
+    return (g11 + g12 * r2) * exp(-a1 * r2) + (g21 + g22 * r2) * exp(-a2 * r2);
+  }
+};
+
+template <class S>
+__device__ double cell_average(const S &f, double x, double y, double z, double step, int ns) {
+  double sum = 0.0;
+  const double h = step / (double) ns;
+  for (int a = 0; a < ns; a++) {
+    const double xs = x + ((double) a + 0.5) * h - 0.5 * step;
+    for (int b = 0; b < ns; b++) {
+      const double ys = y + ((double) b + 0.5) * h - 0.5 * step;
+      for (int c = 0; c < ns; c++) {
+        const double zs = z + ((double) c + 0.5) * h - 0.5 * step;
+        sum += f(xs, ys, zs);
+      }
+    }
+  }
+  return sum / (double) (ns * ns * ns);
+}
+
+// Cell averages over ns^3 sub-points, ns doubling from min_ns until two
+// successive averages differ by less than tol or ns would exceed max_ns.
+template <class S>
+__global__ void adaptive_map_kernel(double *out, int nx, int ny, int nz, double step, double x0, double y0,
+                                    double z0, int min_ns, int max_ns, double tol, S f) {
+  const size_t n = (size_t) nx * ny * nz;
+  for (size_t i = (size_t) blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t) gridDim.x * blockDim.x) {
+    const int k = (int) (i % nz), j = (int) ((i / nz) % ny), ii = (int) (i / ((size_t) ny * nz));
+    const double x = (double) (ii - nx / 2) * step - x0;
+    const double y = (double) (j - ny / 2) * step - y0;
+    const double z = (double) (k - nz / 2) * step - z0;
+    int ns = min_ns;
+    double v = cell_average(f, x, y, z, step, ns);
+    while (2 * ns <= max_ns) {
+      const double v2 = cell_average(f, x, y, z, step, 2 * ns);
+      ns *= 2;
+      const double d = v2 - v;
+      v = v2;
+      if (fabs(d) < tol) break;
+    }
+    out[i] = v;
+  }
+}
+
+template <class S> static int adaptive_map(double *out, const OtPriv *P, int min_ns, int max_ns, double tol, const S &f) {
+  const size_t n = (size_t) P->nx * P->ny * P->nz;
+  int blocks = (int) ((n + 127) / 128);
+  adaptive_map_kernel<S><<<blocks, 128, 0, rt().stream>>>(out, P->nx, P->ny, P->nz, P->step, P->x0, P->y0, P->z0,
+                                                          min_ns, max_ns, tol, f);
+  DFT_CHECK_LAUNCH();
+  return DFTGPU_OK;
+}
+
+// central difference along axis of an FP64 field, periodic
+static int fd_field(const double *src, double *dst, const OtPriv *P, int axis) {
+  const int nx = P->nx, ny = P->ny, nz = P->nz;
+  const double inv2h = 1.0 / (2.0 * P->step);
+  return launch_each((size_t) nx * ny * nz, [=] __device__(size_t i) {
+    const int k = (int) (i % nz), j = (int) ((i / nz) % ny), x = (int) (i / ((size_t) ny * nz));
+    size_t ip, im;
+    if (axis == 0) { ip = ((size_t) ((x + 1) % nx) * ny + j) * nz + k; im = ((size_t) ((x - 1 + nx) % nx) * ny + j) * nz + k; }
+    else if (axis == 1) { ip = ((size_t) x * ny + (j + 1) % ny) * nz + k; im = ((size_t) x * ny + (j - 1 + ny) % ny) * nz + k; }
+    else { ip = ((size_t) x * ny + j) * nz + (k + 1) % nz; im = ((size_t) x * ny + j) * nz + (k - 1 + nz) % nz; }
+    dst[i] = (src[ip] - src[im]) * inv2h;
+  });
+}
+
+// FP64 r2c of a real field into the half spectrum [kz][kx][ky]
+static int rfft3_fp64(const double *f, double2 *spec, const OtPriv *P) {
+  RealPairLoad<double> ld{f, P->ny, P->nz};
+  DFT_TRY((rfft_zy<double>(ld, spec, P->nx, P->ny, P->nz)));
+  SpecLineXT<double> io{spec, P->nx, P->ny};
+  return launch_lines<double, LINE_C2C>(P->nx, P->nz / 2 + 1, P->ny, -1.0, 0, 0, io, io);
+}
+
+// octant [kz][kx][ky] of the (re or im) spectrum, times (-1)^(kx+ky+kz) * scale
+template <typename T> static int extract_octant(const double2 *spec, T *oct, const OtPriv *P, int imag, double scale) {
+  const int nx = P->nx, ny = P->ny, kxh = nx / 2 + 1, kyh = ny / 2 + 1, kzh = P->nz / 2 + 1;
+  return launch_each((size_t) kzh * kxh * kyh, [=] __device__(size_t i) {
+    const int iy = (int) (i % kyh), ix = (int) ((i / kyh) % kxh), iz = (int) (i / ((size_t) kxh * kyh));
+    const double2 v = spec[((size_t) iz * nx + ix) * ny + iy];
+    double val = imag ? v.y : v.x;
+    if ((ix + iy + iz) & 1) val = -val;
+    oct[i] = (T) (val * scale);
+  });
+}
+
+int ot_generate_kernels(dft_ot_functional *otf, int min_ns, int max_ns) {
+  OtPriv *P = (OtPriv *) otf->priv;
+  const size_t n = (size_t) P->nx * P->ny * P->nz;
+  const size_t nspec = (size_t) (P->nz / 2 + 1) * P->nx * P->ny;
+  const double tol = 0.01 / GRID_AUTOK;
+  const double dv = P->step * P->step * P->step, inv_n = 1.0 / (double) n;
+  double *f = (double *) dev_alloc(n * sizeof(double));
+  double *g = (double *) dev_alloc(n * sizeof(double));
+  double2 *spec = (double2 *) dev_alloc(nspec * sizeof(double2));
+  int rc = DFTGPU_OK;
+  if (!f || !g || !spec) { rc = DFTGPU_ERR_NOMEM; goto done; }
+
+  for (int kk = 0; kk < OT_NKER; kk++) {
+    if (!P->ker[kk]) P->ker[kk] = dev_alloc(P->oct_n * elem_size(P->prec));
+    if (!P->ker[kk]) { rc = DFTGPU_ERR_NOMEM; goto done; }
+  }
+
+  {
+    // LJ with integral b (src/ot.c:150-161), spherical average with integral 1 (src/ot.c:164-181)
+    for (int which = 0; which < 2; which++) {
+      if (which == 0) {
+        ShapeLJ s{otf->lj_params.h, otf->lj_params.sigma, otf->lj_params.epsilon, otf->lj_params.cval};
+        rc = adaptive_map(f, P, min_ns, max_ns, tol, s);
+      } else {
+        ShapeSA s{otf->lj_params.h};
+        rc = adaptive_map(f, P, min_ns, max_ns, tol, s);
+      }
+      if (rc) goto done;
+      if ((rc = rfft3_fp64(f, spec, P))) goto done;
+      double2 k0;
+      if (cudaMemcpyAsync(&k0, spec, sizeof(k0), cudaMemcpyDeviceToHost, rt().stream) != cudaSuccess ||
+          cudaStreamSynchronize(rt().stream) != cudaSuccess) { rc = DFTGPU_ERR_CUDA; goto done; }
+      const double target = which == 0 ? otf->b : 1.0;
+      const double scale = target / (dv * k0.x) * dv * inv_n;
+      rc = P->prec == DFTGPU_FP32 ? extract_octant<float>(spec, (float *) P->ker[which], P, 0, scale)
+                                  : extract_octant<double>(spec, (double *) P->ker[which], P, 0, scale);
+      if (rc) goto done;
+    }
+    if (otf->model & DFT_OT_KC) {
+      // Gaussian F and its central-difference gradient (src/ot.c:184-200)
+      ShapeGauss s{1.0 / otf->l_g};
+      if ((rc = adaptive_map(f, P, min_ns, max_ns, tol, s))) goto done;
+      for (int which = 2; which < 6; which++) {
+        const double *src = f;
+        if (which > 2) { if ((rc = fd_field(f, g, P, which - 3))) goto done; src = g; }
+        if ((rc = rfft3_fp64(src, spec, P))) goto done;
+        rc = P->prec == DFTGPU_FP32 ? extract_octant<float>(spec, (float *) P->ker[which], P, which > 2, dv * inv_n)
+                                    : extract_octant<double>(spec, (double *) P->ker[which], P, which > 2, dv * inv_n);
+        if (rc) goto done;
+      }
+    }
+    if (otf->model & DFT_OT_BACKFLOW) {
+      // V_j (src/ot.c:207-217)
+      const dft_ot_bf &b = otf->bf_params;
+      ShapeBF s{b.g11, b.g12, b.g21, b.g22, b.a1, b.a2};
+      if ((rc = adaptive_map(f, P, min_ns, max_ns, tol, s))) goto done;
+      if ((rc = rfft3_fp64(f, spec, P))) goto done;
+      rc = P->prec == DFTGPU_FP32 ? extract_octant<float>(spec, (float *) P->ker[6], P, 0, dv * inv_n)
+                                  : extract_octant<double>(spec, (double *) P->ker[6], P, 0, dv * inv_n);
+      if (rc) goto done;
+    }
+    if (cudaStreamSynchronize(rt().stream) != cudaSuccess) rc = DFTGPU_ERR_CUDA;
+  }
+done:
+  dev_free(f);
+  dev_free(g);
+  dev_free(spec);
+  if (rc && !g_last_error) set_error(rc, "kernel generation failed");
+  return rc;
+}
+
+// ------------------------------------------------------------------ helpers
+template <typename T> struct Fields {
+  typedef typename cplx_t<T>::type C;
+  OtPriv *P;
+  int nx, ny, nz;
+  T *r(int i) { return (T *) ot_real(P, i); }
+  C *s(int i) { return (C *) ot_spec(P, i); }
+  const T *k(int i) { return (const T *) P->ker[i]; }
+  int fwd(const T *f, C *spec) {
+    RealPairLoad<T> ld{f, ny, nz};
+    return rfft_zy<T>(ld, spec, nx, ny, nz);
+  }
+  int inv(C *spec, T *f) {
+    RealPairStore<T> st{f, ny, nz, (T) 1};
+    return irfft_yz<T>(spec, st, nx, ny, nz);
+  }
+};
+
+template <typename T> static void xc_init(XConvArgs<T> &A, const OtPriv *P) {
+  memset(&A, 0, sizeof(A));
+  A.nx = P->nx; A.ny = P->ny; A.nkz = P->nz / 2 + 1;
+}
+template <typename T> static void xc_in(XConvArgs<T> &A, const typename cplx_t<T>::type *s) { A.src[A.nin++] = s; }
+template <typename T> static void xc_out(XConvArgs<T> &A, typename cplx_t<T>::type *dst, int acc = 0) {
+  XOut<T> &o = A.out[A.nout++];
+  o.dst = dst; o.accumulate = acc;
+  o.t0 = A.nout > 1 ? A.out[A.nout - 2].t0 + A.out[A.nout - 2].nt : 0;
+  o.nt = 0;
+}
+template <typename T> static void xc_term(XConvArgs<T> &A, int in, const T *ker, int kind, T coef) {
+  XOut<T> &o = A.out[A.nout - 1];
+  XTerm<T> &t = A.term[o.t0 + o.nt];
+  t.ker = ker; t.kind = kind; t.in = in; t.coef = coef;
+  o.nt++;
+}
+
+// periodic neighbour offsets for the central difference along axis a
+struct Stencil {
+  int nx, ny, nz;
+  __device__ void nb(size_t i, int a, size_t &ip, size_t &im) const {
+    const int k = (int) (i % nz), j = (int) ((i / nz) % ny), x = (int) (i / ((size_t) ny * nz));
+    if (a == 0) { ip = ((size_t) ((x + 1) % nx) * ny + j) * nz + k; im = ((size_t) ((x - 1 + nx) % nx) * ny + j) * nz + k; }
+    else if (a == 1) { ip = ((size_t) x * ny + (j + 1) % ny) * nz + k; im = ((size_t) x * ny + (j - 1 + ny) % ny) * nz + k; }
+    else { ip = ((size_t) x * ny + j) * nz + (k + 1) % nz; im = ((size_t) x * ny + j) * nz + (k - 1 + nz) % nz; }
+  }
+};
+
+template <typename T> __device__ __forceinline__ T clampv(T v, T cap) { return v > cap ? cap : (v < -cap ? -cap : v); }
+
+// ------------------------------------------------------------------ potential
+template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, wf *gwf) {
+  typedef typename cplx_t<T>::type C;
+  OtPriv *P = (OtPriv *) otf->priv;
+  Fields<T> F{P, P->nx, P->ny, P->nz};
+  const int nx = P->nx, ny = P->ny, nz = P->nz;
+  const size_t n = (size_t) nx * ny * nz;
+  const bool kc = otf->model & DFT_OT_KC, bf = otf->model & DFT_OT_BACKFLOW;
+  const Stencil S{nx, ny, nz};
+  C *pot = (C *) Pg->value;
+  const C *psi = (const C *) gwf->grid->value;
+  T *rho = (T *) otf->density->value;
+
+  // real-field slots
+  enum { R_U, R_RB, R_RT, R_D0, R_D1, R_D2, R_A, R_Q, R_RST, R_S0, R_S1, R_S2, R_V0, R_V1, R_V2, R_E,
+         R_B0, R_B1, R_B2, R_WQ, R_T1, R_J0, R_J1, R_J2, R_C, R_BB0, R_BB1, R_BB2, R_H, R_HF, R_NREAL };
+  T *r[R_NREAL];
+  for (int i = 0; i < R_NREAL; i++) { r[i] = F.r(i); if (!r[i]) return DFTGPU_ERR_NOMEM; }
+  C *s[9];
+  for (int i = 0; i < 9; i++) { s[i] = F.s(i); if (!s[i]) return DFTGPU_ERR_NOMEM; }
+
+  DFT_TRY(density(gwf->grid, otf->density));                                   // src/ot.c:320
+  DFT_TRY(F.fwd(rho, s[0]));
+
+  // x pass 1: one input, kernels LJ, SA (+F, dF_a) (+V_j)
+  {
+    XConvArgs<T> A; xc_init(A, P); xc_in(A, (const C *) s[0]);
+    xc_out(A, s[1]); xc_term(A, 0, F.k(OT_LJ), KER_EVEN, (T) 1);
+    xc_out(A, s[2]); xc_term(A, 0, F.k(OT_SA), KER_EVEN, (T) 1);
+    if (kc) {
+      xc_out(A, s[3]); xc_term(A, 0, F.k(OT_F), KER_EVEN, (T) 1);
+      xc_out(A, s[4]); xc_term(A, 0, F.k(OT_FX), KER_ODD_X, (T) 1);
+      xc_out(A, s[5]); xc_term(A, 0, F.k(OT_FY), KER_ODD_Y, (T) 1);
+      xc_out(A, s[6]); xc_term(A, 0, F.k(OT_FZ), KER_ODD_Z, (T) 1);
+    }
+    if (bf) { xc_out(A, s[7]); xc_term(A, 0, F.k(OT_VJ), KER_EVEN, (T) 1); }
+    DFT_TRY(launch_xconv<T>(A));
+    DFT_TRY(F.inv(s[1], r[R_U]));
+    DFT_TRY(F.inv(s[2], r[R_RB]));
+    if (kc) {
+      DFT_TRY(F.inv(s[3], r[R_RT]));
+      for (int a = 0; a < 3; a++) DFT_TRY(F.inv(s[4 + a], r[R_D0 + a]));
+    }
+    if (bf) DFT_TRY(F.inv(s[7], r[R_A]));
+  }
+
+  // pointwise 1
+  {
+    const T c2 = (T) otf->c2, c3 = (T) otf->c3, irs = (T) (1.0 / otf->rho_0s);
+    T *u = r[R_U], *rb = r[R_RB], *rt = r[R_RT], *q = r[R_Q], *rst = r[R_RST];
+    T *s0 = r[R_S0], *s1 = r[R_S1], *s2 = r[R_S2];
+    T *v0 = r[R_V0], *v1 = r[R_V1], *v2 = r[R_V2], *e = r[R_E], *b0 = r[R_B0], *b1 = r[R_B1], *b2 = r[R_B2];
+    const T inv2h = (T) (1.0 / (2.0 * P->step));
+    const double vf = 1.0 / (gwf->mass * 2.0 * P->step), deps = otf->div_epsilon;
+    const bool clampv_on = otf->max_veloc < (999.0 / GRID_AUTOMPS);
+    const T vcap = (T) otf->max_veloc;
+    DFT_TRY(launch_each(n, [=] __device__(size_t i) {
+      const T b = rb[i], rh = rho[i];
+      // src/ot.c:530, 557-567, 574-581
+      C p = pot[i];
+      p.x += u[i] + (c2 / (T) 2) * (b * b) + (c3 / (T) 3) * (b * b * b);
+      pot[i] = p;
+      q[i] = (c2 * b + c3 * (b * b)) * rh;
+      if (kc) {  // src/ot.c:608-612, 632-637
+        const T st = (T) 1 - rt[i] * irs;
+        rst[i] = st;
+        T *sa[3] = { s0, s1, s2 };
+        for (int a = 0; a < 3; a++) {
+          size_t ip, im; S.nb(i, a, ip, im);
+          sa[a][i] = (rho[ip] - rho[im]) * inv2h * st;
+        }
+      }
+      if (bf) {  // velocity src/ot.c:390-395; C, B_a inputs src/ot.c:852-888
+        const C z = psi[i];
+        double rr = (double) z.x * z.x + (double) z.y * z.y;
+        if (rr < deps) rr = deps;
+        const double g0 = vf / rr;
+        T va[3];
+        for (int a = 0; a < 3; a++) {
+          size_t ip, im; S.nb(i, a, ip, im);
+          const C d = psi[ip] - psi[im];
+          T vv = (T) (g0 * ((double) z.x * d.y - (double) z.y * d.x));
+          if (clampv_on) vv = clampv<T>(vv, vcap);
+          va[a] = vv;
+        }
+        v0[i] = va[0]; v1[i] = va[1]; v2[i] = va[2];
+        e[i] = (va[2] * va[2] + va[1] * va[1] + va[0] * va[0]) * rh;
+        b0[i] = va[0] * rh; b1[i] = va[1] * rh; b2[i] = va[2] * rh;
+      }
+    }));
+  }
+
+  // forward transforms of the produced fields
+  DFT_TRY(F.fwd(r[R_Q], s[0]));
+  if (kc) for (int a = 0; a < 3; a++) DFT_TRY(F.fwd(r[R_S0 + a], s[1 + a]));
+  if (bf) {
+    DFT_TRY(F.fwd(r[R_E], s[4]));
+    for (int a = 0; a < 3; a++) DFT_TRY(F.fwd(r[R_B0 + a], s[5 + a]));
+  }
+
+  // x pass 2
+  {
+    XConvArgs<T> A; xc_init(A, P); xc_in(A, (const C *) s[0]);
+    xc_out(A, s[0]); xc_term(A, 0, F.k(OT_SA), KER_EVEN, (T) 1);               // w q^   (src/ot.c:582-585)
+    DFT_TRY(launch_xconv<T>(A));
+    DFT_TRY(F.inv(s[0], r[R_WQ]));
+  }
+  if (kc) {
+    XConvArgs<T> A; xc_init(A, P);
+    for (int a = 0; a < 3; a++) xc_in(A, (const C *) s[1 + a]);
+    xc_out(A, s[8]);                                                            // sum_a dF_a s_a^  (src/ot.c:641)
+    xc_term(A, 0, F.k(OT_FX), KER_ODD_X, (T) 1);
+    xc_term(A, 1, F.k(OT_FY), KER_ODD_Y, (T) 1);
+    xc_term(A, 2, F.k(OT_FZ), KER_ODD_Z, (T) 1);
+    DFT_TRY(launch_xconv<T>(A));
+    // J_a = F s_a^ in place (src/ot.c:652)
+    XConvArgs<T> B; xc_init(B, P);
+    for (int a = 0; a < 3; a++) xc_in(B, (const C *) s[1 + a]);
+    for (int a = 0; a < 3; a++) { xc_out(B, s[1 + a]); xc_term(B, a, F.k(OT_F), KER_EVEN, (T) 1); }
+    DFT_TRY(launch_xconv<T>(B));
+    DFT_TRY(F.inv(s[8], r[R_T1]));
+    for (int a = 0; a < 3; a++) DFT_TRY(F.inv(s[1 + a], r[R_J0 + a]));
+  }
+  if (bf) {
+    XConvArgs<T> A; xc_init(A, P);
+    for (int a = 0; a < 4; a++) xc_in(A, (const C *) s[4 + a]);
+    for (int a = 0; a < 4; a++) { xc_out(A, s[4 + a]); xc_term(A, a, F.k(OT_VJ), KER_EVEN, (T) 1); }
+    DFT_TRY(launch_xconv<T>(A));
+    DFT_TRY(F.inv(s[4], r[R_C]));
+    for (int a = 0; a < 3; a++) DFT_TRY(F.inv(s[5 + a], r[R_BB0 + a]));
+  }
+
+  // pointwise 2
+  {
+    const T c = (T) (otf->alpha_s / (2.0 * otf->mass)), hm = (T) (-0.5 * otf->mass), cbf = (T) otf->c_bfpot;
+    const bool clampp = otf->max_bfpot < (10000.0 / GRID_AUTOK);
+    const T pcap = (T) otf->max_bfpot, inv2h = (T) (1.0 / (2.0 * P->step));
+    T *wq = r[R_WQ], *rst = r[R_RST], *t1 = r[R_T1], *J0 = r[R_J0], *J1 = r[R_J1], *J2 = r[R_J2];
+    T *d0 = r[R_D0], *d1 = r[R_D1], *d2 = r[R_D2], *h = r[R_H];
+    T *v0 = r[R_V0], *v1 = r[R_V1], *v2 = r[R_V2], *A = r[R_A], *Cc = r[R_C], *B0 = r[R_BB0], *B1 = r[R_BB1], *B2 = r[R_BB2];
+    DFT_TRY(launch_each(n, [=] __device__(size_t i) {
+      C p = pot[i];
+      p.x += wq[i];
+      if (kc) {  // src/ot.c:643-645, 673-675 summed over axes
+        p.x += c * rst[i] * t1[i] - c * (J0[i] * d0[i] + J1[i] * d1[i] + J2[i] * d2[i]);
+        const T *Ja[3] = { J0, J1, J2 };
+        T hv = 0;
+        for (int a = 0; a < 3; a++) {
+          size_t ip, im; S.nb(i, a, ip, im);
+          hv += (rho[ip] - rho[im]) * inv2h * Ja[a][i];   // src/ot.c:656-657
+        }
+        h[i] = hv;
+      }
+      if (bf) {  // src/ot.c:895-915, 924-931
+        const T x = v0[i], y = v1[i], z = v2[i], a = A[i];
+        T re = hm * (a * (z * z + y * y + x * x) - (T) 2 * (x * B0[i] + y * B1[i] + z * B2[i]) + Cc[i]);
+        if (clampp) re = clampv<T>(re, pcap);
+        p.x += re * cbf;
+        v0[i] = x * a - B0[i]; v1[i] = y * a - B1[i]; v2[i] = z * a - B2[i];
+      }
+      pot[i] = p;
+    }));
+  }
+
+  if (kc) {  // F * h  (src/ot.c:656-664 summed over axes)
+    DFT_TRY(F.fwd(r[R_H], s[0]));
+    XConvArgs<T> A; xc_init(A, P); xc_in(A, (const C *) s[0]);
+    xc_out(A, s[0]); xc_term(A, 0, F.k(OT_F), KER_EVEN, (T) 1);
+    DFT_TRY(launch_xconv<T>(A));
+    DFT_TRY(F.inv(s[0], r[R_HF]));
+  }
+
+  // pointwise 3
+  {
+    const T c = (T) (otf->alpha_s / (2.0 * otf->mass)), cbf = (T) otf->c_bfpot, inv2h = (T) (1.0 / (2.0 * P->step));
+    const T eps = (T) otf->div_epsilon, pcap = (T) otf->max_bfpot;
+    const bool clampp = otf->max_bfpot < (10000.0 / GRID_AUTOK);
+    T *hf = r[R_HF], *w0 = r[R_V0], *w1 = r[R_V1], *w2 = r[R_V2];
+    DFT_TRY(launch_each(n, [=] __device__(size_t i) {
+      C p = pot[i];
+      if (kc) p.x += c * hf[i];
+      if (bf) {  // src/ot.c:933-990
+        const T *wa[3] = { w0, w1, w2 };
+        T rr = rho[i];
+        if (rr < eps) rr = eps;
+        T im = 0;
+        for (int a = 0; a < 3; a++) {
+          size_t ip, imm; S.nb(i, a, ip, imm);
+          im += (T) 0.5 * (((rho[ip] - rho[imm]) * inv2h) / rr) * wa[a][i];
+        }
+        for (int a = 0; a < 3; a++) {
+          size_t ip, imm; S.nb(i, a, ip, imm);
+          im += (T) 0.5 * ((wa[a][ip] - wa[a][imm]) * inv2h);
+        }
+        if (clampp) im = clampv<T>(im, pcap);
+        p.y += im * cbf;
+      }
+      pot[i] = p;
+    }));
+  }
+  return DFTGPU_OK;
+}
+
+int ot_potential(dft_ot_functional *otf, cgrid *P, wf *gwf) {
+  return P->prec == DFTGPU_FP32 ? potential_t<float>(otf, P, gwf) : potential_t<double>(otf, P, gwf);
+}
+
+// ------------------------------------------------------------------ energy density
+template <typename T> static int energy_density_t(dft_ot_functional *otf, rgrid *edg, wf *gwf) {
+  typedef typename cplx_t<T>::type C;
+  OtPriv *P = (OtPriv *) otf->priv;
+  Fields<T> F{P, P->nx, P->ny, P->nz};
+  const int nx = P->nx, ny = P->ny, nz = P->nz;
+  const size_t n = (size_t) nx * ny * nz;
+  const bool kc = otf->model & DFT_OT_KC, bf = otf->model & DFT_OT_BACKFLOW;
+  const Stencil S{nx, ny, nz};
+  const C *psi = (const C *) gwf->grid->value;
+  T *rho = (T *) otf->density->value, *ed = (T *) edg->value;
+  enum { R_U, R_RB, R_RT, R_A, R_RST, R_S0, R_S1, R_S2, R_V0, R_V1, R_V2, R_E, R_B0, R_B1, R_B2, R_NREAL };
+  T *r[R_NREAL];
+  for (int i = 0; i < R_NREAL; i++) { r[i] = F.r(i); if (!r[i]) return DFTGPU_ERR_NOMEM; }
+  C *s[8];
+  for (int i = 0; i < 8; i++) { s[i] = F.s(i); if (!s[i]) return DFTGPU_ERR_NOMEM; }
+
+  DFT_TRY(density(gwf->grid, otf->density));
+  DFT_TRY(F.fwd(rho, s[0]));
+  {
+    XConvArgs<T> A; xc_init(A, P); xc_in(A, (const C *) s[0]);
+    xc_out(A, s[1]); xc_term(A, 0, F.k(OT_LJ), KER_EVEN, (T) 1);
+    xc_out(A, s[2]); xc_term(A, 0, F.k(OT_SA), KER_EVEN, (T) 1);
+    if (kc) { xc_out(A, s[3]); xc_term(A, 0, F.k(OT_F), KER_EVEN, (T) 1); }
+    if (bf) { xc_out(A, s[4]); xc_term(A, 0, F.k(OT_VJ), KER_EVEN, (T) 1); }
+    DFT_TRY(launch_xconv<T>(A));
+    DFT_TRY(F.inv(s[1], r[R_U]));
+    DFT_TRY(F.inv(s[2], r[R_RB]));
+    if (kc) DFT_TRY(F.inv(s[3], r[R_RT]));
+    if (bf) DFT_TRY(F.inv(s[4], r[R_A]));
+  }
+  {
+    const T c2 = (T) otf->c2, c3 = (T) otf->c3, irs = (T) (1.0 / otf->rho_0s), inv2h = (T) (1.0 / (2.0 * P->step));
+    const T cm = (T) (otf->c_bfpot * otf->mass);
+    const double vf = 1.0 / (gwf->mass * 2.0 * P->step);
+    T *u = r[R_U], *rb = r[R_RB], *rt = r[R_RT], *A = r[R_A], *rst = r[R_RST], *s0 = r[R_S0], *s1 = r[R_S1], *s2 = r[R_S2];
+    T *v0 = r[R_V0], *v1 = r[R_V1], *v2 = r[R_V2], *e = r[R_E], *b0 = r[R_B0], *b1 = r[R_B1], *b2 = r[R_B2];
+    DFT_TRY(launch_each(n, [=] __device__(size_t i) {
+      const T rh = rho[i], b = rb[i];
+      // src/ot-energy.c:70-93
+      T acc = (T) 0.5 * rh * u[i] + (c2 / (T) 2) * ((b * b) * rh) + (c3 / (T) 3) * ((b * b * b) * rh);
+      if (kc) {  // src/ot-energy.c:144-161
+        const T st = rt[i] * (-irs) + (T) 1;
+        rst[i] = st;
+        T *sa[3] = { s0, s1, s2 };
+        for (int a = 0; a < 3; a++) {
+          size_t ip, im; S.nb(i, a, ip, im);
+          sa[a][i] = (rho[ip] - rho[im]) * inv2h * st;
+        }
+      }
+      if (bf) {  // src/ot-energy.c:231-251 (velocity regularised with DFT_EPS)
+        const C z = psi[i];
+        double rr = (double) z.x * z.x + (double) z.y * z.y;
+        if (rr < DFT_EPS) rr = DFT_EPS;
+        const double g0 = vf / rr;
+        T va[3];
+        for (int a = 0; a < 3; a++) {
+          size_t ip, im; S.nb(i, a, ip, im);
+          const C d = psi[ip] - psi[im];
+          va[a] = (T) (g0 * ((double) z.x * d.y - (double) z.y * d.x));
+        }
+        v0[i] = va[0]; v1[i] = va[1]; v2[i] = va[2];
+        const T vv = va[0] * va[0] + va[1] * va[1] + va[2] * va[2];
+        acc += -(cm / (T) 4) * (A[i] * vv * rh);
+        e[i] = rh * vv;
+        b0[i] = rh * va[0]; b1[i] = rh * va[1]; b2[i] = rh * va[2];
+      }
+      ed[i] = acc;
+    }));
+  }
+  if (kc) {
+    for (int a = 0; a < 3; a++) DFT_TRY(F.fwd(r[R_S0 + a], s[1 + a]));
+    XConvArgs<T> A; xc_init(A, P);
+    for (int a = 0; a < 3; a++) xc_in(A, (const C *) s[1 + a]);
+    for (int a = 0; a < 3; a++) { xc_out(A, s[1 + a]); xc_term(A, a, F.k(OT_F), KER_EVEN, (T) 1); }
+    DFT_TRY(launch_xconv<T>(A));
+    for (int a = 0; a < 3; a++) DFT_TRY(F.inv(s[1 + a], r[R_S0 + a]));   // s_a <- F * s_a
+  }
+  if (bf) {
+    DFT_TRY(F.fwd(r[R_E], s[4]));
+    for (int a = 0; a < 3; a++) DFT_TRY(F.fwd(r[R_B0 + a], s[5 + a]));
+    XConvArgs<T> A; xc_init(A, P);
+    for (int a = 0; a < 4; a++) xc_in(A, (const C *) s[4 + a]);
+    for (int a = 0; a < 4; a++) { xc_out(A, s[4 + a]); xc_term(A, a, F.k(OT_VJ), KER_EVEN, (T) 1); }
+    DFT_TRY(launch_xconv<T>(A));
+    DFT_TRY(F.inv(s[4], r[R_E]));
+    for (int a = 0; a < 3; a++) DFT_TRY(F.inv(s[5 + a], r[R_B0 + a]));
+  }
+  if (kc || bf) {
+    const T f = (T) (-otf->alpha_s / (4.0 * otf->mass)), cm = (T) (otf->c_bfpot * otf->mass);
+    const T inv2h = (T) (1.0 / (2.0 * P->step));
+    T *rst = r[R_RST], *t0 = r[R_S0], *t1 = r[R_S1], *t2 = r[R_S2];
+    T *v0 = r[R_V0], *v1 = r[R_V1], *v2 = r[R_V2], *cc = r[R_E], *B0 = r[R_B0], *B1 = r[R_B1], *B2 = r[R_B2];
+    DFT_TRY(launch_each(n, [=] __device__(size_t i) {
+      T acc = ed[i];
+      const T rh = rho[i];
+      if (kc) {  // src/ot-energy.c:176-190
+        const T *ta[3] = { t0, t1, t2 };
+        for (int a = 0; a < 3; a++) {
+          size_t ip, im; S.nb(i, a, ip, im);
+          acc += f * (ta[a][i] * ((rho[ip] - rho[im]) * inv2h) * rst[i]);
+        }
+      }
+      if (bf) {  // src/ot-energy.c:253-287
+        acc += (cm / (T) 2) * (B0[i] * rh * v0[i]);
+        acc += (cm / (T) 2) * (B1[i] * rh * v1[i]);
+        acc += (cm / (T) 2) * (B2[i] * rh * v2[i]);
+        acc += -(cm / (T) 4) * (cc[i] * rh);
+      }
+      ed[i] = acc;
+    }));
+  }
+  return DFTGPU_OK;
+}
+
+int ot_energy_density(dft_ot_functional *otf, rgrid *ed, wf *gwf) {
+  return ed->prec == DFTGPU_FP32 ? energy_density_t<float>(otf, ed, gwf) : energy_density_t<double>(otf, ed, gwf);
+}
+
+}  // namespace dftgpu

@@ -1,0 +1,39 @@
+// Private state of a GPU OT functional.
+#pragma once
+
+#include "common.cuh"
+
+namespace dftgpu {
+
+enum { OT_LJ = 0, OT_SA = 1, OT_F = 2, OT_FX = 3, OT_FY = 4, OT_FZ = 5, OT_VJ = 6, OT_NKER = 7 };
+constexpr int OT_MAX_REAL = 32;
+constexpr int OT_MAX_SPEC = 10;
+
+struct OtPriv {
+  int prec = DFTGPU_FP64;
+  int nx = 0, ny = 0, nz = 0;
+  double step = 0, x0 = 0, y0 = 0, z0 = 0;
+  size_t oct_n = 0;                 // (nz/2+1)(nx/2+1)(ny/2+1)
+  void *ker[OT_NKER] = {};          // octant spectra, bulk precision
+  void *real[OT_MAX_REAL] = {};     // nx*ny*nz real work fields
+  void *spec[OT_MAX_SPEC] = {};     // (nz/2+1)*nx*ny complex half spectra
+  cgrid *pot_tmp = nullptr;         // energy report scratch
+  rgrid *ed_tmp = nullptr;
+};
+
+void *dev_alloc(size_t bytes);
+
+inline void *ot_real(OtPriv *P, int i) {
+  if (!P->real[i]) P->real[i] = dev_alloc((size_t) P->nx * P->ny * P->nz * elem_size(P->prec));
+  return P->real[i];
+}
+inline void *ot_spec(OtPriv *P, int i) {
+  if (!P->spec[i]) P->spec[i] = dev_alloc((size_t) (P->nz / 2 + 1) * P->nx * P->ny * 2 * elem_size(P->prec));
+  return P->spec[i];
+}
+
+int ot_generate_kernels(dft_ot_functional *otf, int min_ns, int max_ns);
+int ot_potential(dft_ot_functional *otf, cgrid *P, wf *gwf);
+int ot_energy_density(dft_ot_functional *otf, rgrid *ed, wf *gwf);
+
+}  // namespace dftgpu

@@ -1,0 +1,145 @@
+"""Generate the golden fixtures in tests/golden/ from the reference-built oracle.
+
+Run in a container that has the reference tree (libdft's src/ is compiled
+unmodified against the oracle's libgrid restatement by ``make -C oracle ref``):
+
+    python tests/golden/make_golden.py
+
+Outputs (committed):
+  eos.npz          pressure (bar), density (A^-3), chemical potential (K) parsed
+                   from libdft examples/bulk/equation_of_state.dat
+  plain_16.npz     16^3 plain OT: potential, energy density, 3 imaginary-time
+                   predict-correct steps with renormalisation
+  full_mixed.npz   16x18x20 (2*3^2, 2^2*5) OT+KC+BF: potential (complex),
+                   energy density, kernels, 2 real-time predict-correct steps
+  full_lg11.npz    24^3 OT+KC+BF with l_g = 1.1 A: potential, energy density
+All inputs are seeded numpy draws stored in the fixtures themselves.
+"""
+from __future__ import annotations
+
+import os
+import re
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import Oracle, Grids, build  # noqa: E402
+
+EOS_FILE = "/root/reference/examples/bulk/equation_of_state.dat"
+
+
+def coords(shape, step):
+    ax = [(np.arange(n) - n // 2) * step for n in shape]
+    return np.meshgrid(*ax, indexing="ij")
+
+
+def droplet_psi(shape, step, rho0, seed):
+    """sqrt(rho0) (1 - exp(-r^2 / (2 * 5^2))) (1 + 1e-3 N(0,1))  (64^3 plain-OT case, scaled down)."""
+    rng = np.random.default_rng(seed)
+    X, Y, Z = coords(shape, step)
+    r2 = X ** 2 + Y ** 2 + Z ** 2
+    psi = np.sqrt(rho0) * (1.0 - np.exp(-r2 / (2 * 5.0 ** 2)))
+    return (psi * (1.0 + 1e-3 * rng.standard_normal(shape))).astype(np.complex128)
+
+
+def modulated_psi(shape, step, rho0, seed, amp=0.05):
+    """Uniform liquid with density modulations and a smooth phase (non-zero velocity)."""
+    rng = np.random.default_rng(seed)
+    X, Y, Z = coords(shape, step)
+    L = [n * step for n in shape]
+    ph = rng.uniform(0, 2 * np.pi, 6)
+    rho = rho0 * (1 + amp * np.cos(2 * np.pi * X / L[0] + ph[0]) + 0.5 * amp * np.cos(4 * np.pi * Y / L[1] + ph[1])
+                  + 0.5 * amp * np.cos(2 * np.pi * Z / L[2] + ph[2]))
+    phase = 0.3 * np.sin(2 * np.pi * X / L[0] + ph[3]) + 0.2 * np.cos(2 * np.pi * Y / L[1] + ph[4]) \
+        + 0.2 * np.sin(4 * np.pi * Z / L[2] + ph[5])
+    psi = np.sqrt(rho) * np.exp(1j * phase) * (1 + 1e-3 * rng.standard_normal(shape))
+    return psi.astype(np.complex128)
+
+
+def main():
+    build("ref")
+    o = Oracle("ref")
+    assert o.lib.orc_kind() == 2
+    mass = 4.002602 / o.AUTOAMU
+    out = {}
+
+    # ---- EOS table from the reference's own data file
+    rows = []
+    with open(EOS_FILE) as f:
+        for line in f:
+            m = re.findall(r"[-+]?\d+\.\d+(?:[eE][-+]?\d+)?", line)
+            if len(m) >= 3:
+                rows.append([float(v) for v in m[:3]])
+    eos = np.array(rows)
+    np.savez_compressed(os.path.join(HERE, "eos.npz"), pressure_bar=eos[:, 0], density_A3=eos[:, 1],
+                        chempot_K=eos[:, 2])
+
+    # ---- plain 16^3, imaginary time
+    shape, step = (16, 16, 16), 1.0
+    with Grids(o, shape, step, mass) as g:
+        w0 = g.wf(np.ones(shape))
+        otf = g.ot(0, w0)
+        prm = g.params(otf)
+        rho0 = o.lib.orc_bulk_density(otf, 0.0)
+        mu0 = o.lib.orc_bulk_chempot(otf, 0.0)
+        psi = droplet_psi(shape, step, rho0, 42)
+        X, Y, Z = coords(shape, step)
+        vext = 10.0 / o.AUTOK * np.exp(-(X ** 2 + Y ** 2 + Z ** 2) / (2 * 3.0 ** 2))
+        w = g.wf(psi)
+        P = g.potential(otf, w)
+        ed = g.energy_density(otf, w)
+        ekin = o.lib.orc_wf_kinetic_energy(w)
+        wp, Pc, ve, work = g.wf(), g.cgrid(), g.rgrid(vext), g.rgrid()
+        norm0 = o.lib.orc_wf_norm(w)
+        o.lib.orc_wf_set_norm(w, norm0)
+        dt = -1j * 10.0 / o.AUTOFS
+        for _ in range(3):
+            o.lib.orc_pc_step(otf, w, wp, Pc, ve, mu0, dt.real, dt.imag)
+            o.lib.orc_wf_normalize(w)
+        psi3 = g.get_wf(w)
+        etot = o.lib.orc_total_energy(otf, w, ve, work)
+        np.savez_compressed(os.path.join(HERE, "plain_16.npz"), shape=shape, step=step, model=0, psi=psi, vext=vext,
+                            mu0=mu0, rho0=rho0, P=P, ed=ed, ekin=ekin, dt=dt, psi3=psi3, etot3=etot,
+                            norm0=norm0, params=np.array([prm[k] for k in sorted(prm)]),
+                            param_names=np.array(sorted(prm)))
+    # ---- full model, mixed radix, real time
+    shape, step, model = (16, 18, 20), 0.8, 1 | 8
+    with Grids(o, shape, step, mass) as g:
+        w0 = g.wf(np.ones(shape))
+        otf = g.ot(model, w0)
+        rho0 = o.lib.orc_bulk_density(otf, 0.0)
+        mu0 = o.lib.orc_bulk_chempot(otf, 0.0)
+        psi = modulated_psi(shape, step, rho0, 7)
+        w = g.wf(psi)
+        P = g.potential(otf, w)
+        ed = g.energy_density(otf, w)
+        kers = np.stack([g.kernel(otf, i) for i in range(7)])
+        wp, Pc = g.wf(), g.cgrid()
+        dt = 1.0 / o.AUTOFS + 0j
+        for _ in range(2):
+            o.lib.orc_pc_step(otf, w, wp, Pc, None, mu0, dt.real, dt.imag)
+        psi2 = g.get_wf(w)
+        np.savez_compressed(os.path.join(HERE, "full_mixed.npz"), shape=shape, step=step, model=model, psi=psi,
+                            mu0=mu0, P=P, ed=ed, kernels=kers, dt=dt, psi2=psi2)
+    # ---- full model with l_g = 1.1 A
+    shape, step, model = (24, 24, 24), 0.8, 1 | 8
+    with Grids(o, shape, step, mass) as g:
+        w0 = g.wf(np.ones(shape))
+        lg = 1.1 / o.AUTOANG
+        otf = g.ot(model, w0, lg_bohr=lg)
+        rho0 = o.lib.orc_bulk_density(otf, 0.0)
+        psi = modulated_psi(shape, step, rho0, 11, amp=0.1)
+        w = g.wf(psi)
+        P = g.potential(otf, w)
+        ed = g.energy_density(otf, w)
+        np.savez_compressed(os.path.join(HERE, "full_lg11.npz"), shape=shape, step=step, model=model, lg=lg,
+                            psi=psi, P=P, ed=ed)
+    print("golden fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,274 @@
+"""GPU parity: libdftgpu (through its C ABI) against the FP64 CPU oracle and
+the fixtures produced by libdft's own source (tests/golden).
+
+Tolerances (max-norm error relative to the max-norm of the reference):
+  FP64 grids: 1e-10 (the oracle and the GPU code differ only in rounding order)
+  FP32 grids: 1e-5 for spectra / potentials / energy densities (a few FP32
+              ulps times log2 N accumulation through the 3-D transforms).
+"""
+import numpy as np
+import pytest
+
+from conftest import golden, relerr
+from oracle import Grids
+
+pytestmark = pytest.mark.gpu
+
+TOL = {0: 1e-10, 1: 1e-5}
+PRECS = [0, 1]
+
+
+def coords(shape, step):
+    ax = [(np.arange(n) - n // 2) * step for n in shape]
+    return np.meshgrid(*ax, indexing="ij")
+
+
+def liquid_psi(shape, step, seed, amp=0.1):
+    rng = np.random.default_rng(seed)
+    rho0 = 0.0218360 * 0.529177210903 ** 3
+    X, Y, Z = coords(shape, step)
+    L = [n * step for n in shape]
+    rho = rho0 * (1 + amp * np.cos(2 * np.pi * X / L[0]) * np.cos(2 * np.pi * Y / L[1])
+                  + 0.5 * amp * np.sin(4 * np.pi * Z / L[2]))
+    phase = 0.4 * np.sin(2 * np.pi * X / L[0]) + 0.3 * np.cos(2 * np.pi * (Y / L[1] + Z / L[2]))
+    return (np.sqrt(rho) * np.exp(1j * phase) * (1 + 1e-3 * rng.standard_normal(shape))).astype(np.complex128)
+
+
+@pytest.fixture(params=PRECS, ids=["fp64", "fp32"])
+def prec(request, gpu):
+    gpu.set_precision(request.param)
+    yield request.param
+    gpu.set_precision(0)
+
+
+@pytest.mark.parametrize("shape", [(16, 16, 16), (16, 18, 20), (32, 24, 40), (64, 64, 64), (30, 36, 50)])
+def test_rfft_spectrum(gpu, prec, shape):
+    rng = np.random.default_rng(1)
+    f = rng.standard_normal(shape)
+    r = gpu.RGrid(shape, 1.0)
+    r.set(f)
+    s = r.spectrum()
+    r.free()
+    assert relerr(s, np.fft.rfftn(f)) < TOL[prec] * 3
+
+
+def octant(full, shape, odd_axis=None, scale=1.0):
+    """oracle half spectrum [x][y][kz] -> stored octant [kz][kx][ky] with centring sign"""
+    nx, ny, nz = shape
+    ix, iy, iz = np.arange(nx // 2 + 1), np.arange(ny // 2 + 1), np.arange(nz // 2 + 1)
+    sub = full[np.ix_(ix, iy, iz)]                    # [kx][ky][kz]
+    val = sub.imag if odd_axis is not None else sub.real
+    sign = (-1.0) ** (ix[:, None, None] + iy[None, :, None] + iz[None, None, :])
+    return np.transpose(val * sign * scale, (2, 0, 1))
+
+
+@pytest.mark.parametrize("fixture", ["full_mixed.npz"])
+def test_kernels_match_reference(gpu, prec, fixture):
+    fx = golden(fixture)
+    shape, step = tuple(int(s) for s in fx["shape"]), float(fx["step"])
+    w = gpu.Wf(shape, step)
+    ot = gpu.OT(int(fx["model"]), w)
+    n = np.prod(shape)
+    for i in range(7):
+        ref = octant(fx["kernels"][i], shape, odd_axis=(i - 3) if 3 <= i <= 5 else None, scale=step ** 3 / n)
+        got = ot.kernel(i)
+        assert relerr(got, ref) < max(TOL[prec], 1e-7), i
+    ot.free()
+    w.free()
+
+
+@pytest.mark.parametrize("fixture", ["plain_16.npz", "full_mixed.npz", "full_lg11.npz"])
+def test_potential_and_energy_density_match_reference(gpu, prec, fixture):
+    fx = golden(fixture)
+    shape, step = tuple(int(s) for s in fx["shape"]), float(fx["step"])
+    w = gpu.Wf(shape, step)
+    lg = float(fx["lg"]) if "lg" in fx else None
+    ot = gpu.OT(int(fx["model"]), w, lg_bohr=lg)
+    w.set(fx["psi"])
+    P = gpu.CGrid(shape, step)
+    P.zero()
+    ot.potential(P, w)
+    got = P.get()
+    ref = fx["P"]
+    assert relerr(got.real, ref.real) < TOL[prec]
+    if np.abs(ref.imag).max() > 0:
+        assert relerr(got.imag, ref.imag) < 10 * TOL[prec]
+    ed = gpu.RGrid(shape, step)
+    ot.energy_density(ed, w)
+    assert relerr(ed.get(), fx["ed"]) < TOL[prec]
+    for o in (ed, P, ot, w):
+        o.free()
+
+
+@pytest.mark.parametrize("shape,step,model", [((32, 32, 32), 0.8, 9), ((40, 36, 30), 0.7, 1), ((48, 32, 40), 1.0, 8)])
+def test_potential_vs_oracle_live(gpu, port, prec, shape, step, model):
+    psi = liquid_psi(shape, step, 3)
+    with Grids(port, shape, step, gpu.HELIUM_MASS) as g:
+        wo = g.wf(psi)
+        oo = g.ot(model, wo)
+        Pref = g.potential(oo, wo, base=0.1 + 0.05j)
+        edref = g.energy_density(oo, wo)
+    w = gpu.Wf(shape, step)
+    ot = gpu.OT(model, w)
+    w.set(psi)
+    P = gpu.CGrid(shape, step)
+    P.set(np.full(shape, 0.1 + 0.05j))        # the potential is accumulated into P
+    ot.potential(P, w)
+    got = P.get()
+    assert relerr(got.real - 0.1, Pref.real - 0.1) < TOL[prec] * 2
+    if model & 8:
+        assert relerr(got.imag - 0.05, Pref.imag - 0.05) < 20 * TOL[prec]
+    ed = gpu.RGrid(shape, step)
+    ot.energy_density(ed, w)
+    assert relerr(ed.get(), edref) < TOL[prec] * 2
+    for o in (ed, P, ot, w):
+        o.free()
+
+
+@pytest.mark.parametrize("model", [0, 1, 8, 9])
+def test_uniform_liquid_potential_is_chemical_potential(gpu, prec, model):
+    shape, step = (32, 32, 32), 0.8
+    w = gpu.Wf(shape, step)
+    ot = gpu.OT(model, w)
+    rho0 = ot.bulk_density(0.0)
+    mu0 = ot.bulk_chempot(0.0)
+    assert abs(mu0 * gpu.AUTOK + 7.149933) < 1e-6
+    w.set(np.full(shape, np.sqrt(rho0), dtype=complex))
+    P = gpu.CGrid(shape, step)
+    P.zero()
+    ot.potential(P, w)
+    got = P.get()
+    assert relerr(got.real, np.full(shape, mu0)) < (1e-12 if prec == 0 else 2e-6)
+    assert np.abs(got.imag).max() < (1e-14 if prec == 0 else 1e-6) * abs(mu0)
+    for o in (P, ot, w):
+        o.free()
+
+
+def test_propagate_matches_oracle(gpu, port, prec):
+    shape, step = (24, 20, 30), 0.9
+    rng = np.random.default_rng(9)
+    psi = liquid_psi(shape, step, 9)
+    V = (rng.standard_normal(shape) + 0.2j * rng.standard_normal(shape)) * 1e-5
+    dts = [41.3 + 0j, -20j, 30 - 5j]
+    with Grids(port, shape, step, gpu.HELIUM_MASS) as g:
+        wo, Po = g.wf(psi), g.cgrid(V)
+        ref = []
+        for dt in dts:
+            port.lib.orc_propagate(wo, Po, dt.real, dt.imag)
+            ref.append(g.get_wf(wo))
+        wp = g.wf()
+        port.lib.orc_predict(wo, wp, Po, 10.0, -1.0)
+        refp, refk = g.get_wf(wp), port.lib.orc_wf_kinetic_energy(wo)
+    w = gpu.Wf(shape, step)
+    P = gpu.CGrid(shape, step)
+    w.set(psi)
+    P.set(V)
+    for dt, r in zip(dts, ref):
+        w.propagate(P, dt)
+        assert relerr(w.get(), r) < TOL[prec] * 3
+    wp = gpu.Wf(shape, step)
+    w.predict(wp, P, 10.0 - 1.0j)
+    assert relerr(wp.get(), refp) < TOL[prec] * 3
+    assert abs(w.kinetic_energy() / refk - 1) < TOL[prec] * 3
+    for o in (wp, P, w):
+        o.free()
+
+
+def test_pc_steps_match_reference_plain(gpu, prec):
+    fx = golden("plain_16.npz")
+    shape, step = tuple(int(s) for s in fx["shape"]), float(fx["step"])
+    w, wp = gpu.Wf(shape, step), gpu.Wf(shape, step)
+    ot = gpu.OT(0, w)
+    w.set(fx["psi"])
+    w.norm_target = float(fx["norm0"])
+    P, ve = gpu.CGrid(shape, step), gpu.RGrid(shape, step)
+    ve.set(fx["vext"])
+    for _ in range(3):
+        ot.pc_step(w, wp, P, ve, float(fx["mu0"]), complex(fx["dt"]))
+        w.normalize()
+    assert relerr(w.get(), fx["psi3"]) < TOL[prec] * 3
+    e, n, mu = ot.energy_report(w, ve)
+    assert abs(e / float(fx["etot3"]) - 1) < (1e-10 if prec == 0 else 1e-5)
+    assert abs(n / float(fx["norm0"]) - 1) < (1e-12 if prec == 0 else 1e-6)
+    for o in (ve, P, ot, wp, w):
+        o.free()
+
+
+def test_pc_steps_match_reference_full(gpu, prec):
+    fx = golden("full_mixed.npz")
+    shape, step = tuple(int(s) for s in fx["shape"]), float(fx["step"])
+    w, wp = gpu.Wf(shape, step), gpu.Wf(shape, step)
+    ot = gpu.OT(int(fx["model"]), w)
+    w.set(fx["psi"])
+    P = gpu.CGrid(shape, step)
+    for _ in range(2):
+        ot.pc_step(w, wp, P, None, float(fx["mu0"]), complex(fx["dt"]))
+    assert relerr(w.get(), fx["psi2"]) < TOL[prec] * 3
+    for o in (P, ot, wp, w):
+        o.free()
+
+
+def test_run_graph_is_bitwise_equal_to_steps(gpu, prec):
+    shape, step = (32, 32, 32), 0.8
+    psi = liquid_psi(shape, step, 4)
+    out = []
+    for use_run in (False, True):
+        w, wp = gpu.Wf(shape, step), gpu.Wf(shape, step)
+        ot = gpu.OT(9, w)
+        w.set(psi)
+        w.norm_target = 3.0
+        P = gpu.CGrid(shape, step)
+        mu0 = ot.bulk_chempot(0.0)
+        if use_run:
+            ot.run(w, wp, P, None, mu0, -10j / gpu.AUTOFS, 5, True)
+        else:
+            for _ in range(5):
+                ot.pc_step(w, wp, P, None, mu0, -10j / gpu.AUTOFS)
+                w.normalize()
+        out.append(w.get())
+        for o in (P, ot, wp, w):
+            o.free()
+    assert np.array_equal(out[0], out[1])
+
+
+def test_energy_report_matches_oracle(gpu, port, prec):
+    shape, step, model = (24, 24, 24), 0.8, 9
+    psi = liquid_psi(shape, step, 12)
+    X, Y, Z = coords(shape, step)
+    vext = 5.0 / gpu.AUTOK * np.exp(-(X ** 2 + Y ** 2 + Z ** 2) / 8.0)
+    with Grids(port, shape, step, gpu.HELIUM_MASS) as g:
+        wo, vo, work = g.wf(psi), g.rgrid(vext), g.rgrid()
+        oo = g.ot(model, wo)
+        eref = port.lib.orc_total_energy(oo, wo, vo, work)
+        nref = port.lib.orc_wf_norm(wo)
+    w = gpu.Wf(shape, step)
+    ot = gpu.OT(model, w)
+    w.set(psi)
+    ve = gpu.RGrid(shape, step)
+    ve.set(vext)
+    e, n, mu = ot.energy_report(w, ve)
+    assert abs(e / eref - 1) < (1e-10 if prec == 0 else 1e-5)
+    assert abs(n / nref - 1) < (1e-12 if prec == 0 else 1e-6)
+    assert np.isfinite(mu)
+    for o in (ve, ot, w):
+        o.free()
+
+
+def test_errors_are_reported(gpu):
+    L = gpu.lib()
+    assert not L.grid_wf_alloc(17, 16, 16, 1.0, 7000.0, 3, 1, b"odd")      # odd size
+    assert L.dftgpu_last_error() == 2
+    assert not L.grid_wf_alloc(14, 16, 16, 1.0, 7000.0, 3, 1, b"prime7")   # factor 7
+    assert L.dftgpu_last_error() == 2
+    assert not L.grid_wf_alloc(16, 16, 16, 1.0, 7000.0, 1, 1, b"dirichlet")
+    assert L.dftgpu_last_error() == 6
+    w = gpu.Wf((16, 16, 16), 1.0)
+    assert not L.dft_ot_alloc(2, w.ptr, 4, 32)                             # DFT_OT_HD
+    assert L.dftgpu_last_error() == 6
+    psi = np.ones((16, 16, 16), dtype=complex)
+    psi[3, 4, 5] = np.nan
+    w.set(psi)
+    v = L.grid_wf_norm(w.ptr)
+    assert np.isnan(v)
+    assert L.dftgpu_last_error() == 5
+    w.free()

@@ -1,0 +1,139 @@
+"""CPU: the oracle against the reference's own golden data and fixtures.
+
+The oracle is pinned by (a) libdft's examples/bulk/equation_of_state.dat
+(bulk density and chemical potential for 0-24 bar, committed as
+golden/eos.npz), (b) the exact uniform-liquid identity V_OT[rho0] =
+dE/drho(rho0) that follows from the kernel normalisations at src/ot.c:160,181,
+and (c) fixtures produced by libdft's unmodified src/ot.c, ot-energy.c,
+common.c and helium-ot-bulk.c (golden/*.npz, see make_golden.py).
+"""
+import numpy as np
+import pytest
+
+from conftest import golden, relerr
+from oracle import Grids, Oracle, ref_available
+
+
+def test_eos_table(port):
+    """All 241 rows of equation_of_state.dat.
+
+    The P = 0 row does not depend on any unit constant: density and chemical
+    potential must match to the 6 printed decimals.  For P > 0 the reference
+    stops its Newton solve at |P(rho) - P| < 1e-12 a.u. = 3e-4 bar
+    (src/helium-ot-bulk.c:189,204), so each run carries up to 1e-12/rho a.u.
+    (about 1e-4 K) of solver slack that depends on the exact unit constants
+    (libgrid's are not CODATA 2018's).  Densities must still match to the
+    printed decimals; chemical potentials to 3e-4 K (twice the slack plus
+    the constant difference)."""
+    eos = golden("eos.npz")
+    assert len(eos["pressure_bar"]) == 241
+    with Grids(port, (8, 8, 8), 1.0, 4.002602 / port.AUTOAMU) as g:
+        w = g.wf(np.ones((8, 8, 8)))
+        otf = g.ot(0, w)
+        a3 = port.AUTOANG ** 3
+        assert abs(port.lib.orc_bulk_density(otf, 0.0) / a3 - 0.021836) < 6e-7
+        assert abs(port.lib.orc_bulk_chempot(otf, 0.0) * port.AUTOK - (-7.149933)) < 6e-7
+        for p, rho, mu in zip(eos["pressure_bar"], eos["density_A3"], eos["chempot_K"]):
+            r = port.lib.orc_bulk_density(otf, p / port.AUTOBAR) / a3
+            m = port.lib.orc_bulk_chempot(otf, p / port.AUTOBAR) * port.AUTOK
+            assert abs(r - rho) <= 6e-7, (p, r, rho)
+            assert abs(m - mu) <= 3e-4, (p, m, mu)
+
+
+@pytest.mark.parametrize("model", [0, 1, 8, 9])
+def test_uniform_potential_is_bulk_chempot(port, model):
+    shape = (12, 10, 8)
+    with Grids(port, shape, 0.9, 4.002602 / port.AUTOAMU) as g:
+        w = g.wf(np.ones(shape))
+        otf = g.ot(model, w)
+        rho0 = port.lib.orc_bulk_density(otf, 0.0)
+        g.set_wf(w, np.full(shape, np.sqrt(rho0), dtype=complex))
+        P = g.potential(otf, w)
+        mu = port.lib.orc_bulk_dEdRho(otf, rho0)
+        assert abs(mu * port.AUTOK - (-7.149933)) < 1e-6
+        assert relerr(P.real, np.full(shape, mu)) < 1e-12
+        assert np.abs(P.imag).max() < 1e-14 * abs(mu)
+        ed = g.energy_density(otf, w)
+        assert relerr(ed, np.full(shape, port.lib.orc_bulk_energy(otf, rho0))) < 1e-12
+
+
+def _check_fixture(port, name, model_key="model"):
+    fx = golden(name)
+    shape, step = tuple(int(s) for s in fx["shape"]), float(fx["step"])
+    lg = float(fx["lg"]) if "lg" in fx else 0.0
+    g = Grids(port, shape, step, 4.002602 / port.AUTOAMU)   # caller frees
+    w = g.wf(fx["psi"])
+    otf = g.ot(int(fx[model_key]), w, lg_bohr=lg)
+    P = g.potential(otf, w)
+    assert relerr(P.real, fx["P"].real) < 1e-12
+    if np.abs(fx["P"].imag).max() > 0:
+        assert relerr(P.imag, fx["P"].imag) < 1e-11
+    ed = g.energy_density(otf, w)
+    assert relerr(ed, fx["ed"]) < 1e-12
+    return g, w, otf, fx
+
+
+def test_port_matches_reference_plain(port):
+    g, w, otf, fx = _check_fixture(port, "plain_16.npz")
+    wp, P, ve = g.wf(), g.cgrid(), g.rgrid(fx["vext"])
+    port.lib.orc_wf_set_norm(w, float(fx["norm0"]))
+    for _ in range(3):
+        port.lib.orc_pc_step(otf, w, wp, P, ve, float(fx["mu0"]), fx["dt"].real, fx["dt"].imag)
+        port.lib.orc_wf_normalize(w)
+    assert relerr(g.get_wf(w), fx["psi3"]) < 1e-12
+    g.free()
+
+
+def test_port_matches_reference_full_mixed_radix(port):
+    g, w, otf, fx = _check_fixture(port, "full_mixed.npz")
+    for i in range(7):
+        assert relerr(g.kernel(otf, i), fx["kernels"][i]) < 1e-12
+    wp, P = g.wf(), g.cgrid()
+    for _ in range(2):
+        port.lib.orc_pc_step(otf, w, wp, P, None, float(fx["mu0"]), fx["dt"].real, fx["dt"].imag)
+    assert relerr(g.get_wf(w), fx["psi2"]) < 1e-12
+    g.free()
+
+
+def test_port_matches_reference_lg11(port):
+    g, *_ = _check_fixture(port, "full_lg11.npz")
+    g.free()
+
+
+@pytest.mark.parametrize("n", [8, 12, 16, 18, 20, 30, 45, 64, 96])
+def test_oracle_fft_vs_numpy(port, n):
+    rng = np.random.default_rng(n)
+    x = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    assert relerr(port.fft1d(x, -1), np.fft.fft(x)) < 1e-13
+    assert relerr(port.fft1d(x, +1), np.fft.ifft(x) * n) < 1e-13
+
+
+def test_oracle_3d_fft_vs_numpy(port):
+    shape = (12, 10, 8)
+    rng = np.random.default_rng(3)
+    f = rng.standard_normal(shape)
+    with Grids(port, shape, 1.0, 1.0) as g:
+        r = g.rgrid(f)
+        port.lib.orc_rgrid_fft(r)
+        spec = np.empty((12, 10, 5), dtype=np.complex128)
+        port.lib.orc_rgrid_get_spectrum(r, spec.view(np.float64).ctypes.data_as(
+            __import__("ctypes").POINTER(__import__("ctypes").c_double)))
+        assert relerr(spec, np.fft.rfftn(f)) < 1e-13
+
+
+@pytest.mark.skipif(not ref_available(), reason="reference tree not present")
+def test_reference_build_live_vs_port():
+    ref, prt = Oracle("ref"), Oracle("port")
+    shape = (12, 14, 10)
+    rng = np.random.default_rng(5)
+    out = []
+    for o in (ref, prt):
+        with Grids(o, shape, 0.8, 4.002602 / o.AUTOAMU) as g:
+            rho0 = 0.0218360 * o.AUTOANG ** 3
+            psi = np.sqrt(rho0 * (1 + 0.2 * rng.random(shape))) * np.exp(0.3j * rng.random(shape))
+            rng = np.random.default_rng(5)
+            w = g.wf(psi)
+            otf = g.ot(9, w)
+            out.append((g.potential(otf, w), g.energy_density(otf, w)))
+    assert relerr(out[0][0], out[1][0]) < 1e-12
+    assert relerr(out[0][1], out[1][1]) < 1e-12
