@@ -169,6 +169,13 @@ int dftgpu_synchronize(void);
 /* CUDA stream (cudaStream_t) all work is issued on; NULL = legacy default. */
 int dftgpu_set_stream(void *stream);
 void *dftgpu_get_stream(void);
+/* Kernel profiler (no libdft counterpart; libdft times whole iterations with
+ * grid_timer_*, examples/imag_time/imag_time.c:228,242).  While enabled,
+ * every launch is bracketed by CUDA events on the work stream; the report is
+ * JSON {"class": {"launches": n, "ms": total, "bytes": algorithmic bytes}}.
+ * Enabling clears previous records.  Not usable inside graph capture. */
+int dftgpu_profile(int enable);
+int dftgpu_profile_report(char *buf, size_t len);
 
 /* ------------------------------------------------------------ real grids
  * libgrid rgrid API as used by libdft (src/ot.c:95-244, ot-energy.c:59-72,

@@ -50,6 +50,23 @@ bool rc_shape(const cgrid *c, const rgrid *r) {
 
 int bad_arg(const char *what) { set_error(DFTGPU_ERR_ARG, "%s", what); return DFTGPU_ERR_ARG; }
 
+// Instantiated graph of one predict-correct step, replayed by dftgpu_run when
+// it is called again with the same arguments.  Any free of a grid, wave
+// function or functional bumps g_generation and so invalidates it.
+unsigned long g_generation = 1;
+struct GraphCache {
+  cudaGraphExec_t exec = nullptr;
+  cudaStream_t cap = nullptr, user = nullptr;
+  cudaEvent_t ev = nullptr;
+  unsigned long gen = 0;
+  dft_ot_functional *otf = nullptr;
+  wf *g = nullptr, *gp = nullptr;
+  cgrid *P = nullptr;
+  rgrid *vext = nullptr;
+  double mu0 = 0, dr = 0, di = 0;
+  int renorm = 0;
+} g_graph;
+
 }  // namespace
 
 extern "C" {
@@ -95,6 +112,11 @@ int dftgpu_synchronize(void) {
   return DFTGPU_OK;
 }
 int dftgpu_set_stream(void *stream) { rt().stream = (cudaStream_t) stream; return DFTGPU_OK; }
+int dftgpu_profile(int enable) { return prof_enable(enable); }
+int dftgpu_profile_report(char *buf, size_t len) {
+  if (!buf || !len) return bad_arg("dftgpu_profile_report: buffer");
+  return prof_report(buf, len);
+}
 void *dftgpu_get_stream(void) { return (void *) rt().stream; }
 
 REAL rgrid_value_outside_periodic(rgrid *grid, INT i, INT j, INT k) {
@@ -112,7 +134,7 @@ rgrid *rgrid_alloc(INT nx, INT ny, INT nz, REAL step, rgrid_outside_fn value_out
   return rgrid_new(nx, ny, nz, step, rt().precision, id);
 }
 
-void rgrid_free(rgrid *g) { if (g) { dev_free(g->value); free(g); } }
+void rgrid_free(rgrid *g) { if (g) { g_generation++; dev_free(g->value); free(g); } }
 
 rgrid *rgrid_clone(rgrid *g, char *id) {
   if (!g) return nullptr;
@@ -197,7 +219,7 @@ cgrid *cgrid_alloc(INT nx, INT ny, INT nz, REAL step, void *value_outside, void 
   (void) value_outside; (void) outside_params_ptr;
   return cgrid_new(nx, ny, nz, step, rt().precision, id);
 }
-void cgrid_free(cgrid *g) { if (g) { dev_free(g->value); free(g); } }
+void cgrid_free(cgrid *g) { if (g) { g_generation++; dev_free(g->value); free(g); } }
 cgrid *cgrid_clone(cgrid *g, char *id) {
   if (!g) return nullptr;
   cgrid *c = cgrid_new(g->nx, g->ny, g->nz, g->step, g->prec, id);
@@ -418,6 +440,7 @@ int dft_ot_update_kernels(dft_ot_functional *otf, INT min_substeps, INT max_subs
 
 void dft_ot_free(dft_ot_functional *otf) {
   if (!otf) return;
+  g_generation++;
   OtPriv *P = (OtPriv *) otf->priv;
   if (P) {
     for (int i = 0; i < OT_NKER; i++) dev_free(P->ker[i]);
@@ -557,40 +580,51 @@ int dftgpu_run(dft_ot_functional *otf, wf *gwf, wf *gwfp, cgrid *P, rgrid *vext,
                INT nsteps, int renorm) {
   DFT_TRY(check_step_args(otf, gwf, gwfp, P, vext));
   if (nsteps <= 0) return DFTGPU_OK;
-  // first step eagerly: allocates work buffers and FFT tables outside capture
-  DFT_TRY(step_with_renorm(otf, gwf, gwfp, P, vext, mu0, dr, di, renorm));
-  if (nsteps == 1) return DFTGPU_OK;
-  const bool use_graph = !getenv("DFTGPU_NO_GRAPH");
-  if (!use_graph) {
-    for (INT s = 1; s < nsteps; s++) DFT_TRY(step_with_renorm(otf, gwf, gwfp, P, vext, mu0, dr, di, renorm));
+  if (getenv("DFTGPU_NO_GRAPH")) {
+    for (INT s = 0; s < nsteps; s++) DFT_TRY(step_with_renorm(otf, gwf, gwfp, P, vext, mu0, dr, di, renorm));
     return DFTGPU_OK;
   }
-  cudaStream_t user = rt().stream, cap;
-  DFT_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
-  cudaEvent_t ev;
-  DFT_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
-  DFT_CUDA(cudaEventRecord(ev, user));
-  DFT_CUDA(cudaStreamWaitEvent(cap, ev, 0));
-  rt().stream = cap;
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
-  int rc = DFTGPU_OK;
-  if (cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess) rc = DFTGPU_ERR_CUDA;
-  if (!rc) {
-    rc = step_with_renorm(otf, gwf, gwfp, P, vext, mu0, dr, di, renorm);
-    cudaError_t e = cudaStreamEndCapture(cap, &graph);
-    if (!rc && e != cudaSuccess) { rc = DFTGPU_ERR_CUDA; set_error(rc, "graph capture: %s", cudaGetErrorString(e)); }
+  GraphCache &G = g_graph;
+  const bool hit = G.exec && G.gen == g_generation && G.otf == otf && G.g == gwf && G.gp == gwfp && G.P == P &&
+                   G.vext == vext && G.mu0 == mu0 && G.dr == dr && G.di == di && G.renorm == renorm &&
+                   G.user == rt().stream;
+  if (!hit) {
+    // one step eagerly: allocates work buffers and FFT tables outside capture
+    DFT_TRY(step_with_renorm(otf, gwf, gwfp, P, vext, mu0, dr, di, renorm));
+    if (--nsteps == 0) return DFTGPU_OK;
+    if (G.exec) { cudaGraphExecDestroy(G.exec); G.exec = nullptr; }
+    if (!G.cap) DFT_CUDA(cudaStreamCreateWithFlags(&G.cap, cudaStreamNonBlocking));
+    if (!G.ev) DFT_CUDA(cudaEventCreateWithFlags(&G.ev, cudaEventDisableTiming));
   }
-  if (!rc && cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) { rc = DFTGPU_ERR_CUDA; set_error(rc, "graph instantiate"); }
-  for (INT s = 1; !rc && s < nsteps; s++)
-    if (cudaGraphLaunch(exec, cap) != cudaSuccess) { rc = DFTGPU_ERR_CUDA; set_error(rc, "graph launch"); }
-  cudaEventRecord(ev, cap);
-  cudaStreamWaitEvent(user, ev, 0);
-  rt().stream = user;
-  if (exec) cudaGraphExecDestroy(exec);
-  if (graph) cudaGraphDestroy(graph);
-  cudaEventDestroy(ev);
-  cudaStreamDestroy(cap);
+  cudaStream_t user = rt().stream;
+  DFT_CUDA(cudaEventRecord(G.ev, user));
+  DFT_CUDA(cudaStreamWaitEvent(G.cap, G.ev, 0));
+  int rc = DFTGPU_OK;
+  if (!hit) {
+    cudaGraph_t graph = nullptr;
+    rt().stream = G.cap;
+    if (cudaStreamBeginCapture(G.cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess) rc = DFTGPU_ERR_CUDA;
+    if (!rc) {
+      rc = step_with_renorm(otf, gwf, gwfp, P, vext, mu0, dr, di, renorm);
+      cudaError_t e = cudaStreamEndCapture(G.cap, &graph);
+      if (!rc && e != cudaSuccess) { rc = DFTGPU_ERR_CUDA; set_error(rc, "graph capture: %s", cudaGetErrorString(e)); }
+    }
+    rt().stream = user;
+    if (!rc && cudaGraphInstantiate(&G.exec, graph, 0) != cudaSuccess) {
+      rc = DFTGPU_ERR_CUDA;
+      set_error(rc, "graph instantiate");
+      G.exec = nullptr;
+    }
+    if (graph) cudaGraphDestroy(graph);
+    if (!rc) {
+      G.gen = g_generation; G.otf = otf; G.g = gwf; G.gp = gwfp; G.P = P; G.vext = vext;
+      G.mu0 = mu0; G.dr = dr; G.di = di; G.renorm = renorm; G.user = user;
+    }
+  }
+  for (INT s = 0; !rc && s < nsteps; s++)
+    if (cudaGraphLaunch(G.exec, G.cap) != cudaSuccess) { rc = DFTGPU_ERR_CUDA; set_error(rc, "graph launch"); }
+  cudaEventRecord(G.ev, G.cap);
+  cudaStreamWaitEvent(user, G.ev, 0);
   return rc;
 }
 

@@ -92,6 +92,22 @@ int ensure_device();
 double *reduce_slots();
 int reduce_partials(double **buf, size_t *n);
 
+// ------------------------------------------------------------------ profiler
+// When enabled (dftgpu_profile), every kernel launch is bracketed by CUDA
+// events on the launching stream and tagged with a class name and its
+// algorithmic bytes (each input read once, each output written once).
+bool prof_on();
+int prof_begin();                                     // returns a record id or -1
+void prof_end(int id, const char *name, double bytes);
+
+struct ProfScope {
+  int id;
+  const char *name;
+  double bytes;
+  ProfScope(const char *n, double b) : id(prof_on() ? prof_begin() : -1), name(n), bytes(b) {}
+  ~ProfScope() { if (id >= 0) prof_end(id, name, bytes); }
+};
+
 inline size_t elem_size(int prec) { return prec == DFTGPU_FP32 ? 4 : 8; }
 
 }  // namespace dftgpu

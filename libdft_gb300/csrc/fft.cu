@@ -106,6 +106,22 @@ template <typename T> int launch_xconv(XConvArgs<T> &A) {
     attr = true;
   }
   dim3 grid(A.ny / B, A.nkz);
+  double bytes = 0.0;
+  {
+    const double spec = (double) A.nkz * A.nx * A.ny * sizeof(C);
+    bytes = spec * A.nin;
+    for (int o = 0; o < A.nout; o++) bytes += spec * (A.out[o].accumulate ? 2 : 1);
+    const T *seen[XC_MAX_TERMS];
+    int nseen = 0;
+    for (int t = 0; t < XC_MAX_TERMS; t++) {
+      const T *k = A.term[t].ker;
+      if (!k || A.term[t].kind == KER_UNIT) continue;
+      bool dup = false;
+      for (int s = 0; s < nseen; s++) dup |= seen[s] == k;
+      if (!dup) { seen[nseen++] = k; bytes += (double) A.nkz * A.kxh * A.kyh * sizeof(T); }
+    }
+  }
+  ProfScope prof("fft_x_conv", bytes);
   xconv_kernel<T><<<grid, FFT_THREADS, smem, rt().stream>>>(A);
   DFT_CHECK_LAUNCH();
   return DFTGPU_OK;
@@ -123,6 +139,7 @@ template <typename T> int launch_xkinetic(KinArgs<T> &A) {
     attr = true;
   }
   dim3 grid(A.ny / B, A.nz);
+  ProfScope prof("fft_x_kinetic", 2.0 * A.nx * A.ny * A.nz * sizeof(C));
   xkinetic_kernel<T><<<grid, FFT_THREADS, smem, rt().stream>>>(A);
   DFT_CHECK_LAUNCH();
   return DFTGPU_OK;

@@ -384,9 +384,16 @@ __global__ void __launch_bounds__(FFT_THREADS) xkinetic_kernel(const KinArgs<T> 
 // ------------------------------------------------------------ launch helpers
 int choose_tile(int n, int nb, size_t cplx_bytes, int nbufs, int *B, size_t *smem);
 
+// extra_bytes: algorithmic bytes read / written by the fused functors beyond
+// the transformed line data itself (e.g. the potential read by a phase load).
 template <typename T, int MODE, class Ld, class St>
-int launch_lines(int n_fft, int na, int nb, T sign, int e_fast, int e_fast_store, const Ld &ld, const St &st) {
+int launch_lines(int n_fft, int na, int nb, T sign, int e_fast, int e_fast_store, const Ld &ld, const St &st,
+                 double extra_bytes = 0.0) {
   typedef typename cplx_t<T>::type C;
+  const double lines = (double) na * nb;
+  const double data = MODE == LINE_C2C ? 2.0 * n_fft : (2.0 * n_fft + 1.0);
+  ProfScope prof(MODE == LINE_C2C ? "fft_line_c2c" : (MODE == LINE_R2C ? "fft_line_r2c" : "fft_line_c2r"),
+                 lines * data * sizeof(C) + extra_bytes);
   LineArgs<T> args;
   DFT_TRY(get_plan<T>(n_fft, &args.plan));
   args.sign = sign;

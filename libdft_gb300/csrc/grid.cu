@@ -60,6 +60,75 @@ int ensure_device() {
   return DFTGPU_OK;
 }
 
+// ------------------------------------------------------------------ profiler
+namespace {
+struct ProfRec { cudaEvent_t a, b; const char *name; double bytes; };
+bool g_prof = false;
+std::vector<ProfRec> g_recs;      // records of the current profile window
+std::vector<cudaEvent_t> g_pool;  // spare events
+size_t g_used = 0;
+
+cudaEvent_t pool_event() {
+  if (g_used < g_pool.size()) return g_pool[g_used++];
+  cudaEvent_t e;
+  cudaEventCreate(&e);
+  g_pool.push_back(e);
+  g_used++;
+  return e;
+}
+}  // namespace
+
+bool prof_on() { return g_prof; }
+
+int prof_begin() {
+  ProfRec r;
+  r.a = pool_event();
+  r.b = pool_event();
+  r.name = nullptr;
+  r.bytes = 0;
+  cudaEventRecord(r.a, rt().stream);
+  g_recs.push_back(r);
+  return (int) g_recs.size() - 1;
+}
+
+void prof_end(int id, const char *name, double bytes) {
+  ProfRec &r = g_recs[id];
+  r.name = name;
+  r.bytes = bytes;
+  cudaEventRecord(r.b, rt().stream);
+}
+
+int prof_enable(int on) {
+  DFT_TRY(ensure_device());
+  g_prof = on != 0;
+  g_recs.clear();
+  g_used = 0;
+  return DFTGPU_OK;
+}
+
+// JSON {"class": {"launches": n, "ms": t, "bytes": b}, ...}
+int prof_report(char *buf, size_t len) {
+  DFT_CUDA(cudaDeviceSynchronize());
+  struct Acc { const char *name; long n; double ms, bytes; };
+  std::vector<Acc> acc;
+  for (const ProfRec &r : g_recs) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, r.a, r.b) != cudaSuccess) { cudaGetLastError(); continue; }
+    size_t k = 0;
+    while (k < acc.size() && strcmp(acc[k].name, r.name)) k++;
+    if (k == acc.size()) acc.push_back({r.name, 0, 0.0, 0.0});
+    acc[k].n++;
+    acc[k].ms += ms;
+    acc[k].bytes += r.bytes;
+  }
+  size_t off = (size_t) snprintf(buf, len, "{");
+  for (size_t k = 0; k < acc.size() && off < len; k++)
+    off += (size_t) snprintf(buf + off, len - off, "%s\"%s\": {\"launches\": %ld, \"ms\": %.6f, \"bytes\": %.0f}",
+                             k ? ", " : "", acc[k].name, acc[k].n, acc[k].ms, acc[k].bytes);
+  if (off < len) snprintf(buf + off, len - off, "}");
+  return DFTGPU_OK;
+}
+
 static double *g_slots = nullptr;
 static double *g_partials = nullptr;
 

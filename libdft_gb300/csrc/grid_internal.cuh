@@ -49,6 +49,8 @@ int rbinary(rgrid *d, rgrid *a, rgrid *b, double c, int op);
 int rintegral(rgrid *g, double *out);
 int density(cgrid *c, rgrid *d);
 int rspectrum(rgrid *g, double *host);
+int prof_enable(int on);
+int prof_report(char *buf, size_t len);
 int rho_dot_re(rgrid *rho, cgrid *P, double *out);   // sum rho Re(P) dV
 
 }  // namespace dftgpu

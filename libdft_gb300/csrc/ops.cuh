@@ -11,11 +11,13 @@ template <class F> __global__ void each_kernel(size_t n, F f) {
   for (size_t i = (size_t) blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t) gridDim.x * blockDim.x) f(i);
 }
 
-template <class F> int launch_each(size_t n, F f) {
+// bytes: algorithmic bytes the lambda reads and writes (0 if not stated)
+template <class F> int launch_each(size_t n, F f, double bytes = 0.0, const char *name = "pointwise") {
   if (n == 0) return DFTGPU_OK;
   int blocks = (int) ((n + 255) / 256);
   int cap = rt().num_sms * 8;
   if (blocks > cap) blocks = cap;
+  ProfScope prof(name, bytes);
   each_kernel<<<blocks, 256, 0, rt().stream>>>(n, f);
   DFT_CHECK_LAUNCH();
   return DFTGPU_OK;
@@ -73,6 +75,7 @@ template <int NV> __global__ void reduce_final_kernel(const double *partial, dou
 template <int NV, class F> int reduce_dev(size_t n, F f, double *slot, double scale) {
   double *part; size_t np;
   DFT_TRY(reduce_partials(&part, &np));
+  ProfScope prof("reduce_fp64", 0.0);
   reduce_partial_kernel<NV><<<RED_BLOCKS, RED_THREADS, 0, rt().stream>>>(n, f, part);
   DFT_CHECK_LAUNCH();
   reduce_final_kernel<NV><<<1, RED_THREADS, 0, rt().stream>>>(part, slot, scale);

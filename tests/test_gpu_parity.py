@@ -106,18 +106,18 @@ def test_potential_vs_oracle_live(gpu, port, prec, shape, step, model):
     with Grids(port, shape, step, gpu.HELIUM_MASS) as g:
         wo = g.wf(psi)
         oo = g.ot(model, wo)
-        Pref = g.potential(oo, wo, base=0.1 + 0.05j)
+        Pref = g.potential(oo, wo, base=2e-5 + 1e-5j)
         edref = g.energy_density(oo, wo)
     w = gpu.Wf(shape, step)
     ot = gpu.OT(model, w)
     w.set(psi)
     P = gpu.CGrid(shape, step)
-    P.set(np.full(shape, 0.1 + 0.05j))        # the potential is accumulated into P
+    P.set(np.full(shape, 2e-5 + 1e-5j))      # the potential is accumulated into P
     ot.potential(P, w)
     got = P.get()
-    assert relerr(got.real - 0.1, Pref.real - 0.1) < TOL[prec] * 2
+    assert relerr(got.real - 2e-5, Pref.real - 2e-5) < TOL[prec] * 2
     if model & 8:
-        assert relerr(got.imag - 0.05, Pref.imag - 0.05) < 20 * TOL[prec]
+        assert relerr(got.imag - 1e-5, Pref.imag - 1e-5) < 20 * TOL[prec]
     ed = gpu.RGrid(shape, step)
     ot.energy_density(ed, w)
     assert relerr(ed.get(), edref) < TOL[prec] * 2
