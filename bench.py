@@ -176,7 +176,7 @@ def run_gpu(args):
     G.check(G.lib().dftgpu_init(local), "dftgpu_init")
 
     dt = -1j * DT_FS / 0.024188843265857
-    psi0 = droplet_psi()
+    psi0 = droplet_psi(NX)
     K, W = args.steps, args.warmup
 
     # ---- FP32-bulk headline
@@ -288,7 +288,7 @@ def cpu_baseline(args, steps=1):
     """The FP64 CPU oracle on the same 256^3 workload, all host cores."""
     from oracle import Grids, Oracle
     o = Oracle("port")
-    psi0 = droplet_psi()
+    psi0 = droplet_psi(NX)
     mass = 4.002602 / o.AUTOAMU
     with Grids(o, (NX, NX, NX), STEP, mass) as g:
         w = g.wf(psi0)
