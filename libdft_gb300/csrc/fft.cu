@@ -102,7 +102,7 @@ template <typename T> int launch_xconv(XConvArgs<T> &A) {
   A.kyh = A.ny / 2 + 1;
   static bool attr = false;
   if (!attr) {
-    DFT_CUDA(cudaFuncSetAttribute(xconv_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+    DFT_CUDA(cudaFuncSetAttribute(xconv_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) rt().max_smem_optin));
     attr = true;
   }
   dim3 grid(A.ny / B, A.nkz);
@@ -135,7 +135,7 @@ template <typename T> int launch_xkinetic(KinArgs<T> &A) {
   A.B = B;
   static bool attr = false;
   if (!attr) {
-    DFT_CUDA(cudaFuncSetAttribute(xkinetic_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+    DFT_CUDA(cudaFuncSetAttribute(xkinetic_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) rt().max_smem_optin));
     attr = true;
   }
   dim3 grid(A.ny / B, A.nz);

@@ -384,6 +384,15 @@ __global__ void __launch_bounds__(FFT_THREADS) xkinetic_kernel(const KinArgs<T> 
 // ------------------------------------------------------------ launch helpers
 int choose_tile(int n, int nb, size_t cplx_bytes, int nbufs, int *B, size_t *smem);
 
+// "Opt-in shared memory already requested" flag per kernel instantiation.
+// It lives in an anonymous namespace so that every translation unit keeps its
+// own flag: without relocatable device code each translation unit registers
+// its own copy of a template kernel, and the attribute must be set on each.
+namespace {
+template <class Kernel> struct SmemOptIn { static bool done; };
+template <class Kernel> bool SmemOptIn<Kernel>::done = false;
+}  // namespace
+
 // extra_bytes: algorithmic bytes read / written by the fused functors beyond
 // the transformed line data itself (e.g. the potential read by a phase load).
 template <typename T, int MODE, class Ld, class St>
@@ -407,13 +416,17 @@ int launch_lines(int n_fft, int na, int nb, T sign, int e_fast, int e_fast_store
     args.tw2 = p2.tw;
   }
   int B; size_t smem;
-  DFT_TRY(choose_tile(n_fft + 1, nb, sizeof(C), 2, &B, &smem));
+  DFT_TRY(choose_tile(n_fft, nb, sizeof(C), 2, &B, &smem));
   args.B = B;
   auto kfn = line_fft_kernel<T, MODE, Ld, St>;
-  static thread_local bool attr_done = false;  // per instantiation
-  if (!attr_done) {
-    DFT_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
-    attr_done = true;
+  typedef SmemOptIn<LineArgs<T> (*)(Ld *, St *, int (*)[MODE + 1])> Flag;
+  if (smem > 48 * 1024 && !Flag::done) {
+    DFT_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) rt().max_smem_optin));
+    Flag::done = true;
+  }
+  if (smem > rt().max_smem_optin) {
+    set_error(DFTGPU_ERR_SIZE, "line FFT n=%d needs %zu bytes of shared memory", n_fft, smem);
+    return DFTGPU_ERR_SIZE;
   }
   dim3 grid(nb / B, na);
   kfn<<<grid, FFT_THREADS, smem, rt().stream>>>(args, ld, st);

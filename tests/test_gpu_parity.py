@@ -41,7 +41,8 @@ def prec(request, gpu):
     gpu.set_precision(0)
 
 
-@pytest.mark.parametrize("shape", [(16, 16, 16), (16, 18, 20), (32, 24, 40), (64, 64, 64), (30, 36, 50)])
+@pytest.mark.parametrize("shape", [(16, 16, 16), (16, 18, 20), (32, 24, 40), (64, 64, 64), (30, 36, 50),
+                                   (8, 16, 512), (64, 256, 32), (128, 128, 128), (96, 120, 160)])
 def test_rfft_spectrum(gpu, prec, shape):
     rng = np.random.default_rng(1)
     f = rng.standard_normal(shape)
@@ -100,16 +101,18 @@ def test_potential_and_energy_density_match_reference(gpu, prec, fixture):
         o.free()
 
 
-@pytest.mark.parametrize("shape,step,model", [((32, 32, 32), 0.8, 9), ((40, 36, 30), 0.7, 1), ((48, 32, 40), 1.0, 8)])
+@pytest.mark.parametrize("shape,step,model", [((32, 32, 32), 0.8, 9), ((40, 36, 30), 0.7, 1), ((48, 32, 40), 1.0, 8),
+                                              ((96, 80, 128), 0.8, 9)])
 def test_potential_vs_oracle_live(gpu, port, prec, shape, step, model):
     psi = liquid_psi(shape, step, 3)
+    ns = (2, 4) if np.prod(shape) > 200000 else (4, 32)      # coarser kernel sampling on big grids (CPU time)
     with Grids(port, shape, step, gpu.HELIUM_MASS) as g:
         wo = g.wf(psi)
-        oo = g.ot(model, wo)
+        oo = g.ot(model, wo, min_ns=ns[0], max_ns=ns[1])
         Pref = g.potential(oo, wo, base=2e-5 + 1e-5j)
         edref = g.energy_density(oo, wo)
     w = gpu.Wf(shape, step)
-    ot = gpu.OT(model, w)
+    ot = gpu.OT(model, w, min_ns=ns[0], max_ns=ns[1])
     w.set(psi)
     P = gpu.CGrid(shape, step)
     P.set(np.full(shape, 2e-5 + 1e-5j))      # the potential is accumulated into P
@@ -144,8 +147,9 @@ def test_uniform_liquid_potential_is_chemical_potential(gpu, prec, model):
         o.free()
 
 
-def test_propagate_matches_oracle(gpu, port, prec):
-    shape, step = (24, 20, 30), 0.9
+@pytest.mark.parametrize("shape", [(24, 20, 30), (128, 128, 128), (64, 96, 160)])
+def test_propagate_matches_oracle(gpu, port, prec, shape):
+    step = 0.9
     rng = np.random.default_rng(9)
     psi = liquid_psi(shape, step, 9)
     V = (rng.standard_normal(shape) + 0.2j * rng.standard_normal(shape)) * 1e-5
