@@ -246,6 +246,22 @@ int dftgpu_wf_propagate(wf *gwf, cgrid *potential, double dt_re, double dt_im);
 int dftgpu_wf_propagate_predict(wf *gwf, wf *gwfp, cgrid *potential, double dt_re, double dt_im);
 int dftgpu_wf_propagate_correct(wf *gwf, cgrid *potential, double dt_re, double dt_im);
 
+/* Allocation-free form of dftgpu_wf_propagate (no counterpart in the
+ * reference: libgrid allocates its own work grids).  For callers that may not
+ * call cudaMalloc -- code running inside someone else's stream capture, hosts
+ * whose memory pool owns all device memory, services that must not grow after
+ * start-up.  The caller passes device pointers it owns: psi_in and potential
+ * (nx*ny*nz interleaved complex values of precision prec, [x][y][z] order) and
+ * psi_out (same size; may equal psi_in); one step psi_out = S(V, dt) psi_in on
+ * `stream` (NULL = legacy default stream).  Work memory is a static 32 MiB
+ * device array plus twiddle tables, held by every GPU that loads the library
+ * until exit: grids up to 2,097,152 points in FP64 or 4,194,304 in FP32;
+ * larger ones are rejected with DFTGPU_ERR_SIZE.  All calls share that array
+ * (overlapping calls on the GPU race); the first call on a device resolves
+ * its address and should come before any stream capture. */
+int dftgpu_wf_propagate_noalloc(void *psi_out, const void *psi_in, const void *potential, INT nx, INT ny, INT nz,
+                                REAL step, REAL mass, double dt_re, double dt_im, int prec, void *stream);
+
 /* ---------------------------------------------------------- OT functional */
 dft_ot_functional *dft_ot_alloc(INT model, wf *gwf, INT min_substeps, INT max_substeps);   /* src/ot.c:66 */
 void dft_ot_free(dft_ot_functional *otf);                                                   /* src/ot.c:268 */

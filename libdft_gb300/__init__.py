@@ -129,6 +129,7 @@ SIGNATURES = {
     "dft_ot_bulk_dispersion": (_d, [_vp, _dp, _d]),
     "dftgpu_ot_kernel": (_i, [_vp, _i, _dp]),
     "dftgpu_rgrid_spectrum": (_i, [_vp, _dp]),
+    "dftgpu_wf_propagate_noalloc": (_i, [_vp, _vp, _vp, _l, _l, _l, _d, _d, _d, _d, _i, _vp]),
     "dftgpu_pc_step": (_i, [_vp, _vp, _vp, _vp, _vp, _d, _d, _d]),
     "dftgpu_run": (_i, [_vp, _vp, _vp, _vp, _vp, _d, _d, _d, _l, _i]),
     "dftgpu_energy_report": (_i, [_vp, _vp, _vp, _dp, _dp, _dp]),

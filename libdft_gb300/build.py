@@ -20,7 +20,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libdftgpu.so")
 INCLUDE = os.path.join(ROOT, "include")
 
-CU_SOURCES = ["fft.cu", "grid.cu", "ot.cu", "api.cu", "adjoint.cu"]
+CU_SOURCES = ["fft.cu", "grid.cu", "ot.cu", "api.cu", "adjoint.cu", "noalloc.cu"]
 C_SOURCES = ["compat.c"]
 
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"

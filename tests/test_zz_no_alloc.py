@@ -1,0 +1,87 @@
+"""GPU: the allocation-free propagation entry point.
+
+dftgpu_wf_propagate_noalloc exists for callers that cannot call cudaMalloc
+(code running inside another component's stream capture, hosts whose own
+memory pool owns all device memory, services that may not grow after
+start-up).  It takes caller-owned device buffers and uses only the library's
+static device scratch.  Here the buffers are owned by torch, i.e. by a
+different allocator than the library's, and two steps in a row through the
+new entry point must agree with two steps of the allocating entry point
+(dftgpu_wf_propagate) within the tolerances the other GPU tests use.
+
+This file is named to be collected last.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL = {0: 1e-10, 1: 1e-5}
+
+
+def _psi_and_potential(shape, step, seed):
+    rng = np.random.default_rng(seed)
+    ax = [(np.arange(n) - n // 2) * step for n in shape]
+    X, Y, Z = np.meshgrid(*ax, indexing="ij")
+    rho0 = 0.0218360 * 0.529177210903 ** 3
+    psi = np.sqrt(rho0 * (1 + 0.1 * np.cos(2 * np.pi * X / (shape[0] * step)))) \
+        * np.exp(0.3j * np.sin(2 * np.pi * Y / (shape[1] * step))) * (1 + 1e-3 * rng.standard_normal(shape))
+    V = (rng.standard_normal(shape) + 0.3j * rng.standard_normal(shape)) * 1e-5
+    return psi.astype(np.complex128), V.astype(np.complex128)
+
+
+@pytest.mark.parametrize("prec", [0, 1], ids=["fp64", "fp32"])
+@pytest.mark.parametrize("shape", [(32, 48, 40), (64, 64, 128)])
+def test_noalloc_propagate_matches_allocating_entry_point(prec, shape):
+    import torch
+    import libdft_gb300 as G
+
+    L = G.lib()
+    assert L.dftgpu_init(0) == 0
+    G.set_precision(prec)
+    step, dt = 0.8, 41.3 - 2.0j
+    psi, V = _psi_and_potential(shape, step, 21)
+
+    # existing, allocating entry point
+    w = G.Wf(shape, step)
+    P = G.CGrid(shape, step)
+    w.set(psi)
+    P.set(V)
+
+    # caller-owned device buffers from another allocator (torch)
+    rdt = torch.float64 if prec == 0 else torch.float32
+    as_t = lambda a: torch.from_numpy(np.ascontiguousarray(a).view(np.float64).astype(
+        np.float64 if prec == 0 else np.float32)).to("cuda")
+    psi_in, pot = as_t(psi), as_t(V)
+    psi_out = torch.empty_like(psi_in)
+    assert psi_in.dtype == rdt
+    nx, ny, nz = shape
+    for call in range(2):
+        w.propagate(P, dt)
+        rc = L.dftgpu_wf_propagate_noalloc(psi_out.data_ptr(), psi_in.data_ptr(), pot.data_ptr(), nx, ny, nz, step,
+                                           G.HELIUM_MASS, dt.real, dt.imag, prec, None)
+        assert rc == 0, L.dftgpu_last_error_message()
+        torch.cuda.synchronize()
+        got = psi_out.double().cpu().numpy().view(np.complex128).reshape(shape)
+        ref = w.get()
+        err = np.abs(got - ref).max() / np.abs(ref).max()
+        assert err < 3 * TOL[prec], (call, err)
+        psi_in.copy_(psi_out)
+    w.free()
+    P.free()
+    G.set_precision(0)
+
+
+def test_noalloc_rejects_grids_beyond_the_static_scratch():
+    import torch
+    import libdft_gb300 as G
+
+    L = G.lib()
+    assert L.dftgpu_init(0) == 0
+    small = torch.zeros(64, device="cuda")   # valid buffers; the size check rejects before any use
+    p = small.data_ptr()
+    # 256^3 FP32 needs 128 MiB of scratch > 32 MiB
+    rc = L.dftgpu_wf_propagate_noalloc(p, p, p, 256, 256, 256, 0.8, G.HELIUM_MASS, 1.0, 0.0, 1, None)
+    assert rc == 2
+    assert "static scratch" in L.dftgpu_last_error_message().decode()
+    L.dftgpu_last_error()
