@@ -137,10 +137,12 @@ def time_steps(G, torch, w, wp, ot, P, mu0, dt, steps, dist):
         torch.distributed.barrier()
     torch.cuda.synchronize()
     t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.nvtx.range_push("timed_steps")
     t0.record()
     ot.run(w, wp, P, None, mu0, dt, steps, True)
     t1.record()
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
     ms = t0.elapsed_time(t1)
     if dist:
         x = torch.tensor([ms], device="cuda")

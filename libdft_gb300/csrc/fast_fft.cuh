@@ -1,0 +1,365 @@
+// Register-resident line FFTs for FP32 power-of-two lengths N = 64..512.
+//
+// Each thread owns E = 8 or 16 elements of one line; TL = N / E threads work
+// on a line and a CTA of 256 threads holds B = 256 / TL lines.  A length-N
+// transform is 2 or 3 Stockham stages with compile-time radices
+//   N = 64: 8 x 8     N = 128: 16 x 8     N = 256: 16 x 16     N = 512: 16 x 16 x 2
+// computed entirely in registers; only the stage boundaries exchange data
+// through shared memory (one store + one load per element, padded so that
+// neither mapping below causes bank conflicts).  The first stage reads
+// element t + TL*q of its line and the last stage produces elements
+// t + TL*j, so loads and stores go straight between HBM and registers:
+//   EFAST mapping (thread t fast within a line): lines contiguous in memory
+//     (y lines of the spectral layout, rows of real space);
+//   LFAST mapping (line index fast): pencils strided in memory with adjacent
+//     lines adjacent (x pencils) -- B lines give one contiguous run per element.
+// Passes whose other side is transposed (the z pass writes [kz][x][y]) stage
+// that side through shared memory with a cooperative line-fast loop.  The
+// forward transform's output layout equals the inverse's input layout, so the
+// x-pencil kernels apply k-space factors in registers between the two.
+#pragma once
+
+#include "common.cuh"
+
+namespace dftgpu {
+namespace ff {
+
+typedef float2 C;
+
+template <int N> struct Shape {
+  static constexpr int E = (N == 64) ? 8 : 16;
+  static constexpr int NS = (N == 512) ? 3 : 2;
+  static constexpr int TL = N / E;           // threads per line
+  static constexpr int B = 256 / TL;         // lines per CTA
+  static constexpr int LP = N + N / 16 + 1;  // padded line pitch in shared memory (odd)
+  static constexpr int SMEM = B * LP * (int) sizeof(C);
+  template <int S> __host__ __device__ static constexpr int R() {
+    return N == 64 ? 8 : N == 128 ? (S == 0 ? 16 : 8) : N == 256 ? 16 : (S < 2 ? 16 : 2);
+  }
+  template <int S> __host__ __device__ static constexpr int P() {   // product of the radices before stage S
+    if constexpr (S == 0) return 1;
+    else return P<S - 1>() * R<S - 1>();
+  }
+};
+
+template <int N> constexpr bool supported() { return N == 64 || N == 128 || N == 256 || N == 512; }
+
+__device__ __forceinline__ int sidx(int l, int e, int LP) { return l * LP + e + (e >> 4); }
+
+// --------------------------------------------------------------- butterflies
+__device__ __forceinline__ C rot(C a, float s) { return make_float2(-s * a.y, s * a.x); }   // * (s i)
+
+__device__ __forceinline__ void bf2(C *u) { C a = u[0]; u[0] = a + u[1]; u[1] = a - u[1]; }
+
+__device__ __forceinline__ void bf4(C &a, C &b, C &c, C &d, float s) {   // in place, natural order
+  C t0 = a + c, t1 = a - c, t2 = b + d, t3 = b - d;
+  a = t0 + t2; c = t0 - t2; b = t1 + rot(t3, s); d = t1 - rot(t3, s);
+}
+
+__device__ __forceinline__ void bf8(C *u, float s) {
+  const float h = 0.70710678118654752440f;
+  C a0 = u[0] + u[4], a1 = u[0] - u[4], b0 = u[2] + u[6], b1 = u[2] - u[6];
+  C c0 = u[1] + u[5], c1 = u[1] - u[5], d0 = u[3] + u[7], d1 = u[3] - u[7];
+  C e0 = a0 + b0, e1 = a0 - b0, f0 = c0 + d0, f1 = c0 - d0;
+  u[0] = e0 + f0; u[4] = e0 - f0; u[2] = e1 + rot(f1, s); u[6] = e1 - rot(f1, s);
+  C b1w = rot(b1, s);
+  C c1w = make_float2(h * (c1.x - s * c1.y), h * (c1.y + s * c1.x));
+  C d1w = make_float2(h * (-d1.x - s * d1.y), h * (-d1.y + s * d1.x));
+  C g0 = a1 + b1w, g1 = a1 - b1w, k0 = c1w + d1w, k1 = c1w - d1w;
+  u[1] = g0 + k0; u[5] = g0 - k0; u[3] = g1 + rot(k1, s); u[7] = g1 - rot(k1, s);
+}
+
+// 16-point DFT as 4 x 4 with W16 twiddles; output in natural order
+__device__ __forceinline__ void bf16(C *u, float s) {
+  const float c1 = 0.92387953251128675613f, s1 = 0.38268343236508977173f, h = 0.70710678118654752440f;
+  // step 1: for n2 = 0..3, 4-point DFT over n1 of x[4 n1 + n2] -> y[n2][k1]
+#pragma unroll
+  for (int n2 = 0; n2 < 4; n2++) bf4(u[n2], u[4 + n2], u[8 + n2], u[12 + n2], s);
+  // now u[4 k1 + n2] = y[n2][k1]; step 2: y[n2][k1] *= W16^(n2 k1), W16 = exp(s 2 pi i / 16)
+  // n2 = 1: k1 = 1,2,3 -> W^1, W^2, W^3 ; n2 = 2 -> W^2, W^4, W^6 ; n2 = 3 -> W^3, W^6, W^9
+  auto tw = [&](C &v, float cr, float ci) {   // v *= (cr + s i ci)
+    const float im = s * ci;
+    v = make_float2(v.x * cr - v.y * im, v.x * im + v.y * cr);
+  };
+  tw(u[4 + 1], c1, s1);  tw(u[8 + 1], h, h);     tw(u[12 + 1], s1, c1);
+  tw(u[4 + 2], h, h);    u[8 + 2] = rot(u[8 + 2], s); tw(u[12 + 2], -h, h);
+  tw(u[4 + 3], s1, c1);  tw(u[8 + 3], -h, h);    tw(u[12 + 3], -c1, -s1);
+  // step 3: for k1 = 0..3, 4-point DFT over n2 of y[n2][k1] = u[4 k1 + n2] -> X[k1 + 4 k2]
+#pragma unroll
+  for (int k1 = 0; k1 < 4; k1++) bf4(u[4 * k1 + 0], u[4 * k1 + 1], u[4 * k1 + 2], u[4 * k1 + 3], s);
+  // u[4 k1 + k2] = X[k1 + 4 k2]: transpose the 4 x 4 block into natural order
+  C t[16];
+#pragma unroll
+  for (int k1 = 0; k1 < 4; k1++)
+#pragma unroll
+    for (int k2 = 0; k2 < 4; k2++) t[k1 + 4 * k2] = u[4 * k1 + k2];
+#pragma unroll
+  for (int i = 0; i < 16; i++) u[i] = t[i];
+}
+
+template <int R> __device__ __forceinline__ void bfR(C *u, float s) {
+  if constexpr (R == 2) bf2(u);
+  else if constexpr (R == 8) bf8(u, s);
+  else bf16(u, s);
+}
+
+// --------------------------------------------------------------- stages
+// Register slot m*R + q of a thread holds input q of its butterfly m before a
+// stage and output q after it; butterfly m of thread t is i = t + m*TL.
+template <int N, int S>
+__device__ __forceinline__ void stage(C (&v)[Shape<N>::E], int t, float s, const C *__restrict__ tw) {
+  constexpr int E = Shape<N>::E, TL = Shape<N>::TL;
+  constexpr int R = Shape<N>::template R<S>(), P = Shape<N>::template P<S>(), NB = E / R;
+  constexpr int TWS = N / (P * R);
+#pragma unroll
+  for (int m = 0; m < NB; m++) {
+    const int i = t + m * TL, k = i % P;
+    if (P > 1) {
+#pragma unroll
+      for (int q = 1; q < R; q++) {
+        C w = __ldg(&tw[q * k * TWS]);
+        w.y *= -s;
+        v[m * R + q] = cmul(v[m * R + q], w);
+      }
+    }
+    bfR<R>(&v[m * R], s);
+  }
+}
+
+// output position of register slot m*R + q after stage S
+template <int N, int S> __host__ __device__ constexpr int out_pos(int t, int slot) {
+  constexpr int TL = Shape<N>::TL, R = Shape<N>::template R<S>(), P = Shape<N>::template P<S>();
+  const int m = slot / R, q = slot % R, i = t + m * TL, k = i % P;
+  return (i - k) * R + k + q * P;
+}
+// input position of register slot m*R + q before stage S
+template <int N, int S> __host__ __device__ constexpr int in_pos(int t, int slot) {
+  constexpr int TL = Shape<N>::TL, R = Shape<N>::template R<S>();
+  const int m = slot / R, q = slot % R;
+  return t + m * TL + q * (N / R);
+}
+
+// Full transform in registers: on entry v[q] = x[t + TL q]; on exit v[slot]
+// = X[out_pos<N, NS-1>(t, slot)], which is t + TL * j(slot).
+template <int N, int S = 0>
+__device__ __forceinline__ void transform(C (&v)[Shape<N>::E], int t, int l, float s, const C *__restrict__ tw,
+                                          C *__restrict__ sm) {
+  constexpr int E = Shape<N>::E, LP = Shape<N>::LP;
+  stage<N, S>(v, t, s, tw);
+  if constexpr (S + 1 < Shape<N>::NS) {
+#pragma unroll
+    for (int j = 0; j < E; j++) sm[sidx(l, out_pos<N, S>(t, j), LP)] = v[j];
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < E; j++) v[j] = sm[sidx(l, in_pos<N, S + 1>(t, j), LP)];
+    __syncthreads();
+    transform<N, S + 1>(v, t, l, s, tw, sm);
+  }
+}
+
+// element index held by register slot j after a full transform (= t + TL * jj)
+template <int N> __host__ __device__ constexpr int final_pos(int t, int j) { return out_pos<N, Shape<N>::NS - 1>(t, j); }
+
+// register slot that holds element t + TL*q after a forward transform (the
+// inverse transform wants element t + TL*q in slot q)
+template <int N> __host__ __device__ constexpr int slot_of(int q) {
+  // final_pos(t, j) = t + TL * jj(j) independent of t; invert jj
+  for (int j = 0; j < Shape<N>::E; j++)
+    if (out_pos<N, Shape<N>::NS - 1>(0, j) == Shape<N>::TL * q) return j;
+  return 0;
+}
+
+template <int N> __device__ __forceinline__ void to_input_order(C (&v)[Shape<N>::E]) {
+  constexpr int E = Shape<N>::E;
+  C t[E];
+#pragma unroll
+  for (int q = 0; q < E; q++) t[q] = v[slot_of<N>(q)];
+#pragma unroll
+  for (int q = 0; q < E; q++) v[q] = t[q];
+}
+
+// --------------------------------------------------------------- line pass
+enum { MAP_E = 0, MAP_L = 1 };
+
+// MODE 0 C2C, 1 R2C (N = nz/2, post-processed to N+1 outputs), 2 C2R.
+// LDS / STS: stage the load / store side through shared memory with a
+// line-fast cooperative loop (used for the transposed side of z passes).
+template <int N, int MODE, int MAP, int LDS, int STS, class Ld, class St>
+__global__ void __launch_bounds__(256) line_kernel(const C *__restrict__ tw, const C *__restrict__ tw2, float sign,
+                                                   const Ld ld, const St st) {
+  constexpr int E = Shape<N>::E, TL = Shape<N>::TL, B = Shape<N>::B, LP = Shape<N>::LP;
+  __shared__ C sm[B * LP];
+  const int a = blockIdx.y, b0 = blockIdx.x * B;
+  const int t = MAP == MAP_E ? threadIdx.x % TL : threadIdx.x / B;
+  const int l = MAP == MAP_E ? threadIdx.x / TL : threadIdx.x % B;
+  C v[E];
+  if constexpr (LDS == 0) {
+#pragma unroll
+    for (int q = 0; q < E; q++) v[q] = ld(a, b0 + l, t + TL * q);
+  } else {
+    for (int idx = threadIdx.x; idx < B * N; idx += 256) {
+      const int ll = idx % B, e = idx / B;
+      C z;
+      if constexpr (MODE == 2) {
+        // Z[k] = (X[k] + X*[N-k]) + i w^-k (X[k] - X*[N-k]),  w = exp(-2 pi i / 2N)
+        C xk = ld(a, b0 + ll, e), xm = ld(a, b0 + ll, N - e);
+        if (e == 0) { xk.y = 0.f; xm.y = 0.f; }
+        const C sum = make_float2(xk.x + xm.x, xk.y - xm.y), dif = make_float2(xk.x - xm.x, xk.y + xm.y);
+        C w = __ldg(&tw2[e]);
+        w.y = -w.y;
+        const C tt = cmul(dif, w);
+        z = make_float2(sum.x - tt.y, sum.y + tt.x);
+      } else {
+        z = ld(a, b0 + ll, e);
+      }
+      sm[sidx(ll, e, LP)] = z;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < E; q++) v[q] = sm[sidx(l, t + TL * q, LP)];
+    __syncthreads();
+  }
+  transform<N>(v, t, l, sign, tw, sm);
+  if constexpr (STS == 0) {
+#pragma unroll
+    for (int j = 0; j < E; j++) st(a, b0 + l, final_pos<N>(t, j), v[j]);
+  } else {
+#pragma unroll
+    for (int j = 0; j < E; j++) sm[sidx(l, final_pos<N>(t, j), LP)] = v[j];
+    __syncthreads();
+    if constexpr (MODE == 1) {
+      // X[k] = (Z[k] + Z*[N-k]) / 2 - (i/2) w^k (Z[k] - Z*[N-k]),  k = 0..N
+      for (int idx = threadIdx.x; idx < B * (N + 1); idx += 256) {
+        const int ll = idx % B, k = idx / B;
+        const C zk = sm[sidx(ll, k == N ? 0 : k, LP)], zm = sm[sidx(ll, k == 0 ? 0 : N - k, LP)];
+        const C sum = make_float2(zk.x + zm.x, zk.y - zm.y), dif = make_float2(zk.x - zm.x, zk.y + zm.y);
+        const C w = k == N ? make_float2(-1.f, 0.f) : __ldg(&tw2[k]);
+        const C tt = cmul(dif, w);
+        st(a, b0 + ll, k, make_float2(0.5f * (sum.x + tt.y), 0.5f * (sum.y - tt.x)));
+      }
+    } else {
+      for (int idx = threadIdx.x; idx < B * N; idx += 256) {
+        const int ll = idx % B, e = idx / B;
+        st(a, b0 + ll, e, sm[sidx(ll, e, LP)]);
+      }
+    }
+  }
+}
+
+// --------------------------------------------------------------- x pencils
+// LFAST pencils of the spectral layout [kz][x][y]: line (kz, y), element x.
+struct XArgsF {
+  int nx, ny, kxh, kyh;
+  int nin, nout;
+  const C *src[4];
+  C *dst[8];
+  int acc_out[8];         // 1: dst += result
+  int nterm[8], t0[8];    // terms of each output
+  const float *ker[16];
+  int kind[16], in[16];
+  float coef[16];
+};
+
+__device__ __forceinline__ C kmul(const XArgsF &A, int tm, C v, int kx, int ky, int kz) {
+  const int kind = A.kind[tm];
+  if (kind == 4) return v * A.coef[tm];                                // unit
+  const int ix = kx <= A.nx / 2 ? kx : A.nx - kx;
+  const int iy = ky <= A.ny / 2 ? ky : A.ny - ky;
+  const float kv = __ldg(&A.ker[tm][((size_t) kz * A.kxh + ix) * A.kyh + iy]) * A.coef[tm];
+  if (kind == 0) return v * kv;
+  float sg = 1.f;
+  if (kind == 1 && kx > A.nx / 2) sg = -1.f;
+  if (kind == 2 && ky > A.ny / 2) sg = -1.f;
+  return make_float2(-sg * kv * v.y, sg * kv * v.x);                   // (i sg kv) v
+}
+
+// Inputs are processed one after the other (forward FFT in registers).  An
+// output with one term is produced right after its input; at most one output
+// with several terms is accumulated in registers and produced at the end.
+template <int N>
+__global__ void __launch_bounds__(256) xconv_kernel(const C *__restrict__ tw, const XArgsF A, int multi) {
+  constexpr int E = Shape<N>::E, TL = Shape<N>::TL, B = Shape<N>::B, LP = Shape<N>::LP;
+  __shared__ C sm[B * LP];
+  const int kz = blockIdx.y, l = threadIdx.x % B, t = threadIdx.x / B, y = blockIdx.x * B + l;
+  const size_t plane = (size_t) A.nx * A.ny;
+  C acc[E];
+#pragma unroll
+  for (int j = 0; j < E; j++) acc[j] = make_float2(0.f, 0.f);
+  for (int in = 0; in < A.nin; in++) {
+    const C *src = A.src[in] + kz * plane + y;
+    C v[E];
+#pragma unroll
+    for (int q = 0; q < E; q++) v[q] = src[(size_t) (t + TL * q) * A.ny];
+    transform<N>(v, t, l, -1.f, tw, sm);
+    for (int o = 0; o < A.nout; o++) {
+      if (o == multi) {
+        for (int tm = A.t0[o]; tm < A.t0[o] + A.nterm[o]; tm++) {
+          if (A.in[tm] != in) continue;
+#pragma unroll
+          for (int j = 0; j < E; j++) acc[j] = acc[j] + kmul(A, tm, v[j], final_pos<N>(t, j), y, kz);
+        }
+        continue;
+      }
+      const int tm = A.t0[o];
+      if (A.in[tm] != in) continue;
+      C w[E];
+#pragma unroll
+      for (int j = 0; j < E; j++) w[j] = kmul(A, tm, v[j], final_pos<N>(t, j), y, kz);
+      to_input_order<N>(w);
+      transform<N>(w, t, l, 1.f, tw, sm);
+      C *dst = A.dst[o] + kz * plane + y;
+#pragma unroll
+      for (int j = 0; j < E; j++) {
+        C r = w[j];
+        const size_t off = (size_t) final_pos<N>(t, j) * A.ny;
+        if (A.acc_out[o]) r = r + dst[off];
+        dst[off] = r;
+      }
+    }
+  }
+  if (multi >= 0) {
+    to_input_order<N>(acc);
+    transform<N>(acc, t, l, 1.f, tw, sm);
+    C *dst = A.dst[multi] + kz * plane + y;
+#pragma unroll
+    for (int j = 0; j < E; j++) {
+      C r = acc[j];
+      const size_t off = (size_t) final_pos<N>(t, j) * A.ny;
+      if (A.acc_out[multi]) r = r + dst[off];
+      dst[off] = r;
+    }
+  }
+}
+
+// psi(k) *= exp(cdt k^2) / N between forward and inverse x transforms
+template <int N>
+__global__ void __launch_bounds__(256) xkinetic_kernel(const C *__restrict__ tw, C *data, int nx, int ny, int nz,
+                                                      float2 cdt, float inv_n, float dkx, float dky, float dkz) {
+  constexpr int E = Shape<N>::E, TL = Shape<N>::TL, B = Shape<N>::B, LP = Shape<N>::LP;
+  __shared__ C sm[B * LP];
+  const int kz = blockIdx.y, l = threadIdx.x % B, t = threadIdx.x / B, y = blockIdx.x * B + l;
+  C *base = data + kz * (size_t) nx * ny + y;
+  C v[E];
+#pragma unroll
+  for (int q = 0; q < E; q++) v[q] = base[(size_t) (t + TL * q) * ny];
+  transform<N>(v, t, l, -1.f, tw, sm);
+  const float kzv = (float) (kz < (nz + 1) / 2 ? kz : kz - nz) * dkz;
+  const float kyv = (float) (y < (ny + 1) / 2 ? y : y - ny) * dky;
+#pragma unroll
+  for (int j = 0; j < E; j++) {
+    const int x = final_pos<N>(t, j);
+    const float kxv = (float) (x < (nx + 1) / 2 ? x : x - nx) * dkx;
+    const float k2 = kxv * kxv + kyv * kyv + kzv * kzv;
+    float sn, cs;
+    const float e = expf(cdt.x * k2) * inv_n;
+    sincosf(cdt.y * k2, &sn, &cs);
+    v[j] = cmul(v[j], make_float2(e * cs, e * sn));
+  }
+  to_input_order<N>(v);
+  transform<N>(v, t, l, 1.f, tw, sm);
+#pragma unroll
+  for (int j = 0; j < E; j++) base[(size_t) final_pos<N>(t, j) * ny] = v[j];
+}
+
+}  // namespace ff
+}  // namespace dftgpu

@@ -92,8 +92,96 @@ int choose_tile(int n, int nb, size_t cplx_bytes, int nbufs, int *B, size_t *sme
   return DFTGPU_ERR_SIZE;
 }
 
+bool generic_fft_only() {
+  static int v = -1;
+  if (v < 0) {
+    const char *e = getenv("DFTGPU_GENERIC_FFT");
+    v = (e && e[0] == '1') ? 1 : 0;
+  }
+  return v == 1;
+}
+
+namespace {
+
+double xconv_bytes(const XConvArgs<float> &A, int kxh, int kyh) {
+  const double spec = (double) A.nkz * A.nx * A.ny * sizeof(float2);
+  double bytes = spec * A.nin;
+  for (int o = 0; o < A.nout; o++) bytes += spec * (A.out[o].accumulate ? 2 : 1);
+  const float *seen[XC_MAX_TERMS];
+  int nseen = 0;
+  for (int t = 0; t < XC_MAX_TERMS; t++) {
+    const float *k = A.term[t].ker;
+    if (!k || A.term[t].kind == KER_UNIT) continue;
+    bool dup = false;
+    for (int s = 0; s < nseen; s++) dup |= seen[s] == k;
+    if (!dup) { seen[nseen++] = k; bytes += (double) A.nkz * kxh * kyh * sizeof(float); }
+  }
+  return bytes;
+}
+
+template <int N> int fast_xconv(const XConvArgs<float> &A) {
+  constexpr int B = ff::Shape<N>::B;
+  if (A.ny % B || A.nin > 4 || A.nout > 8) return -1;
+  ff::XArgsF F;
+  memset(&F, 0, sizeof(F));
+  F.nx = A.nx; F.ny = A.ny; F.kxh = A.nx / 2 + 1; F.kyh = A.ny / 2 + 1;
+  F.nin = A.nin; F.nout = A.nout;
+  for (int i = 0; i < A.nin; i++) F.src[i] = A.src[i];
+  int multi = -1, nt = 0;
+  for (int o = 0; o < A.nout; o++) {
+    F.dst[o] = A.out[o].dst;
+    F.acc_out[o] = A.out[o].accumulate;
+    F.t0[o] = A.out[o].t0;
+    F.nterm[o] = A.out[o].nt;
+    if (A.out[o].nt > 1) {
+      if (multi >= 0) return -1;   // at most one output accumulated in registers
+      multi = o;
+    }
+    if (A.out[o].nt < 1) return -1;
+    nt = A.out[o].t0 + A.out[o].nt > nt ? A.out[o].t0 + A.out[o].nt : nt;
+  }
+  if (nt > 16) return -1;
+  for (int t = 0; t < nt; t++) {
+    F.ker[t] = A.term[t].ker; F.kind[t] = A.term[t].kind; F.in[t] = A.term[t].in; F.coef[t] = A.term[t].coef;
+  }
+  FftPlan<float> p;
+  DFT_TRY(get_plan<float>(N, &p));
+  ProfScope prof("fft_x_conv", xconv_bytes(A, F.kxh, F.kyh));
+  ff::xconv_kernel<N><<<dim3(A.ny / B, A.nkz), 256, 0, rt().stream>>>(p.tw, F, multi);
+  DFT_CHECK_LAUNCH();
+  return DFTGPU_OK;
+}
+
+template <int N> int fast_xkinetic(const KinArgs<float> &A) {
+  constexpr int B = ff::Shape<N>::B;
+  if (A.ny % B) return -1;
+  FftPlan<float> p;
+  DFT_TRY(get_plan<float>(N, &p));
+  ProfScope prof("fft_x_kinetic", 2.0 * A.nx * A.ny * A.nz * sizeof(float2));
+  ff::xkinetic_kernel<N><<<dim3(A.ny / B, A.nz), 256, 0, rt().stream>>>(
+      p.tw, A.data, A.nx, A.ny, A.nz, make_float2((float) A.cdt.x, (float) A.cdt.y), (float) A.inv_n,
+      (float) A.dkx, (float) A.dky, (float) A.dkz);
+  DFT_CHECK_LAUNCH();
+  return DFTGPU_OK;
+}
+
+}  // namespace
+
 template <typename T> int launch_xconv(XConvArgs<T> &A) {
   typedef typename cplx_t<T>::type C;
+  if constexpr (std::is_same<T, float>::value) {
+    if (!generic_fft_only()) {
+      int rc = -1;
+      switch (A.nx) {
+        case 64: rc = fast_xconv<64>(A); break;
+        case 128: rc = fast_xconv<128>(A); break;
+        case 256: rc = fast_xconv<256>(A); break;
+        case 512: rc = fast_xconv<512>(A); break;
+        default: break;
+      }
+      if (rc >= 0) return rc;
+    }
+  }
   DFT_TRY(get_plan<T>(A.nx, &A.plan));
   int B; size_t smem;
   DFT_TRY(choose_tile(A.nx, A.ny, sizeof(C), A.nin + 2, &B, &smem));
@@ -129,6 +217,19 @@ template <typename T> int launch_xconv(XConvArgs<T> &A) {
 
 template <typename T> int launch_xkinetic(KinArgs<T> &A) {
   typedef typename cplx_t<T>::type C;
+  if constexpr (std::is_same<T, float>::value) {
+    if (!generic_fft_only()) {
+      int rc = -1;
+      switch (A.nx) {
+        case 64: rc = fast_xkinetic<64>(A); break;
+        case 128: rc = fast_xkinetic<128>(A); break;
+        case 256: rc = fast_xkinetic<256>(A); break;
+        case 512: rc = fast_xkinetic<512>(A); break;
+        default: break;
+      }
+      if (rc >= 0) return rc;
+    }
+  }
   DFT_TRY(get_plan<T>(A.nx, &A.plan));
   int B; size_t smem;
   DFT_TRY(choose_tile(A.nx, A.ny, sizeof(C), 2, &B, &smem));

@@ -19,7 +19,10 @@
 // FP64 on the host and rounded once to the bulk precision.
 #pragma once
 
+#include <type_traits>
+
 #include "common.cuh"
+#include "fast_fft.cuh"
 
 namespace dftgpu {
 
@@ -393,22 +396,57 @@ template <class Kernel> struct SmemOptIn { static bool done; };
 template <class Kernel> bool SmemOptIn<Kernel>::done = false;
 }  // namespace
 
+bool generic_fft_only();   // DFTGPU_GENERIC_FFT=1 disables the register kernels
+
+// FP32 power-of-two lengths: register-resident kernel.  EF / EFS: the fast
+// address index of the load / store side is the element (1) or the line (0).
+// Returns -1 when the shape does not fit the kernel (caller falls back).
+template <int N, int MODE, int EF, int EFS, class Ld, class St>
+int launch_fast_lines(int na, int nb, float sign, const Ld &ld, const St &st) {
+  static_assert(MODE != LINE_R2C || (EF == 1 && EFS == 0), "r2c z pass: element-fast load, line-fast store");
+  static_assert(MODE != LINE_C2R || (EF == 0 && EFS == 1), "c2r z pass: line-fast load, element-fast store");
+  constexpr int MAP = (EF == 0 && EFS == 0) ? ff::MAP_L : ff::MAP_E;
+  constexpr int LDS = (EF == 0 && EFS == 1) ? 1 : 0;
+  constexpr int STS = (EF == 1 && EFS == 0) ? 1 : 0;
+  constexpr int B = ff::Shape<N>::B;
+  if (nb % B) return -1;
+  FftPlan<float> p1, p2;
+  DFT_TRY(get_plan<float>(N, &p1));
+  p2.tw = nullptr;
+  if (MODE != LINE_C2C) DFT_TRY(get_plan<float>(2 * N, &p2));
+  ff::line_kernel<N, MODE, MAP, LDS, STS, Ld, St><<<dim3(nb / B, na), 256, 0, rt().stream>>>(p1.tw, p2.tw, sign, ld, st);
+  DFT_CHECK_LAUNCH();
+  return DFTGPU_OK;
+}
+
 // extra_bytes: algorithmic bytes read / written by the fused functors beyond
 // the transformed line data itself (e.g. the potential read by a phase load).
-template <typename T, int MODE, class Ld, class St>
-int launch_lines(int n_fft, int na, int nb, T sign, int e_fast, int e_fast_store, const Ld &ld, const St &st,
-                 double extra_bytes = 0.0) {
+template <typename T, int MODE, int EF, int EFS, class Ld, class St>
+int launch_lines(int n_fft, int na, int nb, T sign, const Ld &ld, const St &st, double extra_bytes = 0.0) {
   typedef typename cplx_t<T>::type C;
   const double lines = (double) na * nb;
   const double data = MODE == LINE_C2C ? 2.0 * n_fft : (2.0 * n_fft + 1.0);
   ProfScope prof(MODE == LINE_C2C ? "fft_line_c2c" : (MODE == LINE_R2C ? "fft_line_r2c" : "fft_line_c2r"),
                  lines * data * sizeof(C) + extra_bytes);
+  if constexpr (std::is_same<T, float>::value) {
+    if (!generic_fft_only()) {
+      int rc = -1;
+      switch (n_fft) {
+        case 64: rc = launch_fast_lines<64, MODE, EF, EFS>(na, nb, sign, ld, st); break;
+        case 128: rc = launch_fast_lines<128, MODE, EF, EFS>(na, nb, sign, ld, st); break;
+        case 256: rc = launch_fast_lines<256, MODE, EF, EFS>(na, nb, sign, ld, st); break;
+        case 512: rc = launch_fast_lines<512, MODE, EF, EFS>(na, nb, sign, ld, st); break;
+        default: break;
+      }
+      if (rc >= 0) return rc;
+    }
+  }
   LineArgs<T> args;
   DFT_TRY(get_plan<T>(n_fft, &args.plan));
   args.sign = sign;
   args.nb = nb;
-  args.e_fast = e_fast;
-  args.e_fast_store = e_fast_store;
+  args.e_fast = EF;
+  args.e_fast_store = EFS;
   args.tw2 = nullptr;
   if (MODE != LINE_C2C) {
     FftPlan<T> p2;

@@ -221,7 +221,7 @@ template <typename T> int strang(wf *g, cgrid *dst, cgrid *src, cgrid *V, double
   const T hr = (T) (0.5 * dr), hi = (T) (0.5 * di);
   PhaseLoad<T> ld{(const C *) src->value, (const C *) V->value, ny, nz, hr, hi};
   SpecStoreZ<T> sz{spec, nx, ny};
-  DFT_TRY((launch_lines<T, LINE_C2C>(nz, nx, ny, (T) -1, 1, 0, ld, sz)));
+  DFT_TRY((launch_lines<T, LINE_C2C, 1, 0>(nz, nx, ny, (T) -1, ld, sz)));
   DFT_TRY(ypass<T>(spec, nx, ny, nz, (T) -1));
   KinArgs<T> K;
   K.nx = nx; K.ny = ny; K.nz = nz;
@@ -236,7 +236,7 @@ template <typename T> int strang(wf *g, cgrid *dst, cgrid *src, cgrid *V, double
   DFT_TRY(ypass<T>(spec, nx, ny, nz, (T) 1));
   SpecLoadZ<T> lz{spec, nx, ny};
   PhaseStore<T> st{(C *) dst->value, (const C *) V->value, ny, nz, hr, hi};
-  return launch_lines<T, LINE_C2C>(nz, nx, ny, (T) 1, 0, 1, lz, st);
+  return launch_lines<T, LINE_C2C, 0, 1>(nz, nx, ny, (T) 1, lz, st);
 }
 
 int propagate(wf *g, cgrid *dst, cgrid *src, cgrid *V, double dr, double di) {
@@ -253,10 +253,10 @@ template <typename T> int cfft3_forward(cgrid *src, typename cplx_t<T>::type *sp
   const int nx = (int) src->nx, ny = (int) src->ny, nz = (int) src->nz;
   CplxLoad<T> ld{(const typename cplx_t<T>::type *) src->value, ny, nz};
   SpecStoreZ<T> sz{spec, nx, ny};
-  DFT_TRY((launch_lines<T, LINE_C2C>(nz, nx, ny, (T) -1, 1, 0, ld, sz)));
+  DFT_TRY((launch_lines<T, LINE_C2C, 1, 0>(nz, nx, ny, (T) -1, ld, sz)));
   DFT_TRY(ypass<T>(spec, nx, ny, nz, (T) -1));
   SpecLineXT<T> io{spec, nx, ny};
-  return launch_lines<T, LINE_C2C>(nx, nz, ny, (T) -1, 0, 0, io, io);
+  return launch_lines<T, LINE_C2C, 0, 0>(nx, nz, ny, (T) -1, io, io);
 }
 
 template <typename T> int kinetic_energy_t(wf *g, double *out) {
@@ -347,7 +347,7 @@ template <typename T> static int rspectrum_t(rgrid *g, double *host) {
   RealPairLoad<T> ld{(const T *) g->value, ny, nz};
   int rc = rfft_zy<T>(ld, spec, nx, ny, nz);
   SpecLineXT<T> io{spec, nx, ny};
-  if (!rc) rc = launch_lines<T, LINE_C2C>(nx, nzh, ny, (T) -1, 0, 0, io, io);
+  if (!rc) rc = launch_lines<T, LINE_C2C, 0, 0>(nx, nzh, ny, (T) -1, io, io);
   std::vector<C> h(ns);
   if (!rc && (cudaMemcpyAsync(h.data(), spec, ns * sizeof(C), cudaMemcpyDeviceToHost, rt().stream) != cudaSuccess ||
               cudaStreamSynchronize(rt().stream) != cudaSuccess)) rc = DFTGPU_ERR_CUDA;

@@ -140,14 +140,14 @@ template <typename T> struct CplxLoad {
 // y passes over nkz planes of a spectral buffer
 template <typename T> int ypass(typename cplx_t<T>::type *spec, int nx, int ny, int nkz, T sign) {
   SpecLineY<T> io{spec, nx, ny};
-  return launch_lines<T, LINE_C2C>(ny, nkz, nx, sign, 1, 1, io, io);
+  return launch_lines<T, LINE_C2C, 1, 1>(ny, nkz, nx, sign, io, io);
 }
 
 // forward r2c of a real field through its z and y passes, with a custom
 // packed-pair loader (fused producer); spec is [nz/2+1][nx][ny]
 template <typename T, class Ld> int rfft_zy(const Ld &ld, typename cplx_t<T>::type *spec, int nx, int ny, int nz) {
   SpecStoreZ<T> st{spec, nx, ny};
-  DFT_TRY((launch_lines<T, LINE_R2C>(nz / 2, nx, ny, (T) -1, 1, 0, ld, st)));
+  DFT_TRY((launch_lines<T, LINE_R2C, 1, 0>(nz / 2, nx, ny, (T) -1, ld, st)));
   return ypass<T>(spec, nx, ny, nz / 2 + 1, (T) -1);
 }
 
@@ -155,7 +155,7 @@ template <typename T, class Ld> int rfft_zy(const Ld &ld, typename cplx_t<T>::ty
 template <typename T, class St> int irfft_yz(typename cplx_t<T>::type *spec, const St &st, int nx, int ny, int nz) {
   DFT_TRY(ypass<T>(spec, nx, ny, nz / 2 + 1, (T) 1));
   SpecLoadZ<T> ld{spec, nx, ny};
-  return launch_lines<T, LINE_C2R>(nz / 2, nx, ny, (T) 1, 0, 1, ld, st);
+  return launch_lines<T, LINE_C2R, 0, 1>(nz / 2, nx, ny, (T) 1, ld, st);
 }
 
 }  // namespace dftgpu

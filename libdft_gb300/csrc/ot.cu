@@ -124,7 +124,7 @@ static int rfft3_fp64(const double *f, double2 *spec, const OtPriv *P) {
   RealPairLoad<double> ld{f, P->ny, P->nz};
   DFT_TRY((rfft_zy<double>(ld, spec, P->nx, P->ny, P->nz)));
   SpecLineXT<double> io{spec, P->nx, P->ny};
-  return launch_lines<double, LINE_C2C>(P->nx, P->nz / 2 + 1, P->ny, -1.0, 0, 0, io, io);
+  return launch_lines<double, LINE_C2C, 0, 0>(P->nx, P->nz / 2 + 1, P->ny, -1.0, io, io);
 }
 
 // octant [kz][kx][ky] of the (re or im) spectrum, times (-1)^(kx+ky+kz) * scale

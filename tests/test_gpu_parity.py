@@ -102,7 +102,8 @@ def test_potential_and_energy_density_match_reference(gpu, prec, fixture):
 
 
 @pytest.mark.parametrize("shape,step,model", [((32, 32, 32), 0.8, 9), ((40, 36, 30), 0.7, 1), ((48, 32, 40), 1.0, 8),
-                                              ((96, 80, 128), 0.8, 9)])
+                                              ((96, 80, 128), 0.8, 9), ((64, 64, 64), 0.8, 9),
+                                              ((128, 64, 80), 0.8, 9), ((64, 128, 128), 0.8, 1)])
 def test_potential_vs_oracle_live(gpu, port, prec, shape, step, model):
     psi = liquid_psi(shape, step, 3)
     ns = (2, 4) if np.prod(shape) > 200000 else (4, 32)      # coarser kernel sampling on big grids (CPU time)
