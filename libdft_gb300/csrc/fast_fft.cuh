@@ -276,8 +276,8 @@ __device__ __forceinline__ C kmul(const XArgsF &A, int tm, C v, int kx, int ky, 
 // Inputs are processed one after the other (forward FFT in registers).  An
 // output with one term is produced right after its input; at most one output
 // with several terms is accumulated in registers and produced at the end.
-template <int N>
-__global__ void __launch_bounds__(256) xconv_kernel(const C *__restrict__ tw, const XArgsF A, int multi) {
+template <int N, bool MULTI>
+__global__ void __launch_bounds__(256, MULTI ? 1 : 2) xconv_kernel(const C *__restrict__ tw, const XArgsF A, int multi) {
   constexpr int E = Shape<N>::E, TL = Shape<N>::TL, B = Shape<N>::B, LP = Shape<N>::LP;
   __shared__ C sm[B * LP];
   const int kz = blockIdx.y, l = threadIdx.x % B, t = threadIdx.x / B, y = blockIdx.x * B + l;
@@ -292,7 +292,7 @@ __global__ void __launch_bounds__(256) xconv_kernel(const C *__restrict__ tw, co
     for (int q = 0; q < E; q++) v[q] = src[(size_t) (t + TL * q) * A.ny];
     transform<N>(v, t, l, -1.f, tw, sm);
     for (int o = 0; o < A.nout; o++) {
-      if (o == multi) {
+      if (MULTI && o == multi) {
         for (int tm = A.t0[o]; tm < A.t0[o] + A.nterm[o]; tm++) {
           if (A.in[tm] != in) continue;
 #pragma unroll
@@ -317,7 +317,7 @@ __global__ void __launch_bounds__(256) xconv_kernel(const C *__restrict__ tw, co
       }
     }
   }
-  if (multi >= 0) {
+  if (MULTI && multi >= 0) {
     to_input_order<N>(acc);
     transform<N>(acc, t, l, 1.f, tw, sm);
     C *dst = A.dst[multi] + kz * plane + y;

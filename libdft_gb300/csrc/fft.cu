@@ -147,7 +147,8 @@ template <int N> int fast_xconv(const XConvArgs<float> &A) {
   FftPlan<float> p;
   DFT_TRY(get_plan<float>(N, &p));
   ProfScope prof("fft_x_conv", xconv_bytes(A, F.kxh, F.kyh));
-  ff::xconv_kernel<N><<<dim3(A.ny / B, A.nkz), 256, 0, rt().stream>>>(p.tw, F, multi);
+  if (multi >= 0) ff::xconv_kernel<N, true><<<dim3(A.ny / B, A.nkz), 256, 0, rt().stream>>>(p.tw, F, multi);
+  else ff::xconv_kernel<N, false><<<dim3(A.ny / B, A.nkz), 256, 0, rt().stream>>>(p.tw, F, multi);
   DFT_CHECK_LAUNCH();
   return DFTGPU_OK;
 }

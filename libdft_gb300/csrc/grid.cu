@@ -306,7 +306,7 @@ template <typename T> int scale_by_norm_t(cgrid *c, const double *slot, double t
     C z = p[i];
     z.x *= f; z.y *= f;
     p[i] = z;
-  });
+  }, 4.0 * gsize(c) * sizeof(T), "normalize");
 }
 
 int scale_by_norm(cgrid *c, const double *slot, double target) {
@@ -420,7 +420,8 @@ template <typename T> static int cmuladd_t(cgrid *g, double mr, double mi, doubl
   typedef typename cplx_t<T>::type C;
   C *p = (C *) g->value;
   const C m = mk<T>((T) mr, (T) mi), a = mk<T>((T) ar, (T) ai);
-  return launch_each(gsize(g), [=] __device__(size_t i) { p[i] = cmul(p[i], m) + a; });
+  return launch_each(gsize(g), [=] __device__(size_t i) { p[i] = cmul(p[i], m) + a; }, 4.0 * gsize(g) * sizeof(T),
+                     "cgrid_muladd");
 }
 int cmuladd(cgrid *g, double mr, double mi, double ar, double ai) {
   return g->prec == DFTGPU_FP32 ? cmuladd_t<float>(g, mr, mi, ar, ai) : cmuladd_t<double>(g, mr, mi, ar, ai);
@@ -437,7 +438,7 @@ template <typename T> static int r2c_t(cgrid *d, rgrid *s, int mode) {
     else if (mode == 1) v.x += q[i];
     else v.y += q[i];
     p[i] = v;
-  });
+  }, (mode == 0 ? 3.0 : 5.0) * gsize(d) * sizeof(T), "real_to_complex");
 }
 int real_to_complex(cgrid *d, rgrid *s, int mode) {
   return d->prec == DFTGPU_FP32 ? r2c_t<float>(d, s, mode) : r2c_t<double>(d, s, mode);
@@ -472,7 +473,8 @@ template <typename T> static int density_t(cgrid *c, rgrid *d) {
   typedef typename cplx_t<T>::type C;
   const C *p = (const C *) c->value;
   T *q = (T *) d->value;
-  return launch_each(gsize(c), [=] __device__(size_t i) { const C z = p[i]; q[i] = z.x * z.x + z.y * z.y; });
+  return launch_each(gsize(c), [=] __device__(size_t i) { const C z = p[i]; q[i] = z.x * z.x + z.y * z.y; },
+                     3.0 * gsize(c) * sizeof(T), "density");
 }
 int density(cgrid *c, rgrid *d) {
   return c->prec == DFTGPU_FP32 ? density_t<float>(c, d) : density_t<double>(c, d);

@@ -23,6 +23,40 @@ template <class F> int launch_each(size_t n, F f, double bytes = 0.0, const char
   return DFTGPU_OK;
 }
 
+// One CTA per (x, y) row of an [nx][ny][nz] grid, threads along z: the
+// lambda gets f(x, y, z, i) with i the linear index, no index division.
+template <class F> __global__ void rows_kernel(int ny, int nz, F f) {
+  const int y = blockIdx.x, x = blockIdx.y;
+  const int base = (x * ny + y) * nz;
+  for (int z = threadIdx.x; z < nz; z += blockDim.x) f(x, y, z, base + z);
+}
+
+template <class F> int launch_rows(int nx, int ny, int nz, F f, double bytes = 0.0, const char *name = "pointwise") {
+  int bd = nz < 256 ? ((nz + 31) / 32) * 32 : 256;
+  ProfScope prof(name, bytes);
+  rows_kernel<<<dim3(ny, nx), bd, 0, rt().stream>>>(ny, nz, f);
+  DFT_CHECK_LAUNCH();
+  return DFTGPU_OK;
+}
+
+// periodic neighbours of (x, y, z) along axis a, by comparison (no division)
+struct Stencil3 {
+  int nx, ny, nz;
+  __device__ __forceinline__ void nb(int x, int y, int z, int i, int a, int &ip, int &im) const {
+    if (a == 0) {
+      const int s = ny * nz;
+      ip = x + 1 < nx ? i + s : i + s - nx * s;
+      im = x > 0 ? i - s : i - s + nx * s;
+    } else if (a == 1) {
+      ip = y + 1 < ny ? i + nz : i + nz - ny * nz;
+      im = y > 0 ? i - nz : i - nz + ny * nz;
+    } else {
+      ip = z + 1 < nz ? i + 1 : i + 1 - nz;
+      im = z > 0 ? i - 1 : i - 1 + nz;
+    }
+  }
+};
+
 // ---------------------------------------------------------------- reductions
 // Deterministic FP64 sum of f(i) over i < n: a fixed grid of RED_BLOCKS
 // blocks each sums a fixed strided subset, block partials are combined by a

@@ -246,17 +246,6 @@ template <typename T> static void xc_term(XConvArgs<T> &A, int in, const T *ker,
   o.nt++;
 }
 
-// periodic neighbour offsets for the central difference along axis a
-struct Stencil {
-  int nx, ny, nz;
-  __device__ void nb(size_t i, int a, size_t &ip, size_t &im) const {
-    const int k = (int) (i % nz), j = (int) ((i / nz) % ny), x = (int) (i / ((size_t) ny * nz));
-    if (a == 0) { ip = ((size_t) ((x + 1) % nx) * ny + j) * nz + k; im = ((size_t) ((x - 1 + nx) % nx) * ny + j) * nz + k; }
-    else if (a == 1) { ip = ((size_t) x * ny + (j + 1) % ny) * nz + k; im = ((size_t) x * ny + (j - 1 + ny) % ny) * nz + k; }
-    else { ip = ((size_t) x * ny + j) * nz + (k + 1) % nz; im = ((size_t) x * ny + j) * nz + (k - 1 + nz) % nz; }
-  }
-};
-
 template <typename T> __device__ __forceinline__ T clampv(T v, T cap) { return v > cap ? cap : (v < -cap ? -cap : v); }
 
 // ------------------------------------------------------------------ potential
@@ -265,9 +254,9 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
   OtPriv *P = (OtPriv *) otf->priv;
   Fields<T> F{P, P->nx, P->ny, P->nz};
   const int nx = P->nx, ny = P->ny, nz = P->nz;
-  const size_t n = (size_t) nx * ny * nz;
+  const double nb = (double) nx * ny * nz * sizeof(T);   // bytes of one real field
   const bool kc = otf->model & DFT_OT_KC, bf = otf->model & DFT_OT_BACKFLOW;
-  const Stencil S{nx, ny, nz};
+  const Stencil3 S{nx, ny, nz};
   C *pot = (C *) Pg->value;
   const C *psi = (const C *) gwf->grid->value;
   T *rho = (T *) otf->density->value;
@@ -315,7 +304,7 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
     const double vf = 1.0 / (gwf->mass * 2.0 * P->step), deps = otf->div_epsilon;
     const bool clampv_on = otf->max_veloc < (999.0 / GRID_AUTOMPS);
     const T vcap = (T) otf->max_veloc;
-    DFT_TRY(launch_each(n, [=] __device__(size_t i) {
+    DFT_TRY(launch_rows(nx, ny, nz, [=] __device__(int x, int y, int z, int i) {
       const T b = rb[i], rh = rho[i];
       // src/ot.c:530, 557-567, 574-581
       C p = pot[i];
@@ -327,20 +316,20 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
         rst[i] = st;
         T *sa[3] = { s0, s1, s2 };
         for (int a = 0; a < 3; a++) {
-          size_t ip, im; S.nb(i, a, ip, im);
+          int ip, im; S.nb(x, y, z, i, a, ip, im);
           sa[a][i] = (rho[ip] - rho[im]) * inv2h * st;
         }
       }
       if (bf) {  // velocity src/ot.c:390-395; C, B_a inputs src/ot.c:852-888
-        const C z = psi[i];
-        double rr = (double) z.x * z.x + (double) z.y * z.y;
+        const C pz = psi[i];
+        double rr = (double) pz.x * pz.x + (double) pz.y * pz.y;
         if (rr < deps) rr = deps;
         const double g0 = vf / rr;
         T va[3];
         for (int a = 0; a < 3; a++) {
-          size_t ip, im; S.nb(i, a, ip, im);
+          int ip, im; S.nb(x, y, z, i, a, ip, im);
           const C d = psi[ip] - psi[im];
-          T vv = (T) (g0 * ((double) z.x * d.y - (double) z.y * d.x));
+          T vv = (T) (g0 * ((double) pz.x * d.y - (double) pz.y * d.x));
           if (clampv_on) vv = clampv<T>(vv, vcap);
           va[a] = vv;
         }
@@ -348,7 +337,7 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
         e[i] = (va[2] * va[2] + va[1] * va[1] + va[0] * va[0]) * rh;
         b0[i] = va[0] * rh; b1[i] = va[1] * rh; b2[i] = va[2] * rh;
       }
-    }));
+    }, nb * (7 + (kc ? 5 : 0) + (bf ? 9 : 0)), "ot_pointwise_1"));
   }
 
   // forward transforms of the produced fields
@@ -399,7 +388,7 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
     T *wq = r[R_WQ], *rst = r[R_RST], *t1 = r[R_T1], *J0 = r[R_J0], *J1 = r[R_J1], *J2 = r[R_J2];
     T *d0 = r[R_D0], *d1 = r[R_D1], *d2 = r[R_D2], *h = r[R_H];
     T *v0 = r[R_V0], *v1 = r[R_V1], *v2 = r[R_V2], *A = r[R_A], *Cc = r[R_C], *B0 = r[R_BB0], *B1 = r[R_BB1], *B2 = r[R_BB2];
-    DFT_TRY(launch_each(n, [=] __device__(size_t i) {
+    DFT_TRY(launch_rows(nx, ny, nz, [=] __device__(int x, int y, int z, int i) {
       C p = pot[i];
       p.x += wq[i];
       if (kc) {  // src/ot.c:643-645, 673-675 summed over axes
@@ -407,7 +396,7 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
         const T *Ja[3] = { J0, J1, J2 };
         T hv = 0;
         for (int a = 0; a < 3; a++) {
-          size_t ip, im; S.nb(i, a, ip, im);
+          int ip, im; S.nb(x, y, z, i, a, ip, im);
           hv += (rho[ip] - rho[im]) * inv2h * Ja[a][i];   // src/ot.c:656-657
         }
         h[i] = hv;
@@ -420,7 +409,7 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
         v0[i] = x * a - B0[i]; v1[i] = y * a - B1[i]; v2[i] = z * a - B2[i];
       }
       pot[i] = p;
-    }));
+    }, nb * (5 + (kc ? 10 : 0) + (bf ? 11 : 0)), "ot_pointwise_2"));
   }
 
   if (kc) {  // F * h  (src/ot.c:656-664 summed over axes)
@@ -437,7 +426,7 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
     const T eps = (T) otf->div_epsilon, pcap = (T) otf->max_bfpot;
     const bool clampp = otf->max_bfpot < (10000.0 / GRID_AUTOK);
     T *hf = r[R_HF], *w0 = r[R_V0], *w1 = r[R_V1], *w2 = r[R_V2];
-    DFT_TRY(launch_each(n, [=] __device__(size_t i) {
+    DFT_TRY(launch_rows(nx, ny, nz, [=] __device__(int x, int y, int z, int i) {
       C p = pot[i];
       if (kc) p.x += c * hf[i];
       if (bf) {  // src/ot.c:933-990
@@ -446,18 +435,18 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
         if (rr < eps) rr = eps;
         T im = 0;
         for (int a = 0; a < 3; a++) {
-          size_t ip, imm; S.nb(i, a, ip, imm);
+          int ip, imm; S.nb(x, y, z, i, a, ip, imm);
           im += (T) 0.5 * (((rho[ip] - rho[imm]) * inv2h) / rr) * wa[a][i];
         }
         for (int a = 0; a < 3; a++) {
-          size_t ip, imm; S.nb(i, a, ip, imm);
+          int ip, imm; S.nb(x, y, z, i, a, ip, imm);
           im += (T) 0.5 * ((wa[a][ip] - wa[a][imm]) * inv2h);
         }
         if (clampp) im = clampv<T>(im, pcap);
         p.y += im * cbf;
       }
       pot[i] = p;
-    }));
+    }, nb * (4 + (kc ? 1 : 0) + (bf ? 4 : 0)), "ot_pointwise_3"));
   }
   return DFTGPU_OK;
 }
@@ -472,9 +461,9 @@ template <typename T> static int energy_density_t(dft_ot_functional *otf, rgrid 
   OtPriv *P = (OtPriv *) otf->priv;
   Fields<T> F{P, P->nx, P->ny, P->nz};
   const int nx = P->nx, ny = P->ny, nz = P->nz;
-  const size_t n = (size_t) nx * ny * nz;
+  const double nb = (double) nx * ny * nz * sizeof(T);   // bytes of one real field
   const bool kc = otf->model & DFT_OT_KC, bf = otf->model & DFT_OT_BACKFLOW;
-  const Stencil S{nx, ny, nz};
+  const Stencil3 S{nx, ny, nz};
   const C *psi = (const C *) gwf->grid->value;
   T *rho = (T *) otf->density->value, *ed = (T *) edg->value;
   enum { R_U, R_RB, R_RT, R_A, R_RST, R_S0, R_S1, R_S2, R_V0, R_V1, R_V2, R_E, R_B0, R_B1, R_B2, R_NREAL };
@@ -503,7 +492,7 @@ template <typename T> static int energy_density_t(dft_ot_functional *otf, rgrid 
     const double vf = 1.0 / (gwf->mass * 2.0 * P->step);
     T *u = r[R_U], *rb = r[R_RB], *rt = r[R_RT], *A = r[R_A], *rst = r[R_RST], *s0 = r[R_S0], *s1 = r[R_S1], *s2 = r[R_S2];
     T *v0 = r[R_V0], *v1 = r[R_V1], *v2 = r[R_V2], *e = r[R_E], *b0 = r[R_B0], *b1 = r[R_B1], *b2 = r[R_B2];
-    DFT_TRY(launch_each(n, [=] __device__(size_t i) {
+    DFT_TRY(launch_rows(nx, ny, nz, [=] __device__(int x, int y, int z, int i) {
       const T rh = rho[i], b = rb[i];
       // src/ot-energy.c:70-93
       T acc = (T) 0.5 * rh * u[i] + (c2 / (T) 2) * ((b * b) * rh) + (c3 / (T) 3) * ((b * b * b) * rh);
@@ -512,20 +501,20 @@ template <typename T> static int energy_density_t(dft_ot_functional *otf, rgrid 
         rst[i] = st;
         T *sa[3] = { s0, s1, s2 };
         for (int a = 0; a < 3; a++) {
-          size_t ip, im; S.nb(i, a, ip, im);
+          int ip, im; S.nb(x, y, z, i, a, ip, im);
           sa[a][i] = (rho[ip] - rho[im]) * inv2h * st;
         }
       }
       if (bf) {  // src/ot-energy.c:231-251 (velocity regularised with DFT_EPS)
-        const C z = psi[i];
-        double rr = (double) z.x * z.x + (double) z.y * z.y;
+        const C pz = psi[i];
+        double rr = (double) pz.x * pz.x + (double) pz.y * pz.y;
         if (rr < DFT_EPS) rr = DFT_EPS;
         const double g0 = vf / rr;
         T va[3];
         for (int a = 0; a < 3; a++) {
-          size_t ip, im; S.nb(i, a, ip, im);
+          int ip, im; S.nb(x, y, z, i, a, ip, im);
           const C d = psi[ip] - psi[im];
-          va[a] = (T) (g0 * ((double) z.x * d.y - (double) z.y * d.x));
+          va[a] = (T) (g0 * ((double) pz.x * d.y - (double) pz.y * d.x));
         }
         v0[i] = va[0]; v1[i] = va[1]; v2[i] = va[2];
         const T vv = va[0] * va[0] + va[1] * va[1] + va[2] * va[2];
@@ -534,7 +523,7 @@ template <typename T> static int energy_density_t(dft_ot_functional *otf, rgrid 
         b0[i] = rh * va[0]; b1[i] = rh * va[1]; b2[i] = rh * va[2];
       }
       ed[i] = acc;
-    }));
+    }, nb * (4 + (kc ? 5 : 0) + (bf ? 10 : 0)), "ed_pointwise_1"));
   }
   if (kc) {
     for (int a = 0; a < 3; a++) DFT_TRY(F.fwd(r[R_S0 + a], s[1 + a]));
@@ -559,13 +548,13 @@ template <typename T> static int energy_density_t(dft_ot_functional *otf, rgrid 
     const T inv2h = (T) (1.0 / (2.0 * P->step));
     T *rst = r[R_RST], *t0 = r[R_S0], *t1 = r[R_S1], *t2 = r[R_S2];
     T *v0 = r[R_V0], *v1 = r[R_V1], *v2 = r[R_V2], *cc = r[R_E], *B0 = r[R_B0], *B1 = r[R_B1], *B2 = r[R_B2];
-    DFT_TRY(launch_each(n, [=] __device__(size_t i) {
+    DFT_TRY(launch_rows(nx, ny, nz, [=] __device__(int x, int y, int z, int i) {
       T acc = ed[i];
       const T rh = rho[i];
       if (kc) {  // src/ot-energy.c:176-190
         const T *ta[3] = { t0, t1, t2 };
         for (int a = 0; a < 3; a++) {
-          size_t ip, im; S.nb(i, a, ip, im);
+          int ip, im; S.nb(x, y, z, i, a, ip, im);
           acc += f * (ta[a][i] * ((rho[ip] - rho[im]) * inv2h) * rst[i]);
         }
       }
@@ -576,7 +565,7 @@ template <typename T> static int energy_density_t(dft_ot_functional *otf, rgrid 
         acc += -(cm / (T) 4) * (cc[i] * rh);
       }
       ed[i] = acc;
-    }));
+    }, nb * (3 + (kc ? 5 : 0) + (bf ? 8 : 0)), "ed_pointwise_2"));
   }
   return DFTGPU_OK;
 }
