@@ -206,8 +206,9 @@ def run_gpu(args):
 
     # ---- accuracy: FP32 vs FP64 energy per atom after the same steps from psi0
     acc_steps = args.acc_steps
-    energies = {}
-    for prec in (G.FP32, G.FP64):
+    energies = {G.FP32: (float("nan"), float("nan")), G.FP64: (float("nan"), float("nan"))}
+    ms64, k64 = float("nan"), 1
+    for prec in (() if args.fp32_only else (G.FP32, G.FP64)):
         w, wp, ot, P, mu0 = gpu_setup(G, prec, psi0)
         ot.run(w, wp, P, None, mu0, dt, acc_steps, True)
         e, n, mu = ot.energy_report(w)
@@ -335,6 +336,7 @@ def main():
     ap.add_argument("--acc-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--grid", type=int, default=256, help="grid points per axis (profiling of smaller cases)")
+    ap.add_argument("--fp32-only", action="store_true", help="skip the FP64 and accuracy phases (profiling runs)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -298,11 +298,19 @@ int norm_dev(cgrid *c, double *slot) {
 }
 
 // psi *= sqrt(target / norm) with norm read from the device slot
+// factor sqrt(target / norm) computed once in FP64, stored in the grid's precision
+template <typename T> __global__ void norm_factor_kernel(const double *slot, double target, T *factor) {
+  *factor = (T) sqrt(target / slot[0]);
+}
+
 template <typename T> int scale_by_norm_t(cgrid *c, const double *slot, double target) {
   typedef typename cplx_t<T>::type C;
   C *p = (C *) c->value;
+  T *factor = (T *) (reduce_slots() + 48);   // scratch slot, written here and read below on the same stream
+  norm_factor_kernel<T><<<1, 1, 0, rt().stream>>>(slot, target, factor);
+  DFT_CHECK_LAUNCH();
   return launch_each(gsize(c), [=] __device__(size_t i) {
-    const T f = (T) sqrt(target / slot[0]);
+    const T f = *factor;
     C z = p[i];
     z.x *= f; z.y *= f;
     p[i] = z;

@@ -322,14 +322,14 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
       }
       if (bf) {  // velocity src/ot.c:390-395; C, B_a inputs src/ot.c:852-888
         const C pz = psi[i];
-        double rr = (double) pz.x * pz.x + (double) pz.y * pz.y;
-        if (rr < deps) rr = deps;
-        const double g0 = vf / rr;
+        T rr = pz.x * pz.x + pz.y * pz.y;             // velocity in the grid's precision
+        if (rr < (T) deps) rr = (T) deps;
+        const T g0 = (T) vf / rr;
         T va[3];
         for (int a = 0; a < 3; a++) {
           int ip, im; S.nb(x, y, z, i, a, ip, im);
           const C d = psi[ip] - psi[im];
-          T vv = (T) (g0 * ((double) pz.x * d.y - (double) pz.y * d.x));
+          T vv = g0 * (pz.x * d.y - pz.y * d.x);
           if (clampv_on) vv = clampv<T>(vv, vcap);
           va[a] = vv;
         }
@@ -507,14 +507,14 @@ template <typename T> static int energy_density_t(dft_ot_functional *otf, rgrid 
       }
       if (bf) {  // src/ot-energy.c:231-251 (velocity regularised with DFT_EPS)
         const C pz = psi[i];
-        double rr = (double) pz.x * pz.x + (double) pz.y * pz.y;
-        if (rr < DFT_EPS) rr = DFT_EPS;
-        const double g0 = vf / rr;
+        T rr = pz.x * pz.x + pz.y * pz.y;
+        if (rr < (T) DFT_EPS) rr = (T) DFT_EPS;
+        const T g0 = (T) vf / rr;
         T va[3];
         for (int a = 0; a < 3; a++) {
           int ip, im; S.nb(x, y, z, i, a, ip, im);
           const C d = psi[ip] - psi[im];
-          va[a] = (T) (g0 * ((double) pz.x * d.y - (double) pz.y * d.x));
+          va[a] = g0 * (pz.x * d.y - pz.y * d.x);
         }
         v0[i] = va[0]; v1[i] = va[1]; v2[i] = va[2];
         const T vv = va[0] * va[0] + va[1] * va[1] + va[2] * va[2];
