@@ -250,22 +250,32 @@ __global__ void __launch_bounds__(256) line_kernel(const C *__restrict__ tw, con
 // LFAST pencils of the spectral layout [kz][x][y]: line (kz, y), element x.
 struct XArgsF {
   int nx, ny, kxh, kyh;
-  int nin, nout;
+  int nin, nout, nslice, pad_;
   const C *src[4];
   C *dst[8];
-  int acc_out[8];         // 1: dst += result
-  int nterm[8], t0[8];    // terms of each output
-  const float *ker[16];
-  int kind[16], in[16];
+  int acc_out[8];             // 1: dst += result
+  int nterm[8], t0[8];        // terms of each output
+  int kind[16], in[16];       // kernel symmetry (0 even, 1 odd x, 2 odd y, 3 odd z, 4 unit), input
+  int slot[16];               // kernel slice used by the term (-1: unit)
   float coef[16];
+  const float *slice_src[8];  // distinct kernel octants of this launch
 };
 
-__device__ __forceinline__ C kmul(const XArgsF &A, int tm, C v, int kx, int ky, int kz) {
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem) {
+  const unsigned s = (unsigned) __cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::); }
+
+// v * K(kx, ky, kz) for term tm; the kernel value comes from this CTA's slice
+// ks[slot][ix][iy - iylo] of the octant
+__device__ __forceinline__ C kmul(const XArgsF &A, const float *ks, int kxh, int B, int tm, C v, int kx, int ky,
+                                  int iyo) {
   const int kind = A.kind[tm];
-  if (kind == 4) return v * A.coef[tm];                                // unit
+  if (kind == 4) return v * A.coef[tm];
   const int ix = kx <= A.nx / 2 ? kx : A.nx - kx;
-  const int iy = ky <= A.ny / 2 ? ky : A.ny - ky;
-  const float kv = __ldg(&A.ker[tm][((size_t) kz * A.kxh + ix) * A.kyh + iy]) * A.coef[tm];
+  const float kv = ks[(A.slot[tm] * kxh + ix) * B + iyo] * A.coef[tm];
   if (kind == 0) return v * kv;
   float sg = 1.f;
   if (kind == 1 && kx > A.nx / 2) sg = -1.f;
@@ -273,60 +283,94 @@ __device__ __forceinline__ C kmul(const XArgsF &A, int tm, C v, int kx, int ky, 
   return make_float2(-sg * kv * v.y, sg * kv * v.x);                   // (i sg kv) v
 }
 
+template <int N> constexpr int xconv_smem(int nslice) {
+  return Shape<N>::B * Shape<N>::LP * (int) sizeof(C) + nslice * (N / 2 + 1) * Shape<N>::B * (int) sizeof(float);
+}
+
 // Inputs are processed one after the other (forward FFT in registers).  An
 // output with one term is produced right after its input; at most one output
-// with several terms is accumulated in registers and produced at the end.
+// with several terms (MULTI) is accumulated in registers and produced at the
+// end.  The launch parameters are staged in shared memory, and this CTA's
+// slice of every kernel octant (all kx, the B ky of its pencils) is fetched
+// with cp.async while the first input is loaded and transformed.
+// Requires B | ny/2 so that a CTA's pencils lie on one side of ny/2.
 template <int N, bool MULTI>
 __global__ void __launch_bounds__(256, MULTI ? 1 : 2) xconv_kernel(const C *__restrict__ tw, const XArgsF A, int multi) {
-  constexpr int E = Shape<N>::E, TL = Shape<N>::TL, B = Shape<N>::B, LP = Shape<N>::LP;
-  __shared__ C sm[B * LP];
-  const int kz = blockIdx.y, l = threadIdx.x % B, t = threadIdx.x / B, y = blockIdx.x * B + l;
+  constexpr int E = Shape<N>::E, TL = Shape<N>::TL, B = Shape<N>::B, LP = Shape<N>::LP, KXH = N / 2 + 1;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C *sm = reinterpret_cast<C *>(smraw);
+  float *ks = reinterpret_cast<float *>(sm + B * LP);
+  __shared__ XArgsF sA;
+  {
+    const int *sw = reinterpret_cast<const int *>(&A);
+    int *dw = reinterpret_cast<int *>(&sA);
+    for (int i = threadIdx.x; i < (int) (sizeof(XArgsF) / sizeof(int)); i += 256) dw[i] = sw[i];
+  }
+  const int kz = blockIdx.y, y0 = blockIdx.x * B, l = threadIdx.x % B, t = threadIdx.x / B, y = y0 + l;
+  const int half = A.ny / 2;
+  const int iylo = y0 < half ? y0 : A.ny - (y0 + B - 1);
+  const int iyo = (y <= half ? y : A.ny - y) - iylo;
+  for (int idx = threadIdx.x; idx < A.nslice * KXH * B; idx += 256) {
+    const int s = idx / (KXH * B), r = idx % (KXH * B), ix = r / B, c = r % B;
+    cp_async4(&ks[idx], A.slice_src[s] + ((size_t) kz * A.kxh + ix) * A.kyh + iylo + c);
+  }
+  cp_async_commit();
   const size_t plane = (size_t) A.nx * A.ny;
-  C acc[E];
+  C acc[MULTI ? E : 1];
+  if constexpr (MULTI) {
 #pragma unroll
-  for (int j = 0; j < E; j++) acc[j] = make_float2(0.f, 0.f);
-  for (int in = 0; in < A.nin; in++) {
-    const C *src = A.src[in] + kz * plane + y;
+    for (int j = 0; j < E; j++) acc[j] = make_float2(0.f, 0.f);
+  }
+  __syncthreads();   // sA ready
+  for (int in = 0; in < sA.nin; in++) {
+    const C *src = sA.src[in] + kz * plane + y;
     C v[E];
 #pragma unroll
     for (int q = 0; q < E; q++) v[q] = src[(size_t) (t + TL * q) * A.ny];
     transform<N>(v, t, l, -1.f, tw, sm);
-    for (int o = 0; o < A.nout; o++) {
+    if (in == 0) {
+      cp_async_wait_all();
+      __syncthreads();   // kernel slices visible to all threads
+    }
+    for (int o = 0; o < sA.nout; o++) {
       if (MULTI && o == multi) {
-        for (int tm = A.t0[o]; tm < A.t0[o] + A.nterm[o]; tm++) {
-          if (A.in[tm] != in) continue;
+        for (int tm = sA.t0[o]; tm < sA.t0[o] + sA.nterm[o]; tm++) {
+          if (sA.in[tm] != in) continue;
 #pragma unroll
-          for (int j = 0; j < E; j++) acc[j] = acc[j] + kmul(A, tm, v[j], final_pos<N>(t, j), y, kz);
+          for (int j = 0; j < E; j++) acc[j] = acc[j] + kmul(sA, ks, KXH, B, tm, v[j], final_pos<N>(t, j), y, iyo);
         }
         continue;
       }
-      const int tm = A.t0[o];
-      if (A.in[tm] != in) continue;
+      const int tm = sA.t0[o];
+      if (sA.in[tm] != in) continue;
       C w[E];
 #pragma unroll
-      for (int j = 0; j < E; j++) w[j] = kmul(A, tm, v[j], final_pos<N>(t, j), y, kz);
+      for (int j = 0; j < E; j++) w[j] = kmul(sA, ks, KXH, B, tm, v[j], final_pos<N>(t, j), y, iyo);
       to_input_order<N>(w);
       transform<N>(w, t, l, 1.f, tw, sm);
-      C *dst = A.dst[o] + kz * plane + y;
+      C *dst = sA.dst[o] + kz * plane + y;
+      const bool accum = sA.acc_out[o];
 #pragma unroll
       for (int j = 0; j < E; j++) {
         C r = w[j];
         const size_t off = (size_t) final_pos<N>(t, j) * A.ny;
-        if (A.acc_out[o]) r = r + dst[off];
+        if (accum) r = r + dst[off];
         dst[off] = r;
       }
     }
   }
-  if (MULTI && multi >= 0) {
-    to_input_order<N>(acc);
-    transform<N>(acc, t, l, 1.f, tw, sm);
-    C *dst = A.dst[multi] + kz * plane + y;
+  if constexpr (MULTI) {
+    if (multi >= 0) {
+      to_input_order<N>(acc);
+      transform<N>(acc, t, l, 1.f, tw, sm);
+      C *dst = sA.dst[multi] + kz * plane + y;
 #pragma unroll
-    for (int j = 0; j < E; j++) {
-      C r = acc[j];
-      const size_t off = (size_t) final_pos<N>(t, j) * A.ny;
-      if (A.acc_out[multi]) r = r + dst[off];
-      dst[off] = r;
+      for (int j = 0; j < E; j++) {
+        C r = acc[j];
+        const size_t off = (size_t) final_pos<N>(t, j) * A.ny;
+        if (sA.acc_out[multi]) r = r + dst[off];
+        dst[off] = r;
+      }
     }
   }
 }

@@ -121,7 +121,7 @@ double xconv_bytes(const XConvArgs<float> &A, int kxh, int kyh) {
 
 template <int N> int fast_xconv(const XConvArgs<float> &A) {
   constexpr int B = ff::Shape<N>::B;
-  if (A.ny % B || A.nin > 4 || A.nout > 8) return -1;
+  if (A.ny % B || (A.ny / 2) % B || A.nin > 4 || A.nout > 8) return -1;
   ff::XArgsF F;
   memset(&F, 0, sizeof(F));
   F.nx = A.nx; F.ny = A.ny; F.kxh = A.nx / 2 + 1; F.kyh = A.ny / 2 + 1;
@@ -141,14 +141,31 @@ template <int N> int fast_xconv(const XConvArgs<float> &A) {
     nt = A.out[o].t0 + A.out[o].nt > nt ? A.out[o].t0 + A.out[o].nt : nt;
   }
   if (nt > 16) return -1;
+  F.nslice = 0;
   for (int t = 0; t < nt; t++) {
-    F.ker[t] = A.term[t].ker; F.kind[t] = A.term[t].kind; F.in[t] = A.term[t].in; F.coef[t] = A.term[t].coef;
+    F.kind[t] = A.term[t].kind; F.in[t] = A.term[t].in; F.coef[t] = A.term[t].coef;
+    F.slot[t] = -1;
+    if (A.term[t].kind == KER_UNIT) continue;
+    for (int s = 0; s < F.nslice; s++)
+      if (F.slice_src[s] == A.term[t].ker) F.slot[t] = s;
+    if (F.slot[t] < 0) {
+      if (F.nslice == 8) return -1;
+      F.slice_src[F.nslice] = A.term[t].ker;
+      F.slot[t] = F.nslice++;
+    }
   }
   FftPlan<float> p;
   DFT_TRY(get_plan<float>(N, &p));
+  const int smem = ff::xconv_smem<N>(F.nslice);
+  static bool attr[2] = { false, false };
+  if (smem > 48 * 1024 && !attr[multi >= 0]) {
+    if (multi >= 0) DFT_CUDA(cudaFuncSetAttribute(ff::xconv_kernel<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) rt().max_smem_optin));
+    else DFT_CUDA(cudaFuncSetAttribute(ff::xconv_kernel<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) rt().max_smem_optin));
+    attr[multi >= 0] = true;
+  }
   ProfScope prof("fft_x_conv", xconv_bytes(A, F.kxh, F.kyh));
-  if (multi >= 0) ff::xconv_kernel<N, true><<<dim3(A.ny / B, A.nkz), 256, 0, rt().stream>>>(p.tw, F, multi);
-  else ff::xconv_kernel<N, false><<<dim3(A.ny / B, A.nkz), 256, 0, rt().stream>>>(p.tw, F, multi);
+  if (multi >= 0) ff::xconv_kernel<N, true><<<dim3(A.ny / B, A.nkz), 256, smem, rt().stream>>>(p.tw, F, multi);
+  else ff::xconv_kernel<N, false><<<dim3(A.ny / B, A.nkz), 256, smem, rt().stream>>>(p.tw, F, multi);
   DFT_CHECK_LAUNCH();
   return DFTGPU_OK;
 }
