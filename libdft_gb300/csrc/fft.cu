@@ -157,11 +157,13 @@ template <int N> int fast_xconv(const XConvArgs<float> &A) {
   FftPlan<float> p;
   DFT_TRY(get_plan<float>(N, &p));
   const int smem = ff::xconv_smem<N>(F.nslice);
-  static bool attr[2] = { false, false };
-  if (smem > 48 * 1024 && !attr[multi >= 0]) {
-    if (multi >= 0) DFT_CUDA(cudaFuncSetAttribute(ff::xconv_kernel<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) rt().max_smem_optin));
-    else DFT_CUDA(cudaFuncSetAttribute(ff::xconv_kernel<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) rt().max_smem_optin));
-    attr[multi >= 0] = true;
+  // request exactly the dynamic shared memory this launch needs (the kernel
+  // also has static shared memory, so the opt-in maximum itself is not valid)
+  static int granted[2] = { 48 * 1024, 48 * 1024 };
+  if (smem > granted[multi >= 0]) {
+    if (multi >= 0) DFT_CUDA(cudaFuncSetAttribute(ff::xconv_kernel<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    else DFT_CUDA(cudaFuncSetAttribute(ff::xconv_kernel<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    granted[multi >= 0] = smem;
   }
   ProfScope prof("fft_x_conv", xconv_bytes(A, F.kxh, F.kyh));
   if (multi >= 0) ff::xconv_kernel<N, true><<<dim3(A.ny / B, A.nkz), 256, smem, rt().stream>>>(p.tw, F, multi);
