@@ -544,13 +544,11 @@ REAL dft_ot_bulk_dispersion(dft_ot_functional *o, REAL *kp, REAL rho0) {
 
 // ------------------------------------------------------------------ fused step
 static int pc_step_impl(dft_ot_functional *otf, wf *gwf, wf *gwfp, cgrid *P, rgrid *vext, double mu0, double dr, double di) {
-  if (vext) DFT_TRY(real_to_complex(P, vext, 0)); else DFT_TRY(cfill(P, 0.0, 0.0));
-  DFT_TRY(ot_potential(otf, P, gwf));
-  DFT_TRY(cmuladd(P, 1.0, 0.0, -mu0, 0.0));
+  // P = Vext + V_OT[psi] - mu0   (the fills and shifts run inside the potential's pointwise passes)
+  DFT_TRY(ot_potential_ex(otf, P, gwf, 1, vext, -mu0, 1.0));
   DFT_TRY(propagate(gwf, gwfp->grid, gwf->grid, P, dr, di));
-  if (vext) DFT_TRY(real_to_complex(P, vext, 1));
-  DFT_TRY(ot_potential(otf, P, gwfp));
-  DFT_TRY(cmuladd(P, 0.5, 0.0, -0.5 * mu0, 0.0));     // (P - mu0) / 2, bit-identical
+  // P = (P + Vext + V_OT[psi_p] - mu0) / 2
+  DFT_TRY(ot_potential_ex(otf, P, gwfp, 0, vext, -mu0, 0.5));
   return propagate(gwf, gwf->grid, gwf->grid, P, dr, di);
 }
 

@@ -197,26 +197,35 @@ __global__ void __launch_bounds__(256) line_kernel(const C *__restrict__ tw, con
 #pragma unroll
     for (int q = 0; q < E; q++) v[q] = ld(a, b0 + l, t + TL * q);
   } else {
-    for (int idx = threadIdx.x; idx < B * N; idx += 256) {
-      const int ll = idx % B, e = idx / B;
-      C z;
+    // line-fast cooperative load of the whole tile (C2R: also the Nyquist
+    // element N, which lands in the pitch's spare slot), fully unrolled so
+    // that every load is in flight before the first shared-memory store
+    constexpr int NE = MODE == 2 ? N + 1 : N, TOT = B * NE, IT = (TOT + 255) / 256;
+#pragma unroll
+    for (int it = 0; it < IT; it++) {
+      const int idx = threadIdx.x + it * 256;
+      if (TOT % 256 == 0 || idx < TOT) {
+        const int ll = idx % B, e = idx / B;
+        sm[sidx(ll, e, LP)] = ld(a, b0 + ll, e);
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < E; q++) {
+      const int e = t + TL * q;
       if constexpr (MODE == 2) {
         // Z[k] = (X[k] + X*[N-k]) + i w^-k (X[k] - X*[N-k]),  w = exp(-2 pi i / 2N)
-        C xk = ld(a, b0 + ll, e), xm = ld(a, b0 + ll, N - e);
+        C xk = sm[sidx(l, e, LP)], xm = sm[sidx(l, N - e, LP)];
         if (e == 0) { xk.y = 0.f; xm.y = 0.f; }
         const C sum = make_float2(xk.x + xm.x, xk.y - xm.y), dif = make_float2(xk.x - xm.x, xk.y + xm.y);
         C w = __ldg(&tw2[e]);
         w.y = -w.y;
         const C tt = cmul(dif, w);
-        z = make_float2(sum.x - tt.y, sum.y + tt.x);
+        v[q] = make_float2(sum.x - tt.y, sum.y + tt.x);
       } else {
-        z = ld(a, b0 + ll, e);
+        v[q] = sm[sidx(l, e, LP)];
       }
-      sm[sidx(ll, e, LP)] = z;
     }
-    __syncthreads();
-#pragma unroll
-    for (int q = 0; q < E; q++) v[q] = sm[sidx(l, t + TL * q, LP)];
     __syncthreads();
   }
   transform<N>(v, t, l, sign, tw, sm);
@@ -229,16 +238,24 @@ __global__ void __launch_bounds__(256) line_kernel(const C *__restrict__ tw, con
     __syncthreads();
     if constexpr (MODE == 1) {
       // X[k] = (Z[k] + Z*[N-k]) / 2 - (i/2) w^k (Z[k] - Z*[N-k]),  k = 0..N
-      for (int idx = threadIdx.x; idx < B * (N + 1); idx += 256) {
-        const int ll = idx % B, k = idx / B;
-        const C zk = sm[sidx(ll, k == N ? 0 : k, LP)], zm = sm[sidx(ll, k == 0 ? 0 : N - k, LP)];
-        const C sum = make_float2(zk.x + zm.x, zk.y - zm.y), dif = make_float2(zk.x - zm.x, zk.y + zm.y);
-        const C w = k == N ? make_float2(-1.f, 0.f) : __ldg(&tw2[k]);
-        const C tt = cmul(dif, w);
-        st(a, b0 + ll, k, make_float2(0.5f * (sum.x + tt.y), 0.5f * (sum.y - tt.x)));
+      constexpr int TOT = B * (N + 1), IT = (TOT + 255) / 256;
+#pragma unroll
+      for (int it = 0; it < IT; it++) {
+        const int idx = threadIdx.x + it * 256;
+        if (idx < TOT) {
+          const int ll = idx % B, k = idx / B;
+          const C zk = sm[sidx(ll, k == N ? 0 : k, LP)], zm = sm[sidx(ll, k == 0 ? 0 : N - k, LP)];
+          const C sum = make_float2(zk.x + zm.x, zk.y - zm.y), dif = make_float2(zk.x - zm.x, zk.y + zm.y);
+          const C w = k == N ? make_float2(-1.f, 0.f) : __ldg(&tw2[k]);
+          const C tt = cmul(dif, w);
+          st(a, b0 + ll, k, make_float2(0.5f * (sum.x + tt.y), 0.5f * (sum.y - tt.x)));
+        }
       }
     } else {
-      for (int idx = threadIdx.x; idx < B * N; idx += 256) {
+      constexpr int IT = B * N / 256;
+#pragma unroll
+      for (int it = 0; it < IT; it++) {
+        const int idx = threadIdx.x + it * 256;
         const int ll = idx % B, e = idx / B;
         st(a, b0 + ll, e, sm[sidx(ll, e, LP)]);
       }

@@ -283,13 +283,20 @@ int kinetic_energy(wf *g, double *out) {
   return g->grid->prec == DFTGPU_FP32 ? kinetic_energy_t<float>(g, out) : kinetic_energy_t<double>(g, out);
 }
 
+// sum |psi|^2 dV: each reduction item is a run of 8 consecutive values summed
+// in the grid's precision (FP32: within 8 ulps of the run's sum), runs are
+// accumulated in FP64 -- one FP64 add per 8 values instead of per value.
+// Grid sizes are products of three even numbers, so 8 divides the count.
 template <typename T> int norm_dev_t(cgrid *c, double *slot) {
   typedef typename cplx_t<T>::type C;
   const C *p = (const C *) c->value;
   const double dv = c->step * c->step * c->step;
-  return reduce_dev<1>(gsize(c), [=] __device__(size_t i, double *v) {
-    const C z = p[i];
-    v[0] = (double) z.x * z.x + (double) z.y * z.y;
+  return reduce_dev<1>(gsize(c) / 8, [=] __device__(size_t r, double *v) {
+    const C *q = p + 8 * r;
+    T s = (T) 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) { const C z = q[k]; s += z.x * z.x + z.y * z.y; }
+    v[0] = (double) s;
   }, slot, dv);
 }
 

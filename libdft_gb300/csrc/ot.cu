@@ -249,7 +249,13 @@ template <typename T> static void xc_term(XConvArgs<T> &A, int in, const T *ker,
 template <typename T> __device__ __forceinline__ T clampv(T v, T cap) { return v > cap ? cap : (v < -cap ? -cap : v); }
 
 // ------------------------------------------------------------------ potential
-template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, wf *gwf) {
+// P <- scale * ((overwrite ? 0 : P) + base + add + V_OT[psi]); base may be NULL.
+// dft_ot_potential is overwrite = 0, base = NULL, add = 0, scale = 1 (src/ot.c:296:
+// the potential is added to P); the predict-correct step folds its
+// P = Vext, -mu0 and *0.5 (examples/imag_time/imag_time.c:231-238) in here.
+template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, wf *gwf, int overwrite, const T *base,
+                                             double add_d, double scale_d) {
+  const T add = (T) add_d, scale = (T) scale_d;
   typedef typename cplx_t<T>::type C;
   OtPriv *P = (OtPriv *) otf->priv;
   Fields<T> F{P, P->nx, P->ny, P->nz};
@@ -307,7 +313,9 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
     DFT_TRY(launch_rows(nx, ny, nz, [=] __device__(int x, int y, int z, int i) {
       const T b = rb[i], rh = rho[i];
       // src/ot.c:530, 557-567, 574-581
-      C p = pot[i];
+      C p = overwrite ? mk<T>((T) 0, (T) 0) : pot[i];
+      if (base) p.x += base[i];
+      p.x += add;
       p.x += u[i] + (c2 / (T) 2) * (b * b) + (c3 / (T) 3) * (b * b * b);
       pot[i] = p;
       q[i] = (c2 * b + c3 * (b * b)) * rh;
@@ -445,6 +453,7 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
         if (clampp) im = clampv<T>(im, pcap);
         p.y += im * cbf;
       }
+      if (scale != (T) 1) { p.x *= scale; p.y *= scale; }
       pot[i] = p;
     }, nb * (4 + (kc ? 1 : 0) + (bf ? 4 : 0)), "ot_pointwise_3"));
   }
@@ -452,7 +461,13 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
 }
 
 int ot_potential(dft_ot_functional *otf, cgrid *P, wf *gwf) {
-  return P->prec == DFTGPU_FP32 ? potential_t<float>(otf, P, gwf) : potential_t<double>(otf, P, gwf);
+  return ot_potential_ex(otf, P, gwf, 0, nullptr, 0.0, 1.0);
+}
+
+int ot_potential_ex(dft_ot_functional *otf, cgrid *P, wf *gwf, int overwrite, rgrid *base, double add, double scale) {
+  return P->prec == DFTGPU_FP32
+             ? potential_t<float>(otf, P, gwf, overwrite, base ? (const float *) base->value : nullptr, add, scale)
+             : potential_t<double>(otf, P, gwf, overwrite, base ? (const double *) base->value : nullptr, add, scale);
 }
 
 // ------------------------------------------------------------------ energy density

@@ -34,6 +34,7 @@ inline void *ot_spec(OtPriv *P, int i) {
 
 int ot_generate_kernels(dft_ot_functional *otf, int min_ns, int max_ns);
 int ot_potential(dft_ot_functional *otf, cgrid *P, wf *gwf);
+int ot_potential_ex(dft_ot_functional *otf, cgrid *P, wf *gwf, int overwrite, rgrid *base, double add, double scale);
 int ot_energy_density(dft_ot_functional *otf, rgrid *ed, wf *gwf);
 
 }  // namespace dftgpu
