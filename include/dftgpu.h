@@ -318,6 +318,37 @@ int dftgpu_run(dft_ot_functional *otf, wf *gwf, wf *gwfp, cgrid *potential, rgri
 int dftgpu_energy_report(dft_ot_functional *otf, wf *gwf, rgrid *vext, double *energy,
                          double *natoms, double *mu);
 
+/* ---- Reverse mode (no reference counterpart: libdft has no adjoint) ----
+ * Cotangent convention: for a real objective J, the cotangent of a complex
+ * field psi is g = 2 dJ/dpsi^* (dJ = Re sum conj(g) dpsi); the cotangent of a
+ * complex potential V is gamma with dJ = sum Re(gamma) dRe V + Im(gamma) dIm V.
+ * Sums run over grid points.  Backflow with max_veloc / max_bfpot limits or
+ * c_bfpot != 1 is not differentiated (DFTGPU_ERR_UNSUPPORTED). */
+/* grad_psi += (d dft_ot_potential / d psi)^H cot (vector-Jacobian product of
+ * the OT potential, src/ot.c:296, with respect to the wave function). */
+int dftgpu_ot_potential_vjp(dft_ot_functional *otf, wf *gwf, cgrid *cot, cgrid *grad_psi);
+/* Adjoint of psi_out = S(pot, dt) psi_in (grid_wf_propagate, libgrid wf
+ * propagation): cot_in = S^H cot_out (cot_in may alias cot_out), cot_pot +=
+ * dJ/dpot.  psi_out must hold S(pot, dt) psi_in. */
+int dftgpu_wf_propagate_vjp(wf *gwf, cgrid *pot, double dt_re, double dt_im, cgrid *psi_in,
+                            cgrid *psi_out, cgrid *cot_out, cgrid *cot_in, cgrid *cot_pot);
+/* Adjoint of one dftgpu_pc_step from psi = gwf (unchanged), followed by
+ * grid_wf_normalize when renorm: on entry cot is the cotangent of the step's
+ * output, on return that of its input; grad_vext (may be NULL) += dJ/dVext. */
+int dftgpu_pc_step_vjp(dft_ot_functional *otf, wf *gwf, rgrid *vext, double mu0, double dt_re,
+                       double dt_im, int renorm, cgrid *cot, rgrid *grad_vext);
+/* J = int (|psi_T|^2 - rho_target)^2 dV after nsteps predict-correct steps
+ * from psi_0 = gwf (gwf is left at psi_T, as dftgpu_run), and its gradient
+ * with respect to every Vext grid value (grad_vext, overwritten) and psi_0
+ * (grad_psi0, cotangent convention above); either may be NULL.  The reverse
+ * sweep recomputes each segment of checkpoint_every steps from a stored
+ * checkpoint (0: ceil(sqrt(nsteps))), holding about 2 sqrt(nsteps) wave
+ * functions on the device.  With both gradients NULL only the forward
+ * sweep and J are computed. */
+int dftgpu_adjoint_run(dft_ot_functional *otf, wf *gwf, rgrid *vext, double mu0, double dt_re,
+                       double dt_im, INT nsteps, int renorm, INT checkpoint_every,
+                       rgrid *rho_target, double *J, rgrid *grad_vext, cgrid *grad_psi0);
+
 #ifndef __cplusplus
 #include <complex.h>
 /* REAL complex forms of the libgrid / libdft entry points (C only). */

@@ -31,6 +31,7 @@ AUTOANG = 0.529177210903
 AUTOK = 3.1577502480407e5
 AUTOFS = 0.024188843265857
 AUTOAMU = 1.0 / 1822.888486209
+AUTOMPS = 2.18769126364e6
 HELIUM_MASS = 4.002602 / AUTOAMU
 
 ERRORS = {0: "ok", 1: "invalid argument", 2: "unsupported size", 3: "out of device memory",
@@ -133,6 +134,10 @@ SIGNATURES = {
     "dftgpu_pc_step": (_i, [_vp, _vp, _vp, _vp, _vp, _d, _d, _d]),
     "dftgpu_run": (_i, [_vp, _vp, _vp, _vp, _vp, _d, _d, _d, _l, _i]),
     "dftgpu_energy_report": (_i, [_vp, _vp, _vp, _dp, _dp, _dp]),
+    "dftgpu_ot_potential_vjp": (_i, [_vp, _vp, _vp, _vp]),
+    "dftgpu_wf_propagate_vjp": (_i, [_vp, _vp, _d, _d, _vp, _vp, _vp, _vp, _vp]),
+    "dftgpu_pc_step_vjp": (_i, [_vp, _vp, _vp, _d, _d, _d, _i, _vp, _vp]),
+    "dftgpu_adjoint_run": (_i, [_vp, _vp, _vp, _d, _d, _d, _l, _i, _l, _vp, _dp, _vp, _vp]),
 }
 
 OPTIONAL = set()   # entry points allowed to be absent (none)
@@ -300,6 +305,12 @@ class Wf:
     def predict(self, wfp: "Wf", pot: CGrid, dt: complex):
         check(lib().dftgpu_wf_propagate_predict(self.ptr, wfp.ptr, pot.ptr, dt.real, dt.imag), "predict")
 
+    def propagate_vjp(self, pot: CGrid, dt: complex, psi_in: CGrid, psi_out: CGrid, cot_out: CGrid, cot_in: CGrid,
+                      cot_pot: CGrid):
+        """cot_in = S(pot,dt)^H cot_out, cot_pot += dJ/dpot (psi_out = S(pot,dt) psi_in)."""
+        check(lib().dftgpu_wf_propagate_vjp(self.ptr, pot.ptr, dt.real, dt.imag, psi_in.ptr, psi_out.ptr, cot_out.ptr,
+                                            cot_in.ptr, cot_pot.ptr), "dftgpu_wf_propagate_vjp")
+
     def correct(self, pot: CGrid, dt: complex):
         check(lib().dftgpu_wf_propagate_correct(self.ptr, pot.ptr, dt.real, dt.imag), "correct")
 
@@ -368,6 +379,29 @@ class OT:
         check(lib().dftgpu_energy_report(self.ptr, wf.ptr, vext.ptr if vext else None, C.byref(e), C.byref(n),
                                          C.byref(mu)), "dftgpu_energy_report")
         return e.value, n.value, mu.value
+
+    # ---- reverse mode (cotangent of psi: g = 2 dJ/dpsi^*)
+    def potential_vjp(self, wf: Wf, cot: CGrid, grad_psi: CGrid):
+        """grad_psi += (dV_OT/dpsi)^H cot."""
+        check(lib().dftgpu_ot_potential_vjp(self.ptr, wf.ptr, cot.ptr, grad_psi.ptr), "dftgpu_ot_potential_vjp")
+
+    def pc_step_vjp(self, wf: Wf, vext: RGrid | None, mu0: float, dt: complex, renorm: bool, cot: CGrid,
+                    grad_vext: RGrid | None = None):
+        """cot <- cotangent of the step input; grad_vext += dJ/dVext."""
+        check(lib().dftgpu_pc_step_vjp(self.ptr, wf.ptr, vext.ptr if vext else None, mu0, dt.real, dt.imag,
+                                       int(renorm), cot.ptr, grad_vext.ptr if grad_vext else None),
+              "dftgpu_pc_step_vjp")
+
+    def adjoint_run(self, wf: Wf, vext: RGrid | None, mu0: float, dt: complex, nsteps: int, renorm: bool,
+                    rho_target: RGrid, grad_vext: RGrid | None = None, grad_psi0: CGrid | None = None,
+                    checkpoint_every: int = 0) -> float:
+        """J = int (|psi_T|^2 - rho_target)^2 dV after nsteps steps, with its gradients."""
+        J = C.c_double()
+        check(lib().dftgpu_adjoint_run(self.ptr, wf.ptr, vext.ptr if vext else None, mu0, dt.real, dt.imag, nsteps,
+                                       int(renorm), checkpoint_every, rho_target.ptr, C.byref(J),
+                                       grad_vext.ptr if grad_vext else None, grad_psi0.ptr if grad_psi0 else None),
+              "dftgpu_adjoint_run")
+        return J.value
 
     def free(self):
         if self.ptr:

@@ -448,6 +448,7 @@ void dft_ot_free(dft_ot_functional *otf) {
     for (int i = 0; i < OT_MAX_SPEC; i++) dev_free(P->spec[i]);
     cgrid_free(P->pot_tmp);
     rgrid_free(P->ed_tmp);
+    adj_free(P);
     delete P;
   }
   rgrid_free(otf->density);

@@ -17,9 +17,8 @@
 #include <math.h>
 #include <string.h>
 
-#include "ops.cuh"
 #include "grid_internal.cuh"
-#include "ot_internal.cuh"
+#include "ot_work.cuh"
 
 namespace dftgpu {
 
@@ -210,43 +209,6 @@ done:
   return rc;
 }
 
-// ------------------------------------------------------------------ helpers
-template <typename T> struct Fields {
-  typedef typename cplx_t<T>::type C;
-  OtPriv *P;
-  int nx, ny, nz;
-  T *r(int i) { return (T *) ot_real(P, i); }
-  C *s(int i) { return (C *) ot_spec(P, i); }
-  const T *k(int i) { return (const T *) P->ker[i]; }
-  int fwd(const T *f, C *spec) {
-    RealPairLoad<T> ld{f, ny, nz};
-    return rfft_zy<T>(ld, spec, nx, ny, nz);
-  }
-  int inv(C *spec, T *f) {
-    RealPairStore<T> st{f, ny, nz, (T) 1};
-    return irfft_yz<T>(spec, st, nx, ny, nz);
-  }
-};
-
-template <typename T> static void xc_init(XConvArgs<T> &A, const OtPriv *P) {
-  memset(&A, 0, sizeof(A));
-  A.nx = P->nx; A.ny = P->ny; A.nkz = P->nz / 2 + 1;
-}
-template <typename T> static void xc_in(XConvArgs<T> &A, const typename cplx_t<T>::type *s) { A.src[A.nin++] = s; }
-template <typename T> static void xc_out(XConvArgs<T> &A, typename cplx_t<T>::type *dst, int acc = 0) {
-  XOut<T> &o = A.out[A.nout++];
-  o.dst = dst; o.accumulate = acc;
-  o.t0 = A.nout > 1 ? A.out[A.nout - 2].t0 + A.out[A.nout - 2].nt : 0;
-  o.nt = 0;
-}
-template <typename T> static void xc_term(XConvArgs<T> &A, int in, const T *ker, int kind, T coef) {
-  XOut<T> &o = A.out[A.nout - 1];
-  XTerm<T> &t = A.term[o.t0 + o.nt];
-  t.ker = ker; t.kind = kind; t.in = in; t.coef = coef;
-  o.nt++;
-}
-
-template <typename T> __device__ __forceinline__ T clampv(T v, T cap) { return v > cap ? cap : (v < -cap ? -cap : v); }
 
 // ------------------------------------------------------------------ potential
 // P <- scale * ((overwrite ? 0 : P) + base + add + V_OT[psi]); base may be NULL.
@@ -268,9 +230,7 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
   T *rho = (T *) otf->density->value;
 
   // real-field slots
-  enum { R_U, R_RB, R_RT, R_D0, R_D1, R_D2, R_A, R_Q, R_RST, R_S0, R_S1, R_S2, R_V0, R_V1, R_V2, R_E,
-         R_B0, R_B1, R_B2, R_WQ, R_T1, R_J0, R_J1, R_J2, R_C, R_BB0, R_BB1, R_BB2, R_H, R_HF, R_NREAL };
-  T *r[R_NREAL];
+  T *r[R_NREAL];   // slots of PotSlot (ot_work.cuh)
   for (int i = 0; i < R_NREAL; i++) { r[i] = F.r(i); if (!r[i]) return DFTGPU_ERR_NOMEM; }
   C *s[9];
   for (int i = 0; i < 9; i++) { s[i] = F.s(i); if (!s[i]) return DFTGPU_ERR_NOMEM; }

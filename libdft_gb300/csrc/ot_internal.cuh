@@ -6,8 +6,8 @@
 namespace dftgpu {
 
 enum { OT_LJ = 0, OT_SA = 1, OT_F = 2, OT_FX = 3, OT_FY = 4, OT_FZ = 5, OT_VJ = 6, OT_NKER = 7 };
-constexpr int OT_MAX_REAL = 32;
-constexpr int OT_MAX_SPEC = 10;
+constexpr int OT_MAX_REAL = 80;
+constexpr int OT_MAX_SPEC = 12;
 
 struct OtPriv {
   int prec = DFTGPU_FP64;
@@ -19,6 +19,7 @@ struct OtPriv {
   void *spec[OT_MAX_SPEC] = {};     // (nz/2+1)*nx*ny complex half spectra
   cgrid *pot_tmp = nullptr;         // energy report scratch
   rgrid *ed_tmp = nullptr;
+  void *adj = nullptr;              // adjoint work state (adjoint.cu)
 };
 
 void *dev_alloc(size_t bytes);
@@ -36,5 +37,6 @@ int ot_generate_kernels(dft_ot_functional *otf, int min_ns, int max_ns);
 int ot_potential(dft_ot_functional *otf, cgrid *P, wf *gwf);
 int ot_potential_ex(dft_ot_functional *otf, cgrid *P, wf *gwf, int overwrite, rgrid *base, double add, double scale);
 int ot_energy_density(dft_ot_functional *otf, rgrid *ed, wf *gwf);
+void adj_free(OtPriv *P);
 
 }  // namespace dftgpu

@@ -1,0 +1,63 @@
+// Work-buffer helpers shared by the OT potential (ot.cu) and its adjoint
+// (adjoint.cu): real-field / half-spectrum slots, forward and inverse real
+// transforms, and builders for the x-pencil convolution arguments.
+#pragma once
+
+#include <string.h>
+
+#include "ops.cuh"
+#include "ot_internal.cuh"
+
+namespace dftgpu {
+
+// Real-field slots written by the potential evaluation (potential_t).  After a
+// potential evaluation they hold, for the wave function it was evaluated on:
+// R_U LJ*rho, R_RB rho_bar, R_RT F*rho, R_D0..2 dF_a*rho, R_A V_j*rho,
+// R_Q (c2 rb + c3 rb^2) rho, R_RST rho_st, R_S0..2 G_a = (d_a rho) rho_st,
+// R_V0..2 w_a = v_a A - B_a (BF; the velocity itself is overwritten),
+// R_E rho|v|^2, R_B0..2 rho v_a, R_WQ w*q, R_T1 sum_a dF_a*G_a,
+// R_J0..2 J_a = F*G_a, R_C V_j*(rho|v|^2), R_BB0..2 B_a = V_j*(rho v_a),
+// R_H sum_a (d_a rho) J_a, R_HF F*h.  Slots from R_NREAL on are free.
+enum PotSlot {
+  R_U, R_RB, R_RT, R_D0, R_D1, R_D2, R_A, R_Q, R_RST, R_S0, R_S1, R_S2, R_V0, R_V1, R_V2, R_E,
+  R_B0, R_B1, R_B2, R_WQ, R_T1, R_J0, R_J1, R_J2, R_C, R_BB0, R_BB1, R_BB2, R_H, R_HF, R_NREAL
+};
+
+template <typename T> struct Fields {
+  typedef typename cplx_t<T>::type C;
+  OtPriv *P;
+  int nx, ny, nz;
+  T *r(int i) { return (T *) ot_real(P, i); }
+  C *s(int i) { return (C *) ot_spec(P, i); }
+  const T *k(int i) { return (const T *) P->ker[i]; }
+  int fwd(const T *f, C *spec) {
+    RealPairLoad<T> ld{f, ny, nz};
+    return rfft_zy<T>(ld, spec, nx, ny, nz);
+  }
+  int inv(C *spec, T *f) {
+    RealPairStore<T> st{f, ny, nz, (T) 1};
+    return irfft_yz<T>(spec, st, nx, ny, nz);
+  }
+};
+
+template <typename T> inline void xc_init(XConvArgs<T> &A, const OtPriv *P) {
+  memset(&A, 0, sizeof(A));
+  A.nx = P->nx; A.ny = P->ny; A.nkz = P->nz / 2 + 1;
+}
+template <typename T> inline void xc_in(XConvArgs<T> &A, const typename cplx_t<T>::type *s) { A.src[A.nin++] = s; }
+template <typename T> inline void xc_out(XConvArgs<T> &A, typename cplx_t<T>::type *dst, int acc = 0) {
+  XOut<T> &o = A.out[A.nout++];
+  o.dst = dst; o.accumulate = acc;
+  o.t0 = A.nout > 1 ? A.out[A.nout - 2].t0 + A.out[A.nout - 2].nt : 0;
+  o.nt = 0;
+}
+template <typename T> inline void xc_term(XConvArgs<T> &A, int in, const T *ker, int kind, T coef) {
+  XOut<T> &o = A.out[A.nout - 1];
+  XTerm<T> &t = A.term[o.t0 + o.nt];
+  t.ker = ker; t.kind = kind; t.in = in; t.coef = coef;
+  o.nt++;
+}
+
+template <typename T> __device__ __forceinline__ T clampv(T v, T cap) { return v > cap ? cap : (v < -cap ? -cap : v); }
+
+}  // namespace dftgpu

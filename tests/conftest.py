@@ -43,3 +43,19 @@ def relerr(a, b):
     a = np.asarray(a)
     b = np.asarray(b)
     return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def coords(shape, step):
+    ax = [(np.arange(n) - n // 2) * step for n in shape]
+    return np.meshgrid(*ax, indexing="ij")
+
+
+def liquid_psi(shape, step, seed, amp=0.1):
+    rng = np.random.default_rng(seed)
+    rho0 = 0.0218360 * 0.529177210903 ** 3
+    X, Y, Z = coords(shape, step)
+    L = [n * step for n in shape]
+    rho = rho0 * (1 + amp * np.cos(2 * np.pi * X / L[0]) * np.cos(2 * np.pi * Y / L[1])
+                  + 0.5 * amp * np.sin(4 * np.pi * Z / L[2]))
+    phase = 0.4 * np.sin(2 * np.pi * X / L[0]) + 0.3 * np.cos(2 * np.pi * (Y / L[1] + Z / L[2]))
+    return (np.sqrt(rho) * np.exp(1j * phase) * (1 + 1e-3 * rng.standard_normal(shape))).astype(np.complex128)
