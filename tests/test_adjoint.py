@@ -80,10 +80,12 @@ def test_propagate_vjp_adjoint_identity_and_potential_gradient(gpu, fp64, dt):
     an = float(np.sum(gV.real * dV.real + gV.imag * dV.imag))
     assert abs(fd - an) < 1e-6 * abs(an)
     # cot_in may alias cot_out
+    P.set(V)
     gpi.set(g_out)
     gpot.zero()
     w.propagate_vjp(P, dt, gin, gout, gpi, gpi, gpot)
-    assert relerr(gpi.get(), gpsi) < 1e-14
+    assert np.array_equal(gpi.get(), gpsi)
+    assert np.array_equal(gpot.get(), gV)
     for o in grids + [P, w]:
         o.free()
 
@@ -162,15 +164,13 @@ def test_adjoint_run_gradients_match_gpu_finite_differences(gpu, fp64, model, dt
     assert J0 == J(V0, psi)
     G, Gp = gv.get(), gp.get()
     an = float(np.sum(G * dV))
-    h = 1e-2
-    fd = (J(V0 + h * dV, psi) - J(V0 - h * dV, psi)) / (2 * h)
-    assert abs(fd - an) < 2e-6 * abs(an), (fd, an)
+    errs = [abs((J(V0 + h * dV, psi) - J(V0 - h * dV, psi)) / (2 * h) / an - 1) for h in (1e-1, 1e-2)]
+    assert min(errs) < 2e-6, errs
     rng = np.random.default_rng(3)
     d = 0.05 * np.abs(psi) * (rng.standard_normal(shape) + 1j * rng.standard_normal(shape))
     an = rdot(Gp, d)
-    h = 1e-2
-    fd = (J(V0, psi + h * d) - J(V0, psi - h * d)) / (2 * h)
-    assert abs(fd - an) < 2e-6 * abs(an), (fd, an)
+    errs = [abs((J(V0, psi + h * d) - J(V0, psi - h * d)) / (2 * h) / an - 1) for h in (1e-2, 1e-3)]
+    assert min(errs) < 2e-6, errs
     for o in (gp, gv, rt, vext, ot, w):
         o.free()
 
