@@ -163,6 +163,31 @@ def profile_step(G, w, wp, ot, P, mu0, dt):
     return json.loads(buf.value.decode())
 
 
+def time_adjoint(G, torch, w, ot, mu0, dt, nsteps, every):
+    """dJ/dVext and dJ/dpsi_0 of J = int (|psi_T|^2 - rho_t)^2 dV over nsteps
+    renormalised steps (forward sweep, checkpoints every `every` steps, reverse
+    sweep recomputing each segment), timed with CUDA events on the library's stream."""
+    shape = (NX, NX, NX)
+    psi = w.get()
+    vext, rt, gv = G.RGrid(shape, STEP), G.RGrid(shape, STEP), G.RGrid(shape, STEP)
+    gp = G.CGrid(shape, STEP)
+    vext.set(np.zeros(shape))
+    rt.set(np.abs(psi) ** 2 * 1.01)
+    ot.adjoint_run(w, vext, mu0, dt, 2, True, rt, gv, gp, checkpoint_every=every)    # allocations
+    w.set(psi)
+    G.synchronize()
+    torch.cuda.synchronize()
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0.record()
+    ot.adjoint_run(w, vext, mu0, dt, nsteps, True, rt, gv, gp, checkpoint_every=every)
+    t1.record()
+    torch.cuda.synchronize()
+    ms = t0.elapsed_time(t1)
+    ok = bool(np.isfinite(gv.get()).all())
+    free_all(gp, gv, rt, vext)
+    return ms, ok
+
+
 def run_gpu(args):
     import torch
     import libdft_gb300 as G
@@ -202,6 +227,8 @@ def run_gpu(args):
         ot.run(w, wp, P, None, mu0, dt, 1, True)
         G.check(L.cgrid_copy_to_host_raw(w.grid_ptr, host.data_ptr()), "d2h")
     e2e_s = time.perf_counter() - te
+    adj_steps, adj_every = 9, 3
+    ms_adj, adj_ok = time_adjoint(G, torch, w, ot, mu0, dt, adj_steps, adj_every)
     free_all(P, ot, wp, w)
 
     # ---- accuracy: FP32 vs FP64 energy per atom after the same steps from psi0
@@ -262,6 +289,11 @@ def run_gpu(args):
                    "l2": "inputs larger than L2 (psi 134 MB FP32); no flush", "parallelism": "replicas"},
         "e2e": {"value": world * ke / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": 2 * N * 4,
                 "d2h_bytes_per_step": 2 * N * 4},
+        "adjoint": {"value": world * adj_steps / (ms_adj * 1e-3), "unit": "trajectory steps/s",
+                    "what": "gradient of a final-density objective w.r.t. Vext and psi_0: forward sweep + "
+                            "checkpointed reverse sweep (dftgpu_adjoint_run), FP32",
+                    "nsteps": adj_steps, "checkpoint_every": adj_every, "ms_per_step": ms_adj / adj_steps,
+                    "cost_over_forward_step": (ms_adj / adj_steps) / (ms / K), "finite": adj_ok},
         "fp64": {"value": steps_s64, "unit": "steps/s", "steps": k64, "ms_per_step": ms64 / k64},
         "fp32_over_fp64": steps_s / steps_s64,
         "accuracy": {"steps": acc_steps, "E_per_atom_K_fp32": e32 * 3.1577502480407e5,

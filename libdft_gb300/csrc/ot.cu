@@ -3,17 +3,17 @@
 //
 // Potential dataflow (full model), one forward r2c per produced field and
 // one inverse c2r per needed real field; linearity merges the reference's
-// per-axis KC transforms:
+// per-axis KC transforms and every term that enters the potential linearly:
 //   rho = |psi|^2 ;  rho^ = F rho
-//   x pass 1 (one input, up to 7 outputs): V_LJ rho^, w rho^, F rho^,
-//             dF_a rho^ (a = x,y,z), V_j rho^
-//   pointwise 1: P.re += u_LJ + c2/2 rb^2 + c3/3 rb^3 ; q = (c2 rb + c3 rb^2) rho
+//   x pass 1 (one input): w rho^, F rho^, dF_a rho^ (a = x,y,z), V_j rho^
+//   pointwise 1: P.re += c2/2 rb^2 + c3/3 rb^3 ; q = (c2 rb + c3 rb^2) rho
 //             KC: rho_st, s_a = (d_a rho) rho_st ;  BF: v, rho|v|^2, rho v_a
-//   x pass 2: w q^ ; sum_a dF_a s_a^ ; F s_a^ (-> J_a) ; V_j (rho|v|^2)^, V_j (rho v_a)^
-//   pointwise 2: P.re += w*q + c rho_st sum_a(dF_a*s_a) - c sum_a J_a (dF_a*rho)
-//             KC: h = sum_a (d_a rho) J_a ;  BF real part, w_a = v_a A - B_a
-//   x pass 3 (KC): F h^ ;  pointwise 3: P.re += c F*h ; BF imaginary part.
-// KC count: 1 + 3 + 1 forward, 4 + 4 + 1 inverse instead of src/ot.c's 19.
+//   x pass 2: sum_a dF_a s_a^ ; F s_a^ (-> J_a) ; V_j (rho v_a)^ (-> B_a)
+//   pointwise 2: P.re += c rho_st sum_a(dF_a*s_a) - c sum_a J_a (dF_a*rho)
+//             KC: h = sum_a (d_a rho) J_a ;  BF: -m/2 (A|v|^2 - 2 v.B), w_a = v_a A - B_a
+//   x pass 3: V_LJ rho^ + w q^ + c F h^ - m/2 V_j (rho|v|^2)^  (one output)
+//   pointwise 3: P.re += that linear part ; BF imaginary part.
+// Full model: 10 forward and 14 inverse real transforms (src/ot.c: 34).
 #include <math.h>
 #include <string.h>
 
@@ -215,6 +215,10 @@ done:
 // dft_ot_potential is overwrite = 0, base = NULL, add = 0, scale = 1 (src/ot.c:296:
 // the potential is added to P); the predict-correct step folds its
 // P = Vext, -mu0 and *0.5 (examples/imag_time/imag_time.c:231-238) in here.
+//
+// Spectral slots: s0 rho^, s1-3 s_a^ -> J_a^, s4 (rho|v|^2)^, s5-7 (rho v_a)^ ->
+// B_a^, s8 sum_a dF_a s_a^, s9 q^, s10 h^ (or V_j (rho|v|^2)^ when the backflow
+// potential is clamped), s11 the merged linear part.
 template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, wf *gwf, int overwrite, const T *base,
                                              double add_d, double scale_d) {
   const T add = (T) add_d, scale = (T) scale_d;
@@ -224,6 +228,9 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
   const int nx = P->nx, ny = P->ny, nz = P->nz;
   const double nb = (double) nx * ny * nz * sizeof(T);   // bytes of one real field
   const bool kc = otf->model & DFT_OT_KC, bf = otf->model & DFT_OT_BACKFLOW;
+  // the backflow real part is merged into the linear part unless it is clamped
+  const bool clampp = otf->max_bfpot < (10000.0 / GRID_AUTOK);
+  const bool cmerge = bf && !clampp;
   const Stencil3 S{nx, ny, nz};
   C *pot = (C *) Pg->value;
   const C *psi = (const C *) gwf->grid->value;
@@ -232,16 +239,15 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
   // real-field slots
   T *r[R_NREAL];   // slots of PotSlot (ot_work.cuh)
   for (int i = 0; i < R_NREAL; i++) { r[i] = F.r(i); if (!r[i]) return DFTGPU_ERR_NOMEM; }
-  C *s[9];
-  for (int i = 0; i < 9; i++) { s[i] = F.s(i); if (!s[i]) return DFTGPU_ERR_NOMEM; }
+  C *s[12];
+  for (int i = 0; i < 12; i++) { s[i] = F.s(i); if (!s[i]) return DFTGPU_ERR_NOMEM; }
 
   DFT_TRY(density(gwf->grid, otf->density));                                   // src/ot.c:320
   DFT_TRY(F.fwd(rho, s[0]));
 
-  // x pass 1: one input, kernels LJ, SA (+F, dF_a) (+V_j)
+  // x pass 1: one input, kernels SA (+F, dF_a) (+V_j); rho^ stays in s0
   {
     XConvArgs<T> A; xc_init(A, P); xc_in(A, (const C *) s[0]);
-    xc_out(A, s[1]); xc_term(A, 0, F.k(OT_LJ), KER_EVEN, (T) 1);
     xc_out(A, s[2]); xc_term(A, 0, F.k(OT_SA), KER_EVEN, (T) 1);
     if (kc) {
       xc_out(A, s[3]); xc_term(A, 0, F.k(OT_F), KER_EVEN, (T) 1);
@@ -251,7 +257,6 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
     }
     if (bf) { xc_out(A, s[7]); xc_term(A, 0, F.k(OT_VJ), KER_EVEN, (T) 1); }
     DFT_TRY(launch_xconv<T>(A));
-    DFT_TRY(F.inv(s[1], r[R_U]));
     DFT_TRY(F.inv(s[2], r[R_RB]));
     if (kc) {
       DFT_TRY(F.inv(s[3], r[R_RT]));
@@ -263,7 +268,7 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
   // pointwise 1
   {
     const T c2 = (T) otf->c2, c3 = (T) otf->c3, irs = (T) (1.0 / otf->rho_0s);
-    T *u = r[R_U], *rb = r[R_RB], *rt = r[R_RT], *q = r[R_Q], *rst = r[R_RST];
+    T *rb = r[R_RB], *rt = r[R_RT], *q = r[R_Q], *rst = r[R_RST];
     T *s0 = r[R_S0], *s1 = r[R_S1], *s2 = r[R_S2];
     T *v0 = r[R_V0], *v1 = r[R_V1], *v2 = r[R_V2], *e = r[R_E], *b0 = r[R_B0], *b1 = r[R_B1], *b2 = r[R_B2];
     const T inv2h = (T) (1.0 / (2.0 * P->step));
@@ -272,11 +277,11 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
     const T vcap = (T) otf->max_veloc;
     DFT_TRY(launch_rows(nx, ny, nz, [=] __device__(int x, int y, int z, int i) {
       const T b = rb[i], rh = rho[i];
-      // src/ot.c:530, 557-567, 574-581
+      // src/ot.c:557-567 (the LJ term src/ot.c:530 is in the merged linear part)
       C p = overwrite ? mk<T>((T) 0, (T) 0) : pot[i];
       if (base) p.x += base[i];
       p.x += add;
-      p.x += u[i] + (c2 / (T) 2) * (b * b) + (c3 / (T) 3) * (b * b * b);
+      p.x += (c2 / (T) 2) * (b * b) + (c3 / (T) 3) * (b * b * b);
       pot[i] = p;
       q[i] = (c2 * b + c3 * (b * b)) * rh;
       if (kc) {  // src/ot.c:608-612, 632-637
@@ -305,11 +310,11 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
         e[i] = (va[2] * va[2] + va[1] * va[1] + va[0] * va[0]) * rh;
         b0[i] = va[0] * rh; b1[i] = va[1] * rh; b2[i] = va[2] * rh;
       }
-    }, nb * (7 + (kc ? 5 : 0) + (bf ? 9 : 0)), "ot_pointwise_1"));
+    }, nb * (5 + (kc ? 5 : 0) + (bf ? 9 : 0)), "ot_pointwise_1"));
   }
 
   // forward transforms of the produced fields
-  DFT_TRY(F.fwd(r[R_Q], s[0]));
+  DFT_TRY(F.fwd(r[R_Q], s[9]));
   if (kc) for (int a = 0; a < 3; a++) DFT_TRY(F.fwd(r[R_S0 + a], s[1 + a]));
   if (bf) {
     DFT_TRY(F.fwd(r[R_E], s[4]));
@@ -317,12 +322,6 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
   }
 
   // x pass 2
-  {
-    XConvArgs<T> A; xc_init(A, P); xc_in(A, (const C *) s[0]);
-    xc_out(A, s[0]); xc_term(A, 0, F.k(OT_SA), KER_EVEN, (T) 1);               // w q^   (src/ot.c:582-585)
-    DFT_TRY(launch_xconv<T>(A));
-    DFT_TRY(F.inv(s[0], r[R_WQ]));
-  }
   if (kc) {
     XConvArgs<T> A; xc_init(A, P);
     for (int a = 0; a < 3; a++) xc_in(A, (const C *) s[1 + a]);
@@ -339,26 +338,25 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
     DFT_TRY(F.inv(s[8], r[R_T1]));
     for (int a = 0; a < 3; a++) DFT_TRY(F.inv(s[1 + a], r[R_J0 + a]));
   }
-  if (bf) {
+  if (bf) {   // B_a = V_j (rho v_a)^ in place (+ C = V_j (rho|v|^2)^ when clamped)
     XConvArgs<T> A; xc_init(A, P);
-    for (int a = 0; a < 4; a++) xc_in(A, (const C *) s[4 + a]);
-    for (int a = 0; a < 4; a++) { xc_out(A, s[4 + a]); xc_term(A, a, F.k(OT_VJ), KER_EVEN, (T) 1); }
+    for (int a = 0; a < 3; a++) xc_in(A, (const C *) s[5 + a]);
+    for (int a = 0; a < 3; a++) { xc_out(A, s[5 + a]); xc_term(A, a, F.k(OT_VJ), KER_EVEN, (T) 1); }
+    if (!cmerge) { xc_in(A, (const C *) s[4]); xc_out(A, s[10]); xc_term(A, 3, F.k(OT_VJ), KER_EVEN, (T) 1); }
     DFT_TRY(launch_xconv<T>(A));
-    DFT_TRY(F.inv(s[4], r[R_C]));
+    if (!cmerge) DFT_TRY(F.inv(s[10], r[R_C]));
     for (int a = 0; a < 3; a++) DFT_TRY(F.inv(s[5 + a], r[R_BB0 + a]));
   }
 
   // pointwise 2
-  {
+  if (kc || bf) {
     const T c = (T) (otf->alpha_s / (2.0 * otf->mass)), hm = (T) (-0.5 * otf->mass), cbf = (T) otf->c_bfpot;
-    const bool clampp = otf->max_bfpot < (10000.0 / GRID_AUTOK);
     const T pcap = (T) otf->max_bfpot, inv2h = (T) (1.0 / (2.0 * P->step));
-    T *wq = r[R_WQ], *rst = r[R_RST], *t1 = r[R_T1], *J0 = r[R_J0], *J1 = r[R_J1], *J2 = r[R_J2];
+    T *rst = r[R_RST], *t1 = r[R_T1], *J0 = r[R_J0], *J1 = r[R_J1], *J2 = r[R_J2];
     T *d0 = r[R_D0], *d1 = r[R_D1], *d2 = r[R_D2], *h = r[R_H];
     T *v0 = r[R_V0], *v1 = r[R_V1], *v2 = r[R_V2], *A = r[R_A], *Cc = r[R_C], *B0 = r[R_BB0], *B1 = r[R_BB1], *B2 = r[R_BB2];
     DFT_TRY(launch_rows(nx, ny, nz, [=] __device__(int x, int y, int z, int i) {
       C p = pot[i];
-      p.x += wq[i];
       if (kc) {  // src/ot.c:643-645, 673-675 summed over axes
         p.x += c * rst[i] * t1[i] - c * (J0[i] * d0[i] + J1[i] * d1[i] + J2[i] * d2[i]);
         const T *Ja[3] = { J0, J1, J2 };
@@ -369,34 +367,44 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
         }
         h[i] = hv;
       }
-      if (bf) {  // src/ot.c:895-915, 924-931
+      if (bf) {  // src/ot.c:895-915, 924-931; V_j*(rho|v|^2) is in the linear part unless clamped
         const T x = v0[i], y = v1[i], z = v2[i], a = A[i];
-        T re = hm * (a * (z * z + y * y + x * x) - (T) 2 * (x * B0[i] + y * B1[i] + z * B2[i]) + Cc[i]);
-        if (clampp) re = clampv<T>(re, pcap);
+        T re = hm * (a * (z * z + y * y + x * x) - (T) 2 * (x * B0[i] + y * B1[i] + z * B2[i]));
+        if (clampp) re = clampv<T>(re + hm * Cc[i], pcap);
         p.x += re * cbf;
         v0[i] = x * a - B0[i]; v1[i] = y * a - B1[i]; v2[i] = z * a - B2[i];
       }
       pot[i] = p;
-    }, nb * (5 + (kc ? 10 : 0) + (bf ? 11 : 0)), "ot_pointwise_2"));
+    }, nb * (2 + (kc ? 10 : 0) + (bf ? (clampp ? 11 : 10) : 0)), "ot_pointwise_2"));
   }
 
-  if (kc) {  // F * h  (src/ot.c:656-664 summed over axes)
-    DFT_TRY(F.fwd(r[R_H], s[0]));
-    XConvArgs<T> A; xc_init(A, P); xc_in(A, (const C *) s[0]);
-    xc_out(A, s[0]); xc_term(A, 0, F.k(OT_F), KER_EVEN, (T) 1);
+  // merged linear part (one inverse transform):
+  //   V_LJ rho^ + w q^ (src/ot.c:530, 582-585) + c F h^ (KC, src/ot.c:656-664)
+  //   + c_bf (-m/2) V_j (rho|v|^2)^ (BF, src/ot.c:895-915)
+  if (kc) DFT_TRY(F.fwd(r[R_H], s[10]));
+  {
+    XConvArgs<T> A; xc_init(A, P);
+    xc_in(A, (const C *) s[0]);
+    xc_in(A, (const C *) s[9]);
+    if (kc) xc_in(A, (const C *) s[10]);
+    if (cmerge) xc_in(A, (const C *) s[4]);
+    xc_out(A, s[11]);
+    xc_term(A, 0, F.k(OT_LJ), KER_EVEN, (T) 1);
+    xc_term(A, 1, F.k(OT_SA), KER_EVEN, (T) 1);
+    if (kc) xc_term(A, 2, F.k(OT_F), KER_EVEN, (T) (otf->alpha_s / (2.0 * otf->mass)));
+    if (cmerge) xc_term(A, kc ? 3 : 2, F.k(OT_VJ), KER_EVEN, (T) (-0.5 * otf->mass * otf->c_bfpot));
     DFT_TRY(launch_xconv<T>(A));
-    DFT_TRY(F.inv(s[0], r[R_HF]));
+    DFT_TRY(F.inv(s[11], r[R_U]));
   }
 
   // pointwise 3
   {
-    const T c = (T) (otf->alpha_s / (2.0 * otf->mass)), cbf = (T) otf->c_bfpot, inv2h = (T) (1.0 / (2.0 * P->step));
+    const T cbf = (T) otf->c_bfpot, inv2h = (T) (1.0 / (2.0 * P->step));
     const T eps = (T) otf->div_epsilon, pcap = (T) otf->max_bfpot;
-    const bool clampp = otf->max_bfpot < (10000.0 / GRID_AUTOK);
-    T *hf = r[R_HF], *w0 = r[R_V0], *w1 = r[R_V1], *w2 = r[R_V2];
+    T *lin = r[R_U], *w0 = r[R_V0], *w1 = r[R_V1], *w2 = r[R_V2];
     DFT_TRY(launch_rows(nx, ny, nz, [=] __device__(int x, int y, int z, int i) {
       C p = pot[i];
-      if (kc) p.x += c * hf[i];
+      p.x += lin[i];
       if (bf) {  // src/ot.c:933-990
         const T *wa[3] = { w0, w1, w2 };
         T rr = rho[i];
@@ -415,7 +423,7 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
       }
       if (scale != (T) 1) { p.x *= scale; p.y *= scale; }
       pot[i] = p;
-    }, nb * (4 + (kc ? 1 : 0) + (bf ? 4 : 0)), "ot_pointwise_3"));
+    }, nb * (5 + (bf ? 4 : 0)), "ot_pointwise_3"));
   }
   return DFTGPU_OK;
 }

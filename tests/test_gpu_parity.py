@@ -113,6 +113,33 @@ def test_potential_vs_oracle_live(gpu, port, prec, shape, step, model):
         o.free()
 
 
+def test_potential_with_backflow_limits_vs_oracle(gpu, port, prec):
+    """max_veloc, max_bfpot and c_bfpot != 1 (src/ot.c:391-394, 911-914, 985-988)."""
+    shape, step, model = (32, 32, 32), 0.8, 9
+    psi = liquid_psi(shape, step, 5)
+    with Grids(port, shape, step, gpu.HELIUM_MASS) as g:
+        wo = g.wf(psi)
+        full, plain = g.ot(model, wo), g.ot(1, wo)
+        bf_part = g.potential(full, wo) - g.potential(plain, wo)
+        p = g.params(full)
+        vmax = 0.6 * np.abs(np.gradient(np.angle(psi), step, axis=0)).max() / gpu.HELIUM_MASS
+        lim = (p["div_epsilon"], vmax, 0.4 * np.abs(bf_part.real).max(), 0.7)
+        port.lib.orc_ot_set_limits(full, *lim)
+        Pref = g.potential(full, wo)
+    w = gpu.Wf(shape, step)
+    ot = gpu.OT(model, w)
+    ot.params.max_veloc, ot.params.max_bfpot, ot.params.c_bfpot = lim[1], lim[2], lim[3]
+    w.set(psi)
+    P = gpu.CGrid(shape, step)
+    P.zero()
+    ot.potential(P, w)
+    got = P.get()
+    assert relerr(got.real, Pref.real) < TOL[prec] * 2
+    assert relerr(got.imag, Pref.imag) < 20 * TOL[prec]
+    for o in (P, ot, w):
+        o.free()
+
+
 @pytest.mark.parametrize("model", [0, 1, 8, 9])
 def test_uniform_liquid_potential_is_chemical_potential(gpu, prec, model):
     shape, step = (32, 32, 32), 0.8
