@@ -19,6 +19,8 @@
 // x-pencil kernels apply k-space factors in registers between the two.
 #pragma once
 
+#include <cooperative_groups.h>
+
 #include "common.cuh"
 
 namespace dftgpu {
@@ -420,6 +422,187 @@ __global__ void __launch_bounds__(256) xkinetic_kernel(const C *__restrict__ tw,
   transform<N>(v, t, l, 1.f, tw, sm);
 #pragma unroll
   for (int j = 0; j < E; j++) base[(size_t) final_pos<N>(t, j) * ny] = v[j];
+}
+
+// --------------------------------------------------------------- fused z + y plane passes
+// The z and y passes of a real field's 3-D transform done by one cluster of
+// CL CTAs per x plane, the (y, kz) plane held in the CTAs' shared memory and
+// exchanged through distributed shared memory, so the half spectrum crosses
+// HBM once instead of three times.  CTA r of a cluster owns rows
+// y = r*RY .. r*RY+RY-1 of the plane (pitch PZ = NZC+1 complex) and the
+// column lines c = r*CB*BY .. (r+1)*CB*BY-1.  The z = 0 and z = NZC (Nyquist)
+// columns are real in y space; they travel as one complex column
+// X_0 + i X_NZC, so the NZC column lines split evenly over the cluster.
+template <int NY, int NZ, int CL> struct ZYPlane {
+  static constexpr int NZC = NZ / 2;            // packed complex z length
+  static constexpr int BY = Shape<NY>::B;       // column lines per batch
+  static constexpr int BZ = Shape<NZC>::B;      // rows per batch
+  static constexpr int RY = NY / CL;            // rows per CTA
+  static constexpr int CB = NZC / (CL * BY);    // column batches per CTA
+  static constexpr int RB = RY / BZ;            // row batches per CTA
+  static constexpr int PZ = NZC + 1;
+  static constexpr int PLANE = RY * PZ;
+  static constexpr int SCRY = BY * Shape<NY>::LP, SCRZ = BZ * Shape<NZC>::LP;
+  static constexpr int SCR = SCRY > SCRZ ? SCRY : SCRZ;
+  static constexpr int SMEM = (PLANE + SCR) * (int) sizeof(C);
+  static_assert(supported<NY>() && supported<NZC>(), "fused plane pass lengths");
+  static_assert(CB >= 1 && NZC % (CL * BY) == 0 && RB >= 1 && RY % BZ == 0 && NY % CL == 0, "fused plane split");
+};
+
+// forward: real rows f(x, y, .) (packed pairs from ld) -> spec[kz][x][y], kz = 0..NZC
+template <int NY, int NZ, int CL, class Ld>
+__global__ void __launch_bounds__(256) zy_r2c_kernel(const C *__restrict__ twz, const C *__restrict__ tw2z,
+                                                     const C *__restrict__ twy, const Ld ld, C *__restrict__ spec,
+                                                     int nx) {
+  typedef ZYPlane<NY, NZ, CL> Z;
+  namespace cg = cooperative_groups;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C *pl = reinterpret_cast<C *>(smraw);
+  C *scr = pl + Z::PLANE;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int) cluster.block_rank(), x = blockIdx.y;
+  {  // z pass of this CTA's rows into the local plane
+    constexpr int N = Z::NZC, E = Shape<N>::E, TL = Shape<N>::TL, B = Shape<N>::B, LP = Shape<N>::LP;
+    const int t = threadIdx.x % TL, l = threadIdx.x / TL;
+#pragma unroll 1
+    for (int rb = 0; rb < Z::RB; rb++) {
+      const int y = rank * Z::RY + rb * B + l;
+      C v[E];
+#pragma unroll
+      for (int q = 0; q < E; q++) v[q] = ld(x, y, t + TL * q);
+      transform<N>(v, t, l, -1.f, twz, scr);
+#pragma unroll
+      for (int j = 0; j < E; j++) scr[sidx(l, final_pos<N>(t, j), LP)] = v[j];
+      __syncthreads();
+      // X[k] = (Z[k] + Z*[N-k]) / 2 - (i/2) w^k (Z[k] - Z*[N-k]),  k = 0..N
+      constexpr int TOT = B * (N + 1), IT = (TOT + 255) / 256;
+#pragma unroll
+      for (int it = 0; it < IT; it++) {
+        const int idx = threadIdx.x + it * 256;
+        if (idx < TOT) {
+          const int ll = idx % B, k = idx / B;
+          const C zk = scr[sidx(ll, k == N ? 0 : k, LP)], zm = scr[sidx(ll, k == 0 ? 0 : N - k, LP)];
+          const C sum = make_float2(zk.x + zm.x, zk.y - zm.y), dif = make_float2(zk.x - zm.x, zk.y + zm.y);
+          const C w = k == N ? make_float2(-1.f, 0.f) : __ldg(&tw2z[k]);
+          const C tt = cmul(dif, w);
+          pl[(rb * B + ll) * Z::PZ + k] = make_float2(0.5f * (sum.x + tt.y), 0.5f * (sum.y - tt.x));
+        }
+      }
+      __syncthreads();
+    }
+  }
+  cluster.sync();   // every plane row written (and every CTA of the cluster running)
+  {  // y pass of this CTA's column lines, gathered from the cluster's planes
+    constexpr int N = NY, E = Shape<N>::E, TL = Shape<N>::TL, B = Shape<N>::B;
+    const int t = threadIdx.x % TL, l = threadIdx.x / TL;
+#pragma unroll 1
+    for (int cb = 0; cb < Z::CB; cb++) {
+      const int c = (rank * Z::CB + cb) * B + l;
+      C v[E];
+#pragma unroll
+      for (int q = 0; q < E; q++) {
+        const int y = t + TL * q;
+        const C *rp = cluster.map_shared_rank(pl, y / Z::RY) + (y % Z::RY) * Z::PZ;
+        v[q] = c == 0 ? make_float2(rp[0].x, rp[Z::NZC].x) : rp[c];
+      }
+      transform<N>(v, t, l, -1.f, twy, scr);
+      if (c != 0) {
+#pragma unroll
+        for (int j = 0; j < E; j++) spec[((size_t) c * nx + x) * NY + final_pos<N>(t, j)] = v[j];
+      }
+      if (rank == 0 && cb == 0) {   // CTA-uniform: separate the z = 0 and z = NZC columns
+        if (l == 0) {
+#pragma unroll
+          for (int j = 0; j < E; j++) scr[final_pos<N>(t, j)] = v[j];
+        }
+        __syncthreads();
+        if (l == 0) {
+#pragma unroll
+          for (int j = 0; j < E; j++) {
+            const int k = final_pos<N>(t, j);
+            const C zk = scr[k], zm = scr[(N - k) & (N - 1)];
+            // S_0 = (Z[k] + Z*[-k]) / 2 ; S_NZC = (Z[k] - Z*[-k]) / (2i)
+            spec[(size_t) x * NY + k] = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
+            spec[((size_t) Z::NZC * nx + x) * NY + k] = make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
+          }
+        }
+        __syncthreads();
+      }
+    }
+  }
+  cluster.sync();   // the peers have finished reading this CTA's plane
+}
+
+// inverse: spec[kz][x][y] -> real rows through st(x, y, e, (v[2e], v[2e+1]))
+template <int NY, int NZ, int CL, class St>
+__global__ void __launch_bounds__(256) yz_c2r_kernel(const C *__restrict__ twz, const C *__restrict__ tw2z,
+                                                     const C *__restrict__ twy, const C *__restrict__ spec, const St st,
+                                                     int nx) {
+  typedef ZYPlane<NY, NZ, CL> Z;
+  namespace cg = cooperative_groups;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C *pl = reinterpret_cast<C *>(smraw);
+  C *scr = pl + Z::PLANE;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int) cluster.block_rank(), x = blockIdx.y;
+  cluster.sync();   // every CTA of the cluster running before remote stores
+  {  // y pass of this CTA's column lines, scattered into the cluster's planes
+    constexpr int N = NY, E = Shape<N>::E, TL = Shape<N>::TL, B = Shape<N>::B;
+    const int t = threadIdx.x % TL, l = threadIdx.x / TL;
+#pragma unroll 1
+    for (int cb = 0; cb < Z::CB; cb++) {
+      const int c = (rank * Z::CB + cb) * B + l;
+      C v[E];
+      if (c == 0) {   // X_0 + i X_NZC
+#pragma unroll
+        for (int q = 0; q < E; q++) {
+          const C a = spec[(size_t) x * NY + t + TL * q], b = spec[((size_t) Z::NZC * nx + x) * NY + t + TL * q];
+          v[q] = make_float2(a.x - b.y, a.y + b.x);
+        }
+      } else {
+#pragma unroll
+        for (int q = 0; q < E; q++) v[q] = spec[((size_t) c * nx + x) * NY + t + TL * q];
+      }
+      transform<N>(v, t, l, 1.f, twy, scr);
+#pragma unroll
+      for (int j = 0; j < E; j++) {
+        const int y = final_pos<N>(t, j);
+        C *rp = cluster.map_shared_rank(pl, y / Z::RY) + (y % Z::RY) * Z::PZ;
+        if (c == 0) {
+          rp[0] = make_float2(v[j].x, 0.f);
+          rp[Z::NZC] = make_float2(v[j].y, 0.f);
+        } else {
+          rp[c] = v[j];
+        }
+      }
+      __syncthreads();
+    }
+  }
+  cluster.sync();   // this CTA's plane rows complete
+  {  // c2r z pass of this CTA's rows
+    constexpr int N = Z::NZC, E = Shape<N>::E, TL = Shape<N>::TL, B = Shape<N>::B;
+    const int t = threadIdx.x % TL, l = threadIdx.x / TL;
+#pragma unroll 1
+    for (int rb = 0; rb < Z::RB; rb++) {
+      const C *row = pl + (rb * B + l) * Z::PZ;
+      C v[E];
+#pragma unroll
+      for (int q = 0; q < E; q++) {
+        // Z[k] = (X[k] + X*[N-k]) + i w^-k (X[k] - X*[N-k]),  w = exp(-2 pi i / 2N)
+        const int e = t + TL * q;
+        const C xk = row[e], xm = row[N - e];
+        const C sum = make_float2(xk.x + xm.x, xk.y - xm.y), dif = make_float2(xk.x - xm.x, xk.y + xm.y);
+        C w = __ldg(&tw2z[e]);
+        w.y = -w.y;
+        const C tt = cmul(dif, w);
+        v[q] = make_float2(sum.x - tt.y, sum.y + tt.x);
+      }
+      transform<N>(v, t, l, 1.f, twz, scr);
+      const int y = rank * Z::RY + rb * B + l;
+#pragma unroll
+      for (int j = 0; j < E; j++) st(x, y, final_pos<N>(t, j), v[j]);
+    }
+  }
 }
 
 }  // namespace ff

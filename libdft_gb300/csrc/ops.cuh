@@ -180,6 +180,10 @@ template <typename T> int ypass(typename cplx_t<T>::type *spec, int nx, int ny, 
 // forward r2c of a real field through its z and y passes, with a custom
 // packed-pair loader (fused producer); spec is [nz/2+1][nx][ny]
 template <typename T, class Ld> int rfft_zy(const Ld &ld, typename cplx_t<T>::type *spec, int nx, int ny, int nz) {
+  if constexpr (std::is_same<T, float>::value) {
+    const int rc = launch_zy_r2c(ld, spec, nx, ny, nz);
+    if (rc >= 0) return rc;
+  }
   SpecStoreZ<T> st{spec, nx, ny};
   DFT_TRY((launch_lines<T, LINE_R2C, 1, 0>(nz / 2, nx, ny, (T) -1, ld, st)));
   return ypass<T>(spec, nx, ny, nz / 2 + 1, (T) -1);
@@ -187,6 +191,10 @@ template <typename T, class Ld> int rfft_zy(const Ld &ld, typename cplx_t<T>::ty
 
 // inverse: y passes then c2r z pass into a custom consumer st(x, y, e, (v[2e], v[2e+1]))
 template <typename T, class St> int irfft_yz(typename cplx_t<T>::type *spec, const St &st, int nx, int ny, int nz) {
+  if constexpr (std::is_same<T, float>::value) {
+    const int rc = launch_yz_c2r(spec, st, nx, ny, nz);
+    if (rc >= 0) return rc;
+  }
   DFT_TRY(ypass<T>(spec, nx, ny, nz / 2 + 1, (T) 1));
   SpecLoadZ<T> ld{spec, nx, ny};
   return launch_lines<T, LINE_C2R, 0, 1>(nz / 2, nx, ny, (T) 1, ld, st);

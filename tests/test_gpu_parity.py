@@ -26,7 +26,8 @@ def prec(request, gpu):
 
 
 @pytest.mark.parametrize("shape", [(16, 16, 16), (16, 18, 20), (32, 24, 40), (64, 64, 64), (30, 36, 50),
-                                   (8, 16, 512), (64, 256, 32), (128, 128, 128), (96, 120, 160)])
+                                   (8, 16, 512), (64, 256, 32), (128, 128, 128), (96, 120, 160),
+                                   (16, 256, 256), (6, 512, 512)])
 def test_rfft_spectrum(gpu, prec, shape):
     rng = np.random.default_rng(1)
     f = rng.standard_normal(shape)
@@ -87,7 +88,8 @@ def test_potential_and_energy_density_match_reference(gpu, prec, fixture):
 
 @pytest.mark.parametrize("shape,step,model", [((32, 32, 32), 0.8, 9), ((40, 36, 30), 0.7, 1), ((48, 32, 40), 1.0, 8),
                                               ((96, 80, 128), 0.8, 9), ((64, 64, 64), 0.8, 9),
-                                              ((128, 64, 80), 0.8, 9), ((64, 128, 128), 0.8, 1)])
+                                              ((128, 64, 80), 0.8, 9), ((64, 128, 128), 0.8, 1),
+                                              ((16, 256, 256), 0.8, 9), ((4, 512, 512), 0.5, 0)])
 def test_potential_vs_oracle_live(gpu, port, prec, shape, step, model):
     psi = liquid_psi(shape, step, 3)
     ns = (2, 4) if np.prod(shape) > 200000 else (4, 32)      # coarser kernel sampling on big grids (CPU time)
