@@ -1,10 +1,12 @@
 // FFT plans, twiddle tables and launchers for the x-pencil kernels.
 #include <math.h>
+#include <string.h>
 #include <map>
 #include <mutex>
 #include <utility>
 
 #include "fft.cuh"
+#include "ops.cuh"
 
 namespace dftgpu {
 
@@ -279,5 +281,76 @@ template int launch_xconv<float>(XConvArgs<float> &);
 template int launch_xconv<double>(XConvArgs<double> &);
 template int launch_xkinetic<float>(KinArgs<float> &);
 template int launch_xkinetic<double>(KinArgs<double> &);
+
+// ------------------------------------------------------------------ fused z + y passes
+namespace {
+
+template <int NY, int NZ, int CL, bool FWD, class Kern, class... Args>
+int launch_zy_cluster(Kern kfn, int nx, Args... args) {
+  typedef ff::ZYPlane<NY, NZ, CL> Z;
+  static bool attr_done = false;
+  if (!attr_done) {
+    DFT_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, Z::SMEM));
+    attr_done = true;
+  }
+  FftPlan<float> pz, p2, py;
+  DFT_TRY(get_plan<float>(Z::NZC, &pz));
+  DFT_TRY(get_plan<float>(NZ, &p2));
+  DFT_TRY(get_plan<float>(NY, &py));
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(CL, nx);
+  cfg.blockDim = dim3(256);
+  cfg.dynamicSmemBytes = Z::SMEM;
+  cfg.stream = rt().stream;
+  cudaLaunchAttribute at[1];
+  memset(at, 0, sizeof(at));
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = CL;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  const cudaError_t e = cudaLaunchKernelEx(&cfg, kfn, (const float2 *) pz.tw, (const float2 *) p2.tw,
+                                           (const float2 *) py.tw, args..., nx);
+  if (e != cudaSuccess) {
+    cudaFuncAttributes fa = {};
+    cudaFuncGetAttributes(&fa, kfn);
+    int ncl = -1;
+    cudaOccupancyMaxActiveClusters(&ncl, kfn, &cfg);
+    set_error(DFTGPU_ERR_CUDA, "fused %s pass %dx%d (cluster %d, %d B shared, nx %d): %s; function: %d regs, "
+              "max dynamic shared %d B; active clusters %d", FWD ? "zy r2c" : "yz c2r", NY, NZ, CL, Z::SMEM, nx,
+              cudaGetErrorString(e), fa.numRegs, fa.maxDynamicSharedSizeBytes, ncl);
+    return DFTGPU_ERR_CUDA;
+  }
+  return DFTGPU_OK;
+}
+
+bool fused_shape(int ny, int nz) {
+  return !generic_fft_only() && !fused_zy_off() && ny == nz && (ny == 128 || ny == 256 || ny == 512);
+}
+
+}  // namespace
+
+int launch_zy_r2c(const RealPairLoad<float> &ld, float2 *spec, int nx, int ny, int nz) {
+  typedef RealPairLoad<float> Ld;
+  if (!fused_shape(ny, nz)) return -1;
+  ProfScope prof("fft_zy_r2c", (double) nx * ny * nz * 4.0 + (double) nx * ny * (nz / 2 + 1) * 8.0);
+  switch (ny) {
+    case 128: return launch_zy_cluster<128, 128, 2, true>(ff::zy_r2c_kernel<128, 128, 2, Ld>, nx, ld, spec);
+    case 256: return launch_zy_cluster<256, 256, 8, true>(ff::zy_r2c_kernel<256, 256, 8, Ld>, nx, ld, spec);
+    default: return launch_zy_cluster<512, 512, 8, true>(ff::zy_r2c_kernel<512, 512, 8, Ld>, nx, ld, spec);
+  }
+}
+
+int launch_yz_c2r(const float2 *spec, const RealPairStore<float> &st, int nx, int ny, int nz) {
+  typedef RealPairStore<float> St;
+  if (!fused_shape(ny, nz)) return -1;
+  ProfScope prof("fft_yz_c2r", (double) nx * ny * nz * 4.0 + (double) nx * ny * (nz / 2 + 1) * 8.0);
+  switch (ny) {
+    case 128: return launch_zy_cluster<128, 128, 2, false>(ff::yz_c2r_kernel<128, 128, 2, St>, nx, spec, st);
+    case 256: return launch_zy_cluster<256, 256, 8, false>(ff::yz_c2r_kernel<256, 256, 8, St>, nx, spec, st);
+    default: return launch_zy_cluster<512, 512, 8, false>(ff::yz_c2r_kernel<512, 512, 8, St>, nx, spec, st);
+  }
+}
 
 }  // namespace dftgpu

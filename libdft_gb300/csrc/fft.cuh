@@ -478,58 +478,4 @@ template <typename T> int launch_xkinetic(KinArgs<T> &A);
 // ------------------------------------------------------------ fused z + y passes
 bool fused_zy_off();   // DFTGPU_NO_FUSED_ZY=1 selects the separate z and y passes
 
-template <int NY, int NZ, int CL, bool FWD, class Kern, class... Args>
-int launch_zy_cluster(Kern kfn, int nx, Args... args) {
-  typedef ff::ZYPlane<NY, NZ, CL> Z;
-  typedef SmemOptIn<ff::ZYPlane<NY, NZ, CL> (*)(Kern, int (*)[FWD + 1])> Flag;
-  if (!Flag::done) {
-    DFT_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, Z::SMEM));
-    Flag::done = true;
-  }
-  FftPlan<float> pz, p2, py;
-  DFT_TRY(get_plan<float>(Z::NZC, &pz));
-  DFT_TRY(get_plan<float>(NZ, &p2));
-  DFT_TRY(get_plan<float>(NY, &py));
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(CL, nx);
-  cfg.blockDim = dim3(256);
-  cfg.dynamicSmemBytes = Z::SMEM;
-  cfg.stream = rt().stream;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeClusterDimension;
-  at[0].val.clusterDim.x = CL;
-  at[0].val.clusterDim.y = 1;
-  at[0].val.clusterDim.z = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  DFT_CUDA(cudaLaunchKernelEx(&cfg, kfn, (const float2 *) pz.tw, (const float2 *) p2.tw, (const float2 *) py.tw,
-                              args..., nx));
-  return DFTGPU_OK;
-}
-
-// r2c z pass + y pass of a real field (packed pairs from ld) into spec
-// [nz/2+1][nx][ny]; -1 when no fused instantiation fits the shape
-template <class Ld> int launch_zy_r2c(const Ld &ld, float2 *spec, int nx, int ny, int nz) {
-  if (generic_fft_only() || fused_zy_off() || ny != nz || (ny != 128 && ny != 256 && ny != 512)) return -1;
-  ProfScope prof("fft_zy_r2c", (double) nx * ny * nz * 4.0 + (double) nx * ny * (nz / 2 + 1) * 8.0);
-  switch (ny) {
-    case 128: return launch_zy_cluster<128, 128, 2, true>(ff::zy_r2c_kernel<128, 128, 2, Ld>, nx, ld, spec);
-    case 256: return launch_zy_cluster<256, 256, 8, true>(ff::zy_r2c_kernel<256, 256, 8, Ld>, nx, ld, spec);
-    case 512: return launch_zy_cluster<512, 512, 8, true>(ff::zy_r2c_kernel<512, 512, 8, Ld>, nx, ld, spec);
-    default: return -1;
-  }
-}
-
-// y pass + c2r z pass of a half spectrum into st(x, y, e, (v[2e], v[2e+1]))
-template <class St> int launch_yz_c2r(const float2 *spec, const St &st, int nx, int ny, int nz) {
-  if (generic_fft_only() || fused_zy_off() || ny != nz || (ny != 128 && ny != 256 && ny != 512)) return -1;
-  ProfScope prof("fft_yz_c2r", (double) nx * ny * nz * 4.0 + (double) nx * ny * (nz / 2 + 1) * 8.0);
-  switch (ny) {
-    case 128: return launch_zy_cluster<128, 128, 2, false>(ff::yz_c2r_kernel<128, 128, 2, St>, nx, spec, st);
-    case 256: return launch_zy_cluster<256, 256, 8, false>(ff::yz_c2r_kernel<256, 256, 8, St>, nx, spec, st);
-    case 512: return launch_zy_cluster<512, 512, 8, false>(ff::yz_c2r_kernel<512, 512, 8, St>, nx, spec, st);
-    default: return -1;
-  }
-}
-
 }  // namespace dftgpu

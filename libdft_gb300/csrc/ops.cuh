@@ -171,6 +171,12 @@ template <typename T> struct CplxLoad {
   }
 };
 
+// Fused z + y passes of a real field (fft.cu; the cluster kernels are
+// instantiated in that one translation unit).  Return -1 when no fused
+// instantiation fits the shape (the caller runs the separate passes).
+int launch_zy_r2c(const RealPairLoad<float> &ld, float2 *spec, int nx, int ny, int nz);
+int launch_yz_c2r(const float2 *spec, const RealPairStore<float> &st, int nx, int ny, int nz);
+
 // y passes over nkz planes of a spectral buffer
 template <typename T> int ypass(typename cplx_t<T>::type *spec, int nx, int ny, int nkz, T sign) {
   SpecLineY<T> io{spec, nx, ny};
@@ -180,7 +186,7 @@ template <typename T> int ypass(typename cplx_t<T>::type *spec, int nx, int ny, 
 // forward r2c of a real field through its z and y passes, with a custom
 // packed-pair loader (fused producer); spec is [nz/2+1][nx][ny]
 template <typename T, class Ld> int rfft_zy(const Ld &ld, typename cplx_t<T>::type *spec, int nx, int ny, int nz) {
-  if constexpr (std::is_same<T, float>::value) {
+  if constexpr (std::is_same<Ld, RealPairLoad<float>>::value) {
     const int rc = launch_zy_r2c(ld, spec, nx, ny, nz);
     if (rc >= 0) return rc;
   }
@@ -191,7 +197,7 @@ template <typename T, class Ld> int rfft_zy(const Ld &ld, typename cplx_t<T>::ty
 
 // inverse: y passes then c2r z pass into a custom consumer st(x, y, e, (v[2e], v[2e+1]))
 template <typename T, class St> int irfft_yz(typename cplx_t<T>::type *spec, const St &st, int nx, int ny, int nz) {
-  if constexpr (std::is_same<T, float>::value) {
+  if constexpr (std::is_same<St, RealPairStore<float>>::value) {
     const int rc = launch_yz_c2r(spec, st, nx, ny, nz);
     if (rc >= 0) return rc;
   }
