@@ -109,7 +109,7 @@ const char *dftgpu_last_error_message(void);
 int dftgpu_synchronize(void) {
   if (ensure_device() != DFTGPU_OK) return DFTGPU_ERR_NODEVICE;
   DFT_CUDA(cudaStreamSynchronize(rt().stream));
-  return DFTGPU_OK;
+  return fused_zy_fault();
 }
 int dftgpu_set_stream(void *stream) { rt().stream = (cudaStream_t) stream; return DFTGPU_OK; }
 int dftgpu_profile(int enable) { return prof_enable(enable); }

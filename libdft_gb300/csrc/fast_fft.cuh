@@ -426,50 +426,128 @@ __global__ void __launch_bounds__(256) xkinetic_kernel(const C *__restrict__ tw,
 
 // --------------------------------------------------------------- fused z + y plane passes
 // The z and y passes of a real field's 3-D transform done by one cluster of
-// CL CTAs per x plane, the (y, kz) plane held in the CTAs' shared memory and
-// exchanged through distributed shared memory, so the half spectrum crosses
-// HBM once instead of three times.  CTA r of a cluster owns rows
-// y = r*RY .. r*RY+RY-1 of the plane (pitch PZ = NZC+1 complex) and the
-// column lines c = r*CB*BY .. (r+1)*CB*BY-1.  The z = 0 and z = NZC (Nyquist)
-// columns are real in y space; they travel as one complex column
-// X_0 + i X_NZC, so the NZC column lines split evenly over the cluster.
+// CL CTAs per x plane, so the half spectrum crosses HBM once instead of
+// three times.  CTA r of a cluster owns rows y = r*RY .. r*RY+RY-1 of the
+// (y, kz) plane and the KC column lines c = r*KC .. r*KC+KC-1.  Data move by
+// bulk asynchronous copies that complete on mbarriers: rows / columns from
+// global memory into a staging area, and the plane exchange between the
+// CTAs as one contiguous block per (source, destination) pair, laid out
+// [kz][row] on one side and [source][column][row] on the other.  The z = 0
+// and z = NZC (Nyquist) columns are real in y space; they travel as one
+// complex column X_0 + i X_NZC, so the NZC column lines split evenly.
 template <int NY, int NZ, int CL> struct ZYPlane {
   static constexpr int NZC = NZ / 2;            // packed complex z length
   static constexpr int BY = Shape<NY>::B;       // column lines per batch
   static constexpr int BZ = Shape<NZC>::B;      // rows per batch
   static constexpr int RY = NY / CL;            // rows per CTA
-  static constexpr int CB = NZC / (CL * BY);    // column batches per CTA
+  static constexpr int KC = NZC / CL;           // column lines per CTA
+  static constexpr int CB = KC / BY;            // column batches per CTA
   static constexpr int RB = RY / BZ;            // row batches per CTA
-  static constexpr int PZ = NZC + 1;
-  static constexpr int PLANE = RY * PZ;
+  static constexpr int PRW = NZC + 8;           // staged row pitch (complex pairs)
+  static constexpr int PC = NY + 8;             // staged column pitch
+  static constexpr int PLT = (NZC + 2) * RY;    // plane [kz][row]
+  static constexpr int IN = CL * KC * RY;       // exchange blocks [source or destination][column][row]
+  static constexpr int STF = RY * PRW, STI = KC * PC;
+  static constexpr int A1 = IN > STF ? (IN > STI ? IN : STI) : (STF > STI ? STF : STI);
+  static constexpr int NQ = CL * RY;            // Nyquist row blocks
+  static constexpr int NQS = NY;                // staged Nyquist column (inverse, rank 0)
   static constexpr int SCRY = BY * Shape<NY>::LP, SCRZ = BZ * Shape<NZC>::LP;
   static constexpr int SCR = SCRY > SCRZ ? SCRY : SCRZ;
-  static constexpr int SMEM = (PLANE + SCR) * (int) sizeof(C);
+  static constexpr int SMEM = (PLT + A1 + NQ + NQS + SCR) * (int) sizeof(C) + 16;
   static_assert(supported<NY>() && supported<NZC>(), "fused plane pass lengths");
-  static_assert(CB >= 1 && NZC % (CL * BY) == 0 && RB >= 1 && RY % BZ == 0 && NY % CL == 0, "fused plane split");
+  static_assert(CB == 1 && KC == BY && RB >= 1 && RY % BZ == 0 && NY % CL == 0 && NZC % CL == 0,
+                "fused plane split");
+  static_assert(NZC % 16 == 0 && NY % 16 == 0, "staged pitches stay 16-byte multiples");
 };
 
-// forward: real rows f(x, y, .) (packed pairs from ld) -> spec[kz][x][y], kz = 0..NZC
-template <int NY, int NZ, int CL, class Ld>
-__global__ void __launch_bounds__(256) zy_r2c_kernel(const C *__restrict__ twz, const C *__restrict__ tw2z,
-                                                     const C *__restrict__ twy, const Ld ld, C *__restrict__ spec,
-                                                     int nx) {
+__device__ __forceinline__ unsigned su32(const void *p) { return (unsigned) __cvta_generic_to_shared(p); }
+__device__ __forceinline__ unsigned cl_addr(unsigned a, unsigned rank) {   // shared::cluster address in CTA rank
+  unsigned r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ void mbar_init(unsigned bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void mbar_expect_tx(unsigned bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ unsigned long long gtimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// Wait for the completion of phase `parity`; after 0.5 s the wait gives up
+// and records the failure in *fault (read by the host after the launch).
+__device__ __forceinline__ void mbar_wait(unsigned bar, unsigned parity, int *fault) {
+  if (mbar_try_wait(bar, parity)) return;
+  const unsigned long long t0 = gtimer();
+  while (!mbar_try_wait(bar, parity)) {
+    if (gtimer() - t0 > 500000000ull) { atomicExch(fault, 1); return; }
+  }
+}
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void bulk_g2s(unsigned dst, const void *src, unsigned bytes, unsigned bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+               ::"r"(dst), "l"(src), "r"(bytes), "r"(bar)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_s2c(unsigned dst, unsigned src, unsigned bytes, unsigned bar) {
+  asm volatile("cp.async.bulk.shared::cluster.shared::cta.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+               ::"r"(dst), "r"(src), "r"(bytes), "r"(bar)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+
+// forward: real field f[x][y][z] -> spec[kz][x][y], kz = 0..NZC
+template <int NY, int NZ, int CL>
+__global__ void __launch_bounds__(256, 2) zy_r2c_kernel(const C *__restrict__ twz, const C *__restrict__ tw2z,
+                                                        const C *__restrict__ twy, const float *__restrict__ f,
+                                                        C *__restrict__ spec, int nx, int *fault) {
   typedef ZYPlane<NY, NZ, CL> Z;
   namespace cg = cooperative_groups;
-  extern __shared__ __align__(16) unsigned char smraw[];
-  C *pl = reinterpret_cast<C *>(smraw);
-  C *scr = pl + Z::PLANE;
+  extern __shared__ __align__(128) unsigned char smraw[];
+  C *plt = reinterpret_cast<C *>(smraw);   // [NZC+2][RY]
+  C *a1 = plt + Z::PLT;                    // staged rows [RY][PRW], then incoming [CL][KC][RY]
+  C *nq = a1 + Z::A1;                      // incoming Nyquist rows [CL][RY] (rank 0)
+  C *scr = nq + Z::NQ + Z::NQS;
+  unsigned long long *bars = reinterpret_cast<unsigned long long *>(scr + Z::SCR);
   cg::cluster_group cluster = cg::this_cluster();
-  const int rank = (int) cluster.block_rank(), x = blockIdx.y;
-  {  // z pass of this CTA's rows into the local plane
+  const int rank = (int) cluster.block_rank(), x = blockIdx.y, tid = threadIdx.x;
+  const unsigned bar_ld = su32(&bars[0]), bar_in = su32(&bars[1]);
+  if (tid == 0) {
+    mbar_init(bar_ld, 1);
+    mbar_init(bar_in, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (tid == 0) {
+    mbar_expect_tx(bar_ld, Z::RY * NZ * 4);
+    mbar_expect_tx(bar_in, (Z::IN + (rank == 0 ? Z::NQ : 0)) * 8);
+  }
+  __syncthreads();
+  if (tid < Z::RY) bulk_g2s(su32(a1 + tid * Z::PRW), f + ((size_t) x * NY + rank * Z::RY + tid) * NZ, NZ * 4, bar_ld);
+  mbar_wait(bar_ld, 0, fault);
+  {  // z pass of this CTA's rows into the plane [kz][row]
     constexpr int N = Z::NZC, E = Shape<N>::E, TL = Shape<N>::TL, B = Shape<N>::B, LP = Shape<N>::LP;
-    const int t = threadIdx.x % TL, l = threadIdx.x / TL;
+    const int t = tid % TL, l = tid / TL;
 #pragma unroll 1
     for (int rb = 0; rb < Z::RB; rb++) {
-      const int y = rank * Z::RY + rb * B + l;
+      const C *row = a1 + (rb * B + l) * Z::PRW;
       C v[E];
 #pragma unroll
-      for (int q = 0; q < E; q++) v[q] = ld(x, y, t + TL * q);
+      for (int q = 0; q < E; q++) v[q] = row[t + TL * q];
       transform<N>(v, t, l, -1.f, twz, scr);
 #pragma unroll
       for (int j = 0; j < E; j++) scr[sidx(l, final_pos<N>(t, j), LP)] = v[j];
@@ -478,119 +556,148 @@ __global__ void __launch_bounds__(256) zy_r2c_kernel(const C *__restrict__ twz, 
       constexpr int TOT = B * (N + 1), IT = (TOT + 255) / 256;
 #pragma unroll
       for (int it = 0; it < IT; it++) {
-        const int idx = threadIdx.x + it * 256;
+        const int idx = tid + it * 256;
         if (idx < TOT) {
           const int ll = idx % B, k = idx / B;
           const C zk = scr[sidx(ll, k == N ? 0 : k, LP)], zm = scr[sidx(ll, k == 0 ? 0 : N - k, LP)];
           const C sum = make_float2(zk.x + zm.x, zk.y - zm.y), dif = make_float2(zk.x - zm.x, zk.y + zm.y);
           const C w = k == N ? make_float2(-1.f, 0.f) : __ldg(&tw2z[k]);
           const C tt = cmul(dif, w);
-          pl[(rb * B + ll) * Z::PZ + k] = make_float2(0.5f * (sum.x + tt.y), 0.5f * (sum.y - tt.x));
+          plt[k * Z::RY + rb * B + ll] = make_float2(0.5f * (sum.x + tt.y), 0.5f * (sum.y - tt.x));
         }
       }
       __syncthreads();
     }
   }
-  cluster.sync();   // every plane row written (and every CTA of the cluster running)
-  {  // y pass of this CTA's column lines, gathered from the cluster's planes
-    constexpr int N = NY, E = Shape<N>::E, TL = Shape<N>::TL, B = Shape<N>::B;
-    const int t = threadIdx.x % TL, l = threadIdx.x / TL;
-#pragma unroll 1
-    for (int cb = 0; cb < Z::CB; cb++) {
-      const int c = (rank * Z::CB + cb) * B + l;
-      C v[E];
+  fence_proxy_async();
+  cluster.sync();   // planes complete, staging areas free, barriers armed in every CTA
+  if (tid < CL) {
+    bulk_s2c(cl_addr(su32(a1 + rank * Z::KC * Z::RY), tid), su32(plt + tid * Z::KC * Z::RY), Z::KC * Z::RY * 8,
+             cl_addr(bar_in, tid));
+  } else if (tid == CL) {
+    bulk_s2c(cl_addr(su32(nq + rank * Z::RY), 0), su32(plt + Z::NZC * Z::RY), Z::RY * 8, cl_addr(bar_in, 0));
+  }
+  if (tid <= CL) bulk_commit();
+  mbar_wait(bar_in, 0, fault);
+  {  // y pass of this CTA's column lines
+    constexpr int N = NY, E = Shape<N>::E, TL = Shape<N>::TL;
+    const int t = tid % TL, l = tid / TL, c = rank * Z::KC + l;
+    C v[E];
 #pragma unroll
-      for (int q = 0; q < E; q++) {
-        const int y = t + TL * q;
-        const C *rp = cluster.map_shared_rank(pl, y / Z::RY) + (y % Z::RY) * Z::PZ;
-        v[q] = c == 0 ? make_float2(rp[0].x, rp[Z::NZC].x) : rp[c];
+    for (int q = 0; q < E; q++) {
+      const int y = t + TL * q, sr = y / Z::RY, r = y % Z::RY;
+      v[q] = c == 0 ? make_float2(a1[(sr * Z::KC) * Z::RY + r].x, nq[sr * Z::RY + r].x)
+                    : a1[(sr * Z::KC + l) * Z::RY + r];
+    }
+    transform<N>(v, t, l, -1.f, twy, scr);
+    if (c != 0) {
+#pragma unroll
+      for (int j = 0; j < E; j++) spec[((size_t) c * nx + x) * NY + final_pos<N>(t, j)] = v[j];
+    }
+    if (rank == 0) {   // CTA-uniform: separate the z = 0 and z = NZC columns
+      if (l == 0) {
+#pragma unroll
+        for (int j = 0; j < E; j++) scr[final_pos<N>(t, j)] = v[j];
       }
-      transform<N>(v, t, l, -1.f, twy, scr);
-      if (c != 0) {
+      __syncthreads();
+      if (l == 0) {
 #pragma unroll
-        for (int j = 0; j < E; j++) spec[((size_t) c * nx + x) * NY + final_pos<N>(t, j)] = v[j];
-      }
-      if (rank == 0 && cb == 0) {   // CTA-uniform: separate the z = 0 and z = NZC columns
-        if (l == 0) {
-#pragma unroll
-          for (int j = 0; j < E; j++) scr[final_pos<N>(t, j)] = v[j];
+        for (int j = 0; j < E; j++) {
+          const int k = final_pos<N>(t, j);
+          const C zk = scr[k], zm = scr[(N - k) & (N - 1)];
+          // S_0 = (Z[k] + Z*[-k]) / 2 ; S_NZC = (Z[k] - Z*[-k]) / (2i)
+          spec[(size_t) x * NY + k] = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
+          spec[((size_t) Z::NZC * nx + x) * NY + k] = make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
         }
-        __syncthreads();
-        if (l == 0) {
-#pragma unroll
-          for (int j = 0; j < E; j++) {
-            const int k = final_pos<N>(t, j);
-            const C zk = scr[k], zm = scr[(N - k) & (N - 1)];
-            // S_0 = (Z[k] + Z*[-k]) / 2 ; S_NZC = (Z[k] - Z*[-k]) / (2i)
-            spec[(size_t) x * NY + k] = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
-            spec[((size_t) Z::NZC * nx + x) * NY + k] = make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
-          }
-        }
-        __syncthreads();
       }
     }
   }
-  cluster.sync();   // the peers have finished reading this CTA's plane
+  if (tid <= CL) bulk_wait_read();   // own outgoing copies have read the plane
 }
 
-// inverse: spec[kz][x][y] -> real rows through st(x, y, e, (v[2e], v[2e+1]))
-template <int NY, int NZ, int CL, class St>
-__global__ void __launch_bounds__(256) yz_c2r_kernel(const C *__restrict__ twz, const C *__restrict__ tw2z,
-                                                     const C *__restrict__ twy, const C *__restrict__ spec, const St st,
-                                                     int nx) {
+// inverse: spec[kz][x][y] -> real field f[x][y][z] * scale
+template <int NY, int NZ, int CL>
+__global__ void __launch_bounds__(256, 2) yz_c2r_kernel(const C *__restrict__ twz, const C *__restrict__ tw2z,
+                                                        const C *__restrict__ twy, const C *__restrict__ spec,
+                                                        float *__restrict__ f, float scale, int nx, int *fault) {
   typedef ZYPlane<NY, NZ, CL> Z;
   namespace cg = cooperative_groups;
-  extern __shared__ __align__(16) unsigned char smraw[];
-  C *pl = reinterpret_cast<C *>(smraw);
-  C *scr = pl + Z::PLANE;
+  extern __shared__ __align__(128) unsigned char smraw[];
+  C *plt = reinterpret_cast<C *>(smraw);   // incoming plane [NZC+2][RY]
+  C *a1 = plt + Z::PLT;                    // staged columns [KC][PC], then outgoing [CL][KC][RY]
+  C *nq = a1 + Z::A1;                      // outgoing Nyquist rows [CL][RY] (rank 0)
+  C *nqs = nq + Z::NQ;                     // staged Nyquist column [NY] (rank 0)
+  C *scr = nqs + Z::NQS;
+  unsigned long long *bars = reinterpret_cast<unsigned long long *>(scr + Z::SCR);
   cg::cluster_group cluster = cg::this_cluster();
-  const int rank = (int) cluster.block_rank(), x = blockIdx.y;
-  cluster.sync();   // every CTA of the cluster running before remote stores
-  {  // y pass of this CTA's column lines, scattered into the cluster's planes
-    constexpr int N = NY, E = Shape<N>::E, TL = Shape<N>::TL, B = Shape<N>::B;
-    const int t = threadIdx.x % TL, l = threadIdx.x / TL;
-#pragma unroll 1
-    for (int cb = 0; cb < Z::CB; cb++) {
-      const int c = (rank * Z::CB + cb) * B + l;
-      C v[E];
+  const int rank = (int) cluster.block_rank(), x = blockIdx.y, tid = threadIdx.x;
+  const unsigned bar_ld = su32(&bars[0]), bar_in = su32(&bars[1]);
+  if (tid == 0) {
+    mbar_init(bar_ld, 1);
+    mbar_init(bar_in, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (tid == 0) {
+    mbar_expect_tx(bar_ld, (Z::KC + (rank == 0 ? 1 : 0)) * NY * 8);
+    mbar_expect_tx(bar_in, (Z::IN + Z::RY) * 8);
+  }
+  __syncthreads();
+  if (tid < Z::KC) {
+    bulk_g2s(su32(a1 + tid * Z::PC), spec + ((size_t) (rank * Z::KC + tid) * nx + x) * NY, NY * 8, bar_ld);
+  } else if (tid == Z::KC && rank == 0) {
+    bulk_g2s(su32(nqs), spec + ((size_t) Z::NZC * nx + x) * NY, NY * 8, bar_ld);
+  }
+  mbar_wait(bar_ld, 0, fault);
+  {  // y pass of this CTA's column lines into the outgoing blocks
+    constexpr int N = NY, E = Shape<N>::E, TL = Shape<N>::TL;
+    const int t = tid % TL, l = tid / TL, c = rank * Z::KC + l;
+    C v[E];
+#pragma unroll
+    for (int q = 0; q < E; q++) {
+      const int y = t + TL * q;
       if (c == 0) {   // X_0 + i X_NZC
-#pragma unroll
-        for (int q = 0; q < E; q++) {
-          const C a = spec[(size_t) x * NY + t + TL * q], b = spec[((size_t) Z::NZC * nx + x) * NY + t + TL * q];
-          v[q] = make_float2(a.x - b.y, a.y + b.x);
-        }
+        const C a = a1[y], b = nqs[y];
+        v[q] = make_float2(a.x - b.y, a.y + b.x);
       } else {
-#pragma unroll
-        for (int q = 0; q < E; q++) v[q] = spec[((size_t) c * nx + x) * NY + t + TL * q];
+        v[q] = a1[l * Z::PC + y];
       }
-      transform<N>(v, t, l, 1.f, twy, scr);
+    }
+    transform<N>(v, t, l, 1.f, twy, scr);   // its barriers order every staged read before the writes below
 #pragma unroll
-      for (int j = 0; j < E; j++) {
-        const int y = final_pos<N>(t, j);
-        C *rp = cluster.map_shared_rank(pl, y / Z::RY) + (y % Z::RY) * Z::PZ;
-        if (c == 0) {
-          rp[0] = make_float2(v[j].x, 0.f);
-          rp[Z::NZC] = make_float2(v[j].y, 0.f);
-        } else {
-          rp[c] = v[j];
-        }
+    for (int j = 0; j < E; j++) {
+      const int y = final_pos<N>(t, j), sr = y / Z::RY, r = y % Z::RY;
+      if (c == 0) {
+        a1[(sr * Z::KC) * Z::RY + r] = make_float2(v[j].x, 0.f);
+        nq[sr * Z::RY + r] = make_float2(v[j].y, 0.f);
+      } else {
+        a1[(sr * Z::KC + l) * Z::RY + r] = v[j];
       }
-      __syncthreads();
     }
   }
-  cluster.sync();   // this CTA's plane rows complete
-  {  // c2r z pass of this CTA's rows
-    constexpr int N = Z::NZC, E = Shape<N>::E, TL = Shape<N>::TL, B = Shape<N>::B;
-    const int t = threadIdx.x % TL, l = threadIdx.x / TL;
+  fence_proxy_async();
+  cluster.sync();   // outgoing blocks complete, barriers armed in every CTA
+  if (tid < CL) {
+    bulk_s2c(cl_addr(su32(plt + rank * Z::KC * Z::RY), tid), su32(a1 + tid * Z::KC * Z::RY), Z::KC * Z::RY * 8,
+             cl_addr(bar_in, tid));
+  } else if (tid < 2 * CL && rank == 0) {
+    bulk_s2c(cl_addr(su32(plt + Z::NZC * Z::RY), tid - CL), su32(nq + (tid - CL) * Z::RY), Z::RY * 8,
+             cl_addr(bar_in, tid - CL));
+  }
+  if (tid < 2 * CL) bulk_commit();
+  mbar_wait(bar_in, 0, fault);
+  {  // c2r z pass of this CTA's rows (line-fast), rows stored through shared memory
+    constexpr int N = Z::NZC, E = Shape<N>::E, TL = Shape<N>::TL, B = Shape<N>::B, LP = Shape<N>::LP;
+    const int t = tid / B, l = tid % B;
 #pragma unroll 1
     for (int rb = 0; rb < Z::RB; rb++) {
-      const C *row = pl + (rb * B + l) * Z::PZ;
+      const int r = rb * B + l;
       C v[E];
 #pragma unroll
       for (int q = 0; q < E; q++) {
         // Z[k] = (X[k] + X*[N-k]) + i w^-k (X[k] - X*[N-k]),  w = exp(-2 pi i / 2N)
         const int e = t + TL * q;
-        const C xk = row[e], xm = row[N - e];
+        const C xk = plt[e * Z::RY + r], xm = plt[(N - e) * Z::RY + r];
         const C sum = make_float2(xk.x + xm.x, xk.y - xm.y), dif = make_float2(xk.x - xm.x, xk.y + xm.y);
         C w = __ldg(&tw2z[e]);
         w.y = -w.y;
@@ -598,11 +705,21 @@ __global__ void __launch_bounds__(256) yz_c2r_kernel(const C *__restrict__ twz, 
         v[q] = make_float2(sum.x - tt.y, sum.y + tt.x);
       }
       transform<N>(v, t, l, 1.f, twz, scr);
-      const int y = rank * Z::RY + rb * B + l;
 #pragma unroll
-      for (int j = 0; j < E; j++) st(x, y, final_pos<N>(t, j), v[j]);
+      for (int j = 0; j < E; j++) scr[sidx(l, final_pos<N>(t, j), LP)] = v[j];
+      __syncthreads();
+      constexpr int IT = B * N / 256;
+#pragma unroll
+      for (int it = 0; it < IT; it++) {
+        const int idx = tid + it * 256, e = idx % N, ll = idx / N;
+        const C val = scr[sidx(ll, e, LP)];
+        C *row = reinterpret_cast<C *>(f + ((size_t) x * NY + rank * Z::RY + rb * B + ll) * NZ);
+        row[e] = make_float2(val.x * scale, val.y * scale);
+      }
+      __syncthreads();
     }
   }
+  if (tid < 2 * CL) bulk_wait_read();   // own outgoing copies have read their blocks
 }
 
 }  // namespace ff

@@ -1,5 +1,6 @@
 // FFT plans, twiddle tables and launchers for the x-pencil kernels.
 #include <math.h>
+#include <stdlib.h>
 #include <string.h>
 #include <map>
 #include <mutex>
@@ -285,6 +286,8 @@ template int launch_xkinetic<double>(KinArgs<double> &);
 // ------------------------------------------------------------------ fused z + y passes
 namespace {
 
+int *g_zy_fault = nullptr;   // set by a fused kernel whose barrier wait gave up
+
 template <int NY, int NZ, int CL, bool FWD, class Kern, class... Args>
 int launch_zy_cluster(Kern kfn, int nx, Args... args) {
   typedef ff::ZYPlane<NY, NZ, CL> Z;
@@ -292,6 +295,10 @@ int launch_zy_cluster(Kern kfn, int nx, Args... args) {
   if (!attr_done) {
     DFT_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, Z::SMEM));
     attr_done = true;
+  }
+  if (!g_zy_fault) {
+    DFT_CUDA(cudaMalloc(&g_zy_fault, sizeof(int)));
+    DFT_CUDA(cudaMemset(g_zy_fault, 0, sizeof(int)));
   }
   FftPlan<float> pz, p2, py;
   DFT_TRY(get_plan<float>(Z::NZC, &pz));
@@ -311,46 +318,48 @@ int launch_zy_cluster(Kern kfn, int nx, Args... args) {
   cfg.attrs = at;
   cfg.numAttrs = 1;
   const cudaError_t e = cudaLaunchKernelEx(&cfg, kfn, (const float2 *) pz.tw, (const float2 *) p2.tw,
-                                           (const float2 *) py.tw, args..., nx);
+                                           (const float2 *) py.tw, args..., nx, g_zy_fault);
   if (e != cudaSuccess) {
     cudaFuncAttributes fa = {};
     cudaFuncGetAttributes(&fa, kfn);
-    int ncl = -1;
-    cudaOccupancyMaxActiveClusters(&ncl, kfn, &cfg);
     set_error(DFTGPU_ERR_CUDA, "fused %s pass %dx%d (cluster %d, %d B shared, nx %d): %s; function: %d regs, "
-              "max dynamic shared %d B; active clusters %d", FWD ? "zy r2c" : "yz c2r", NY, NZ, CL, Z::SMEM, nx,
-              cudaGetErrorString(e), fa.numRegs, fa.maxDynamicSharedSizeBytes, ncl);
+              "max dynamic shared %d B", FWD ? "zy r2c" : "yz c2r", NY, NZ, CL, Z::SMEM, nx, cudaGetErrorString(e),
+              fa.numRegs, fa.maxDynamicSharedSizeBytes);
     return DFTGPU_ERR_CUDA;
   }
   return DFTGPU_OK;
 }
 
 bool fused_shape(int ny, int nz) {
-  return !generic_fft_only() && !fused_zy_off() && ny == nz && (ny == 128 || ny == 256 || ny == 512);
+  return !generic_fft_only() && !fused_zy_off() && ny == nz && (ny == 128 || ny == 256);
 }
 
 }  // namespace
 
+int fused_zy_fault() {
+  if (!g_zy_fault) return DFTGPU_OK;
+  int v = 0;
+  DFT_CUDA(cudaMemcpy(&v, g_zy_fault, sizeof(int), cudaMemcpyDeviceToHost));
+  if (v) {
+    cudaMemset(g_zy_fault, 0, sizeof(int));
+    set_error(DFTGPU_ERR_CUDA, "fused plane pass: a barrier wait timed out");
+    return DFTGPU_ERR_CUDA;
+  }
+  return DFTGPU_OK;
+}
+
 int launch_zy_r2c(const RealPairLoad<float> &ld, float2 *spec, int nx, int ny, int nz) {
-  typedef RealPairLoad<float> Ld;
   if (!fused_shape(ny, nz)) return -1;
   ProfScope prof("fft_zy_r2c", (double) nx * ny * nz * 4.0 + (double) nx * ny * (nz / 2 + 1) * 8.0);
-  switch (ny) {
-    case 128: return launch_zy_cluster<128, 128, 2, true>(ff::zy_r2c_kernel<128, 128, 2, Ld>, nx, ld, spec);
-    case 256: return launch_zy_cluster<256, 256, 8, true>(ff::zy_r2c_kernel<256, 256, 8, Ld>, nx, ld, spec);
-    default: return launch_zy_cluster<512, 512, 8, true>(ff::zy_r2c_kernel<512, 512, 8, Ld>, nx, ld, spec);
-  }
+  if (ny == 128) return launch_zy_cluster<128, 128, 2, true>(ff::zy_r2c_kernel<128, 128, 2>, nx, ld.f, spec);
+  return launch_zy_cluster<256, 256, 8, true>(ff::zy_r2c_kernel<256, 256, 8>, nx, ld.f, spec);
 }
 
 int launch_yz_c2r(const float2 *spec, const RealPairStore<float> &st, int nx, int ny, int nz) {
-  typedef RealPairStore<float> St;
   if (!fused_shape(ny, nz)) return -1;
   ProfScope prof("fft_yz_c2r", (double) nx * ny * nz * 4.0 + (double) nx * ny * (nz / 2 + 1) * 8.0);
-  switch (ny) {
-    case 128: return launch_zy_cluster<128, 128, 2, false>(ff::yz_c2r_kernel<128, 128, 2, St>, nx, spec, st);
-    case 256: return launch_zy_cluster<256, 256, 8, false>(ff::yz_c2r_kernel<256, 256, 8, St>, nx, spec, st);
-    default: return launch_zy_cluster<512, 512, 8, false>(ff::yz_c2r_kernel<512, 512, 8, St>, nx, spec, st);
-  }
+  if (ny == 128) return launch_zy_cluster<128, 128, 2, false>(ff::yz_c2r_kernel<128, 128, 2>, nx, spec, st.f, st.scale);
+  return launch_zy_cluster<256, 256, 8, false>(ff::yz_c2r_kernel<256, 256, 8>, nx, spec, st.f, st.scale);
 }
 
 }  // namespace dftgpu

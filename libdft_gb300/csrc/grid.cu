@@ -411,7 +411,8 @@ template <typename T> static int copy_in(void *dev, const double *host, size_t n
 }
 
 int copy_values_out(int prec, const void *dev, double *host, size_t n) {
-  return prec == DFTGPU_FP32 ? copy_out<float>(dev, host, n) : copy_out<double>(dev, host, n);
+  DFT_TRY(prec == DFTGPU_FP32 ? copy_out<float>(dev, host, n) : copy_out<double>(dev, host, n));
+  return fused_zy_fault();
 }
 int copy_values_in(int prec, void *dev, const double *host, size_t n) {
   return prec == DFTGPU_FP32 ? copy_in<float>(dev, host, n) : copy_in<double>(dev, host, n);

@@ -52,5 +52,8 @@ int rspectrum(rgrid *g, double *host);
 int prof_enable(int on);
 int prof_report(char *buf, size_t len);
 int rho_dot_re(rgrid *rho, cgrid *P, double *out);   // sum rho Re(P) dV
+// DFTGPU_ERR_CUDA (with a message) if a fused plane pass's barrier wait timed
+// out since the last call (fft.cu); synchronous.
+int fused_zy_fault();
 
 }  // namespace dftgpu
