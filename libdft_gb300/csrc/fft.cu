@@ -98,8 +98,8 @@ int choose_tile(int n, int nb, size_t cplx_bytes, int nbufs, int *B, size_t *sme
 bool fused_zy_off() {
   static int v = -1;
   if (v < 0) {
-    const char *e = getenv("DFTGPU_NO_FUSED_ZY");
-    v = (e && e[0] == '1') ? 1 : 0;
+    const char *e = getenv("DFTGPU_FUSED_ZY");
+    v = (e && e[0] == '1') ? 0 : 1;
   }
   return v == 1;
 }

@@ -476,6 +476,9 @@ template <typename T> int launch_xconv(XConvArgs<T> &A);
 template <typename T> int launch_xkinetic(KinArgs<T> &A);
 
 // ------------------------------------------------------------ fused z + y passes
-bool fused_zy_off();   // DFTGPU_NO_FUSED_ZY=1 selects the separate z and y passes
+// The fused z + y plane passes (cluster kernels, fast_fft.cuh) are selected
+// with DFTGPU_FUSED_ZY=1; by default the separate passes run (measured
+// faster at 256^3: 60-64 us against 73-83 us per real transform).
+bool fused_zy_off();
 
 }  // namespace dftgpu
