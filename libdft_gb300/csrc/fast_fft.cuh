@@ -306,15 +306,20 @@ template <int N> constexpr int xconv_smem(int nslice) {
   return Shape<N>::B * Shape<N>::LP * (int) sizeof(C) + nslice * (N / 2 + 1) * Shape<N>::B * (int) sizeof(float);
 }
 
-// Inputs are processed one after the other (forward FFT in registers).  An
-// output with one term is produced right after its input; at most one output
-// with several terms (MULTI) is accumulated in registers and produced at the
-// end.  The launch parameters are staged in shared memory, and this CTA's
-// slice of every kernel octant (all kx, the B ky of its pencils) is fetched
-// with cp.async while the first input is loaded and transformed.
+// Inputs are processed one after the other (forward FFT in registers).
+// MODE 0: every output has one term and is produced right after its input.
+// MODE 1: as 0, plus at most one output with several terms (index `multi`)
+//         accumulated in registers and produced at the end.
+// MODE 2: a single output, the sum of all terms, accumulated in registers;
+//         the next input's loads are issued before the current input's
+//         transform, so two inputs are in flight per thread.
+// The launch parameters are staged in shared memory, and this CTA's slice of
+// every kernel octant (all kx, the B ky of its pencils) is fetched with
+// cp.async while the first input is loaded and transformed.
 // Requires B | ny/2 so that a CTA's pencils lie on one side of ny/2.
-template <int N, bool MULTI>
-__global__ void __launch_bounds__(256, MULTI ? 1 : 2) xconv_kernel(const C *__restrict__ tw, const XArgsF A, int multi) {
+template <int N, int MODE>
+__global__ void __launch_bounds__(256, MODE == 1 ? 1 : 2) xconv_kernel(const C *__restrict__ tw, const XArgsF A, int multi) {
+  constexpr bool MULTI = MODE == 1;
   constexpr int E = Shape<N>::E, TL = Shape<N>::TL, B = Shape<N>::B, LP = Shape<N>::LP, KXH = N / 2 + 1;
   extern __shared__ __align__(16) unsigned char smraw[];
   C *sm = reinterpret_cast<C *>(smraw);
@@ -335,6 +340,48 @@ __global__ void __launch_bounds__(256, MULTI ? 1 : 2) xconv_kernel(const C *__re
   }
   cp_async_commit();
   const size_t plane = (size_t) A.nx * A.ny;
+  if constexpr (MODE == 2) {
+    C acc[E], nxt[E];
+#pragma unroll
+    for (int j = 0; j < E; j++) acc[j] = make_float2(0.f, 0.f);
+    {
+      const C *src = A.src[0] + kz * plane + y;
+#pragma unroll
+      for (int q = 0; q < E; q++) nxt[q] = src[(size_t) (t + TL * q) * A.ny];
+    }
+    __syncthreads();   // sA ready
+    for (int in = 0; in < sA.nin; in++) {
+      C v[E];
+#pragma unroll
+      for (int q = 0; q < E; q++) v[q] = nxt[q];
+      if (in + 1 < sA.nin) {
+        const C *src = sA.src[in + 1] + kz * plane + y;
+#pragma unroll
+        for (int q = 0; q < E; q++) nxt[q] = src[(size_t) (t + TL * q) * A.ny];
+      }
+      transform<N>(v, t, l, -1.f, tw, sm);
+      if (in == 0) {
+        cp_async_wait_all();
+        __syncthreads();   // kernel slices visible to all threads
+      }
+      for (int tm = 0; tm < sA.nterm[0]; tm++) {
+        if (sA.in[tm] != in) continue;
+#pragma unroll
+        for (int j = 0; j < E; j++) acc[j] = acc[j] + kmul(sA, ks, KXH, B, tm, v[j], final_pos<N>(t, j), y, iyo);
+      }
+    }
+    to_input_order<N>(acc);
+    transform<N>(acc, t, l, 1.f, tw, sm);
+    C *dst = sA.dst[0] + kz * plane + y;
+#pragma unroll
+    for (int j = 0; j < E; j++) {
+      C r = acc[j];
+      const size_t off = (size_t) final_pos<N>(t, j) * A.ny;
+      if (sA.acc_out[0]) r = r + dst[off];
+      dst[off] = r;
+    }
+    return;
+  }
   C acc[MULTI ? E : 1];
   if constexpr (MULTI) {
 #pragma unroll

@@ -171,15 +171,20 @@ template <int N> int fast_xconv(const XConvArgs<float> &A) {
   const int smem = ff::xconv_smem<N>(F.nslice);
   // request exactly the dynamic shared memory this launch needs (the kernel
   // also has static shared memory, so the opt-in maximum itself is not valid)
-  static int granted[2] = { 48 * 1024, 48 * 1024 };
-  if (smem > granted[multi >= 0]) {
-    if (multi >= 0) DFT_CUDA(cudaFuncSetAttribute(ff::xconv_kernel<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    else DFT_CUDA(cudaFuncSetAttribute(ff::xconv_kernel<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    granted[multi >= 0] = smem;
+  // MODE 2: one output summing every term; 1: mixed with one multi-term output; 0: single-term outputs
+  const int mode = (A.nout == 1 && multi == 0) ? 2 : (multi >= 0 ? 1 : 0);
+  static int granted[3] = { 48 * 1024, 48 * 1024, 48 * 1024 };
+  if (smem > granted[mode]) {
+    if (mode == 2) DFT_CUDA(cudaFuncSetAttribute(ff::xconv_kernel<N, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    else if (mode == 1) DFT_CUDA(cudaFuncSetAttribute(ff::xconv_kernel<N, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    else DFT_CUDA(cudaFuncSetAttribute(ff::xconv_kernel<N, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    granted[mode] = smem;
   }
   ProfScope prof("fft_x_conv", xconv_bytes(A, F.kxh, F.kyh));
-  if (multi >= 0) ff::xconv_kernel<N, true><<<dim3(A.ny / B, A.nkz), 256, smem, rt().stream>>>(p.tw, F, multi);
-  else ff::xconv_kernel<N, false><<<dim3(A.ny / B, A.nkz), 256, smem, rt().stream>>>(p.tw, F, multi);
+  const dim3 grid(A.ny / B, A.nkz);
+  if (mode == 2) ff::xconv_kernel<N, 2><<<grid, 256, smem, rt().stream>>>(p.tw, F, multi);
+  else if (mode == 1) ff::xconv_kernel<N, 1><<<grid, 256, smem, rt().stream>>>(p.tw, F, multi);
+  else ff::xconv_kernel<N, 0><<<grid, 256, smem, rt().stream>>>(p.tw, F, multi);
   DFT_CHECK_LAUNCH();
   return DFTGPU_OK;
 }
