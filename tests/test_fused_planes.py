@@ -34,8 +34,8 @@ for shape, step, model in json.loads(sys.argv[2]):
     r = G.RGrid(shape, step); r.set(f); s = r.spectrum(); r.free()
     w = G.Wf(shape, step); ot = G.OT(model, w); w.set(liquid_psi(shape, step, 2))
     P = G.CGrid(shape, step); P.zero(); ot.potential(P, w); p = P.get()
-    np.save(sys.argv[3] + "/spec_%d.npy" % shape[1] + "_%d" % shape[0], s)
-    np.save(sys.argv[3] + "/pot_%d.npy" % shape[1] + "_%d" % shape[0], p)
+    np.save(sys.argv[3] + "/spec_%d_%d.npy" % (shape[1], shape[0]), s)
+    np.save(sys.argv[3] + "/pot_%d_%d.npy" % (shape[1], shape[0]), p)
     for o in (P, ot, w): o.free()
 print("ok")
 """
