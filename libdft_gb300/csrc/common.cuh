@@ -88,6 +88,12 @@ struct Runtime {
 Runtime &rt();
 int ensure_device();
 
+// Streams for parallel graph branches: returns how many streams to use (the
+// work stream included); aux[0..n-2] are the others, ev[0..n-1] fork / join
+// events.
+constexpr int PAR_MAX = 4;
+int par_streams(cudaStream_t **aux, cudaEvent_t **ev);
+
 // Device-resident FP64 accumulator slots used by reductions.
 double *reduce_slots();
 int reduce_partials(double **buf, size_t *n);

@@ -60,6 +60,29 @@ int ensure_device() {
   return DFTGPU_OK;
 }
 
+// ------------------------------------------------------------------ parallel branches
+// Auxiliary streams for independent transforms (par_for in ops.cuh).  The
+// number of streams used (work stream included) is DFTGPU_STREAMS, default 2.
+int par_streams(cudaStream_t **aux, cudaEvent_t **ev) {
+  static int n = -1;
+  static cudaStream_t s[PAR_MAX - 1];
+  static cudaEvent_t e[PAR_MAX];
+  if (n < 0) {
+    const char *v = getenv("DFTGPU_STREAMS");
+    int want = v ? atoi(v) : 2;
+    if (want < 1) want = 1;
+    if (want > PAR_MAX) want = PAR_MAX;
+    for (int i = 0; i < want - 1; i++)
+      if (cudaStreamCreateWithFlags(&s[i], cudaStreamNonBlocking) != cudaSuccess) { want = i + 1; break; }
+    for (int i = 0; i < want; i++)
+      if (cudaEventCreateWithFlags(&e[i], cudaEventDisableTiming) != cudaSuccess) { want = 1; break; }
+    n = want;
+  }
+  *aux = s;
+  *ev = e;
+  return n;
+}
+
 // ------------------------------------------------------------------ profiler
 namespace {
 struct ProfRec { cudaEvent_t a, b; const char *name; double bytes; };

@@ -11,6 +11,35 @@ template <class F> __global__ void each_kernel(size_t n, F f) {
   for (size_t i = (size_t) blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t) gridDim.x * blockDim.x) f(i);
 }
 
+// f(0..n-1), independent of one another, spread round-robin over the work
+// stream and the auxiliary streams with event fork / join, so that a CUDA
+// graph captured from the work stream gets them as parallel branches.  Runs
+// on the work stream alone while the profiler is on (per-launch timings).
+template <class F> int par_for(int n, F f) {
+  cudaStream_t *aux;
+  cudaEvent_t *ev;
+  const int ns = prof_on() || n < 2 ? 1 : par_streams(&aux, &ev);
+  if (ns < 2) {
+    for (int i = 0; i < n; i++) DFT_TRY(f(i));
+    return DFTGPU_OK;
+  }
+  const cudaStream_t main = rt().stream;
+  const int use = ns < n ? ns : n;
+  DFT_CUDA(cudaEventRecord(ev[0], main));
+  for (int k = 0; k < use - 1; k++) DFT_CUDA(cudaStreamWaitEvent(aux[k], ev[0], 0));
+  int rc = DFTGPU_OK;
+  for (int i = 0; i < n && rc == DFTGPU_OK; i++) {
+    rt().stream = i % use == 0 ? main : aux[i % use - 1];
+    rc = f(i);
+  }
+  rt().stream = main;
+  for (int k = 0; k < use - 1; k++) {
+    DFT_CUDA(cudaEventRecord(ev[k + 1], aux[k]));
+    DFT_CUDA(cudaStreamWaitEvent(main, ev[k + 1], 0));
+  }
+  return rc;
+}
+
 // bytes: algorithmic bytes the lambda reads and writes (0 if not stated)
 template <class F> int launch_each(size_t n, F f, double bytes = 0.0, const char *name = "pointwise") {
   if (n == 0) return DFTGPU_OK;

@@ -257,12 +257,14 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
     }
     if (bf) { xc_out(A, s[7]); xc_term(A, 0, F.k(OT_VJ), KER_EVEN, (T) 1); }
     DFT_TRY(launch_xconv<T>(A));
-    DFT_TRY(F.inv(s[2], r[R_RB]));
+    C *sp[6]; T *dst[6]; int n = 0;
+    sp[n] = s[2]; dst[n++] = r[R_RB];
     if (kc) {
-      DFT_TRY(F.inv(s[3], r[R_RT]));
-      for (int a = 0; a < 3; a++) DFT_TRY(F.inv(s[4 + a], r[R_D0 + a]));
+      sp[n] = s[3]; dst[n++] = r[R_RT];
+      for (int a = 0; a < 3; a++) { sp[n] = s[4 + a]; dst[n++] = r[R_D0 + a]; }
     }
-    if (bf) DFT_TRY(F.inv(s[7], r[R_A]));
+    if (bf) { sp[n] = s[7]; dst[n++] = r[R_A]; }
+    DFT_TRY(par_for(n, [&](int i) { return F.inv(sp[i], dst[i]); }));
   }
 
   // pointwise 1
@@ -313,16 +315,20 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
     }, nb * (5 + (kc ? 5 : 0) + (bf ? 9 : 0)), "ot_pointwise_1"));
   }
 
-  // forward transforms of the produced fields
-  DFT_TRY(F.fwd(r[R_Q], s[9]));
-  if (kc) for (int a = 0; a < 3; a++) DFT_TRY(F.fwd(r[R_S0 + a], s[1 + a]));
-  if (bf) {
-    DFT_TRY(F.fwd(r[R_E], s[4]));
-    for (int a = 0; a < 3; a++) DFT_TRY(F.fwd(r[R_B0 + a], s[5 + a]));
+  // forward transforms of the produced fields (independent: parallel branches)
+  {
+    const T *src[8]; C *sp[8]; int n = 0;
+    src[n] = r[R_Q]; sp[n++] = s[9];
+    if (kc) for (int a = 0; a < 3; a++) { src[n] = r[R_S0 + a]; sp[n++] = s[1 + a]; }
+    if (bf) {
+      src[n] = r[R_E]; sp[n++] = s[4];
+      for (int a = 0; a < 3; a++) { src[n] = r[R_B0 + a]; sp[n++] = s[5 + a]; }
+    }
+    DFT_TRY(par_for(n, [&](int i) { return F.fwd(src[i], sp[i]); }));
   }
 
-  // x pass 2
-  if (kc) {
+  // x pass 2: the KC and BF chains are independent
+  auto kc_chain = [&]() -> int {
     XConvArgs<T> A; xc_init(A, P);
     for (int a = 0; a < 3; a++) xc_in(A, (const C *) s[1 + a]);
     xc_out(A, s[8]);                                                            // sum_a dF_a s_a^  (src/ot.c:641)
@@ -337,8 +343,9 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
     DFT_TRY(launch_xconv<T>(B));
     DFT_TRY(F.inv(s[8], r[R_T1]));
     for (int a = 0; a < 3; a++) DFT_TRY(F.inv(s[1 + a], r[R_J0 + a]));
-  }
-  if (bf) {   // B_a = V_j (rho v_a)^ in place (+ C = V_j (rho|v|^2)^ when clamped)
+    return DFTGPU_OK;
+  };
+  auto bf_chain = [&]() -> int {   // B_a = V_j (rho v_a)^ in place (+ C = V_j (rho|v|^2)^ when clamped)
     XConvArgs<T> A; xc_init(A, P);
     for (int a = 0; a < 3; a++) xc_in(A, (const C *) s[5 + a]);
     for (int a = 0; a < 3; a++) { xc_out(A, s[5 + a]); xc_term(A, a, F.k(OT_VJ), KER_EVEN, (T) 1); }
@@ -346,7 +353,11 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
     DFT_TRY(launch_xconv<T>(A));
     if (!cmerge) DFT_TRY(F.inv(s[10], r[R_C]));
     for (int a = 0; a < 3; a++) DFT_TRY(F.inv(s[5 + a], r[R_BB0 + a]));
-  }
+    return DFTGPU_OK;
+  };
+  if (kc && bf) DFT_TRY(par_for(2, [&](int i) { return i == 0 ? kc_chain() : bf_chain(); }));
+  else if (kc) DFT_TRY(kc_chain());
+  else if (bf) DFT_TRY(bf_chain());
 
   // pointwise 2
   if (kc || bf) {
