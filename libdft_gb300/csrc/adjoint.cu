@@ -95,29 +95,32 @@ static int ot_vjp_t(dft_ot_functional *otf, wf *gwf, const typename cplx_t<T>::t
     if (kc) DFT_TRY(F.inv(s[2], r[A_GAM]));
   }
   // pointwise 1: X = gamma (c2 rb + c3 rb^2) + Wg (c2 + 2 c3 rb) rho ; lambda_loc = Wg (c2 rb + c3 rb^2)
-  //   KC: Y = gamma rho_st, Z_a = gamma J_a, lJ_a = c (Gam g_a - gamma d_a)
+  //   KC: Y = gamma rho_st, divZ = sum_a D_a (gamma J_a), lJ_a = c (Gam g_a - gamma D_a (F*rho))
+  //   (dF_a = D_a F, so sum_a dF_a*(gamma J_a) = F*divZ and dF_a*rho = D_a (F*rho))
   {
     const T c2 = (T) otf->c2, c3 = (T) otf->c3, ck = (T) (otf->alpha_s / (2.0 * otf->mass));
     T *gr = r[A_GR], *wg = r[A_WG], *gm = r[A_GAM], *X = r[A_X], *loc = r[A_LOC], *Y = r[A_Y];
-    T *rb = r[R_RB], *rst = r[R_RST];
-    T *Z0 = r[A_Z0], *Z1 = r[A_Z1], *Z2 = r[A_Z2], *L0 = r[A_LJ0], *L1 = r[A_LJ1], *L2 = r[A_LJ2];
-    T *J0 = r[R_J0], *J1 = r[R_J1], *J2 = r[R_J2], *d0 = r[R_D0], *d1 = r[R_D1], *d2 = r[R_D2];
+    T *rb = r[R_RB], *rst = r[R_RST], *rt = r[R_RT], *dz = r[A_Z0];
+    T *L0 = r[A_LJ0], *L1 = r[A_LJ1], *L2 = r[A_LJ2];
+    T *J0 = r[R_J0], *J1 = r[R_J1], *J2 = r[R_J2];
     DFT_TRY(launch_rows(nx, ny, nz, [=] __device__(int x, int y, int z, int i) {
       const T b = rb[i], ga = gr[i], w = wg[i], q1 = c2 * b + c3 * b * b;
       X[i] = ga * q1 + w * (c2 + (T) 2 * c3 * b) * rho[i];
       loc[i] = w * q1;
       if (kc) {
         Y[i] = ga * rst[i];
-        const T *Ja[3] = { J0, J1, J2 }, *da[3] = { d0, d1, d2 };
-        T *Za[3] = { Z0, Z1, Z2 }, *La[3] = { L0, L1, L2 };
+        const T *Ja[3] = { J0, J1, J2 };
+        T *La[3] = { L0, L1, L2 };
+        T dv = 0;
         for (int a = 0; a < 3; a++) {
           int ip, im; S.nb(x, y, z, i, a, ip, im);
           const T ga_ = (rho[ip] - rho[im]) * inv2h;
-          Za[a][i] = ga * Ja[a][i];
-          La[a][i] = ck * (gm[i] * ga_ - ga * da[a][i]);
+          dv += (gr[ip] * Ja[a][ip] - gr[im] * Ja[a][im]) * inv2h;
+          La[a][i] = ck * (gm[i] * ga_ - ga * ((rt[ip] - rt[im]) * inv2h));
         }
+        dz[i] = dv;
       }
-    }));
+    }, 0.0, "adj_pointwise_1"));
   }
   DFT_TRY(F.fwd(r[A_X], s[3]));
   {
@@ -128,46 +131,40 @@ static int ot_vjp_t(dft_ot_functional *otf, wf *gwf, const typename cplx_t<T>::t
   if (kc) {
     const T ck = (T) (otf->alpha_s / (2.0 * otf->mass));
     DFT_TRY(F.fwd(r[A_Y], s[4]));
-    for (int a = 0; a < 3; a++) DFT_TRY(F.fwd(r[A_Z0 + a], s[5 + a]));
+    DFT_TRY(F.fwd(r[A_Z0], s[5]));
     for (int a = 0; a < 3; a++) DFT_TRY(F.fwd(r[A_LJ0 + a], s[8 + a]));
-    XConvArgs<T> A; xc_init(A, P); xc_in(A, (const C *) s[4]);             // Q_a = dF_a * Y
-    xc_out(A, s[1]); xc_term(A, 0, F.k(OT_FX), KER_ODD_X, (T) 1);
-    xc_out(A, s[2]); xc_term(A, 0, F.k(OT_FY), KER_ODD_Y, (T) 1);
-    xc_out(A, s[4]); xc_term(A, 0, F.k(OT_FZ), KER_ODD_Z, (T) 1);
+    XConvArgs<T> A; xc_init(A, P);                                          // F*Y ; lacc += c F*divZ
+    xc_in(A, (const C *) s[4]);
+    xc_in(A, (const C *) s[5]);
+    xc_out(A, s[4]); xc_term(A, 0, F.k(OT_F), KER_EVEN, (T) 1);
+    xc_out(A, lacc, 1); xc_term(A, 1, F.k(OT_F), KER_EVEN, ck);
     DFT_TRY(launch_xconv<T>(A));
-    XConvArgs<T> B; xc_init(B, P);                                          // + c sum_a dF_a * Z_a
-    for (int a = 0; a < 3; a++) xc_in(B, (const C *) s[5 + a]);
-    xc_out(B, lacc, 1);
-    xc_term(B, 0, F.k(OT_FX), KER_ODD_X, ck);
-    xc_term(B, 1, F.k(OT_FY), KER_ODD_Y, ck);
-    xc_term(B, 2, F.k(OT_FZ), KER_ODD_Z, ck);
-    DFT_TRY(launch_xconv<T>(B));
     XConvArgs<T> D; xc_init(D, P);                                          // F * lJ_a
     for (int a = 0; a < 3; a++) xc_in(D, (const C *) s[8 + a]);
     for (int a = 0; a < 3; a++) { xc_out(D, s[8 + a]); xc_term(D, a, F.k(OT_F), KER_EVEN, (T) 1); }
     DFT_TRY(launch_xconv<T>(D));
-    DFT_TRY(F.inv(s[1], r[A_Q0]));
-    DFT_TRY(F.inv(s[2], r[A_Q1]));
-    DFT_TRY(F.inv(s[4], r[A_Q2]));
+    DFT_TRY(F.inv(s[4], r[A_Q0]));
     for (int a = 0; a < 3; a++) DFT_TRY(F.inv(s[8 + a], r[A_FLJ0 + a]));
-    // pointwise 2: lG_a = -c Q_a + F*lJ_a ; lg_a = c Gam J_a + lG_a rho_st ; lst = c gamma T + sum lG_a g_a
+    // pointwise 2: Q_a = dF_a*Y = D_a (F*Y) ; lG_a = -c Q_a + F*lJ_a ; lg_a = c Gam J_a + lG_a rho_st ;
+    //              lst = c gamma sum_a D_a J_a + sum lG_a g_a
     {
-      T *gr = r[A_GR], *gm = r[A_GAM], *rst = r[R_RST], *T1 = r[R_T1], *lst = r[A_LST];
-      T *Q0 = r[A_Q0], *Q1 = r[A_Q1], *Q2 = r[A_Q2], *F0 = r[A_FLJ0], *F1 = r[A_FLJ1], *F2 = r[A_FLJ2];
+      T *gr = r[A_GR], *gm = r[A_GAM], *rst = r[R_RST], *lst = r[A_LST], *fy = r[A_Q0];
+      T *F0 = r[A_FLJ0], *F1 = r[A_FLJ1], *F2 = r[A_FLJ2];
       T *J0 = r[R_J0], *J1 = r[R_J1], *J2 = r[R_J2], *G0 = r[A_LG0], *G1 = r[A_LG1], *G2 = r[A_LG2];
       DFT_TRY(launch_rows(nx, ny, nz, [=] __device__(int x, int y, int z, int i) {
-        const T *Qa[3] = { Q0, Q1, Q2 }, *Fa[3] = { F0, F1, F2 }, *Ja[3] = { J0, J1, J2 };
+        const T *Fa[3] = { F0, F1, F2 }, *Ja[3] = { J0, J1, J2 };
         T *Ga[3] = { G0, G1, G2 };
-        T acc = ck * gr[i] * T1[i];
+        T acc = 0, t1 = 0;
         for (int a = 0; a < 3; a++) {
           int ip, im; S.nb(x, y, z, i, a, ip, im);
           const T ga_ = (rho[ip] - rho[im]) * inv2h;
-          const T lG = -ck * Qa[a][i] + Fa[a][i];
+          const T lG = -ck * ((fy[ip] - fy[im]) * inv2h) + Fa[a][i];
           Ga[a][i] = ck * gm[i] * Ja[a][i] + lG * rst[i];
           acc += lG * ga_;
+          t1 += (Ja[a][ip] - Ja[a][im]) * inv2h;
         }
-        lst[i] = acc;
-      }));
+        lst[i] = acc + ck * gr[i] * t1;
+      }, 0.0, "adj_pointwise_2"));
     }
     // pointwise 3: lambda_loc -= sum_a D_a(lg_a)
     {

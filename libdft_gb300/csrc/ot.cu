@@ -5,15 +5,16 @@
 // one inverse c2r per needed real field; linearity merges the reference's
 // per-axis KC transforms and every term that enters the potential linearly:
 //   rho = |psi|^2 ;  rho^ = F rho
-//   x pass 1 (one input): w rho^, F rho^, dF_a rho^ (a = x,y,z), V_j rho^
+//   x pass 1 (one input): w rho^, F rho^, V_j rho^
 //   pointwise 1: P.re += c2/2 rb^2 + c3/3 rb^3 ; q = (c2 rb + c3 rb^2) rho
 //             KC: rho_st, s_a = (d_a rho) rho_st ;  BF: v, rho|v|^2, rho v_a
-//   x pass 2: sum_a dF_a s_a^ ; F s_a^ (-> J_a) ; V_j (rho v_a)^ (-> B_a)
-//   pointwise 2: P.re += c rho_st sum_a(dF_a*s_a) - c sum_a J_a (dF_a*rho)
+//   x pass 2: F s_a^ (-> J_a) ; V_j (rho v_a)^ (-> B_a)
+//   pointwise 2: P.re += c rho_st sum_a D_a J_a - c sum_a J_a D_a(F*rho)
+//             (dF_a = D_a F: the derivative kernels are central differences)
 //             KC: h = sum_a (d_a rho) J_a ;  BF: -m/2 (A|v|^2 - 2 v.B), w_a = v_a A - B_a
 //   x pass 3: V_LJ rho^ + w q^ + c F h^ - m/2 V_j (rho|v|^2)^  (one output)
 //   pointwise 3: P.re += that linear part ; BF imaginary part.
-// Full model: 10 forward and 14 inverse real transforms (src/ot.c: 34).
+// Full model: 10 forward and 10 inverse real transforms (src/ot.c: 34).
 #include <math.h>
 #include <string.h>
 
@@ -245,24 +246,19 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
   DFT_TRY(density(gwf->grid, otf->density));                                   // src/ot.c:320
   DFT_TRY(F.fwd(rho, s[0]));
 
-  // x pass 1: one input, kernels SA (+F, dF_a) (+V_j); rho^ stays in s0
+  // x pass 1: one input, kernels SA (+F) (+V_j); rho^ stays in s0.  The
+  // derivative kernels dF_a are the central-difference gradient of the
+  // sampled F (src/ot.c:195-196), so dF_a*f = D_a (F*f) on the periodic grid:
+  // dF_a*rho and sum_a dF_a*G_a are taken as stencils of F*rho and J_a.
   {
     XConvArgs<T> A; xc_init(A, P); xc_in(A, (const C *) s[0]);
     xc_out(A, s[2]); xc_term(A, 0, F.k(OT_SA), KER_EVEN, (T) 1);
-    if (kc) {
-      xc_out(A, s[3]); xc_term(A, 0, F.k(OT_F), KER_EVEN, (T) 1);
-      xc_out(A, s[4]); xc_term(A, 0, F.k(OT_FX), KER_ODD_X, (T) 1);
-      xc_out(A, s[5]); xc_term(A, 0, F.k(OT_FY), KER_ODD_Y, (T) 1);
-      xc_out(A, s[6]); xc_term(A, 0, F.k(OT_FZ), KER_ODD_Z, (T) 1);
-    }
+    if (kc) { xc_out(A, s[3]); xc_term(A, 0, F.k(OT_F), KER_EVEN, (T) 1); }
     if (bf) { xc_out(A, s[7]); xc_term(A, 0, F.k(OT_VJ), KER_EVEN, (T) 1); }
     DFT_TRY(launch_xconv<T>(A));
-    C *sp[6]; T *dst[6]; int n = 0;
+    C *sp[3]; T *dst[3]; int n = 0;
     sp[n] = s[2]; dst[n++] = r[R_RB];
-    if (kc) {
-      sp[n] = s[3]; dst[n++] = r[R_RT];
-      for (int a = 0; a < 3; a++) { sp[n] = s[4 + a]; dst[n++] = r[R_D0 + a]; }
-    }
+    if (kc) { sp[n] = s[3]; dst[n++] = r[R_RT]; }
     if (bf) { sp[n] = s[7]; dst[n++] = r[R_A]; }
     DFT_TRY(par_for(n, [&](int i) { return F.inv(sp[i], dst[i]); }));
   }
@@ -329,19 +325,11 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
 
   // x pass 2: the KC and BF chains are independent
   auto kc_chain = [&]() -> int {
-    XConvArgs<T> A; xc_init(A, P);
-    for (int a = 0; a < 3; a++) xc_in(A, (const C *) s[1 + a]);
-    xc_out(A, s[8]);                                                            // sum_a dF_a s_a^  (src/ot.c:641)
-    xc_term(A, 0, F.k(OT_FX), KER_ODD_X, (T) 1);
-    xc_term(A, 1, F.k(OT_FY), KER_ODD_Y, (T) 1);
-    xc_term(A, 2, F.k(OT_FZ), KER_ODD_Z, (T) 1);
-    DFT_TRY(launch_xconv<T>(A));
     // J_a = F s_a^ in place (src/ot.c:652)
     XConvArgs<T> B; xc_init(B, P);
     for (int a = 0; a < 3; a++) xc_in(B, (const C *) s[1 + a]);
     for (int a = 0; a < 3; a++) { xc_out(B, s[1 + a]); xc_term(B, a, F.k(OT_F), KER_EVEN, (T) 1); }
     DFT_TRY(launch_xconv<T>(B));
-    DFT_TRY(F.inv(s[8], r[R_T1]));
     for (int a = 0; a < 3; a++) DFT_TRY(F.inv(s[1 + a], r[R_J0 + a]));
     return DFTGPU_OK;
   };
@@ -363,19 +351,21 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
   if (kc || bf) {
     const T c = (T) (otf->alpha_s / (2.0 * otf->mass)), hm = (T) (-0.5 * otf->mass), cbf = (T) otf->c_bfpot;
     const T pcap = (T) otf->max_bfpot, inv2h = (T) (1.0 / (2.0 * P->step));
-    T *rst = r[R_RST], *t1 = r[R_T1], *J0 = r[R_J0], *J1 = r[R_J1], *J2 = r[R_J2];
-    T *d0 = r[R_D0], *d1 = r[R_D1], *d2 = r[R_D2], *h = r[R_H];
+    T *rst = r[R_RST], *rt = r[R_RT], *J0 = r[R_J0], *J1 = r[R_J1], *J2 = r[R_J2], *h = r[R_H];
     T *v0 = r[R_V0], *v1 = r[R_V1], *v2 = r[R_V2], *A = r[R_A], *Cc = r[R_C], *B0 = r[R_BB0], *B1 = r[R_BB1], *B2 = r[R_BB2];
     DFT_TRY(launch_rows(nx, ny, nz, [=] __device__(int x, int y, int z, int i) {
       C p = pot[i];
-      if (kc) {  // src/ot.c:643-645, 673-675 summed over axes
-        p.x += c * rst[i] * t1[i] - c * (J0[i] * d0[i] + J1[i] * d1[i] + J2[i] * d2[i]);
+      if (kc) {  // src/ot.c:641-645, 656-657, 673-675 summed over axes
         const T *Ja[3] = { J0, J1, J2 };
-        T hv = 0;
+        T hv = 0, t1 = 0, jd = 0;
         for (int a = 0; a < 3; a++) {
           int ip, im; S.nb(x, y, z, i, a, ip, im);
-          hv += (rho[ip] - rho[im]) * inv2h * Ja[a][i];   // src/ot.c:656-657
+          const T ja = Ja[a][i];
+          hv += (rho[ip] - rho[im]) * inv2h * ja;        // (d_a rho) J_a
+          t1 += (Ja[a][ip] - Ja[a][im]) * inv2h;         // dF_a * G_a = D_a J_a
+          jd += ja * ((rt[ip] - rt[im]) * inv2h);        // J_a (dF_a * rho) = J_a D_a (F*rho)
         }
+        p.x += c * rst[i] * t1 - c * jd;
         h[i] = hv;
       }
       if (bf) {  // src/ot.c:895-915, 924-931; V_j*(rho|v|^2) is in the linear part unless clamped
@@ -386,7 +376,7 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
         v0[i] = x * a - B0[i]; v1[i] = y * a - B1[i]; v2[i] = z * a - B2[i];
       }
       pot[i] = p;
-    }, nb * (2 + (kc ? 10 : 0) + (bf ? (clampp ? 11 : 10) : 0)), "ot_pointwise_2"));
+    }, nb * (2 + (kc ? 7 : 0) + (bf ? (clampp ? 11 : 10) : 0)), "ot_pointwise_2"));
   }
 
   // merged linear part (one inverse transform):
