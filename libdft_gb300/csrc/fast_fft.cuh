@@ -198,29 +198,6 @@ __global__ void __launch_bounds__(256) line_kernel(const C *__restrict__ tw, con
   if constexpr (LDS == 0) {
 #pragma unroll
     for (int q = 0; q < E; q++) v[q] = ld(a, b0 + l, t + TL * q);
-  } else if constexpr (LDS == 2) {
-    // C2R with the mirrored element X[N-k] loaded directly (it is another
-    // thread's primary element of the same line: served by L1 / L2)
-    static_assert(MODE == 2, "direct mirrored loads: c2r only");
-    C xk[E], xm[E];
-#pragma unroll
-    for (int q = 0; q < E; q++) {
-      const int e = t + TL * q;
-      xk[q] = ld(a, b0 + l, e);
-      xm[q] = ld(a, b0 + l, N - e);
-    }
-#pragma unroll
-    for (int q = 0; q < E; q++) {
-      // Z[k] = (X[k] + X*[N-k]) + i w^-k (X[k] - X*[N-k]),  w = exp(-2 pi i / 2N)
-      const int e = t + TL * q;
-      C a0 = xk[q], a1 = xm[q];
-      if (e == 0) { a0.y = 0.f; a1.y = 0.f; }
-      const C sum = make_float2(a0.x + a1.x, a0.y - a1.y), dif = make_float2(a0.x - a1.x, a0.y + a1.y);
-      C w = __ldg(&tw2[e]);
-      w.y = -w.y;
-      const C tt = cmul(dif, w);
-      v[q] = make_float2(sum.x - tt.y, sum.y + tt.x);
-    }
   } else {
     // line-fast cooperative load of the whole tile (C2R: also the Nyquist
     // element N, which lands in the pitch's spare slot), fully unrolled so

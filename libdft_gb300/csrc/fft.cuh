@@ -406,7 +406,7 @@ int launch_fast_lines(int na, int nb, float sign, const Ld &ld, const St &st) {
   static_assert(MODE != LINE_R2C || (EF == 1 && EFS == 0), "r2c z pass: element-fast load, line-fast store");
   static_assert(MODE != LINE_C2R || (EF == 0 && EFS == 1), "c2r z pass: line-fast load, element-fast store");
   constexpr int MAP = (EF == 0 && EFS == 0) ? ff::MAP_L : ff::MAP_E;
-  constexpr int LDS = (EF == 0 && EFS == 1) ? (MODE == LINE_C2R ? 2 : 1) : 0;
+  constexpr int LDS = (EF == 0 && EFS == 1) ? 1 : 0;
   constexpr int STS = (EF == 1 && EFS == 0) ? 1 : 0;
   constexpr int B = ff::Shape<N>::B;
   if (nb % B) return -1;
