@@ -1,7 +1,7 @@
 // Register-resident line FFTs for FP32 power-of-two lengths N = 64..512.
 //
 // Each thread owns E = 8 or 16 elements of one line; TL = N / E threads work
-// on a line and a CTA of NT (256 or 512) threads holds B = NT / TL lines.  A length-N
+// on a line and a CTA of 256 threads holds B = 256 / TL lines.  A length-N
 // transform is 2 or 3 Stockham stages with compile-time radices
 //   N = 64: 8 x 8     N = 128: 16 x 8     N = 256: 16 x 16     N = 512: 16 x 16 x 2
 // computed entirely in registers; only the stage boundaries exchange data
@@ -186,14 +186,11 @@ enum { MAP_E = 0, MAP_L = 1 };
 // MODE 0 C2C, 1 R2C (N = nz/2, post-processed to N+1 outputs), 2 C2R.
 // LDS / STS: stage the load / store side through shared memory with a
 // line-fast cooperative loop (used for the transposed side of z passes).
-template <int N, int MODE, int MAP, int LDS, int STS, class Ld, class St, int NT = 256>
-__global__ void __launch_bounds__(NT) line_kernel(const C *__restrict__ tw, const C *__restrict__ tw2, float sign,
+template <int N, int MODE, int MAP, int LDS, int STS, class Ld, class St>
+__global__ void __launch_bounds__(256) line_kernel(const C *__restrict__ tw, const C *__restrict__ tw2, float sign,
                                                    const Ld ld, const St st) {
-  constexpr int E = Shape<N>::E, TL = Shape<N>::TL, B = NT / TL, LP = Shape<N>::LP;
-  // B * LP elements: static for 256 threads, dynamic (above 48 KB) for 512
-  __shared__ C sm_static[NT == 256 ? B * LP : 1];
-  extern __shared__ __align__(16) unsigned char sm_dyn[];
-  C *sm = NT == 256 ? sm_static : reinterpret_cast<C *>(sm_dyn);
+  constexpr int E = Shape<N>::E, TL = Shape<N>::TL, B = Shape<N>::B, LP = Shape<N>::LP;
+  __shared__ C sm[B * LP];
   const int a = blockIdx.y, b0 = blockIdx.x * B;
   const int t = MAP == MAP_E ? threadIdx.x % TL : threadIdx.x / B;
   const int l = MAP == MAP_E ? threadIdx.x / TL : threadIdx.x % B;
@@ -205,11 +202,11 @@ __global__ void __launch_bounds__(NT) line_kernel(const C *__restrict__ tw, cons
     // line-fast cooperative load of the whole tile (C2R: also the Nyquist
     // element N, which lands in the pitch's spare slot), fully unrolled so
     // that every load is in flight before the first shared-memory store
-    constexpr int NE = MODE == 2 ? N + 1 : N, TOT = B * NE, IT = (TOT + NT - 1) / NT;
+    constexpr int NE = MODE == 2 ? N + 1 : N, TOT = B * NE, IT = (TOT + 255) / 256;
 #pragma unroll
     for (int it = 0; it < IT; it++) {
-      const int idx = threadIdx.x + it * NT;
-      if (TOT % NT == 0 || idx < TOT) {
+      const int idx = threadIdx.x + it * 256;
+      if (TOT % 256 == 0 || idx < TOT) {
         const int ll = idx % B, e = idx / B;
         sm[sidx(ll, e, LP)] = ld(a, b0 + ll, e);
       }
@@ -243,10 +240,10 @@ __global__ void __launch_bounds__(NT) line_kernel(const C *__restrict__ tw, cons
     __syncthreads();
     if constexpr (MODE == 1) {
       // X[k] = (Z[k] + Z*[N-k]) / 2 - (i/2) w^k (Z[k] - Z*[N-k]),  k = 0..N
-      constexpr int TOT = B * (N + 1), IT = (TOT + NT - 1) / NT;
+      constexpr int TOT = B * (N + 1), IT = (TOT + 255) / 256;
 #pragma unroll
       for (int it = 0; it < IT; it++) {
-        const int idx = threadIdx.x + it * NT;
+        const int idx = threadIdx.x + it * 256;
         if (idx < TOT) {
           const int ll = idx % B, k = idx / B;
           const C zk = sm[sidx(ll, k == N ? 0 : k, LP)], zm = sm[sidx(ll, k == 0 ? 0 : N - k, LP)];
@@ -257,10 +254,10 @@ __global__ void __launch_bounds__(NT) line_kernel(const C *__restrict__ tw, cons
         }
       }
     } else {
-      constexpr int IT = B * N / NT;
+      constexpr int IT = B * N / 256;
 #pragma unroll
       for (int it = 0; it < IT; it++) {
-        const int idx = threadIdx.x + it * NT;
+        const int idx = threadIdx.x + it * 256;
         const int ll = idx % B, e = idx / B;
         st(a, b0 + ll, e, sm[sidx(ll, e, LP)]);
       }

@@ -104,15 +104,6 @@ bool fused_zy_off() {
   return v == 1;
 }
 
-bool z_wide() {
-  static int v = -1;
-  if (v < 0) {
-    const char *e = getenv("DFTGPU_Z_WIDE");
-    v = (e && e[0] == '0') ? 0 : 1;
-  }
-  return v == 1;
-}
-
 bool generic_fft_only() {
   static int v = -1;
   if (v < 0) {

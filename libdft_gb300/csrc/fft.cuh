@@ -397,7 +397,6 @@ template <class Kernel> bool SmemOptIn<Kernel>::done = false;
 }  // namespace
 
 bool generic_fft_only();   // DFTGPU_GENERIC_FFT=1 disables the register kernels
-bool z_wide();             // DFTGPU_Z_WIDE=0 keeps 256-thread z-pass CTAs
 
 // FP32 power-of-two lengths: register-resident kernel.  EF / EFS: the fast
 // address index of the load / store side is the element (1) or the line (0).
@@ -415,22 +414,6 @@ int launch_fast_lines(int na, int nb, float sign, const Ld &ld, const St &st) {
   DFT_TRY(get_plan<float>(N, &p1));
   p2.tw = nullptr;
   if (MODE != LINE_C2C) DFT_TRY(get_plan<float>(2 * N, &p2));
-  // z passes (one side transposed): 512-thread CTAs, so that each spectral
-  // row segment a CTA touches is twice as long (DRAM locality)
-  if constexpr ((LDS || STS) && N <= 256) {
-    if (z_wide() && nb % (2 * B) == 0) {
-      constexpr int smem = 2 * B * ff::Shape<N>::LP * (int) sizeof(float2);
-      auto kfn = ff::line_kernel<N, MODE, MAP, LDS, STS, Ld, St, 512>;
-      typedef SmemOptIn<ff::Shape<N> (*)(Ld *, St *, int (*)[MODE + 1][MAP + 1][LDS + 1][STS + 1])> Flag;
-      if (!Flag::done) {
-        DFT_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-        Flag::done = true;
-      }
-      kfn<<<dim3(nb / (2 * B), na), 512, smem, rt().stream>>>(p1.tw, p2.tw, sign, ld, st);
-      DFT_CHECK_LAUNCH();
-      return DFTGPU_OK;
-    }
-  }
   ff::line_kernel<N, MODE, MAP, LDS, STS, Ld, St><<<dim3(nb / B, na), 256, 0, rt().stream>>>(p1.tw, p2.tw, sign, ld, st);
   DFT_CHECK_LAUNCH();
   return DFTGPU_OK;
