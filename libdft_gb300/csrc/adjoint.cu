@@ -187,7 +187,7 @@ static int ot_vjp_t(dft_ot_functional *otf, wf *gwf, const typename cplx_t<T>::t
   if (bf) {
     const T m = (T) otf->mass, eps = (T) otf->div_epsilon;
     const T vf = (T) (1.0 / (gwf->mass * 2.0 * P->step)), invm = (T) (1.0 / gwf->mass);
-    T *gr = r[A_GR], *gi = r[A_GI], *Aa = r[R_A], *w0 = r[R_V0], *w1 = r[R_V1], *w2 = r[R_V2];
+    T *gr = r[A_GR], *gi = r[A_GI], *Aa = r[R_A];
     T *B0 = r[R_BB0], *B1 = r[R_BB1], *B2 = r[R_BB2];
     T *vx = r[A_VX], *vy = r[A_VY], *vz = r[A_VZ], *lA = r[A_LA], *lC = r[A_LC];
     T *lB0 = r[A_LB0], *lB1 = r[A_LB1], *lB2 = r[A_LB2], *mu0 = r[A_MU0], *mu1 = r[A_MU1], *mu2 = r[A_MU2];
@@ -199,7 +199,7 @@ static int ot_vjp_t(dft_ot_functional *otf, wf *gwf, const typename cplx_t<T>::t
       if (rr < eps) rr = eps;
       const T g0 = vf / rr;
       T v[3];
-      const T *wa[3] = { w0, w1, w2 }, *Ba[3] = { B0, B1, B2 };
+      const T *Ba[3] = { B0, B1, B2 };
       T *lBa[3] = { lB0, lB1, lB2 }, *mua[3] = { mu0, mu1, mu2 }, *pa[3] = { p0, p1, p2 };
       for (int a = 0; a < 3; a++) {
         int ip, im; S.nb(x, y, z, i, a, ip, im);
@@ -219,8 +219,9 @@ static int ot_vjp_t(dft_ot_functional *otf, wf *gwf, const typename cplx_t<T>::t
         la += lw * v[a];
         lBa[a][i] = m * ga * v[a] - lw;
         mua[a][i] = -m * ga * (A * v[a] - Ba[a][i]) + lw * A;
-        pa[a][i] = (T) 0.5 * gb * wa[a][i] / re;                         // for - D_a(1/2 gamma_i w_a / rho_eps)
-        if (rh > eps) lrho -= (T) 0.5 * gb * drho * wa[a][i] / (re * re);
+        const T wa = v[a] * A - Ba[a][i];                                 // w_a = v_a A - B_a
+        pa[a][i] = (T) 0.5 * gb * wa / re;                               // for - D_a(1/2 gamma_i w_a / rho_eps)
+        if (rh > eps) lrho -= (T) 0.5 * gb * drho * wa / (re * re);
       }
       lA[i] = la;
       lC[i] = -(T) 0.5 * m * ga;

@@ -11,9 +11,10 @@
 //   x pass 2: F s_a^ (-> J_a) ; V_j (rho v_a)^ (-> B_a)
 //   pointwise 2: P.re += c rho_st sum_a D_a J_a - c sum_a J_a D_a(F*rho)
 //             (dF_a = D_a F: the derivative kernels are central differences)
-//             KC: h = sum_a (d_a rho) J_a ;  BF: -m/2 (A|v|^2 - 2 v.B), w_a = v_a A - B_a
+//             KC: h = sum_a (d_a rho) J_a ;  BF: -m/2 (A|v|^2 - 2 v.B) and the
+//             imaginary part from w_a = v_a A - B_a (formed at each stencil point)
 //   x pass 3: V_LJ rho^ + w q^ + c F h^ - m/2 V_j (rho|v|^2)^  (one output)
-//   pointwise 3: P.re += that linear part ; BF imaginary part.
+//   pointwise 3: P.re += that linear part.
 // Full model: 10 forward and 10 inverse real transforms (src/ot.c: 34).
 #include <math.h>
 #include <string.h>
@@ -351,6 +352,7 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
   if (kc || bf) {
     const T c = (T) (otf->alpha_s / (2.0 * otf->mass)), hm = (T) (-0.5 * otf->mass), cbf = (T) otf->c_bfpot;
     const T pcap = (T) otf->max_bfpot, inv2h = (T) (1.0 / (2.0 * P->step));
+    const T eps = (T) otf->div_epsilon;
     T *rst = r[R_RST], *rt = r[R_RT], *J0 = r[R_J0], *J1 = r[R_J1], *J2 = r[R_J2], *h = r[R_H];
     T *v0 = r[R_V0], *v1 = r[R_V1], *v2 = r[R_V2], *A = r[R_A], *Cc = r[R_C], *B0 = r[R_BB0], *B1 = r[R_BB1], *B2 = r[R_BB2];
     DFT_TRY(launch_rows(nx, ny, nz, [=] __device__(int x, int y, int z, int i) {
@@ -368,15 +370,30 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
         p.x += c * rst[i] * t1 - c * jd;
         h[i] = hv;
       }
-      if (bf) {  // src/ot.c:895-915, 924-931; V_j*(rho|v|^2) is in the linear part unless clamped
-        const T x = v0[i], y = v1[i], z = v2[i], a = A[i];
-        T re = hm * (a * (z * z + y * y + x * x) - (T) 2 * (x * B0[i] + y * B1[i] + z * B2[i]));
+      if (bf) {
+        // real part src/ot.c:895-915 (V_j*(rho|v|^2) is in the linear part unless clamped)
+        const T *va[3] = { v0, v1, v2 }, *Ba[3] = { B0, B1, B2 };
+        const T a = A[i];
+        T vv = 0, vb = 0;
+        for (int k = 0; k < 3; k++) { vv += va[k][i] * va[k][i]; vb += va[k][i] * Ba[k][i]; }
+        T re = hm * (a * vv - (T) 2 * vb);
         if (clampp) re = clampv<T>(re + hm * Cc[i], pcap);
         p.x += re * cbf;
-        v0[i] = x * a - B0[i]; v1[i] = y * a - B1[i]; v2[i] = z * a - B2[i];
+        // imaginary part src/ot.c:924-990 with w_a = v_a A - B_a (src/ot.c:924-931)
+        T rr = rho[i];
+        if (rr < eps) rr = eps;
+        T im = 0;
+        for (int k = 0; k < 3; k++) {
+          int ip, imm; S.nb(x, y, z, i, k, ip, imm);
+          const T w = va[k][i] * a - Ba[k][i];
+          const T wp = va[k][ip] * A[ip] - Ba[k][ip], wm = va[k][imm] * A[imm] - Ba[k][imm];
+          im += (T) 0.5 * (((rho[ip] - rho[imm]) * inv2h) / rr) * w + (T) 0.5 * ((wp - wm) * inv2h);
+        }
+        if (clampp) im = clampv<T>(im, pcap);
+        p.y += im * cbf;
       }
       pot[i] = p;
-    }, nb * (2 + (kc ? 7 : 0) + (bf ? (clampp ? 11 : 10) : 0)), "ot_pointwise_2"));
+    }, nb * (2 + (kc ? 7 : 0) + (bf ? (clampp ? 9 : 8) : 0)), "ot_pointwise_2"));
   }
 
   // merged linear part (one inverse transform):
@@ -398,33 +415,15 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
     DFT_TRY(F.inv(s[11], r[R_U]));
   }
 
-  // pointwise 3
+  // pointwise 3: P.re += linear part ; scale
   {
-    const T cbf = (T) otf->c_bfpot, inv2h = (T) (1.0 / (2.0 * P->step));
-    const T eps = (T) otf->div_epsilon, pcap = (T) otf->max_bfpot;
-    T *lin = r[R_U], *w0 = r[R_V0], *w1 = r[R_V1], *w2 = r[R_V2];
+    T *lin = r[R_U];
     DFT_TRY(launch_rows(nx, ny, nz, [=] __device__(int x, int y, int z, int i) {
       C p = pot[i];
       p.x += lin[i];
-      if (bf) {  // src/ot.c:933-990
-        const T *wa[3] = { w0, w1, w2 };
-        T rr = rho[i];
-        if (rr < eps) rr = eps;
-        T im = 0;
-        for (int a = 0; a < 3; a++) {
-          int ip, imm; S.nb(x, y, z, i, a, ip, imm);
-          im += (T) 0.5 * (((rho[ip] - rho[imm]) * inv2h) / rr) * wa[a][i];
-        }
-        for (int a = 0; a < 3; a++) {
-          int ip, imm; S.nb(x, y, z, i, a, ip, imm);
-          im += (T) 0.5 * ((wa[a][ip] - wa[a][imm]) * inv2h);
-        }
-        if (clampp) im = clampv<T>(im, pcap);
-        p.y += im * cbf;
-      }
       if (scale != (T) 1) { p.x *= scale; p.y *= scale; }
       pot[i] = p;
-    }, nb * (5 + (bf ? 4 : 0)), "ot_pointwise_3"));
+    }, nb * 5, "ot_pointwise_3"));
   }
   return DFTGPU_OK;
 }

@@ -15,7 +15,7 @@ namespace dftgpu {
 // R_U the merged linear part (LJ*rho + w*q + c F*h - m/2 V_j*(rho|v|^2)),
 // R_RB rho_bar, R_RT F*rho, R_A V_j*rho,
 // R_Q (c2 rb + c3 rb^2) rho, R_RST rho_st, R_S0..2 G_a = (d_a rho) rho_st,
-// R_V0..2 w_a = v_a A - B_a (BF; the velocity itself is overwritten),
+// R_V0..2 the velocity v_a (BF),
 // R_E rho|v|^2, R_B0..2 rho v_a, R_J0..2 J_a = F*G_a,
 // R_C V_j*(rho|v|^2) (only with a clamped backflow potential),
 // R_BB0..2 B_a = V_j*(rho v_a), R_H sum_a (d_a rho) J_a.  Slots from
