@@ -145,10 +145,15 @@ def time_steps(G, torch, w, wp, ot, P, mu0, dt, steps, dist):
     torch.cuda.nvtx.range_pop()
     ms = t0.elapsed_time(t1)
     if dist:
-        x = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(x, op=torch.distributed.ReduceOp.MAX)
-        ms = float(x.item())
+        ms = max_over_ranks(torch, ms, "cuda")
     return ms
+
+
+def max_over_ranks(torch, ms, device):
+    """Replica timing: the slowest rank's milliseconds (all ranks get it)."""
+    x = torch.tensor([ms], device=device, dtype=torch.float64)
+    torch.distributed.all_reduce(x, op=torch.distributed.ReduceOp.MAX)
+    return float(x.item())
 
 
 def profile_step(G, w, wp, ot, P, mu0, dt):
