@@ -274,37 +274,47 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
     const double vf = 1.0 / (gwf->mass * 2.0 * P->step), deps = otf->div_epsilon;
     const bool clampv_on = otf->max_veloc < (999.0 / GRID_AUTOMPS);
     const T vcap = (T) otf->max_veloc;
+    // every load is issued before the first store (stores through the other
+    // pointers could alias the loaded arrays, so the compiler keeps the order)
     DFT_TRY(launch_rows(nx, ny, nz, [=] __device__(int x, int y, int z, int i) {
       const T b = rb[i], rh = rho[i];
-      // src/ot.c:557-567 (the LJ term src/ot.c:530 is in the merged linear part)
       C p = overwrite ? mk<T>((T) 0, (T) 0) : pot[i];
       if (base) p.x += base[i];
+      T st = 0, dr[3] = { 0, 0, 0 };
+      if (kc) {
+        st = (T) 1 - rt[i] * irs;
+        for (int a = 0; a < 3; a++) {
+          int ip, im; S.nb(x, y, z, i, a, ip, im);
+          dr[a] = (rho[ip] - rho[im]) * inv2h;
+        }
+      }
+      T va[3] = { 0, 0, 0 };
+      if (bf) {  // velocity src/ot.c:390-395
+        const C pz = psi[i];
+        C d[3];
+        for (int a = 0; a < 3; a++) {
+          int ip, im; S.nb(x, y, z, i, a, ip, im);
+          d[a] = psi[ip] - psi[im];
+        }
+        T rr = pz.x * pz.x + pz.y * pz.y;             // velocity in the grid's precision
+        if (rr < (T) deps) rr = (T) deps;
+        const T g0 = (T) vf / rr;
+        for (int a = 0; a < 3; a++) {
+          T vv = g0 * (pz.x * d[a].y - pz.y * d[a].x);
+          if (clampv_on) vv = clampv<T>(vv, vcap);
+          va[a] = vv;
+        }
+      }
+      // src/ot.c:557-567 (the LJ term src/ot.c:530 is in the merged linear part)
       p.x += add;
       p.x += (c2 / (T) 2) * (b * b) + (c3 / (T) 3) * (b * b * b);
       pot[i] = p;
       q[i] = (c2 * b + c3 * (b * b)) * rh;
       if (kc) {  // src/ot.c:608-612, 632-637
-        const T st = (T) 1 - rt[i] * irs;
         rst[i] = st;
-        T *sa[3] = { s0, s1, s2 };
-        for (int a = 0; a < 3; a++) {
-          int ip, im; S.nb(x, y, z, i, a, ip, im);
-          sa[a][i] = (rho[ip] - rho[im]) * inv2h * st;
-        }
+        s0[i] = dr[0] * st; s1[i] = dr[1] * st; s2[i] = dr[2] * st;
       }
-      if (bf) {  // velocity src/ot.c:390-395; C, B_a inputs src/ot.c:852-888
-        const C pz = psi[i];
-        T rr = pz.x * pz.x + pz.y * pz.y;             // velocity in the grid's precision
-        if (rr < (T) deps) rr = (T) deps;
-        const T g0 = (T) vf / rr;
-        T va[3];
-        for (int a = 0; a < 3; a++) {
-          int ip, im; S.nb(x, y, z, i, a, ip, im);
-          const C d = psi[ip] - psi[im];
-          T vv = g0 * (pz.x * d.y - pz.y * d.x);
-          if (clampv_on) vv = clampv<T>(vv, vcap);
-          va[a] = vv;
-        }
+      if (bf) {  // C, B_a inputs src/ot.c:852-888
         v0[i] = va[0]; v1[i] = va[1]; v2[i] = va[2];
         e[i] = (va[2] * va[2] + va[1] * va[1] + va[0] * va[0]) * rh;
         b0[i] = va[0] * rh; b1[i] = va[1] * rh; b2[i] = va[2] * rh;
@@ -357,6 +367,7 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
     T *v0 = r[R_V0], *v1 = r[R_V1], *v2 = r[R_V2], *A = r[R_A], *Cc = r[R_C], *B0 = r[R_BB0], *B1 = r[R_BB1], *B2 = r[R_BB2];
     DFT_TRY(launch_rows(nx, ny, nz, [=] __device__(int x, int y, int z, int i) {
       C p = pot[i];
+      T hval = 0;   // stores last: every load is issued before them
       if (kc) {  // src/ot.c:641-645, 656-657, 673-675 summed over axes
         const T *Ja[3] = { J0, J1, J2 };
         T hv = 0, t1 = 0, jd = 0;
@@ -368,7 +379,7 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
           jd += ja * ((rt[ip] - rt[im]) * inv2h);        // J_a (dF_a * rho) = J_a D_a (F*rho)
         }
         p.x += c * rst[i] * t1 - c * jd;
-        h[i] = hv;
+        hval = hv;
       }
       if (bf) {
         // real part src/ot.c:895-915 (V_j*(rho|v|^2) is in the linear part unless clamped)
@@ -392,6 +403,7 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
         if (clampp) im = clampv<T>(im, pcap);
         p.y += im * cbf;
       }
+      if (kc) h[i] = hval;
       pot[i] = p;
     }, nb * (2 + (kc ? 7 : 0) + (bf ? (clampp ? 9 : 8) : 0)), "ot_pointwise_2"));
   }
