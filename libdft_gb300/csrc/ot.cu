@@ -13,8 +13,7 @@
 //             (dF_a = D_a F: the derivative kernels are central differences)
 //             KC: h = sum_a (d_a rho) J_a ;  BF: -m/2 (A|v|^2 - 2 v.B) and the
 //             imaginary part from w_a = v_a A - B_a (formed at each stencil point)
-//   x pass 3: V_LJ rho^ + w q^ - m/2 V_j (rho|v|^2)^ (concurrently with x pass 2),
-//             then + c F h^ once h is known; one inverse transform
+//   x pass 3: V_LJ rho^ + w q^ + c F h^ - m/2 V_j (rho|v|^2)^  (one output)
 //   pointwise 3: P.re += that linear part.
 // Full model: 10 forward and 10 inverse real transforms (src/ot.c: 34).
 #include <math.h>
@@ -355,27 +354,9 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
     for (int a = 0; a < 3; a++) DFT_TRY(F.inv(s[5 + a], r[R_BB0 + a]));
     return DFTGPU_OK;
   };
-  // the linear part's terms that are known now: V_LJ rho^ + w q^ (src/ot.c:530,
-  // 582-585) + c_bf (-m/2) V_j (rho|v|^2)^ (src/ot.c:895-915) into s11
-  auto lin_early = [&]() -> int {
-    XConvArgs<T> A; xc_init(A, P);
-    xc_in(A, (const C *) s[0]);
-    xc_in(A, (const C *) s[9]);
-    if (cmerge) xc_in(A, (const C *) s[4]);
-    xc_out(A, s[11]);
-    xc_term(A, 0, F.k(OT_LJ), KER_EVEN, (T) 1);
-    xc_term(A, 1, F.k(OT_SA), KER_EVEN, (T) 1);
-    if (cmerge) xc_term(A, 2, F.k(OT_VJ), KER_EVEN, (T) (-0.5 * otf->mass * otf->c_bfpot));
-    return launch_xconv<T>(A);
-  };
-  {
-    int n = 0;
-    int which[3];
-    if (kc) which[n++] = 0;
-    if (bf) which[n++] = 1;
-    which[n++] = 2;
-    DFT_TRY(par_for(n, [&](int i) { return which[i] == 0 ? kc_chain() : which[i] == 1 ? bf_chain() : lin_early(); }));
-  }
+  if (kc && bf) DFT_TRY(par_for(2, [&](int i) { return i == 0 ? kc_chain() : bf_chain(); }));
+  else if (kc) DFT_TRY(kc_chain());
+  else if (bf) DFT_TRY(bf_chain());
 
   // pointwise 2
   if (kc || bf) {
@@ -427,17 +408,24 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
     }, nb * (2 + (kc ? 7 : 0) + (bf ? (clampp ? 9 : 8) : 0)), "ot_pointwise_2"));
   }
 
-  // merged linear part (one inverse transform): the early terms in s11
-  // + c F h^ (KC, src/ot.c:656-664)
-  if (kc) {
-    DFT_TRY(F.fwd(r[R_H], s[10]));
+  // merged linear part (one inverse transform):
+  //   V_LJ rho^ + w q^ (src/ot.c:530, 582-585) + c F h^ (KC, src/ot.c:656-664)
+  //   + c_bf (-m/2) V_j (rho|v|^2)^ (BF, src/ot.c:895-915)
+  if (kc) DFT_TRY(F.fwd(r[R_H], s[10]));
+  {
     XConvArgs<T> A; xc_init(A, P);
-    xc_in(A, (const C *) s[10]);
-    xc_out(A, s[11], 1);
-    xc_term(A, 0, F.k(OT_F), KER_EVEN, (T) (otf->alpha_s / (2.0 * otf->mass)));
+    xc_in(A, (const C *) s[0]);
+    xc_in(A, (const C *) s[9]);
+    if (kc) xc_in(A, (const C *) s[10]);
+    if (cmerge) xc_in(A, (const C *) s[4]);
+    xc_out(A, s[11]);
+    xc_term(A, 0, F.k(OT_LJ), KER_EVEN, (T) 1);
+    xc_term(A, 1, F.k(OT_SA), KER_EVEN, (T) 1);
+    if (kc) xc_term(A, 2, F.k(OT_F), KER_EVEN, (T) (otf->alpha_s / (2.0 * otf->mass)));
+    if (cmerge) xc_term(A, kc ? 3 : 2, F.k(OT_VJ), KER_EVEN, (T) (-0.5 * otf->mass * otf->c_bfpot));
     DFT_TRY(launch_xconv<T>(A));
+    DFT_TRY(F.inv(s[11], r[R_U]));
   }
-  DFT_TRY(F.inv(s[11], r[R_U]));
 
   // pointwise 3: P.re += linear part ; scale
   {
