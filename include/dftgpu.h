@@ -267,6 +267,31 @@ dft_ot_functional *dft_ot_alloc(INT model, wf *gwf, INT min_substeps, INT max_su
 void dft_ot_free(dft_ot_functional *otf);                                                   /* src/ot.c:268 */
 void dft_ot_potential(dft_ot_functional *otf, cgrid *potential, wf *gwf);                    /* src/ot.c:314 */
 void dft_ot_energy_density(dft_ot_functional *otf, rgrid *energy_density, wf *gwf);         /* src/ot-energy.c:38 */
+/* The potential from a given density and velocity field instead of a wave
+ * function (src/ot.c:431).  With backflow the velocity grids are clamped to
+ * max_veloc and overwritten with w_a = v_a (V_j*rho) - V_j*(rho v_a), as the
+ * reference does (src/ot.c:494-497, 924-931). */
+void dft_ot_potential2(dft_ot_functional *otf, cgrid *potential, rgrid *density, rgrid *veloc_x,
+                       rgrid *veloc_y, rgrid *veloc_z);                                    /* src/ot.c:431 */
+/* Single terms, added to potential from the given density (src/ot.c:524, 547,
+ * 840; "usually not called directly").  The workspace / rho_tf arguments are
+ * accepted for signature compatibility and not used: the library keeps its
+ * spectra in its own work buffers, so rho_tf does not receive FFT(rho). */
+void dft_ot_add_lennard_jones_potential(dft_ot_functional *otf, cgrid *potential, rgrid *density,
+                                        rgrid *workspace1, rgrid *workspace2);             /* src/ot.c:524 */
+void dft_ot_add_local_correlation_potential(dft_ot_functional *otf, cgrid *potential, rgrid *rho,
+                                            rgrid *rho_tf, rgrid *workspace1,
+                                            rgrid *workspace2);                            /* src/ot.c:547 */
+void dft_ot_backflow_potential(dft_ot_functional *otf, cgrid *potential, rgrid *density, rgrid *veloc_x,
+                               rgrid *veloc_y, rgrid *veloc_z, rgrid *workspace1, rgrid *workspace2,
+                               rgrid *workspace3, rgrid *workspace4, rgrid *workspace5,
+                               rgrid *workspace6);                                         /* src/ot.c:840 */
+/* KC and backflow parts of the energy density, added to energy_density, with
+ * the given density (src/ot-energy.c:123, 202). */
+void dft_ot_energy_density_kc(dft_ot_functional *otf, rgrid *energy_density, wf *gwf,
+                              rgrid *density);                                             /* src/ot-energy.c:123 */
+void dft_ot_energy_density_bf(dft_ot_functional *otf, rgrid *energy_density, wf *gwf,
+                              rgrid *density);                                             /* src/ot-energy.c:202 */
 void dft_ot_init_params(dft_ot_functional *otf, INT model);                                 /* src/ot.c:1002 */
 /* Regenerate the k-space kernels after changing otf parameters such as l_g
  * (src/ot.c:138-217 run again); libdft has no separate entry for this. */

@@ -134,6 +134,12 @@ SIGNATURES = {
     "dftgpu_pc_step": (_i, [_vp, _vp, _vp, _vp, _vp, _d, _d, _d]),
     "dftgpu_run": (_i, [_vp, _vp, _vp, _vp, _vp, _d, _d, _d, _l, _i]),
     "dftgpu_energy_report": (_i, [_vp, _vp, _vp, _dp, _dp, _dp]),
+    "dft_ot_potential2": (None, [_vp] * 6),
+    "dft_ot_add_lennard_jones_potential": (None, [_vp] * 5),
+    "dft_ot_add_local_correlation_potential": (None, [_vp] * 6),
+    "dft_ot_backflow_potential": (None, [_vp] * 12),
+    "dft_ot_energy_density_kc": (None, [_vp] * 4),
+    "dft_ot_energy_density_bf": (None, [_vp] * 4),
     "dftgpu_ot_potential_vjp": (_i, [_vp, _vp, _vp, _vp]),
     "dftgpu_wf_propagate_vjp": (_i, [_vp, _vp, _d, _d, _vp, _vp, _vp, _vp, _vp]),
     "dftgpu_pc_step_vjp": (_i, [_vp, _vp, _vp, _d, _d, _d, _i, _vp, _vp]),

@@ -465,6 +465,76 @@ void dft_ot_potential(dft_ot_functional *otf, cgrid *potential, wf *gwf) {
   ot_potential(otf, potential, gwf);
 }
 
+static bool ot_matches_r(dft_ot_functional *otf, const rgrid *r) {
+  OtPriv *P = otf ? (OtPriv *) otf->priv : nullptr;
+  return r && P && r->nx == P->nx && r->ny == P->ny && r->nz == P->nz && r->prec == P->prec;
+}
+
+static void potential_from_fields(const char *what, dft_ot_functional *otf, cgrid *potential, rgrid *density,
+                                  rgrid *vx, rgrid *vy, rgrid *vz, int terms, bool vclamp) {
+  if (!otf || !ot_matches(otf, potential) || !ot_matches_r(otf, density)) { bad_arg(what); return; }
+  PotSrc src;
+  src.terms = terms;
+  src.dens = density->value;
+  src.vclamp = vclamp;
+  if ((terms & POT_BF) && (otf->model & DFT_OT_BACKFLOW)) {
+    if (!ot_matches_r(otf, vx) || !ot_matches_r(otf, vy) || !ot_matches_r(otf, vz)) { bad_arg(what); return; }
+    src.vel[0] = vx->value; src.vel[1] = vy->value; src.vel[2] = vz->value;
+    src.wout[0] = vx->value; src.wout[1] = vy->value; src.wout[2] = vz->value;
+  }
+  ot_potential_src(otf, potential, nullptr, 0, nullptr, 0.0, 1.0, src);
+}
+
+void dft_ot_potential2(dft_ot_functional *otf, cgrid *potential, rgrid *density, rgrid *veloc_x, rgrid *veloc_y,
+                       rgrid *veloc_z) {
+  potential_from_fields("dft_ot_potential2: grid mismatch", otf, potential, density, veloc_x, veloc_y, veloc_z,
+                        POT_ALL, true);
+}
+
+void dft_ot_add_lennard_jones_potential(dft_ot_functional *otf, cgrid *potential, rgrid *density, rgrid *workspace1,
+                                        rgrid *workspace2) {
+  (void) workspace1; (void) workspace2;
+  potential_from_fields("dft_ot_add_lennard_jones_potential: grid mismatch", otf, potential, density, nullptr,
+                        nullptr, nullptr, POT_LJ, true);
+}
+
+void dft_ot_add_local_correlation_potential(dft_ot_functional *otf, cgrid *potential, rgrid *rho, rgrid *rho_tf,
+                                            rgrid *workspace1, rgrid *workspace2) {
+  (void) rho_tf; (void) workspace1; (void) workspace2;
+  potential_from_fields("dft_ot_add_local_correlation_potential: grid mismatch", otf, potential, rho, nullptr,
+                        nullptr, nullptr, POT_LOCAL, true);
+}
+
+void dft_ot_backflow_potential(dft_ot_functional *otf, cgrid *potential, rgrid *density, rgrid *veloc_x,
+                               rgrid *veloc_y, rgrid *veloc_z, rgrid *workspace1, rgrid *workspace2,
+                               rgrid *workspace3, rgrid *workspace4, rgrid *workspace5, rgrid *workspace6) {
+  (void) workspace1; (void) workspace2; (void) workspace3; (void) workspace4; (void) workspace5; (void) workspace6;
+  if (otf && !(otf->model & DFT_OT_BACKFLOW)) {
+    set_error(DFTGPU_ERR_UNSUPPORTED, "dft_ot_backflow_potential: functional allocated without DFT_OT_BACKFLOW");
+    return;
+  }
+  potential_from_fields("dft_ot_backflow_potential: grid mismatch", otf, potential, density, veloc_x, veloc_y,
+                        veloc_z, POT_BF, false);
+}
+
+static void energy_density_part(const char *what, dft_ot_functional *otf, rgrid *ed, wf *gwf, rgrid *density,
+                                int terms, int model_bit) {
+  if (!otf || !gwf || !ot_matches(otf, gwf->grid) || !ot_matches_r(otf, ed) || !ot_matches_r(otf, density)) {
+    bad_arg(what);
+    return;
+  }
+  if (!(otf->model & model_bit)) { set_error(DFTGPU_ERR_UNSUPPORTED, "%s: term not in the functional's model", what); return; }
+  ot_energy_density_terms(otf, ed, gwf, terms, density, true);
+}
+
+void dft_ot_energy_density_kc(dft_ot_functional *otf, rgrid *ed, wf *gwf, rgrid *density) {
+  energy_density_part("dft_ot_energy_density_kc", otf, ed, gwf, density, POT_KC, DFT_OT_KC);
+}
+
+void dft_ot_energy_density_bf(dft_ot_functional *otf, rgrid *ed, wf *gwf, rgrid *density) {
+  energy_density_part("dft_ot_energy_density_bf", otf, ed, gwf, density, POT_BF, DFT_OT_BACKFLOW);
+}
+
 void dft_ot_energy_density(dft_ot_functional *otf, rgrid *ed, wf *gwf) {
   OtPriv *P = otf ? (OtPriv *) otf->priv : nullptr;
   if (!P || !gwf || !ot_matches(otf, gwf->grid) || !ed || ed->nx != P->nx || ed->ny != P->ny || ed->nz != P->nz || ed->prec != P->prec) {

@@ -221,22 +221,30 @@ done:
 // Spectral slots: s0 rho^, s1-3 s_a^ -> J_a^, s4 (rho|v|^2)^, s5-7 (rho v_a)^ ->
 // B_a^, s8 sum_a dF_a s_a^, s9 q^, s10 h^ (or V_j (rho|v|^2)^ when the backflow
 // potential is clamped), s11 the merged linear part.
+//
+// src selects the terms (LJ, local correlation, KC, BF) and where rho and v
+// come from: psi (dft_ot_potential) or given grids (dft_ot_potential2 and the
+// per-term entry points, src/ot.c:431-507, 524-586, 840-991).
 template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, wf *gwf, int overwrite, const T *base,
-                                             double add_d, double scale_d) {
+                                             double add_d, double scale_d, const PotSrc &src) {
   const T add = (T) add_d, scale = (T) scale_d;
   typedef typename cplx_t<T>::type C;
   OtPriv *P = (OtPriv *) otf->priv;
   Fields<T> F{P, P->nx, P->ny, P->nz};
   const int nx = P->nx, ny = P->ny, nz = P->nz;
   const double nb = (double) nx * ny * nz * sizeof(T);   // bytes of one real field
-  const bool kc = otf->model & DFT_OT_KC, bf = otf->model & DFT_OT_BACKFLOW;
+  const bool lj = src.terms & POT_LJ, loc = src.terms & POT_LOCAL;
+  const bool kc = (src.terms & POT_KC) && (otf->model & DFT_OT_KC);
+  const bool bf = (src.terms & POT_BF) && (otf->model & DFT_OT_BACKFLOW);
   // the backflow real part is merged into the linear part unless it is clamped
   const bool clampp = otf->max_bfpot < (10000.0 / GRID_AUTOK);
   const bool cmerge = bf && !clampp;
   const Stencil3 S{nx, ny, nz};
   C *pot = (C *) Pg->value;
-  const C *psi = (const C *) gwf->grid->value;
+  const C *psi = gwf ? (const C *) gwf->grid->value : nullptr;
   T *rho = (T *) otf->density->value;
+  const T *vin0 = (const T *) src.vel[0], *vin1 = (const T *) src.vel[1], *vin2 = (const T *) src.vel[2];
+  const bool vgiven = vin0 != nullptr;
 
   // real-field slots
   T *r[R_NREAL];   // slots of PotSlot (ot_work.cuh)
@@ -244,21 +252,26 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
   C *s[12];
   for (int i = 0; i < 12; i++) { s[i] = F.s(i); if (!s[i]) return DFTGPU_ERR_NOMEM; }
 
-  DFT_TRY(density(gwf->grid, otf->density));                                   // src/ot.c:320
+  if (src.dens) {
+    if (src.dens != otf->density->value)
+      DFT_CUDA(cudaMemcpyAsync(rho, src.dens, nb, cudaMemcpyDeviceToDevice, rt().stream));
+  } else {
+    DFT_TRY(density(gwf->grid, otf->density));                                 // src/ot.c:320
+  }
   DFT_TRY(F.fwd(rho, s[0]));
 
   // x pass 1: one input, kernels SA (+F) (+V_j); rho^ stays in s0.  The
   // derivative kernels dF_a are the central-difference gradient of the
   // sampled F (src/ot.c:195-196), so dF_a*f = D_a (F*f) on the periodic grid:
   // dF_a*rho and sum_a dF_a*G_a are taken as stencils of F*rho and J_a.
-  {
+  if (loc || kc || bf) {
     XConvArgs<T> A; xc_init(A, P); xc_in(A, (const C *) s[0]);
-    xc_out(A, s[2]); xc_term(A, 0, F.k(OT_SA), KER_EVEN, (T) 1);
+    if (loc) { xc_out(A, s[2]); xc_term(A, 0, F.k(OT_SA), KER_EVEN, (T) 1); }
     if (kc) { xc_out(A, s[3]); xc_term(A, 0, F.k(OT_F), KER_EVEN, (T) 1); }
     if (bf) { xc_out(A, s[7]); xc_term(A, 0, F.k(OT_VJ), KER_EVEN, (T) 1); }
     DFT_TRY(launch_xconv<T>(A));
     C *sp[3]; T *dst[3]; int n = 0;
-    sp[n] = s[2]; dst[n++] = r[R_RB];
+    if (loc) { sp[n] = s[2]; dst[n++] = r[R_RB]; }
     if (kc) { sp[n] = s[3]; dst[n++] = r[R_RT]; }
     if (bf) { sp[n] = s[7]; dst[n++] = r[R_A]; }
     DFT_TRY(par_for(n, [&](int i) { return F.inv(sp[i], dst[i]); }));
@@ -272,12 +285,12 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
     T *v0 = r[R_V0], *v1 = r[R_V1], *v2 = r[R_V2], *e = r[R_E], *b0 = r[R_B0], *b1 = r[R_B1], *b2 = r[R_B2];
     const T inv2h = (T) (1.0 / (2.0 * P->step));
     const double vf = 1.0 / (gwf->mass * 2.0 * P->step), deps = otf->div_epsilon;
-    const bool clampv_on = otf->max_veloc < (999.0 / GRID_AUTOMPS);
+    const bool clampv_on = src.vclamp && otf->max_veloc < (999.0 / GRID_AUTOMPS);
     const T vcap = (T) otf->max_veloc;
     // every load is issued before the first store (stores through the other
     // pointers could alias the loaded arrays, so the compiler keeps the order)
     DFT_TRY(launch_rows(nx, ny, nz, [=] __device__(int x, int y, int z, int i) {
-      const T b = rb[i], rh = rho[i];
+      const T b = loc ? rb[i] : (T) 0, rh = rho[i];
       C p = overwrite ? mk<T>((T) 0, (T) 0) : pot[i];
       if (base) p.x += base[i];
       T st = 0, dr[3] = { 0, 0, 0 };
@@ -289,7 +302,10 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
         }
       }
       T va[3] = { 0, 0, 0 };
-      if (bf) {  // velocity src/ot.c:390-395
+      if (bf && vgiven) {   // given velocity (clamped as src/ot.c:494-497 when asked)
+        va[0] = vin0[i]; va[1] = vin1[i]; va[2] = vin2[i];
+        if (clampv_on) for (int a = 0; a < 3; a++) va[a] = clampv<T>(va[a], vcap);
+      } else if (bf) {  // velocity src/ot.c:390-395
         const C pz = psi[i];
         C d[3];
         for (int a = 0; a < 3; a++) {
@@ -307,9 +323,9 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
       }
       // src/ot.c:557-567 (the LJ term src/ot.c:530 is in the merged linear part)
       p.x += add;
-      p.x += (c2 / (T) 2) * (b * b) + (c3 / (T) 3) * (b * b * b);
+      if (loc) p.x += (c2 / (T) 2) * (b * b) + (c3 / (T) 3) * (b * b * b);
       pot[i] = p;
-      q[i] = (c2 * b + c3 * (b * b)) * rh;
+      if (loc) q[i] = (c2 * b + c3 * (b * b)) * rh;
       if (kc) {  // src/ot.c:608-612, 632-637
         rst[i] = st;
         s0[i] = dr[0] * st; s1[i] = dr[1] * st; s2[i] = dr[2] * st;
@@ -324,14 +340,14 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
 
   // forward transforms of the produced fields (independent: parallel branches)
   {
-    const T *src[8]; C *sp[8]; int n = 0;
-    src[n] = r[R_Q]; sp[n++] = s[9];
-    if (kc) for (int a = 0; a < 3; a++) { src[n] = r[R_S0 + a]; sp[n++] = s[1 + a]; }
+    const T *in[8]; C *sp[8]; int n = 0;
+    if (loc) { in[n] = r[R_Q]; sp[n++] = s[9]; }
+    if (kc) for (int a = 0; a < 3; a++) { in[n] = r[R_S0 + a]; sp[n++] = s[1 + a]; }
     if (bf) {
-      src[n] = r[R_E]; sp[n++] = s[4];
-      for (int a = 0; a < 3; a++) { src[n] = r[R_B0 + a]; sp[n++] = s[5 + a]; }
+      in[n] = r[R_E]; sp[n++] = s[4];
+      for (int a = 0; a < 3; a++) { in[n] = r[R_B0 + a]; sp[n++] = s[5 + a]; }
     }
-    DFT_TRY(par_for(n, [&](int i) { return F.fwd(src[i], sp[i]); }));
+    DFT_TRY(par_for(n, [&](int i) { return F.fwd(in[i], sp[i]); }));
   }
 
   // x pass 2: the KC and BF chains are independent
@@ -365,9 +381,10 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
     const T eps = (T) otf->div_epsilon;
     T *rst = r[R_RST], *rt = r[R_RT], *J0 = r[R_J0], *J1 = r[R_J1], *J2 = r[R_J2], *h = r[R_H];
     T *v0 = r[R_V0], *v1 = r[R_V1], *v2 = r[R_V2], *A = r[R_A], *Cc = r[R_C], *B0 = r[R_BB0], *B1 = r[R_BB1], *B2 = r[R_BB2];
+    T *wo0 = (T *) src.wout[0], *wo1 = (T *) src.wout[1], *wo2 = (T *) src.wout[2];
     DFT_TRY(launch_rows(nx, ny, nz, [=] __device__(int x, int y, int z, int i) {
       C p = pot[i];
-      T hval = 0;   // stores last: every load is issued before them
+      T hval = 0, wv[3] = { 0, 0, 0 };   // stores last: every load is issued before them
       if (kc) {  // src/ot.c:641-645, 656-657, 673-675 summed over axes
         const T *Ja[3] = { J0, J1, J2 };
         T hv = 0, t1 = 0, jd = 0;
@@ -397,6 +414,7 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
         for (int k = 0; k < 3; k++) {
           int ip, imm; S.nb(x, y, z, i, k, ip, imm);
           const T w = va[k][i] * a - Ba[k][i];
+          wv[k] = w;
           const T wp = va[k][ip] * A[ip] - Ba[k][ip], wm = va[k][imm] * A[imm] - Ba[k][imm];
           im += (T) 0.5 * (((rho[ip] - rho[imm]) * inv2h) / rr) * w + (T) 0.5 * ((wp - wm) * inv2h);
         }
@@ -404,6 +422,7 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
         p.y += im * cbf;
       }
       if (kc) h[i] = hval;
+      if (bf && wo0) { wo0[i] = wv[0]; wo1[i] = wv[1]; wo2[i] = wv[2]; }   // src/ot.c:924-931
       pot[i] = p;
     }, nb * (2 + (kc ? 7 : 0) + (bf ? (clampp ? 9 : 8) : 0)), "ot_pointwise_2"));
   }
@@ -411,28 +430,29 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
   // merged linear part (one inverse transform):
   //   V_LJ rho^ + w q^ (src/ot.c:530, 582-585) + c F h^ (KC, src/ot.c:656-664)
   //   + c_bf (-m/2) V_j (rho|v|^2)^ (BF, src/ot.c:895-915)
+  const bool linear = lj || loc || kc || cmerge;
   if (kc) DFT_TRY(F.fwd(r[R_H], s[10]));
-  {
+  if (linear) {
     XConvArgs<T> A; xc_init(A, P);
-    xc_in(A, (const C *) s[0]);
-    xc_in(A, (const C *) s[9]);
-    if (kc) xc_in(A, (const C *) s[10]);
-    if (cmerge) xc_in(A, (const C *) s[4]);
+    int nin = 0;
     xc_out(A, s[11]);
-    xc_term(A, 0, F.k(OT_LJ), KER_EVEN, (T) 1);
-    xc_term(A, 1, F.k(OT_SA), KER_EVEN, (T) 1);
-    if (kc) xc_term(A, 2, F.k(OT_F), KER_EVEN, (T) (otf->alpha_s / (2.0 * otf->mass)));
-    if (cmerge) xc_term(A, kc ? 3 : 2, F.k(OT_VJ), KER_EVEN, (T) (-0.5 * otf->mass * otf->c_bfpot));
+    if (lj) { xc_in(A, (const C *) s[0]); xc_term(A, nin++, F.k(OT_LJ), KER_EVEN, (T) 1); }
+    if (loc) { xc_in(A, (const C *) s[9]); xc_term(A, nin++, F.k(OT_SA), KER_EVEN, (T) 1); }
+    if (kc) { xc_in(A, (const C *) s[10]); xc_term(A, nin++, F.k(OT_F), KER_EVEN, (T) (otf->alpha_s / (2.0 * otf->mass))); }
+    if (cmerge) {
+      xc_in(A, (const C *) s[4]);
+      xc_term(A, nin++, F.k(OT_VJ), KER_EVEN, (T) (-0.5 * otf->mass * otf->c_bfpot));
+    }
     DFT_TRY(launch_xconv<T>(A));
     DFT_TRY(F.inv(s[11], r[R_U]));
   }
 
   // pointwise 3: P.re += linear part ; scale
-  {
+  if (linear || scale != (T) 1) {
     T *lin = r[R_U];
     DFT_TRY(launch_rows(nx, ny, nz, [=] __device__(int x, int y, int z, int i) {
       C p = pot[i];
-      p.x += lin[i];
+      if (linear) p.x += lin[i];
       if (scale != (T) 1) { p.x *= scale; p.y *= scale; }
       pot[i] = p;
     }, nb * 5, "ot_pointwise_3"));
@@ -445,19 +465,29 @@ int ot_potential(dft_ot_functional *otf, cgrid *P, wf *gwf) {
 }
 
 int ot_potential_ex(dft_ot_functional *otf, cgrid *P, wf *gwf, int overwrite, rgrid *base, double add, double scale) {
+  return ot_potential_src(otf, P, gwf, overwrite, base, add, scale, PotSrc());
+}
+
+int ot_potential_src(dft_ot_functional *otf, cgrid *P, wf *gwf, int overwrite, rgrid *base, double add, double scale,
+                     const PotSrc &src) {
   return P->prec == DFTGPU_FP32
-             ? potential_t<float>(otf, P, gwf, overwrite, base ? (const float *) base->value : nullptr, add, scale)
-             : potential_t<double>(otf, P, gwf, overwrite, base ? (const double *) base->value : nullptr, add, scale);
+             ? potential_t<float>(otf, P, gwf, overwrite, base ? (const float *) base->value : nullptr, add, scale, src)
+             : potential_t<double>(otf, P, gwf, overwrite, base ? (const double *) base->value : nullptr, add, scale, src);
 }
 
 // ------------------------------------------------------------------ energy density
-template <typename T> static int energy_density_t(dft_ot_functional *otf, rgrid *edg, wf *gwf) {
+// terms: POT_LJ | POT_LOCAL (the plain part), POT_KC, POT_BF; dens: rho grid
+// to use instead of |psi|^2; add: ed += instead of ed = (the _kc / _bf entry
+// points add to the plain part, src/ot-energy.c:108-109).
+template <typename T> static int energy_density_t(dft_ot_functional *otf, rgrid *edg, wf *gwf, int terms,
+                                                  const rgrid *dens, bool add) {
   typedef typename cplx_t<T>::type C;
   OtPriv *P = (OtPriv *) otf->priv;
   Fields<T> F{P, P->nx, P->ny, P->nz};
   const int nx = P->nx, ny = P->ny, nz = P->nz;
   const double nb = (double) nx * ny * nz * sizeof(T);   // bytes of one real field
-  const bool kc = otf->model & DFT_OT_KC, bf = otf->model & DFT_OT_BACKFLOW;
+  const bool plain = terms & (POT_LJ | POT_LOCAL);
+  const bool kc = (terms & POT_KC) && (otf->model & DFT_OT_KC), bf = (terms & POT_BF) && (otf->model & DFT_OT_BACKFLOW);
   const Stencil3 S{nx, ny, nz};
   const C *psi = (const C *) gwf->grid->value;
   T *rho = (T *) otf->density->value, *ed = (T *) edg->value;
@@ -467,17 +497,26 @@ template <typename T> static int energy_density_t(dft_ot_functional *otf, rgrid 
   C *s[8];
   for (int i = 0; i < 8; i++) { s[i] = F.s(i); if (!s[i]) return DFTGPU_ERR_NOMEM; }
 
-  DFT_TRY(density(gwf->grid, otf->density));
+  if (dens) {
+    if (dens != otf->density) DFT_CUDA(cudaMemcpyAsync(rho, dens->value, nb, cudaMemcpyDeviceToDevice, rt().stream));
+  } else {
+    DFT_TRY(density(gwf->grid, otf->density));
+  }
+  if (!plain && !kc && !bf) return add ? DFTGPU_OK : rfill(edg, 0.0);
   DFT_TRY(F.fwd(rho, s[0]));
   {
     XConvArgs<T> A; xc_init(A, P); xc_in(A, (const C *) s[0]);
-    xc_out(A, s[1]); xc_term(A, 0, F.k(OT_LJ), KER_EVEN, (T) 1);
-    xc_out(A, s[2]); xc_term(A, 0, F.k(OT_SA), KER_EVEN, (T) 1);
+    if (plain) {
+      xc_out(A, s[1]); xc_term(A, 0, F.k(OT_LJ), KER_EVEN, (T) 1);
+      xc_out(A, s[2]); xc_term(A, 0, F.k(OT_SA), KER_EVEN, (T) 1);
+    }
     if (kc) { xc_out(A, s[3]); xc_term(A, 0, F.k(OT_F), KER_EVEN, (T) 1); }
     if (bf) { xc_out(A, s[4]); xc_term(A, 0, F.k(OT_VJ), KER_EVEN, (T) 1); }
     DFT_TRY(launch_xconv<T>(A));
-    DFT_TRY(F.inv(s[1], r[R_U]));
-    DFT_TRY(F.inv(s[2], r[R_RB]));
+    if (plain) {
+      DFT_TRY(F.inv(s[1], r[R_U]));
+      DFT_TRY(F.inv(s[2], r[R_RB]));
+    }
     if (kc) DFT_TRY(F.inv(s[3], r[R_RT]));
     if (bf) DFT_TRY(F.inv(s[4], r[R_A]));
   }
@@ -488,9 +527,12 @@ template <typename T> static int energy_density_t(dft_ot_functional *otf, rgrid 
     T *u = r[R_U], *rb = r[R_RB], *rt = r[R_RT], *A = r[R_A], *rst = r[R_RST], *s0 = r[R_S0], *s1 = r[R_S1], *s2 = r[R_S2];
     T *v0 = r[R_V0], *v1 = r[R_V1], *v2 = r[R_V2], *e = r[R_E], *b0 = r[R_B0], *b1 = r[R_B1], *b2 = r[R_B2];
     DFT_TRY(launch_rows(nx, ny, nz, [=] __device__(int x, int y, int z, int i) {
-      const T rh = rho[i], b = rb[i];
-      // src/ot-energy.c:70-93
-      T acc = (T) 0.5 * rh * u[i] + (c2 / (T) 2) * ((b * b) * rh) + (c3 / (T) 3) * ((b * b * b) * rh);
+      const T rh = rho[i];
+      T acc = add ? ed[i] : (T) 0;
+      if (plain) {  // src/ot-energy.c:70-93
+        const T b = rb[i];
+        acc += (T) 0.5 * rh * u[i] + (c2 / (T) 2) * ((b * b) * rh) + (c3 / (T) 3) * ((b * b * b) * rh);
+      }
       if (kc) {  // src/ot-energy.c:144-161
         const T st = rt[i] * (-irs) + (T) 1;
         rst[i] = st;
@@ -566,7 +608,12 @@ template <typename T> static int energy_density_t(dft_ot_functional *otf, rgrid 
 }
 
 int ot_energy_density(dft_ot_functional *otf, rgrid *ed, wf *gwf) {
-  return ed->prec == DFTGPU_FP32 ? energy_density_t<float>(otf, ed, gwf) : energy_density_t<double>(otf, ed, gwf);
+  return ot_energy_density_terms(otf, ed, gwf, POT_ALL, nullptr, false);
+}
+
+int ot_energy_density_terms(dft_ot_functional *otf, rgrid *ed, wf *gwf, int terms, const rgrid *dens, bool add) {
+  return ed->prec == DFTGPU_FP32 ? energy_density_t<float>(otf, ed, gwf, terms, dens, add)
+                                 : energy_density_t<double>(otf, ed, gwf, terms, dens, add);
 }
 
 }  // namespace dftgpu

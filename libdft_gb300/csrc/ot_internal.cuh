@@ -33,10 +33,24 @@ inline void *ot_spec(OtPriv *P, int i) {
   return P->spec[i];
 }
 
+// Terms of the OT potential and the sources of rho and v (default: every
+// term of the model, rho and v from the wave function).
+enum { POT_LJ = 1, POT_LOCAL = 2, POT_KC = 4, POT_BF = 8, POT_ALL = 15 };
+struct PotSrc {
+  int terms = POT_ALL;
+  const void *dens = nullptr;                      // rho grid (bulk precision) instead of |psi|^2
+  const void *vel[3] = { nullptr, nullptr, nullptr };   // velocity grids instead of the psi stencil
+  void *wout[3] = { nullptr, nullptr, nullptr };   // receive w_a = v_a A - B_a (BF)
+  bool vclamp = true;                              // apply max_veloc to the velocities
+};
+
 int ot_generate_kernels(dft_ot_functional *otf, int min_ns, int max_ns);
 int ot_potential(dft_ot_functional *otf, cgrid *P, wf *gwf);
 int ot_potential_ex(dft_ot_functional *otf, cgrid *P, wf *gwf, int overwrite, rgrid *base, double add, double scale);
+int ot_potential_src(dft_ot_functional *otf, cgrid *P, wf *gwf, int overwrite, rgrid *base, double add, double scale,
+                     const PotSrc &src);
 int ot_energy_density(dft_ot_functional *otf, rgrid *ed, wf *gwf);
+int ot_energy_density_terms(dft_ot_functional *otf, rgrid *ed, wf *gwf, int terms, const rgrid *dens, bool add);
 void adj_free(OtPriv *P);
 
 }  // namespace dftgpu

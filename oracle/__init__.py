@@ -119,6 +119,19 @@ class Oracle:
             f = getattr(L, name)
             f.restype = res
             f.argtypes = args
+        if L.orc_kind() == 2:   # libdft's own term-level entry points (reference build only)
+            ref_sig = {
+                "orc_ref_potential2": (None, [_vp] * 6),
+                "orc_ref_add_lj": (None, [_vp] * 3),
+                "orc_ref_add_local": (None, [_vp] * 3),
+                "orc_ref_backflow": (None, [_vp] * 6),
+                "orc_ref_energy_density_kc": (None, [_vp] * 4),
+                "orc_ref_energy_density_bf": (None, [_vp] * 4),
+            }
+            for name, (res, args) in ref_sig.items():
+                f = getattr(L, name)
+                f.restype = res
+                f.argtypes = args
 
     # constants
     @property

@@ -177,3 +177,40 @@ double orc_const(int which) {
   default: return 0.0;
   }
 }
+
+#ifdef ORACLE_REF
+/* ---------------- reference-only entry points (golden fixtures) ----------------
+ * Term-level and density-driven calls of libdft (src/ot.c:431, 524, 547, 840;
+ * src/ot-energy.c:123, 202), available only when libdft's own sources are
+ * linked.  The work grids are allocated per call. */
+static rgrid *ref_ws(rgrid *like) { return rgrid_clone(like, "oracle ref workspace"); }
+
+void orc_ref_potential2(dft_ot_functional *o, cgrid *P, rgrid *rho, rgrid *vx, rgrid *vy, rgrid *vz) {
+  dft_ot_potential2(o, P, rho, vx, vy, vz);
+}
+void orc_ref_add_lj(dft_ot_functional *o, cgrid *P, rgrid *rho) {
+  rgrid *w1 = ref_ws(rho), *w2 = ref_ws(rho);
+  dft_ot_add_lennard_jones_potential(o, P, rho, w1, w2);
+  rgrid_free(w1); rgrid_free(w2);
+}
+void orc_ref_add_local(dft_ot_functional *o, cgrid *P, rgrid *rho) {
+  /* rho_tf = FFT(rho), as dft_ot_add_lennard_jones_potential leaves it (src/ot.c:526-527) */
+  rgrid *tf = ref_ws(rho), *w1 = ref_ws(rho), *w2 = ref_ws(rho);
+  rgrid_copy(tf, rho);
+  rgrid_fft(tf);
+  dft_ot_add_local_correlation_potential(o, P, rho, tf, w1, w2);
+  rgrid_free(tf); rgrid_free(w1); rgrid_free(w2);
+}
+void orc_ref_backflow(dft_ot_functional *o, cgrid *P, rgrid *rho, rgrid *vx, rgrid *vy, rgrid *vz) {
+  rgrid *w[6];
+  for (int i = 0; i < 6; i++) w[i] = ref_ws(rho);
+  dft_ot_backflow_potential(o, P, rho, vx, vy, vz, w[0], w[1], w[2], w[3], w[4], w[5]);
+  for (int i = 0; i < 6; i++) rgrid_free(w[i]);
+}
+void orc_ref_energy_density_kc(dft_ot_functional *o, rgrid *ed, wf *g, rgrid *rho) {
+  dft_ot_energy_density_kc(o, ed, g, rho);
+}
+void orc_ref_energy_density_bf(dft_ot_functional *o, rgrid *ed, wf *g, rgrid *rho) {
+  dft_ot_energy_density_bf(o, ed, g, rho);
+}
+#endif

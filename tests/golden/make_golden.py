@@ -13,6 +13,14 @@ Outputs (committed):
   full_mixed.npz   16x18x20 (2*3^2, 2^2*5) OT+KC+BF: potential (complex),
                    energy density, kernels, 2 real-time predict-correct steps
   full_lg11.npz    24^3 OT+KC+BF with l_g = 1.1 A: potential, energy density
+  terms.npz        16x18x20 OT+KC+BF: libdft's term-level and density-driven
+                   entry points (dft_ot_potential2 with its overwritten
+                   velocities, dft_ot_add_lennard_jones_potential,
+                   dft_ot_add_local_correlation_potential,
+                   dft_ot_backflow_potential, dft_ot_energy_density_kc / _bf)
+  dispersion.npz   omega(k) tables (k in 1/A, omega in K) parsed from libdft
+                   examples/dispersion/{plain,plain-kc,plain-bf,plain-bf-kc,
+                   ot_dispersion}.dat
 All inputs are seeded numpy draws stored in the fixtures themselves.
 """
 from __future__ import annotations
@@ -30,6 +38,7 @@ sys.path.insert(0, ROOT)
 from oracle import Oracle, Grids, build  # noqa: E402
 
 EOS_FILE = "/root/reference/examples/bulk/equation_of_state.dat"
+DISPERSION_DIR = "/root/reference/examples/dispersion"
 
 
 def coords(shape, step):
@@ -77,6 +86,13 @@ def main():
     eos = np.array(rows)
     np.savez_compressed(os.path.join(HERE, "eos.npz"), pressure_bar=eos[:, 0], density_A3=eos[:, 1],
                         chempot_K=eos[:, 2])
+
+    # ---- dispersion tables from the reference's own data files
+    tabs = {}
+    for name, key in (("plain", "plain"), ("plain-kc", "plain_kc"), ("plain-bf", "plain_bf"),
+                      ("plain-bf-kc", "plain_bf_kc"), ("ot_dispersion", "experiment")):
+        tabs[key] = np.loadtxt(os.path.join(DISPERSION_DIR, name + ".dat"))
+    np.savez(os.path.join(HERE, "dispersion.npz"), **tabs)
 
     # ---- plain 16^3, imaginary time
     shape, step = (16, 16, 16), 1.0
@@ -141,5 +157,52 @@ def main():
     print("golden fixtures written to", HERE)
 
 
+def terms():
+    """terms.npz (python tests/golden/make_golden.py terms)"""
+    build("ref")
+    o = Oracle("ref")
+    assert o.lib.orc_kind() == 2
+    mass = 4.002602 / o.AUTOAMU
+    shape, step, model = (16, 18, 20), 0.8, 1 | 8
+    L = o.lib
+    with Grids(o, shape, step, mass) as g:
+        w0 = g.wf(np.ones(shape))
+        otf = g.ot(model, w0)
+        rho0 = L.orc_bulk_density(otf, 0.0)
+        psi = modulated_psi(shape, step, rho0, 5, amp=0.08)
+        w = g.wf(psi)
+        rho_g, v = g.rgrid(), [g.rgrid() for _ in range(3)]
+        L.orc_wf_density(w, rho_g)
+        p = g.params(otf)
+        L.orc_wf_velocity(w, v[0], v[1], v[2], p["div_epsilon"])
+        rho, vel = g.get_r(rho_g), np.stack([g.get_r(x) for x in v])
+        out = dict(shape=shape, step=step, model=model, psi=psi, rho=rho, vel=vel)
+        P = g.cgrid(0.0)
+        L.orc_ref_potential2(otf, P, rho_g, v[0], v[1], v[2])
+        out["P2"], out["w2"] = g.get_c(P), np.stack([g.get_r(x) for x in v])
+        for x, val in zip(v, vel):
+            g.set_r(x, val)
+        P = g.cgrid(0.0)
+        L.orc_ref_add_lj(otf, P, rho_g)
+        out["Plj"] = g.get_c(P)
+        P = g.cgrid(0.0)
+        L.orc_ref_add_local(otf, P, rho_g)
+        out["Ploc"] = g.get_c(P)
+        P = g.cgrid(0.0)
+        L.orc_ref_backflow(otf, P, rho_g, v[0], v[1], v[2])
+        out["Pbf"], out["wbf"] = g.get_c(P), np.stack([g.get_r(x) for x in v])
+        ed = g.rgrid(0.0)
+        L.orc_ref_energy_density_kc(otf, ed, w, rho_g)
+        out["edkc"] = g.get_r(ed)
+        ed = g.rgrid(0.0)
+        L.orc_ref_energy_density_bf(otf, ed, w, rho_g)
+        out["edbf"] = g.get_r(ed)
+    np.savez_compressed(os.path.join(HERE, "terms.npz"), **out)
+    print("terms.npz written to", HERE)
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["terms"]:
+        terms()
+    else:
+        main()

@@ -1,0 +1,89 @@
+"""Physics pins of the time step (no bit-level reference output exists):
+a small-amplitude density wave in bulk liquid helium, propagated in real
+time with the predict-correct step, must oscillate at the frequency libdft's
+own runs give (examples/dispersion/plain.dat, plain-bf-kc.dat: omega(k) in
+K at k in 1/Angstrom), and the real-time step must conserve the norm
+(plain model: unitary) and the energy.
+
+The set-up is the reference's examples/dispersion/dispersion.c: a 512-point
+line (the transverse directions are 2 points here, the smallest grid this
+library takes) of step 1 bohr, psi = sqrt(rho0) (1 + a cos(k z)), a = 1e-3,
+dt = 15 fs, mu0 subtracted.  The frequency is fitted to the k-mode of the
+density over 1.2 periods; the step and grid errors of the method are about
+1 %, so the tolerance is 2 %."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+NZ, STEP, DT_FS, AMP = 512, 1.0, 15.0, 1e-3
+
+
+def table(name):
+    import os
+    from conftest import GOLDEN
+    return np.load(os.path.join(GOLDEN, "dispersion.npz"))[name]
+
+
+def run_wave(gpu, model, kidx, nsteps):
+    shape = (2, 2, NZ)
+    w, wp = gpu.Wf(shape, STEP), gpu.Wf(shape, STEP)
+    ot = gpu.OT(model, w)
+    rho0, mu0 = ot.bulk_density(0.0), ot.bulk_chempot(0.0)
+    kz = kidx * 2 * np.pi / (NZ * STEP)
+    z = (np.arange(NZ) - NZ // 2) * STEP
+    psi = np.sqrt(rho0) * (1 + AMP * np.cos(kz * z))
+    w.set(np.broadcast_to(psi, shape).astype(complex))
+    P = gpu.CGrid(shape, STEP)
+    dt = DT_FS / gpu.AUTOFS
+    modes, norms, energies = [], [], []
+    for s in range(nsteps + 1):
+        if s:
+            ot.run(w, wp, P, None, mu0, complex(dt), 1, False)
+        rho = np.abs(w.get()[0, 0]) ** 2
+        modes.append(np.sum((rho - rho.mean()) * np.cos(kz * z)))
+        if s % 50 == 0:
+            norms.append(w.norm())
+            energies.append(ot.energy_report(w)[0])
+    for o in (P, ot, wp, w):
+        o.free()
+    return np.array(modes), dt, np.array(norms), np.array(energies)
+
+
+def fit_omega(m, dt):
+    """omega of m(t) = c0 + c1 cos(omega t) + c2 sin(omega t), least squares"""
+    t = np.arange(len(m)) * dt
+    def resid(om):
+        A = np.stack([np.ones_like(t), np.cos(om * t), np.sin(om * t)], 1)
+        c, *_ = np.linalg.lstsq(A, m, rcond=None)
+        return np.sum((A @ c - m) ** 2)
+    # zero crossings give the start, then a golden-section refinement
+    s = np.sign(m - m.mean())
+    cross = np.nonzero(np.diff(s))[0]
+    om = np.pi / (np.mean(np.diff(cross)) * dt) if len(cross) > 1 else np.pi / (cross[0] * dt * 2)
+    lo, hi = 0.8 * om, 1.2 * om
+    g = (np.sqrt(5) - 1) / 2
+    for _ in range(80):
+        a, b = hi - g * (hi - lo), lo + g * (hi - lo)
+        if resid(a) < resid(b):
+            hi = b
+        else:
+            lo = a
+    return 0.5 * (lo + hi)
+
+
+@pytest.mark.parametrize("model,name", [(0, "plain"), (9, "plain_bf_kc")])
+@pytest.mark.parametrize("kidx", [8, 32])
+def test_density_wave_frequency_matches_reference_runs(gpu, model, name, kidx):
+    gpu.set_precision(0)
+    k_ang = kidx * 2 * np.pi / (NZ * STEP) / gpu.AUTOANG
+    tab = table(name)
+    row = np.argmin(np.abs(tab[:, 0] - k_ang))
+    assert abs(tab[row, 0] - k_ang) < 2e-3
+    period_steps = 2 * np.pi / (tab[row, 1] / gpu.AUTOK) / (DT_FS / gpu.AUTOFS)
+    m, dt, norms, energies = run_wave(gpu, model, kidx, int(1.2 * period_steps) + 2)
+    om_K = fit_omega(m, dt) * gpu.AUTOK
+    assert abs(om_K / tab[row, 1] - 1) < 0.02, (om_K, tab[row, 1])
+    if model == 0:   # unitary step: norm conserved; PC step: energy nearly conserved
+        assert np.abs(norms / norms[0] - 1).max() < 1e-11
+    assert np.abs(energies / energies[0] - 1).max() < 1e-6

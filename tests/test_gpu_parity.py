@@ -142,6 +142,61 @@ def test_potential_with_backflow_limits_vs_oracle(gpu, port, prec):
         o.free()
 
 
+def test_term_entry_points_match_reference(gpu, prec):
+    """dft_ot_potential2 (with the velocities it overwrites), the single-term
+    entry points and the KC / backflow energy-density parts against libdft's
+    own functions (tests/golden/terms.npz)."""
+    fx = golden("terms.npz")
+    shape, step = tuple(int(s) for s in fx["shape"]), float(fx["step"])
+    L = gpu.lib()
+    w = gpu.Wf(shape, step)
+    ot = gpu.OT(int(fx["model"]), w)
+    w.set(fx["psi"])
+    rho = gpu.RGrid(shape, step)
+    rho.set(fx["rho"])
+    v = [gpu.RGrid(shape, step) for _ in range(3)]
+    P = gpu.CGrid(shape, step)
+
+    def setv():
+        for g, a in zip(v, fx["vel"]):
+            g.set(a)
+
+    def check_pot(ref, what):
+        got = P.get()
+        assert relerr(got.real, ref.real) < TOL[prec] * 3, what
+        if np.abs(ref.imag).max() > 0:
+            assert relerr(got.imag, ref.imag) < 20 * TOL[prec], what
+
+    setv()
+    P.zero()
+    L.dft_ot_potential2(ot.ptr, P.ptr, rho.ptr, v[0].ptr, v[1].ptr, v[2].ptr)
+    gpu.check(what="dft_ot_potential2")
+    check_pot(fx["P2"], "potential2")
+    for g, ref in zip(v, fx["w2"]):
+        assert relerr(g.get(), ref) < 20 * TOL[prec]
+    P.zero()
+    L.dft_ot_add_lennard_jones_potential(ot.ptr, P.ptr, rho.ptr, None, None)
+    check_pot(fx["Plj"], "lennard-jones")
+    P.zero()
+    L.dft_ot_add_local_correlation_potential(ot.ptr, P.ptr, rho.ptr, None, None, None)
+    check_pot(fx["Ploc"], "local correlation")
+    setv()
+    P.zero()
+    L.dft_ot_backflow_potential(ot.ptr, P.ptr, rho.ptr, v[0].ptr, v[1].ptr, v[2].ptr, *([None] * 6))
+    gpu.check(what="dft_ot_backflow_potential")
+    check_pot(fx["Pbf"], "backflow")
+    for g, ref in zip(v, fx["wbf"]):
+        assert relerr(g.get(), ref) < 20 * TOL[prec]
+    ed = gpu.RGrid(shape, step)
+    for fn, key in ((L.dft_ot_energy_density_kc, "edkc"), (L.dft_ot_energy_density_bf, "edbf")):
+        ed.set(np.zeros(shape))
+        fn(ot.ptr, ed.ptr, w.ptr, rho.ptr)
+        gpu.check(what=key)
+        assert relerr(ed.get(), fx[key]) < 20 * TOL[prec], key
+    for o in [ed, P, rho, ot, w] + v:
+        o.free()
+
+
 @pytest.mark.parametrize("model", [0, 1, 8, 9])
 def test_uniform_liquid_potential_is_chemical_potential(gpu, prec, model):
     shape, step = (32, 32, 32), 0.8
