@@ -5,12 +5,15 @@ own runs give (examples/dispersion/plain.dat, plain-bf-kc.dat: omega(k) in
 K at k in 1/Angstrom), and the real-time step must conserve the norm
 (plain model: unitary) and the energy.
 
-The set-up is the reference's examples/dispersion/dispersion.c: a 512-point
-line (the transverse directions are 2 points here, the smallest grid this
-library takes) of step 1 bohr, psi = sqrt(rho0) (1 + a cos(k z)), a = 1e-3,
-dt = 15 fs, mu0 subtracted.  The frequency is fitted to the k-mode of the
-density over 1.2 periods; the step and grid errors of the method are about
-1 %, so the tolerance is 2 %."""
+The set-up follows the reference's examples/dispersion/dispersion.c: 512
+points of step 1 bohr along z, psi = sqrt(rho0) (1 + a cos(k z)), a = 1e-3,
+dt = 15 fs, mu0 subtracted.  The reference runs a 1 x 1 x 512 grid with the
+kernels integrated over the transverse plane (its 1-D mode, src/ot.c:186-190,
+not provided here); this test uses a 32 x 32 bohr transverse box instead,
+over which the 3-D kernels sum to nearly the same 1-D kernels.  The
+frequency is fitted to the k-mode of the density over 1.2 periods; the
+time-step, grid and transverse-box errors are about 1 %, so the tolerance
+is 2 %."""
 import numpy as np
 import pytest
 
@@ -26,7 +29,7 @@ def table(name):
 
 
 def run_wave(gpu, model, kidx, nsteps):
-    shape = (2, 2, NZ)
+    shape = (32, 32, NZ)
     w, wp = gpu.Wf(shape, STEP), gpu.Wf(shape, STEP)
     ot = gpu.OT(model, w)
     rho0, mu0 = ot.bulk_density(0.0), ot.bulk_chempot(0.0)
@@ -40,7 +43,7 @@ def run_wave(gpu, model, kidx, nsteps):
     for s in range(nsteps + 1):
         if s:
             ot.run(w, wp, P, None, mu0, complex(dt), 1, False)
-        rho = np.abs(w.get()[0, 0]) ** 2
+        rho = np.abs(w.get()[0, 0]) ** 2      # uniform across x, y
         modes.append(np.sum((rho - rho.mean()) * np.cos(kz * z)))
         if s % 50 == 0:
             norms.append(w.norm())
@@ -50,20 +53,22 @@ def run_wave(gpu, model, kidx, nsteps):
     return np.array(modes), dt, np.array(norms), np.array(energies)
 
 
-def fit_omega(m, dt):
-    """omega of m(t) = c0 + c1 cos(omega t) + c2 sin(omega t), least squares"""
+def fit_omega(m, dt, om_guess):
+    """omega of m(t) = c0 + c1 cos(omega t) + c2 sin(omega t), least squares:
+    a scan over [0.5, 2] x om_guess, then golden-section refinement"""
     t = np.arange(len(m)) * dt
+
     def resid(om):
         A = np.stack([np.ones_like(t), np.cos(om * t), np.sin(om * t)], 1)
         c, *_ = np.linalg.lstsq(A, m, rcond=None)
         return np.sum((A @ c - m) ** 2)
-    # zero crossings give the start, then a golden-section refinement
-    s = np.sign(m - m.mean())
-    cross = np.nonzero(np.diff(s))[0]
-    om = np.pi / (np.mean(np.diff(cross)) * dt) if len(cross) > 1 else np.pi / (cross[0] * dt * 2)
-    lo, hi = 0.8 * om, 1.2 * om
+
+    grid = np.linspace(0.5, 2.0, 301) * om_guess
+    r = [resid(om) for om in grid]
+    j = int(np.argmin(r))
+    lo, hi = grid[max(j - 1, 0)], grid[min(j + 1, len(grid) - 1)]
     g = (np.sqrt(5) - 1) / 2
-    for _ in range(80):
+    for _ in range(60):
         a, b = hi - g * (hi - lo), lo + g * (hi - lo)
         if resid(a) < resid(b):
             hi = b
@@ -82,7 +87,7 @@ def test_density_wave_frequency_matches_reference_runs(gpu, model, name, kidx):
     assert abs(tab[row, 0] - k_ang) < 2e-3
     period_steps = 2 * np.pi / (tab[row, 1] / gpu.AUTOK) / (DT_FS / gpu.AUTOFS)
     m, dt, norms, energies = run_wave(gpu, model, kidx, int(1.2 * period_steps) + 2)
-    om_K = fit_omega(m, dt) * gpu.AUTOK
+    om_K = fit_omega(m, dt, tab[row, 1] / gpu.AUTOK) * gpu.AUTOK
     assert abs(om_K / tab[row, 1] - 1) < 0.02, (om_K, tab[row, 1])
     if model == 0:   # unitary step: norm conserved; PC step: energy nearly conserved
         assert np.abs(norms / norms[0] - 1).max() < 1e-11
