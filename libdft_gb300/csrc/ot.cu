@@ -245,6 +245,10 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
   T *rho = (T *) otf->density->value;
   const T *vin0 = (const T *) src.vel[0], *vin1 = (const T *) src.vel[1], *vin2 = (const T *) src.vel[2];
   const bool vgiven = vin0 != nullptr;
+  if ((!src.dens || (bf && !vgiven)) && !gwf) {
+    set_error(DFTGPU_ERR_ARG, "OT potential: no wave function for the density / velocity");
+    return DFTGPU_ERR_ARG;
+  }
 
   // real-field slots
   T *r[R_NREAL];   // slots of PotSlot (ot_work.cuh)
@@ -284,7 +288,7 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
     T *s0 = r[R_S0], *s1 = r[R_S1], *s2 = r[R_S2];
     T *v0 = r[R_V0], *v1 = r[R_V1], *v2 = r[R_V2], *e = r[R_E], *b0 = r[R_B0], *b1 = r[R_B1], *b2 = r[R_B2];
     const T inv2h = (T) (1.0 / (2.0 * P->step));
-    const double vf = 1.0 / (gwf->mass * 2.0 * P->step), deps = otf->div_epsilon;
+    const double vf = gwf ? 1.0 / (gwf->mass * 2.0 * P->step) : 0.0, deps = otf->div_epsilon;
     const bool clampv_on = src.vclamp && otf->max_veloc < (999.0 / GRID_AUTOMPS);
     const T vcap = (T) otf->max_veloc;
     // every load is issued before the first store (stores through the other
