@@ -15,7 +15,11 @@ the 3-D kernels sampled on it miss only the Lennard-Jones tail beyond 64 bohr
 sampled part).  The frequency is fitted to the k-mode of the density,
 int rho cos(kz) dV, sampled every step over 1.2 periods in FP32 (the
 amplitude is far above FP32 rounding); the time-step, grid and box errors
-are about 1 %, so the tolerance is 2 %.  Norm and energy conservation are
+are about 1 %.  The tables were read by hand from the period of a 15 ps run
+(the comment at the top of dispersion.c): at k = 0.186 1/A that run spans
+1.15 periods, at 0.742 1/A 4.6, so the tolerance is 4 % at the first and
+2 % at the second.  (libdft's semi-analytic dft_ot_bulk_dispersion gives
+3.71 K at 0.186 1/A against the table's 3.661 K.)  Norm and energy conservation are
 checked in FP64 on a 32 x 32 x 512 box."""
 import numpy as np
 import pytest
@@ -98,7 +102,8 @@ def test_density_wave_frequency_matches_reference_runs(gpu, model, name, kidx):
     period_steps = 2 * np.pi / (tab[row, 1] / gpu.AUTOK) / (DT_FS / gpu.AUTOFS)
     m, dt, _, _ = run_wave(gpu, model, kidx, int(1.2 * period_steps) + 2, 1, 128)
     om_K = fit_omega(m, dt, tab[row, 1] / gpu.AUTOK) * gpu.AUTOK
-    assert abs(om_K / tab[row, 1] - 1) < 0.02, (om_K, tab[row, 1])
+    tol = 0.04 if kidx == 8 else 0.02
+    assert abs(om_K / tab[row, 1] - 1) < tol, (om_K, tab[row, 1])
 
 
 @pytest.mark.parametrize("model", [0, 9])
