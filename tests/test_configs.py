@@ -1,0 +1,219 @@
+"""The benchmark specification's other workloads as parity and physics cases
+(the 256^3 droplet relaxation is the bench line itself):
+
+* 64^3 plain OT, 200 imaginary-time steps of 10 fs with a repulsive Gaussian
+  external potential and the norm fixed: GPU FP64 against the FP64 CPU oracle;
+* 128^3 full OT (l_g = 1.1 A), 500 real-time steps of 1 fs from a 1 %
+  density modulation: energy drift of the FP64 run, FP32 against FP64
+  (energy and density);
+* the adjoint on that 128^3 system with an external potential of 4 Gaussians
+  (16 parameters) over 400 real-time steps with sqrt(N) checkpoints:
+  the gradient w.r.t. the parameters against central finite differences of
+  the GPU FP64 run (the FP64 CPU oracle check of the same gradient runs on a
+  reduced case in test_adjoint.py: 400 full-OT steps at 128^3 take the CPU
+  minutes per evaluation);
+* 512^3 FP32 full OT, a vortex ring of radius 40 bohr: energy conservation
+  with FP64 reductions every 10 steps and the ring moving along z.
+"""
+import numpy as np
+import pytest
+
+from conftest import relerr
+from oracle import Grids
+
+pytestmark = pytest.mark.gpu
+
+RHO0_A3 = 0.0218360
+
+
+def centred(shape, step):
+    ax = [(np.arange(n) - n // 2) * step for n in shape]
+    return np.meshgrid(*ax, indexing="ij")
+
+
+def test_cfg0_plain_imaginary_time_matches_oracle(gpu, port):
+    """64^3, step 1 bohr, plain OT, 200 steps of -i 10 fs, norm fixed."""
+    shape, step, nsteps = (64, 64, 64), 1.0, 200
+    rho0 = RHO0_A3 * gpu.AUTOANG ** 3
+    X, Y, Z = centred(shape, step)
+    r2 = X ** 2 + Y ** 2 + Z ** 2
+    rng = np.random.default_rng(42)
+    psi0 = (np.sqrt(rho0) * (1 - np.exp(-r2 / (2 * 5.0 ** 2))) * (1 + 1e-3 * rng.standard_normal(shape))).astype(complex)
+    vext = 10.0 / gpu.AUTOK * np.exp(-r2 / (2 * 3.0 ** 2))
+    norm0 = float(np.sum(np.abs(psi0) ** 2) * step ** 3)
+    dt = -10j / gpu.AUTOFS
+    with Grids(port, shape, step, gpu.HELIUM_MASS) as g:
+        wo, wpo, Po, vo = g.wf(psi0), g.wf(), g.cgrid(), g.rgrid(vext)
+        oo = g.ot(0, wo)
+        mu0 = port.lib.orc_bulk_chempot(oo, 0.0)
+        port.lib.orc_wf_set_norm(wo, norm0)
+        for _ in range(nsteps):
+            port.lib.orc_pc_step(oo, wo, wpo, Po, vo, mu0, dt.real, dt.imag)
+            port.lib.orc_wf_normalize(wo)
+        ref = g.get_wf(wo)
+        work = g.rgrid()
+        eref = port.lib.orc_total_energy(oo, wo, vo, work)
+    gpu.set_precision(0)
+    w, wp = gpu.Wf(shape, step), gpu.Wf(shape, step)
+    ot = gpu.OT(0, w)
+    w.set(psi0)
+    w.norm_target = norm0
+    P, ve = gpu.CGrid(shape, step), gpu.RGrid(shape, step)
+    ve.set(vext)
+    ot.run(w, wp, P, ve, mu0, dt, nsteps, True)
+    assert relerr(w.get(), ref) < 1e-9
+    e, n, _ = ot.energy_report(w, ve)
+    assert abs(e / eref - 1) < 1e-10
+    assert abs(n / norm0 - 1) < 1e-12
+    for o in (ve, P, ot, wp, w):
+        o.free()
+
+
+def cfg1_psi(gpu, shape, step):
+    rho0 = RHO0_A3 * gpu.AUTOANG ** 3
+    X, _, _ = centred(shape, step)
+    phase = np.random.default_rng(7).uniform(0, 2 * np.pi)
+    rho = rho0 * (1 + 0.01 * np.cos(2 * np.pi * X / (32 * step) + phase))
+    return np.sqrt(rho).astype(complex)
+
+
+def run_cfg1(gpu, prec, nsteps):
+    shape, step = (128, 128, 128), 0.8
+    gpu.set_precision(prec)
+    w, wp = gpu.Wf(shape, step), gpu.Wf(shape, step)
+    ot = gpu.OT(9, w, lg_bohr=1.1 / gpu.AUTOANG)
+    psi = cfg1_psi(gpu, shape, step)
+    w.set(psi)
+    mu0 = ot.bulk_chempot(0.0)
+    P = gpu.CGrid(shape, step)
+    e0 = ot.energy_report(w)[0]
+    ot.run(w, wp, P, None, mu0, 1.0 / gpu.AUTOFS + 0j, nsteps, False)
+    e1 = ot.energy_report(w)[0]
+    rho = np.abs(w.get()) ** 2
+    for o in (P, ot, wp, w):
+        o.free()
+    gpu.set_precision(0)
+    return e0, e1, rho
+
+
+@pytest.fixture(scope="module")
+def cfg1_runs(gpu):
+    return {prec: run_cfg1(gpu, prec, 500) for prec in (0, 1)}
+
+
+def test_cfg1_energy_drift_and_fp32_error(cfg1_runs):
+    e0, e1, rho64 = cfg1_runs[0]
+    f0, f1, rho32 = cfg1_runs[1]
+    assert abs(e1 / e0 - 1) < 1e-8                      # FP64 energy drift over 500 fs
+    assert abs(f1 / e1 - 1) < 1e-6                      # FP32 energy vs FP64
+    assert np.linalg.norm(rho32 - rho64) / np.linalg.norm(rho64) < 1e-5
+
+
+def test_cfg3_adjoint_gaussian_parameters(gpu):
+    """Gradient of J = int (rho_T - rho_target)^2 dV w.r.t. 4 Gaussians x
+    (amplitude, width, centre x, centre z), rho_target = the initial density
+    shifted 2 bohr along z; 400 real-time steps of 1 fs, checkpoints every 20."""
+    torch = pytest.importorskip("torch")
+    shape, step, nsteps = (128, 128, 128), 0.8, 400
+    gpu.set_precision(0)
+    w = gpu.Wf(shape, step)
+    ot = gpu.OT(9, w, lg_bohr=1.1 / gpu.AUTOANG)
+    psi = cfg1_psi(gpu, shape, step)
+    rho = np.abs(psi) ** 2
+    kz = 2 * np.pi * np.fft.fftfreq(shape[2], d=step)
+    rho_t = np.real(np.fft.ifft(np.fft.fft(rho, axis=2) * np.exp(-1j * kz * 2.0), axis=2))
+    vext, rt, gv = gpu.RGrid(shape, step), gpu.RGrid(shape, step), gpu.RGrid(shape, step)
+    rt.set(rho_t)
+    mu0 = ot.bulk_chempot(0.0)
+    dt = 1.0 / gpu.AUTOFS
+    X, Y, Z = (torch.from_numpy(a) for a in centred(shape, step))
+    rng = np.random.default_rng(11)
+    theta0 = np.stack([rng.uniform(5, 50, 4), rng.uniform(2, 6, 4), rng.uniform(-10, 10, 4),
+                       rng.uniform(-10, 10, 4)], 1).ravel()
+
+    class Objective(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, V):
+            vext.set(V.detach().numpy())
+            w.set(psi)
+            grad = ctx.needs_input_grad[0]
+            J = ot.adjoint_run(w, vext, mu0, dt, nsteps, False, rt, gv if grad else None, checkpoint_every=20)
+            if grad:
+                ctx.save_for_backward(torch.from_numpy(gv.get()))
+            return torch.tensor(J, dtype=torch.float64)
+
+        @staticmethod
+        def backward(ctx, gJ):
+            (G,) = ctx.saved_tensors
+            return gJ * G
+
+    def vext_of(th):
+        V = torch.zeros(shape, dtype=torch.float64)
+        for a, wd, cx, cz in th.reshape(4, 4):
+            V = V + a / gpu.AUTOK * torch.exp(-((X - cx) ** 2 + Y ** 2 + (Z - cz) ** 2) / (2 * wd ** 2))
+        return V
+
+    theta = torch.tensor(theta0, dtype=torch.float64, requires_grad=True)
+    J = Objective.apply(vext_of(theta))
+    J.backward()
+    grad = theta.grad.numpy().copy()
+    assert np.isfinite(grad).all() and np.abs(grad).max() > 0
+    d = np.random.default_rng(5).standard_normal(16)
+    with torch.no_grad():
+        errs = []
+        for rel in (1e-4, 1e-3):
+            e = torch.from_numpy(rel * d * np.abs(theta0))
+            fd = (Objective.apply(vext_of(theta + e)) - Objective.apply(vext_of(theta - e))).item() / 2
+            an = float(np.dot(grad, e.numpy()))
+            errs.append(abs(fd / an - 1))
+        assert min(errs) < 1e-5, errs
+    for o in (gv, rt, vext, ot, w):
+        o.free()
+
+
+def vortex_ring_psi(shape, step, rho0, R=40.0, core=1.0):
+    X, Y, Z = centred(shape, step)
+    rc = np.sqrt(X ** 2 + Y ** 2)
+    d = np.sqrt((rc - R) ** 2 + Z ** 2)
+    theta = np.arctan2(Z, rc - R)            # winding around the core circle
+    return (np.sqrt(rho0) * np.tanh(d / core) * np.exp(1j * theta)).astype(np.complex64)
+
+
+def test_cfg4_vortex_ring_512_fp32(gpu):
+    """512^3, step 0.6 bohr, FP32 full OT, vortex ring of radius 40 bohr,
+    dt = 0.5 fs: energy (FP64 reductions every 10 steps) conserved and the
+    ring's core plane moving along z."""
+    shape, step, nsteps = (512, 512, 512), 0.6, 40
+    gpu.set_precision(1)
+    w, wp = gpu.Wf(shape, step), gpu.Wf(shape, step)
+    ot = gpu.OT(9, w)
+    rho0 = ot.bulk_density(0.0)
+    w.set(vortex_ring_psi(shape, step, rho0))
+    mu0 = ot.bulk_chempot(0.0)
+    P = gpu.CGrid(shape, step)
+    dt = 0.5 / gpu.AUTOFS + 0j
+
+    def core_z():
+        # the ring core is where the density is lowest on the circle rc = R:
+        # its z position from the density along the line x = R, y = 0
+        a = np.abs(w.get()[shape[0] // 2 + int(round(40.0 / step)), shape[1] // 2]) ** 2
+        z = (np.arange(shape[2]) - shape[2] // 2) * step
+        wgt = np.clip(rho0 - a, 0, None) * (np.abs(z) < 10)
+        return float(np.sum(wgt * z) / np.sum(wgt))
+
+    z0 = core_z()
+    energies, norms = [], []
+    for _ in range(nsteps // 10 + 1):
+        e, n, _ = ot.energy_report(w)
+        energies.append(e)
+        norms.append(n)
+        ot.run(w, wp, P, None, mu0, dt, 10, False)
+    z1 = core_z()
+    energies = np.array(energies)
+    assert np.isfinite(energies).all()
+    assert np.abs(energies / energies[0] - 1).max() < 1e-5
+    assert np.abs(np.array(norms) / norms[0] - 1).max() < 1e-5
+    assert 1e-3 < abs(z1 - z0) < 0.2               # the ring translates (about 8e-3 bohr in 20 fs)
+    for o in (P, ot, wp, w):
+        o.free()
+    gpu.set_precision(0)
