@@ -330,7 +330,7 @@ template <typename T> struct AdjLoad {   // D^H g' = exp(conj a) g'
     const size_t i = ((size_t) x * ny + y) * nz + e;
     C a = half_exponent<T>(V[i], hr, hi);
     a.y = -a.y;
-    return cmul(gp[i], cexp_dev(a));
+    return mul_cexp(gp[i], a);
   }
 };
 // h -> g_out = D^H h ; gamma_V += scale * (Re c, -Im c), c = (-i dt/2)(conj(g') psi' + conj(h) D psi)
@@ -340,8 +340,7 @@ template <typename T> struct AdjStore {
   __device__ void operator()(int x, int y, int e, C h) const {
     const size_t i = ((size_t) x * ny + y) * nz + e;
     const C a = half_exponent<T>(V[i], hr, hi);
-    const C D = cexp_dev(a);
-    const C u = cmul(D, psi[i]);
+    const C u = mul_cexp(psi[i], a);
     const C Y = cmulc(psio[i], gp[i]) + cmulc(u, h);          // conj(g') psi' + conj(h) u
     // c = (-i dt/2) Y with dt/2 = (dr2, di2): (-i)(dr2 + i di2) = di2 - i dr2
     const C cc = mk<T>(di2 * Y.x + dr2 * Y.y, di2 * Y.y - dr2 * Y.x);
@@ -349,7 +348,7 @@ template <typename T> struct AdjStore {
     gv.x += scale * cc.x;
     gv.y -= scale * cc.y;
     gamV[i] = gv;
-    const C o = cmul(h, conjc(D));
+    const C o = mul_cexp(h, conjc(a));
     gout[i] = acc ? gout[i] + o : o;
   }
 };

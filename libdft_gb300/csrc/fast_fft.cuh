@@ -58,22 +58,31 @@ __device__ __forceinline__ void bf4(C &a, C &b, C &c, C &d, float s) {   // in p
   a = t0 + t2; c = t0 - t2; b = t1 + rot(t3, s); d = t1 - rot(t3, s);
 }
 
+// Rotation constants.  No float pair (c, s) has c^2 + s^2 = 1 exactly; the
+// rounded 1/sqrt(2) gives 2 h^2 = 1 - 3.4e-8 and the rounded (cos, sin)(pi/8)
+// 1 - 5.7e-8, a bias that lowers the norm at every stage.  Half of the
+// rotations use the neighbouring float instead (hb: h^2 + hb^2 = 1 + 5.0e-8;
+// c1b: c1b^2 + s1^2 = 1 + 5.3e-8), so that the deviations cancel on average
+// (each constant stays within one ulp of its value).
+constexpr float FF_H = 0.70710678118654752440f, FF_HB = 0.70710682868957519531f;
+constexpr float FF_C1 = 0.92387953251128675613f, FF_C1B = 0.92387956380844116211f, FF_S1 = 0.38268343236508977173f;
+
 __device__ __forceinline__ void bf8(C *u, float s) {
-  const float h = 0.70710678118654752440f;
+  const float h = FF_H, hb = FF_HB;
   C a0 = u[0] + u[4], a1 = u[0] - u[4], b0 = u[2] + u[6], b1 = u[2] - u[6];
   C c0 = u[1] + u[5], c1 = u[1] - u[5], d0 = u[3] + u[7], d1 = u[3] - u[7];
   C e0 = a0 + b0, e1 = a0 - b0, f0 = c0 + d0, f1 = c0 - d0;
   u[0] = e0 + f0; u[4] = e0 - f0; u[2] = e1 + rot(f1, s); u[6] = e1 - rot(f1, s);
   C b1w = rot(b1, s);
   C c1w = make_float2(h * (c1.x - s * c1.y), h * (c1.y + s * c1.x));
-  C d1w = make_float2(h * (-d1.x - s * d1.y), h * (-d1.y + s * d1.x));
+  C d1w = make_float2(-h * d1.x - hb * (s * d1.y), -h * d1.y + hb * (s * d1.x));
   C g0 = a1 + b1w, g1 = a1 - b1w, k0 = c1w + d1w, k1 = c1w - d1w;
   u[1] = g0 + k0; u[5] = g0 - k0; u[3] = g1 + rot(k1, s); u[7] = g1 - rot(k1, s);
 }
 
 // 16-point DFT as 4 x 4 with W16 twiddles; output in natural order
 __device__ __forceinline__ void bf16(C *u, float s) {
-  const float c1 = 0.92387953251128675613f, s1 = 0.38268343236508977173f, h = 0.70710678118654752440f;
+  const float c1 = FF_C1, c1b = FF_C1B, s1 = FF_S1, h = FF_H, hb = FF_HB;
   // step 1: for n2 = 0..3, 4-point DFT over n1 of x[4 n1 + n2] -> y[n2][k1]
 #pragma unroll
   for (int n2 = 0; n2 < 4; n2++) bf4(u[n2], u[4 + n2], u[8 + n2], u[12 + n2], s);
@@ -83,9 +92,9 @@ __device__ __forceinline__ void bf16(C *u, float s) {
     const float im = s * ci;
     v = make_float2(v.x * cr - v.y * im, v.x * im + v.y * cr);
   };
-  tw(u[4 + 1], c1, s1);  tw(u[8 + 1], h, h);     tw(u[12 + 1], s1, c1);
-  tw(u[4 + 2], h, h);    u[8 + 2] = rot(u[8 + 2], s); tw(u[12 + 2], -h, h);
-  tw(u[4 + 3], s1, c1);  tw(u[8 + 3], -h, h);    tw(u[12 + 3], -c1, -s1);
+  tw(u[4 + 1], c1b, s1); tw(u[8 + 1], h, hb);    tw(u[12 + 1], s1, c1);
+  tw(u[4 + 2], h, h);    u[8 + 2] = rot(u[8 + 2], s); tw(u[12 + 2], -h, hb);
+  tw(u[4 + 3], s1, c1);  tw(u[8 + 3], -h, h);    tw(u[12 + 3], -c1b, -s1);
   // step 3: for k1 = 0..3, 4-point DFT over n2 of y[n2][k1] = u[4 k1 + n2] -> X[k1 + 4 k2]
 #pragma unroll
   for (int k1 = 0; k1 < 4; k1++) bf4(u[4 * k1 + 0], u[4 * k1 + 1], u[4 * k1 + 2], u[4 * k1 + 3], s);
@@ -460,10 +469,7 @@ __global__ void __launch_bounds__(256) xkinetic_kernel(const C *__restrict__ tw,
     const int x = final_pos<N>(t, j);
     const float kxv = (float) (x < (nx + 1) / 2 ? x : x - nx) * dkx;
     const float k2 = kxv * kxv + kyv * kyv + kzv * kzv;
-    float sn, cs;
-    const float e = expf(cdt.x * k2) * inv_n;
-    sincosf(cdt.y * k2, &sn, &cs);
-    v[j] = cmul(v[j], make_float2(e * cs, e * sn));
+    v[j] = mul_cexp(make_float2(v[j].x * inv_n, v[j].y * inv_n), make_float2(cdt.x * k2, cdt.y * k2));
   }
   to_input_order<N>(v);
   transform<N>(v, t, l, 1.f, tw, sm);

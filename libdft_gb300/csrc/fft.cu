@@ -56,8 +56,23 @@ template <typename T> int get_plan(int n, FftPlan<T> *plan) {
       // reduce the angle to [-pi, pi] and evaluate in long double, round once
       long tt = (t <= n / 2) ? t : (long) t - n;
       long double ang = -2.0L * 3.14159265358979323846264338327950288L * (long double) tt / (long double) n;
-      h[t].x = (T) cosl(ang);
-      h[t].y = (T) sinl(ang);
+      const long double cr = cosl(ang), ci = sinl(ang);
+      h[t].x = (T) cr;
+      h[t].y = (T) ci;
+      if (sizeof(T) == 4) {
+        // of the float pairs within one ulp of (cos, sin), take the one
+        // closest to the unit circle: independent rounding leaves |w|^2 off 1
+        // by up to 1.2e-7, a fixed pattern that biases the norm
+        const float fx = (float) cr, fy = (float) ci;
+        const float xs[2] = { fx, nextafterf(fx, cr > (long double) fx ? 2.f : -2.f) };
+        const float ys[2] = { fy, nextafterf(fy, ci > (long double) fy ? 2.f : -2.f) };
+        long double best = -1.0L;
+        for (float x : xs)
+          for (float y : ys) {
+            const long double dev = fabsl((long double) x * x + (long double) y * y - 1.0L);
+            if (best < 0 || dev < best) { best = dev; h[t].x = (T) x; h[t].y = (T) y; }
+          }
+      }
     }
     void *d = nullptr;
     cudaError_t err = cudaMalloc(&d, sizeof(C) * (size_t) n);

@@ -364,16 +364,9 @@ __global__ void __launch_bounds__(FFT_THREADS) xkinetic_kernel(const KinArgs<T> 
     const int l = idx % B, e = idx / B;
     const double kxv = kfreq(e, A.nx, A.dkx), kyv = kfreq(y0 + l, A.ny, A.dky);
     const double k2 = kxv * kxv + kyv * kyv + kzv * kzv;
-    C f;
-    if (sizeof(T) == 4) {
-      float2 z = make_float2((float) (A.cdt.x * k2), (float) (A.cdt.y * k2));
-      float2 ex = cexp_dev(z);
-      f.x = (T) (ex.x * A.inv_n); f.y = (T) (ex.y * A.inv_n);
-    } else {
-      double2 ex = cexp_dev(make_double2(A.cdt.x * k2, A.cdt.y * k2));
-      f.x = (T) (ex.x * A.inv_n); f.y = (T) (ex.y * A.inv_n);
-    }
-    r[e * ldb + l] = cmul(r[e * ldb + l], f);
+    const C z = mk<T>((T) (A.cdt.x * k2), (T) (A.cdt.y * k2));
+    const C a = r[e * ldb + l];
+    r[e * ldb + l] = mul_cexp(mk<T>(a.x * (T) A.inv_n, a.y * (T) A.inv_n), z);
   }
   __syncthreads();
   C *other = (r == s0) ? s1 : s0;

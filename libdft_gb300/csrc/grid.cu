@@ -221,7 +221,7 @@ template <typename T> struct PhaseLoad {   // psi * exp(-i V dt / 2)
     C v = V[i];
     // -i V dt/2 = (Im(V dt/2), -Re(V dt/2))
     C z = mk<T>(v.x * hi + v.y * hr, -(v.x * hr - v.y * hi));
-    return cmul(psi[i], cexp_dev(z));
+    return mul_cexp(psi[i], z);
   }
 };
 template <typename T> struct PhaseStore {
@@ -231,7 +231,7 @@ template <typename T> struct PhaseStore {
     const size_t i = ((size_t) x * ny + y) * nz + e;
     C v = V[i];
     C z = mk<T>(v.x * hi + v.y * hr, -(v.x * hr - v.y * hi));
-    psi[i] = cmul(val, cexp_dev(z));
+    psi[i] = mul_cexp(val, z);
   }
 };
 

@@ -99,7 +99,7 @@ template <typename T> struct HalfStepLoad {
   __device__ C operator()(int x, int y, int e) const {
     const size_t i = ((size_t) x * ny + y) * nz + e;
     const C v = V[i];
-    return cmul(psi[i], cexp_dev(mk<T>(v.x * hi + v.y * hr, -(v.x * hr - v.y * hi))));
+    return mul_cexp(psi[i], mk<T>(v.x * hi + v.y * hr, -(v.x * hr - v.y * hi)));
   }
 };
 template <typename T> struct HalfStepStore {
@@ -108,7 +108,7 @@ template <typename T> struct HalfStepStore {
   __device__ void operator()(int x, int y, int e, C val) const {
     const size_t i = ((size_t) x * ny + y) * nz + e;
     const C v = V[i];
-    psi[i] = cmul(val, cexp_dev(mk<T>(v.x * hi + v.y * hr, -(v.x * hr - v.y * hi))));
+    psi[i] = mul_cexp(val, mk<T>(v.x * hi + v.y * hr, -(v.x * hr - v.y * hi)));
   }
 };
 

