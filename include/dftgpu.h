@@ -214,6 +214,11 @@ void cgrid_constant_re_im(cgrid *grid, REAL re, REAL im);
 void cgrid_add_re_im(cgrid *grid, REAL re, REAL im);      /* cgrid_add(P, -mu0), imag_time.c:233 */
 void cgrid_multiply_re_im(cgrid *grid, REAL re, REAL im); /* cgrid_multiply(P, 0.5), imag_time.c:238 */
 void cgrid_copy(cgrid *dst, cgrid *src);
+/* Moving background (examples/gas-bubble/bubble.c:104,173,
+ * examples/added_mass/added_mass.c:78): a wave function on this grid is
+ * propagated with the kinetic operator hbar^2 |k - k0|^2 / 2m and its kinetic
+ * energy is <hbar^2 |k - k0|^2 / 2m>.  Clones copy the momentum. */
+void cgrid_set_momentum(cgrid *grid, REAL kx0, REAL ky0, REAL kz0);
 void cgrid_map_re_im(cgrid *grid, cgrid_map_fn func, void *farg);
 int cgrid_copy_to_host(cgrid *grid, double *host);        /* interleaved re, im */
 int cgrid_copy_from_host(cgrid *grid, const double *host);

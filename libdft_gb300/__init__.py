@@ -80,6 +80,7 @@ SIGNATURES = {
     "cgrid_add_re_im": (None, [_vp, _d, _d]),
     "cgrid_multiply_re_im": (None, [_vp, _d, _d]),
     "cgrid_copy": (None, [_vp, _vp]),
+    "cgrid_set_momentum": (None, [_vp, _d, _d, _d]),
     "cgrid_map_re_im": (None, [_vp, _vp, _vp]),
     "cgrid_copy_to_host": (_i, [_vp, _dp]),
     "cgrid_copy_from_host": (_i, [_vp, _dp]),
@@ -284,6 +285,11 @@ class Wf:
     def set(self, psi):
         a = np.ascontiguousarray(psi, dtype=np.complex128)
         check(lib().cgrid_copy_from_host(self.grid_ptr, _dptr(a.view(np.float64))), "wf set")
+
+    def set_momentum(self, kx0, ky0, kz0):
+        """Moving background: cgrid_set_momentum on the wave function's grid."""
+        lib().cgrid_set_momentum(self.grid_ptr, float(kx0), float(ky0), float(kz0))
+        check(what="cgrid_set_momentum")
 
     def get(self):
         out = np.empty(self.shape, dtype=np.complex128)

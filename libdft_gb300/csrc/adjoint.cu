@@ -369,13 +369,8 @@ static int strang_vjp_t(wf *g, cgrid *V, double dr, double di, const cgrid *psi,
   DFT_TRY((launch_lines<T, LINE_C2C, 1, 0>(nz, nx, ny, (T) -1, ld, sz)));
   DFT_TRY(ypass<T>(spec, nx, ny, nz, (T) -1));
   KinArgs<T> K;
-  K.nx = nx; K.ny = ny; K.nz = nz;
-  K.data = spec;
-  K.cdt = make_double2(di / (2.0 * g->mass), dr / (2.0 * g->mass));   // conj(-i dt / 2m)
-  K.inv_n = 1.0 / ((double) nx * ny * nz);
-  K.dkx = 2.0 * M_PI / (nx * V->step);
-  K.dky = 2.0 * M_PI / (ny * V->step);
-  K.dkz = 2.0 * M_PI / (nz * V->step);
+  kin_args<T>(K, nx, ny, nz, V->step, make_double2(di / (2.0 * g->mass), dr / (2.0 * g->mass)),   // conj(-i dt / 2m)
+              g->grid->kx0, g->grid->ky0, g->grid->kz0, spec);
   DFT_TRY(launch_xkinetic<T>(K));
   DFT_TRY(ypass<T>(spec, nx, ny, nz, (T) 1));
   SpecLoadZ<T> lz{spec, nx, ny};
@@ -413,12 +408,19 @@ void adj_free(OtPriv *P) {
   P->adj = nullptr;
 }
 
+static void same_momentum(wf *dst, const wf *src) {
+  dst->grid->kx0 = src->grid->kx0; dst->grid->ky0 = src->grid->ky0; dst->grid->kz0 = src->grid->kz0;
+}
+
 static AdjWork *work_get(OtPriv *P, wf *gwf) {
   AdjWork *W = (AdjWork *) P->adj;
-  if (W && W->wk->mass == gwf->mass) return W;
+  if (W && W->wk->mass == gwf->mass) {
+    same_momentum(W->wk, gwf); same_momentum(W->wp, gwf);
+    return W;
+  }
   adj_free(P);
   W = new AdjWork();
-  W->wk = grid_wf_clone(gwf, (char *) "adj_psi");
+  W->wk = grid_wf_clone(gwf, (char *) "adj_psi");   // the clones carry gwf's momentum
   W->wp = grid_wf_clone(gwf, (char *) "adj_psip");
   cgrid *c = gwf->grid;
   cgrid **f[] = { &W->V1, &W->V2, &W->psio, &W->gV1, &W->gV2, &W->gp, &W->gt, &W->g };

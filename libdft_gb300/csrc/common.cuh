@@ -50,31 +50,51 @@ __device__ __forceinline__ double2 cexp_dev(double2 z) {
   double e = exp(z.x), s, c; sincos(z.y, &s, &c); return make_double2(e * c, e * s);
 }
 
-// a * exp(z).  For small |z| the factor is applied as a + a (exp(z) - 1), with
-// exp(z) - 1 formed from expm1 and the half-angle sine: a factor rounded as a
-// whole has |exp(i theta)|^2 = c^2 + s^2 off 1 by the rounding of c near 1,
-// which is biased for small angles and changed the norm by ~7e-8 (FP32) at
-// every real-time step; the split form keeps |exp(i theta)| = 1 to the
-// rounding of theta.  Large |z| (strongly damped modes) uses the factor
-// directly, so a damped value keeps its own relative precision.
+// exp(z) - 1 from expm1 and the half-angle sine (cos y - 1 = -2 sin^2(y/2)),
+// so that a factor near 1 keeps the full relative precision of its
+// difference from 1.
+__device__ __forceinline__ float2 cexpm1(float2 z) {
+  float sh, ch;
+  sincosf(0.5f * z.y, &sh, &ch);
+  const float em = expm1f(z.x), s2 = 2.f * sh * sh;
+  return make_float2(em * (1.f - s2) - s2, (1.f + em) * (2.f * sh * ch));
+}
+__device__ __forceinline__ double2 cexpm1(double2 z) {
+  double sh, ch;
+  sincos(0.5 * z.y, &sh, &ch);
+  const double em = expm1(z.x), s2 = 2.0 * sh * sh;
+  return make_double2(em * (1.0 - s2) - s2, (1.0 + em) * (2.0 * sh * ch));
+}
+
+// a (1 + d) evaluated as a + a d
+__device__ __forceinline__ float2 mul_1p(float2 a, float2 d) {
+  return make_float2(a.x + (a.x * d.x - a.y * d.y), a.y + (a.x * d.y + a.y * d.x));
+}
+__device__ __forceinline__ double2 mul_1p(double2 a, double2 d) {
+  return make_double2(a.x + (a.x * d.x - a.y * d.y), a.y + (a.x * d.y + a.y * d.x));
+}
+
+// (1 + p)(1 + q) - 1
+template <typename C> __device__ __forceinline__ C cprod1p(C p, C q) {
+  C r;
+  r.x = p.x + q.x + (p.x * q.x - p.y * q.y);
+  r.y = p.y + q.y + (p.x * q.y + p.y * q.x);
+  return r;
+}
+
+// a * exp(z).  For small |z| the factor is applied as a + a (exp(z) - 1): a
+// factor rounded as a whole has |exp(i theta)|^2 = c^2 + s^2 off 1 by the
+// rounding of c near 1, which is biased for small angles and changed the norm
+// by ~7e-8 (FP32) at every real-time step; the split form keeps
+// |exp(i theta)| = 1 to the rounding of theta.  Large |z| (strongly damped
+// modes) uses the factor directly, so a damped value keeps its own relative
+// precision.
 __device__ __forceinline__ float2 mul_cexp(float2 a, float2 z) {
-  if (fabsf(z.x) + fabsf(z.y) < 0.25f) {
-    float sh, ch;
-    sincosf(0.5f * z.y, &sh, &ch);
-    const float em = expm1f(z.x), s2 = 2.f * sh * sh;
-    const float dx = em * (1.f - s2) - s2, dy = (1.f + em) * (2.f * sh * ch);
-    return make_float2(a.x + (a.x * dx - a.y * dy), a.y + (a.x * dy + a.y * dx));
-  }
+  if (fabsf(z.x) + fabsf(z.y) < 0.25f) return mul_1p(a, cexpm1(z));
   return cmul(a, cexp_dev(z));
 }
 __device__ __forceinline__ double2 mul_cexp(double2 a, double2 z) {
-  if (fabs(z.x) + fabs(z.y) < 0.25) {
-    double sh, ch;
-    sincos(0.5 * z.y, &sh, &ch);
-    const double em = expm1(z.x), s2 = 2.0 * sh * sh;
-    const double dx = em * (1.0 - s2) - s2, dy = (1.0 + em) * (2.0 * sh * ch);
-    return make_double2(a.x + (a.x * dx - a.y * dy), a.y + (a.x * dy + a.y * dx));
-  }
+  if (fabs(z.x) + fabs(z.y) < 0.25) return mul_1p(a, cexpm1(z));
   return cmul(a, cexp_dev(z));
 }
 

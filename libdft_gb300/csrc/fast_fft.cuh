@@ -452,25 +452,33 @@ __global__ void __launch_bounds__(256, MODE == 1 ? 1 : 2) xconv_kernel(const C *
 
 // psi(k) *= exp(cdt k^2) / N between forward and inverse x transforms
 template <int N>
-__global__ void __launch_bounds__(256) xkinetic_kernel(const C *__restrict__ tw, C *data, int nx, int ny, int nz,
-                                                      float2 cdt, float inv_n, float dkx, float dky, float dkz) {
+__global__ void __launch_bounds__(256) xkinetic_kernel(const C *__restrict__ tw, C *data, int ny, int nz, float2 cdt,
+                                                      float inv_n, float dkx, float dky, float dkz, float kx0,
+                                                      float ky0, float kz0) {
   constexpr int E = Shape<N>::E, TL = Shape<N>::TL, B = Shape<N>::B, LP = Shape<N>::LP;
   __shared__ C sm[B * LP];
+  __shared__ C fx[N];   // exp(cdt (kx - kx0)^2) - 1
   const int kz = blockIdx.y, l = threadIdx.x % B, t = threadIdx.x / B, y = blockIdx.x * B + l;
-  C *base = data + kz * (size_t) nx * ny + y;
+  for (int e = threadIdx.x; e < N; e += 256) {
+    const float k = (float) (e < (N + 1) / 2 ? e : e - N) * dkx - kx0;
+    fx[e] = cexpm1(make_float2(cdt.x * (k * k), cdt.y * (k * k)));
+  }
+  C fyz;                // exp(cdt ((ky - ky0)^2 + (kz - kz0)^2)) - 1 of this thread's line
+  {
+    const float kzv = (float) (kz < (nz + 1) / 2 ? kz : kz - nz) * dkz - kz0;
+    const float kyv = (float) (y < (ny + 1) / 2 ? y : y - ny) * dky - ky0;
+    const float q = kyv * kyv + kzv * kzv;
+    fyz = cexpm1(make_float2(cdt.x * q, cdt.y * q));
+  }
+  C *base = data + kz * (size_t) N * ny + y;
   C v[E];
 #pragma unroll
   for (int q = 0; q < E; q++) v[q] = base[(size_t) (t + TL * q) * ny];
   transform<N>(v, t, l, -1.f, tw, sm);
-  const float kzv = (float) (kz < (nz + 1) / 2 ? kz : kz - nz) * dkz;
-  const float kyv = (float) (y < (ny + 1) / 2 ? y : y - ny) * dky;
+  __syncthreads();      // fx complete (the transform's own barriers do not cover the last writes)
 #pragma unroll
-  for (int j = 0; j < E; j++) {
-    const int x = final_pos<N>(t, j);
-    const float kxv = (float) (x < (nx + 1) / 2 ? x : x - nx) * dkx;
-    const float k2 = kxv * kxv + kyv * kyv + kzv * kzv;
-    v[j] = mul_cexp(make_float2(v[j].x * inv_n, v[j].y * inv_n), make_float2(cdt.x * k2, cdt.y * k2));
-  }
+  for (int j = 0; j < E; j++)
+    v[j] = mul_1p(make_float2(v[j].x * inv_n, v[j].y * inv_n), cprod1p(fx[final_pos<N>(t, j)], fyz));
   to_input_order<N>(v);
   transform<N>(v, t, l, 1.f, tw, sm);
 #pragma unroll

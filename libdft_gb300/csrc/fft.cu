@@ -211,8 +211,8 @@ template <int N> int fast_xkinetic(const KinArgs<float> &A) {
   DFT_TRY(get_plan<float>(N, &p));
   ProfScope prof("fft_x_kinetic", 2.0 * A.nx * A.ny * A.nz * sizeof(float2));
   ff::xkinetic_kernel<N><<<dim3(A.ny / B, A.nz), 256, 0, rt().stream>>>(
-      p.tw, A.data, A.nx, A.ny, A.nz, make_float2((float) A.cdt.x, (float) A.cdt.y), (float) A.inv_n,
-      (float) A.dkx, (float) A.dky, (float) A.dkz);
+      p.tw, A.data, A.ny, A.nz, make_float2((float) A.cdt.x, (float) A.cdt.y), (float) A.inv_n, (float) A.dkx,
+      (float) A.dky, (float) A.dkz, (float) A.kx0, (float) A.ky0, (float) A.kz0);
   DFT_CHECK_LAUNCH();
   return DFTGPU_OK;
 }
@@ -285,6 +285,11 @@ template <typename T> int launch_xkinetic(KinArgs<T> &A) {
   DFT_TRY(get_plan<T>(A.nx, &A.plan));
   int B; size_t smem;
   DFT_TRY(choose_tile(A.nx, A.ny, sizeof(C), 2, &B, &smem));
+  smem = kin_smem(A.nx, B, sizeof(C));
+  if (smem > rt().max_smem_optin) {
+    set_error(DFTGPU_ERR_SIZE, "kinetic pass for nx=%d does not fit in shared memory", A.nx);
+    return DFTGPU_ERR_SIZE;
+  }
   A.B = B;
   static bool attr = false;
   if (!attr) {

@@ -330,15 +330,40 @@ __global__ void __launch_bounds__(FFT_THREADS) xconv_kernel(const XConvArgs<T> A
 }
 
 // ------------------------------------------------------------ kinetic x pass
-// psi(k) *= exp(-i hbar k^2 dt / 2m) / N in the middle of an x-pencil FFT pair.
+// psi(k) *= exp(-i hbar |k - k0|^2 dt / 2m) / N in the middle of an x-pencil
+// FFT pair; k0 is the moving-background momentum of the wave function's grid.
+// The factor separates, exp(c |k - k0|^2) = (1 + fx(kx)) (1 + fyz(ky, kz)),
+// so each CTA tabulates fx for its line length and fyz for its lines (two
+// transcendental evaluations per thread instead of one per element) and
+// applies psi + psi ((1 + fx)(1 + fyz) - 1), which keeps |factor| = 1 to the
+// rounding of the exponent in real time.
 template <typename T> struct KinArgs {
   FftPlan<T> plan;
   int B, nx, ny, nz;
-  double2 cdt;          // -i dt / (2 m) * (2 pi)^2 folded: factor = exp(cdt * kk)
+  double2 cdt;          // -i dt / (2 m): factor = exp(cdt |k - k0|^2)
   double inv_n;
   double dkx, dky, dkz; // 2 pi / (n step)
+  double kx0, ky0, kz0; // moving-background momentum
   typename cplx_t<T>::type *data;
 };
+
+template <typename T>
+inline void kin_args(KinArgs<T> &K, int nx, int ny, int nz, double step, double2 cdt, double kx0, double ky0,
+                     double kz0, typename cplx_t<T>::type *data) {
+  K.nx = nx; K.ny = ny; K.nz = nz;
+  K.data = data;
+  K.cdt = cdt;
+  K.inv_n = 1.0 / ((double) nx * ny * nz);
+  K.dkx = 2.0 * M_PI / (nx * step);
+  K.dky = 2.0 * M_PI / (ny * step);
+  K.dkz = 2.0 * M_PI / (nz * step);
+  K.kx0 = kx0; K.ky0 = ky0; K.kz0 = kz0;
+}
+
+// shared memory of the generic kinetic kernel: two tiles + the factor tables
+inline size_t kin_smem(int n, int B, size_t cplx_bytes) {
+  return 2 * (size_t) n * (B + 1) * cplx_bytes + (size_t) (n + B) * cplx_bytes;
+}
 
 __device__ __forceinline__ double kfreq(int i, int n, double dk) {
   return (double) (i < (n + 1) / 2 ? i : i - n) * dk;
@@ -349,24 +374,29 @@ __global__ void __launch_bounds__(FFT_THREADS) xkinetic_kernel(const KinArgs<T> 
   typedef typename cplx_t<T>::type C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int n = A.plan.n, B = A.B, ldb = B + 1, tile = n * ldb;
-  C *s0 = reinterpret_cast<C *>(smem_raw), *s1 = s0 + tile;
+  C *s0 = reinterpret_cast<C *>(smem_raw), *s1 = s0 + tile, *fx = s1 + tile, *fyz = fx + n;
   const int kz = blockIdx.y, y0 = blockIdx.x * B;
   const size_t plane = (size_t) A.nx * A.ny;
   C *base = A.data + kz * plane + y0;
+  for (int e = threadIdx.x; e < n; e += blockDim.x) {
+    const double k = kfreq(e, A.nx, A.dkx) - A.kx0, q = k * k;
+    fx[e] = cexpm1(mk<T>((T) (A.cdt.x * q), (T) (A.cdt.y * q)));
+  }
+  const double kzv = kfreq(kz, A.nz, A.dkz) - A.kz0;
+  for (int l = threadIdx.x; l < B; l += blockDim.x) {
+    const double k = kfreq(y0 + l, A.ny, A.dky) - A.ky0, q = k * k + kzv * kzv;
+    fyz[l] = cexpm1(mk<T>((T) (A.cdt.x * q), (T) (A.cdt.y * q)));
+  }
   for (int idx = threadIdx.x; idx < n * B; idx += blockDim.x) {
     const int l = idx % B, e = idx / B;
     s0[e * ldb + l] = base[(size_t) e * A.ny + l];
   }
   __syncthreads();
   C *r = tile_fft<T>(s0, s1, A.plan, B, ldb, (T) -1);
-  const double kzv = kfreq(kz, A.nz, A.dkz);
   for (int idx = threadIdx.x; idx < n * B; idx += blockDim.x) {
     const int l = idx % B, e = idx / B;
-    const double kxv = kfreq(e, A.nx, A.dkx), kyv = kfreq(y0 + l, A.ny, A.dky);
-    const double k2 = kxv * kxv + kyv * kyv + kzv * kzv;
-    const C z = mk<T>((T) (A.cdt.x * k2), (T) (A.cdt.y * k2));
     const C a = r[e * ldb + l];
-    r[e * ldb + l] = mul_cexp(mk<T>(a.x * (T) A.inv_n, a.y * (T) A.inv_n), z);
+    r[e * ldb + l] = mul_1p(mk<T>(a.x * (T) A.inv_n, a.y * (T) A.inv_n), cprod1p(fx[e], fyz[l]));
   }
   __syncthreads();
   C *other = (r == s0) ? s1 : s0;

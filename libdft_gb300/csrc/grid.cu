@@ -247,14 +247,10 @@ template <typename T> int strang(wf *g, cgrid *dst, cgrid *src, cgrid *V, double
   DFT_TRY((launch_lines<T, LINE_C2C, 1, 0>(nz, nx, ny, (T) -1, ld, sz)));
   DFT_TRY(ypass<T>(spec, nx, ny, nz, (T) -1));
   KinArgs<T> K;
-  K.nx = nx; K.ny = ny; K.nz = nz;
-  K.data = spec;
   const double m = g->mass;
-  K.cdt = make_double2(di / (2.0 * m), -dr / (2.0 * m));   // -i dt / 2m
-  K.inv_n = 1.0 / ((double) nx * ny * nz);
-  K.dkx = 2.0 * M_PI / (nx * src->step);
-  K.dky = 2.0 * M_PI / (ny * src->step);
-  K.dkz = 2.0 * M_PI / (nz * src->step);
+  const cgrid *mg = g->grid;   // moving-background momentum of the wave function
+  kin_args<T>(K, nx, ny, nz, src->step, make_double2(di / (2.0 * m), -dr / (2.0 * m)),   // -i dt / 2m
+              mg->kx0, mg->ky0, mg->kz0, spec);
   DFT_TRY(launch_xkinetic<T>(K));
   DFT_TRY(ypass<T>(spec, nx, ny, nz, (T) 1));
   SpecLoadZ<T> lz{spec, nx, ny};
@@ -290,13 +286,14 @@ template <typename T> int kinetic_energy_t(wf *g, double *out) {
   DFT_TRY(cfft3_forward<T>(c, spec));
   const int nx = (int) c->nx, ny = (int) c->ny, nz = (int) c->nz;
   const double dkx = 2.0 * M_PI / (nx * c->step), dky = 2.0 * M_PI / (ny * c->step), dkz = 2.0 * M_PI / (nz * c->step);
+  const double k0x = c->kx0, k0y = c->ky0, k0z = c->kz0;   // kinetic energy in the moving frame
   const double dv = c->step * c->step * c->step;
   const double scale = 1.0 / (2.0 * g->mass) * dv / ((double) nx * ny * nz);
   const size_t n = (size_t) nx * ny * nz;
   // spectral layout [kz][kx][ky]
   return reduce_host<1>(n, [=] __device__(size_t i, double *v) {
     const int ky = (int) (i % ny), kx = (int) ((i / ny) % nx), kz = (int) (i / ((size_t) nx * ny));
-    const double a = kfreq(kx, nx, dkx), b = kfreq(ky, ny, dky), cc = kfreq(kz, nz, dkz);
+    const double a = kfreq(kx, nx, dkx) - k0x, b = kfreq(ky, ny, dky) - k0y, cc = kfreq(kz, nz, dkz) - k0z;
     const C s = spec[i];
     v[0] = (a * a + b * b + cc * cc) * ((double) s.x * s.x + (double) s.y * s.y);
   }, out, scale);

@@ -151,15 +151,10 @@ int propagate_noalloc_t(void *out, const void *in, const void *pot, int nx, int 
   DFT_TRY((run_lines<T, LINE_C2C>(py, nz, nx, (T) -1, 1, 1, ioy, ioy, s)));
   KinArgs<T> K;
   K.plan = px;
-  K.nx = nx; K.ny = ny; K.nz = nz;
-  K.data = spec;
-  K.cdt = make_double2(di / (2.0 * mass), -dr / (2.0 * mass));
-  K.inv_n = 1.0 / ((double) nx * ny * nz);
-  K.dkx = 2.0 * M_PI / (nx * step);
-  K.dky = 2.0 * M_PI / (ny * step);
-  K.dkz = 2.0 * M_PI / (nz * step);
+  kin_args<T>(K, nx, ny, nz, step, make_double2(di / (2.0 * mass), -dr / (2.0 * mass)), 0.0, 0.0, 0.0, spec);
   int B; size_t smem;
   DFT_TRY(choose_tile(nx, ny, sizeof(C), 2, &B, &smem));
+  smem = kin_smem(nx, B, sizeof(C));
   K.B = B;
   if (smem > 48 * 1024)
     DFT_CUDA(cudaFuncSetAttribute(xkinetic_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));

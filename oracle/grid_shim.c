@@ -549,8 +549,14 @@ cgrid *cgrid_clone(cgrid *g, char *id) {
 
 void cgrid_set_origin(cgrid *g, REAL x0, REAL y0, REAL z0) { g->x0 = x0; g->y0 = y0; g->z0 = z0; }
 
+/* Moving background (called by examples/gas-bubble/bubble.c:104,173,
+ * examples/added_mass/added_mass.c:78, examples/1d-bubble/bubble-1d.c:136).
+ * Restated semantics: the wave function is stored in the frame moving with
+ * momentum hbar k0, where the kinetic operator is hbar^2 |k - k0|^2 / 2m; it
+ * enters the kinetic propagator and the kinetic energy of the wave function
+ * whose grid carries it, and nothing else (the OT terms depend on the density
+ * and on velocity differences only). */
 void cgrid_set_momentum(cgrid *g, REAL kx0, REAL ky0, REAL kz0) {
-  if (kx0 != 0.0 || ky0 != 0.0 || kz0 != 0.0) not_restated("cgrid_set_momentum with non-zero momentum");
   g->kx0 = kx0; g->ky0 = ky0; g->kz0 = kz0;
 }
 
@@ -743,9 +749,9 @@ REAL grid_wf_kinetic_energy(wf *g) {
 #pragma omp parallel for schedule(static)
   for (INT ij = 0; ij < nr; ij++) {
     INT i = ij / ny, j = ij % ny;
-    REAL kx = kval(i, nx, c->step), ky = kval(j, ny, c->step), s = 0.0;
+    REAL kx = kval(i, nx, c->step) - c->kx0, ky = kval(j, ny, c->step) - c->ky0, s = 0.0;
     for (INT k = 0; k < nz; k++) {
-      REAL kz = kval(k, nz, c->step);
+      REAL kz = kval(k, nz, c->step) - c->kz0;
       REAL complex v = w->value[ij * nz + k];
       s += (kx * kx + ky * ky + kz * kz) * (creal(v) * creal(v) + cimag(v) * cimag(v));
     }
@@ -819,16 +825,16 @@ static void apply_potential_half(cgrid *dst, cgrid *src, cgrid *pot, REAL comple
     dst->value[ii] = src->value[ii] * cexp(-I * pot->value[ii] * dt / (2.0 * HBAR));
 }
 
-/* psi(k) *= exp(-i hbar k^2 dt / 2m) / N */
-static void apply_kinetic(cgrid *c, REAL mass, REAL complex dt, int normalize) {
+/* psi(k) *= exp(-i hbar |k - k0|^2 dt / 2m) / N, k0 = the momentum of grid m */
+static void apply_kinetic(cgrid *c, const cgrid *m, REAL mass, REAL complex dt, int normalize) {
   INT nx = c->nx, ny = c->ny, nz = c->nz;
   REAL inv_n = normalize ? 1.0 / (REAL) (nx * ny * nz) : 1.0;
 #pragma omp parallel for schedule(static)
   for (INT ij = 0; ij < nx * ny; ij++) {
     INT i = ij / ny, j = ij % ny;
-    REAL kx = kval(i, nx, c->step), ky = kval(j, ny, c->step);
+    REAL kx = kval(i, nx, c->step) - m->kx0, ky = kval(j, ny, c->step) - m->ky0;
     for (INT k = 0; k < nz; k++) {
-      REAL kz = kval(k, nz, c->step);
+      REAL kz = kval(k, nz, c->step) - m->kz0;
       REAL k2 = kx * kx + ky * ky + kz * kz;
       c->value[ij * nz + k] *= cexp(-I * HBAR * k2 * dt / (2.0 * mass)) * inv_n;
     }
@@ -839,7 +845,7 @@ static void apply_kinetic(cgrid *c, REAL mass, REAL complex dt, int normalize) {
 static void strang_step(wf *g, cgrid *dst, cgrid *src, cgrid *pot, REAL complex dt) {
   apply_potential_half(dst, src, pot, dt);
   cgrid_fft(dst);
-  apply_kinetic(dst, g->mass, dt, 1);
+  apply_kinetic(dst, g->grid, g->mass, dt, 1);
   cgrid_inverse_fft(dst);
   apply_potential_half(dst, dst, pot, dt);
 }
@@ -855,4 +861,4 @@ void grid_wf_propagate_potential(wf *g, REAL complex dt, cgrid *pot, REAL cons) 
     g->grid->value[ii] *= cexp(-I * (pot->value[ii] + cons) * dt / HBAR);
 }
 
-void grid_wf_propagate_kinetic_fft(wf *g, REAL complex dt) { apply_kinetic(g->grid, g->mass, dt, 0); }
+void grid_wf_propagate_kinetic_fft(wf *g, REAL complex dt) { apply_kinetic(g->grid, g->grid, g->mass, dt, 0); }

@@ -13,7 +13,8 @@
   reduced case in test_adjoint.py: 400 full-OT steps at 128^3 take the CPU
   minutes per evaluation);
 * 512^3 full OT, a vortex ring of radius 40 bohr: FP32 against FP64 (energy
-  and norm by FP64 reductions every 10 steps) and the ring moving along z.
+  and norm by FP64 reductions every 10 steps, the density in the plane
+  through the ring's axis after 40 steps).
 """
 import numpy as np
 import pytest
@@ -192,16 +193,6 @@ def run_ring(gpu, prec, shape, step, nsteps):
     mu0 = ot.bulk_chempot(0.0)
     P = gpu.CGrid(shape, step)
     dt = 0.5 / gpu.AUTOFS + 0j
-
-    def core_z():
-        # the ring core crosses the line x = R, y = 0 where the density is
-        # lowest: its z position from the density deficit along that line
-        a = np.abs(w.get()[shape[0] // 2 + int(round(40.0 / step)), shape[1] // 2]) ** 2
-        z = (np.arange(shape[2]) - shape[2] // 2) * step
-        wgt = np.clip(rho0 - a, 0, None) * (np.abs(z) < 10)
-        return float(np.sum(wgt * z) / np.sum(wgt))
-
-    z0 = core_z()
     energies, norms = [], []
     for s in range(nsteps // 10 + 1):
         e, n, _ = ot.energy_report(w)
@@ -209,24 +200,29 @@ def run_ring(gpu, prec, shape, step, nsteps):
         norms.append(n)
         if s < nsteps // 10:
             ot.run(w, wp, P, None, mu0, dt, 10, False)
-    z1 = core_z()
+    plane = np.abs(w.get()[:, shape[1] // 2]) ** 2     # the plane y = 0 through the ring's axis
     for o in (P, ot, wp, w):
         o.free()
     gpu.set_precision(0)
-    return np.array(energies), np.array(norms), z1 - z0
+    return np.array(energies), np.array(norms), plane, rho0
 
 
 def test_cfg4_vortex_ring_512_fp32(gpu):
     """512^3, step 0.6 bohr, full OT, vortex ring of radius 40 bohr, dt =
     0.5 fs, energy and norm (FP64 reductions) every 10 steps: the FP32 run
-    against the FP64 run of the same 40 steps, and the ring moving along z.
-    (The tanh core is not a stationary profile: the core relaxes and the
-    energy of both runs changes by ~2e-4 over the 40 steps.)"""
+    against the FP64 run of the same 40 steps, and the density in the plane
+    through the ring's axis after them.  (The tanh core is not a stationary
+    profile: over these 20 fs the core relaxes -- the energy of both runs
+    changes by ~2e-4 -- while the ring itself moves by < 0.01 bohr.)"""
     shape, step, nsteps = (512, 512, 512), 0.6, 40
-    e32, n32, dz32 = run_ring(gpu, 1, shape, step, nsteps)
-    e64, n64, dz64 = run_ring(gpu, 0, shape, step, nsteps)
+    e32, n32, p32, rho0 = run_ring(gpu, 1, shape, step, nsteps)
+    e64, n64, p64, _ = run_ring(gpu, 0, shape, step, nsteps)
     assert np.isfinite(e32).all()
     assert np.abs(e32 / e64 - 1).max() < 2e-6, e32 / e64 - 1
     assert np.abs(n32 / n64 - 1).max() < 2e-6, n32 / n64 - 1
-    assert 1e-3 < abs(dz64) < 0.2                  # the ring translates (about 8e-3 bohr in 20 fs)
-    assert abs(dz32 / dz64 - 1) < 1e-2
+    # the cores are resolved: the density on the core line stays near zero
+    x = (np.arange(shape[0]) - shape[0] // 2) * step
+    core = np.argmin(np.abs(x - 40.0))
+    assert p64[core, shape[2] // 2] < 0.2 * rho0
+    err = np.linalg.norm(p32 - p64) / np.linalg.norm(p64)
+    assert err < 1e-5, err
