@@ -27,7 +27,9 @@ def prec(request, gpu):
 
 @pytest.mark.parametrize("shape", [(16, 16, 16), (16, 18, 20), (32, 24, 40), (64, 64, 64), (30, 36, 50),
                                    (8, 16, 512), (64, 256, 32), (128, 128, 128), (96, 120, 160),
-                                   (16, 256, 256), (6, 512, 512)])
+                                   (16, 256, 256), (6, 512, 512),
+                                   # smallest and largest axes (2 and 1024: generic kernels in FP32 too)
+                                   (2, 4, 6), (4, 6, 2), (1024, 8, 4), (4, 6, 1024), (8, 1024, 2)])
 def test_rfft_spectrum(gpu, prec, shape):
     rng = np.random.default_rng(1)
     f = rng.standard_normal(shape)
@@ -89,7 +91,8 @@ def test_potential_and_energy_density_match_reference(gpu, prec, fixture):
 @pytest.mark.parametrize("shape,step,model", [((32, 32, 32), 0.8, 9), ((40, 36, 30), 0.7, 1), ((48, 32, 40), 1.0, 8),
                                               ((96, 80, 128), 0.8, 9), ((64, 64, 64), 0.8, 9),
                                               ((128, 64, 80), 0.8, 9), ((64, 128, 128), 0.8, 1),
-                                              ((16, 256, 256), 0.8, 9), ((4, 512, 512), 0.5, 0)])
+                                              ((16, 256, 256), 0.8, 9), ((4, 512, 512), 0.5, 0),
+                                              ((2, 4, 6), 1.0, 9), ((1024, 6, 4), 0.6, 9), ((6, 4, 1024), 0.6, 9)])
 def test_potential_vs_oracle_live(gpu, port, prec, shape, step, model):
     psi = liquid_psi(shape, step, 3)
     ns = (2, 4) if np.prod(shape) > 200000 else (4, 32)      # coarser kernel sampling on big grids (CPU time)
@@ -216,7 +219,8 @@ def test_uniform_liquid_potential_is_chemical_potential(gpu, prec, model):
         o.free()
 
 
-@pytest.mark.parametrize("shape", [(24, 20, 30), (128, 128, 128), (64, 96, 160)])
+@pytest.mark.parametrize("shape", [(24, 20, 30), (128, 128, 128), (64, 96, 160),
+                                   (2, 6, 4), (1024, 4, 6), (6, 4, 1024), (4, 1024, 2)])
 def test_propagate_matches_oracle(gpu, port, prec, shape):
     step = 0.9
     rng = np.random.default_rng(9)
