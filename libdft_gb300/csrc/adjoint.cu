@@ -323,20 +323,36 @@ template <typename T> __device__ __forceinline__ typename cplx_t<T>::type half_e
   return mk<T>(v.x * hi + v.y * hr, -(v.x * hr - v.y * hi));
 }
 
+// Split functors of the line kernels (as the forward propagation's): AdjLoad
+// fetches all of a thread's operands before combining them, AdjStore
+// prefetches its operand lines into L2 before the transform.
 template <typename T> struct AdjLoad {   // D^H g' = exp(conj a) g'
   typedef typename cplx_t<T>::type C;
+  static constexpr bool kSplit = true;
+  struct Raw { C g, v; };
   const C *gp; const C *V; int ny, nz; T hr, hi;
-  __device__ C operator()(int x, int y, int e) const {
+  __device__ Raw fetch(int x, int y, int e) const {
     const size_t i = ((size_t) x * ny + y) * nz + e;
-    C a = half_exponent<T>(V[i], hr, hi);
-    a.y = -a.y;
-    return mul_cexp(gp[i], a);
+    return Raw{ gp[i], V[i] };
   }
+  __device__ C cook(const Raw &r) const {
+    C a = half_exponent<T>(r.v, hr, hi);
+    a.y = -a.y;
+    return mul_cexp(r.g, a);
+  }
+  __device__ C operator()(int x, int y, int e) const { return cook(fetch(x, y, e)); }
 };
 // h -> g_out = D^H h ; gamma_V += scale * (Re c, -Im c), c = (-i dt/2)(conj(g') psi' + conj(h) D psi)
 template <typename T> struct AdjStore {
   typedef typename cplx_t<T>::type C;
+  static constexpr bool kSplit = true;
   C *gout; const C *gp; const C *psi; const C *psio; const C *V; C *gamV; int ny, nz; T hr, hi, dr2, di2, scale; int acc;
+  __device__ void prefetch(int x, int y, int e) const {
+    const size_t i = ((size_t) x * ny + y) * nz + e;
+    if ((i * sizeof(C)) % 32) return;                    // one per 32-byte sector
+    prefetch_l2(V + i); prefetch_l2(psi + i); prefetch_l2(psio + i); prefetch_l2(gp + i); prefetch_l2(gamV + i);
+    if (acc) prefetch_l2(gout + i);
+  }
   __device__ void operator()(int x, int y, int e, C h) const {
     const size_t i = ((size_t) x * ny + y) * nz + e;
     const C a = half_exponent<T>(V[i], hr, hi);

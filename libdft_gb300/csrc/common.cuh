@@ -50,6 +50,9 @@ __device__ __forceinline__ double2 cexp_dev(double2 z) {
   double e = exp(z.x), s, c; sincos(z.y, &s, &c); return make_double2(e * c, e * s);
 }
 
+// Bring the line holding p into L2 (generic address; no register result).
+__device__ __forceinline__ void prefetch_l2(const void *p) { asm volatile("prefetch.L2 [%0];" ::"l"(p)); }
+
 // exp(z) - 1 from expm1 and the half-angle sine (cos y - 1 = -2 sin^2(y/2)),
 // so that a factor near 1 keeps the full relative precision of its
 // difference from 1.

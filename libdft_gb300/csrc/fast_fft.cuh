@@ -192,6 +192,14 @@ template <int N> __device__ __forceinline__ void to_input_order(C (&v)[Shape<N>:
 // --------------------------------------------------------------- line pass
 enum { MAP_E = 0, MAP_L = 1 };
 
+// Optional split interface of the load / store functors, detected by a
+// member kSplit: a split load functor separates fetch(a, b, e) -> Raw from
+// cook(Raw) -> C, so that all global loads of a thread are in flight before
+// the first value is combined; a split store functor has prefetch(a, b, e),
+// called before the transform for the elements it will store.
+template <class F> __host__ __device__ constexpr auto split_of(int) -> decltype(F::kSplit, bool()) { return F::kSplit; }
+template <class F> __host__ __device__ constexpr bool split_of(long) { return false; }
+
 // MODE 0 C2C, 1 R2C (N = nz/2, post-processed to N+1 outputs), 2 C2R.
 // LDS / STS: stage the load / store side through shared memory with a
 // line-fast cooperative loop (used for the transposed side of z passes).
@@ -204,7 +212,13 @@ __global__ void __launch_bounds__(256) line_kernel(const C *__restrict__ tw, con
   const int t = MAP == MAP_E ? threadIdx.x % TL : threadIdx.x / B;
   const int l = MAP == MAP_E ? threadIdx.x / TL : threadIdx.x % B;
   C v[E];
-  if constexpr (LDS == 0) {
+  if constexpr (LDS == 0 && split_of<Ld>(0)) {
+    typename Ld::Raw raw[E];
+#pragma unroll
+    for (int q = 0; q < E; q++) raw[q] = ld.fetch(a, b0 + l, t + TL * q);
+#pragma unroll
+    for (int q = 0; q < E; q++) v[q] = ld.cook(raw[q]);
+  } else if constexpr (LDS == 0) {
 #pragma unroll
     for (int q = 0; q < E; q++) v[q] = ld(a, b0 + l, t + TL * q);
   } else {
@@ -238,6 +252,10 @@ __global__ void __launch_bounds__(256) line_kernel(const C *__restrict__ tw, con
       }
     }
     __syncthreads();
+  }
+  if constexpr (STS == 0 && split_of<St>(0)) {
+#pragma unroll
+    for (int j = 0; j < E; j++) st.prefetch(a, b0 + l, final_pos<N>(t, j));
   }
   transform<N>(v, t, l, sign, tw, sm);
   if constexpr (STS == 0) {

@@ -213,20 +213,34 @@ template <typename T> int k_axpb(T *p, size_t n, T a, T b) {   // p = a p + b
 }
 
 // ------------------------------------------------------------------ propagation
+// The propagation passes' functors use the split interface of the line
+// kernels: PhaseLoad fetches psi and V of all of a thread's elements before
+// any phase factor is formed; PhaseStore prefetches its V lines into L2
+// before the transform, so the loads after it do not wait on DRAM.
 template <typename T> struct PhaseLoad {   // psi * exp(-i V dt / 2)
   typedef typename cplx_t<T>::type C;
+  static constexpr bool kSplit = true;
+  struct Raw { C p, v; };
   const C *psi; const C *V; int ny, nz; T hr, hi;   // (hr, hi) = dt / 2
-  __device__ C operator()(int x, int y, int e) const {
+  __device__ Raw fetch(int x, int y, int e) const {
     const size_t i = ((size_t) x * ny + y) * nz + e;
-    C v = V[i];
-    // -i V dt/2 = (Im(V dt/2), -Re(V dt/2))
-    C z = mk<T>(v.x * hi + v.y * hr, -(v.x * hr - v.y * hi));
-    return mul_cexp(psi[i], z);
+    return Raw{ psi[i], V[i] };
   }
+  __device__ C cook(const Raw &r) const {
+    // -i V dt/2 = (Im(V dt/2), -Re(V dt/2))
+    const C z = mk<T>(r.v.x * hi + r.v.y * hr, -(r.v.x * hr - r.v.y * hi));
+    return mul_cexp(r.p, z);
+  }
+  __device__ C operator()(int x, int y, int e) const { return cook(fetch(x, y, e)); }
 };
 template <typename T> struct PhaseStore {
   typedef typename cplx_t<T>::type C;
+  static constexpr bool kSplit = true;
   C *psi; const C *V; int ny, nz; T hr, hi;
+  __device__ void prefetch(int x, int y, int e) const {
+    const size_t i = ((size_t) x * ny + y) * nz + e;
+    if ((i * sizeof(C)) % 32 == 0) prefetch_l2(V + i);   // one per 32-byte sector
+  }
   __device__ void operator()(int x, int y, int e, C val) const {
     const size_t i = ((size_t) x * ny + y) * nz + e;
     C v = V[i];
