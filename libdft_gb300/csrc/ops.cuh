@@ -193,6 +193,42 @@ template <typename T> struct RealPairStore {        // real row <- scale * (re, 
     row[2 * e + 1] = v.y * scale;
   }
 };
+// (|psi[2e]|^2, |psi[2e+1]|^2) of a wave-function row, also stored into the
+// density grid: the density pass (src/ot.c:320) done by the first z pass of rho.
+// Algorithmic bytes beyond a real-row load: the psi row is twice as wide, and
+// the density row is written (2 real fields).
+template <typename T> struct DensityPairLoad {
+  typedef typename cplx_t<T>::type C;
+  const C *psi; T *rho; int ny, nz;
+  __device__ C operator()(int x, int y, int e) const {
+    const size_t r = ((size_t) x * ny + y) * nz + 2 * e;
+    const C a = psi[r], b = psi[r + 1];
+    const C d = mk<T>(a.x * a.x + a.y * a.y, b.x * b.x + b.y * b.y);
+    *reinterpret_cast<C *>(rho + r) = d;     // rows hold an even number of values
+    return d;
+  }
+};
+// P <- scale * (P + (re, im) added to the real parts of P[2e], P[2e+1]): the
+// last c2r z pass of the potential adds the merged linear part into P and
+// applies the predict-correct scale.  Algorithmic bytes beyond a real-row
+// store: P is read and written (3 real fields).
+template <typename T> struct PotAddPairStore {
+  typedef typename cplx_t<T>::type C;
+  static constexpr bool kSplit = true;
+  C *pot; int ny, nz; T scale;
+  __device__ void prefetch(int x, int y, int e) const {
+    const size_t r = ((size_t) x * ny + y) * nz + 2 * e;
+    if ((r * sizeof(C)) % 32 == 0) prefetch_l2(pot + r);   // one per 32-byte sector
+  }
+  __device__ void operator()(int x, int y, int e, C v) const {
+    const size_t r = ((size_t) x * ny + y) * nz + 2 * e;
+    C p0 = pot[r], p1 = pot[r + 1];
+    p0.x += v.x;
+    p1.x += v.y;
+    pot[r] = mk<T>(p0.x * scale, p0.y * scale);
+    pot[r + 1] = mk<T>(p1.x * scale, p1.y * scale);
+  }
+};
 template <typename T> struct CplxLoad {
   const typename cplx_t<T>::type *f; int ny, nz;
   __device__ typename cplx_t<T>::type operator()(int x, int y, int e) const {
@@ -214,25 +250,28 @@ template <typename T> int ypass(typename cplx_t<T>::type *spec, int nx, int ny, 
 
 // forward r2c of a real field through its z and y passes, with a custom
 // packed-pair loader (fused producer); spec is [nz/2+1][nx][ny]
-template <typename T, class Ld> int rfft_zy(const Ld &ld, typename cplx_t<T>::type *spec, int nx, int ny, int nz) {
+// extra_bytes: algorithmic bytes of the load / store functor beyond one real field
+template <typename T, class Ld>
+int rfft_zy(const Ld &ld, typename cplx_t<T>::type *spec, int nx, int ny, int nz, double extra_bytes = 0.0) {
   if constexpr (std::is_same<Ld, RealPairLoad<float>>::value) {
     const int rc = launch_zy_r2c(ld, spec, nx, ny, nz);
     if (rc >= 0) return rc;
   }
   SpecStoreZ<T> st{spec, nx, ny};
-  DFT_TRY((launch_lines<T, LINE_R2C, 1, 0>(nz / 2, nx, ny, (T) -1, ld, st)));
+  DFT_TRY((launch_lines<T, LINE_R2C, 1, 0>(nz / 2, nx, ny, (T) -1, ld, st, extra_bytes)));
   return ypass<T>(spec, nx, ny, nz / 2 + 1, (T) -1);
 }
 
 // inverse: y passes then c2r z pass into a custom consumer st(x, y, e, (v[2e], v[2e+1]))
-template <typename T, class St> int irfft_yz(typename cplx_t<T>::type *spec, const St &st, int nx, int ny, int nz) {
+template <typename T, class St>
+int irfft_yz(typename cplx_t<T>::type *spec, const St &st, int nx, int ny, int nz, double extra_bytes = 0.0) {
   if constexpr (std::is_same<St, RealPairStore<float>>::value) {
     const int rc = launch_yz_c2r(spec, st, nx, ny, nz);
     if (rc >= 0) return rc;
   }
   DFT_TRY(ypass<T>(spec, nx, ny, nz / 2 + 1, (T) 1));
   SpecLoadZ<T> ld{spec, nx, ny};
-  return launch_lines<T, LINE_C2R, 0, 1>(nz / 2, nx, ny, (T) 1, ld, st);
+  return launch_lines<T, LINE_C2R, 0, 1>(nz / 2, nx, ny, (T) 1, ld, st, extra_bytes);
 }
 
 }  // namespace dftgpu

@@ -259,10 +259,11 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
   if (src.dens) {
     if (src.dens != otf->density->value)
       DFT_CUDA(cudaMemcpyAsync(rho, src.dens, nb, cudaMemcpyDeviceToDevice, rt().stream));
-  } else {
-    DFT_TRY(density(gwf->grid, otf->density));                                 // src/ot.c:320
+    DFT_TRY(F.fwd(rho, s[0]));
+  } else {   // rho = |psi|^2 (src/ot.c:320), formed and stored by the first z pass
+    DensityPairLoad<T> ld{psi, rho, ny, nz};
+    DFT_TRY(rfft_zy<T>(ld, s[0], nx, ny, nz, 2.0 * nb));
   }
-  DFT_TRY(F.fwd(rho, s[0]));
 
   // x pass 1: one input, kernels SA (+F) (+V_j); rho^ stays in s0.  The
   // derivative kernels dF_a are the central-difference gradient of the
@@ -448,18 +449,18 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
       xc_term(A, nin++, F.k(OT_VJ), KER_EVEN, (T) (-0.5 * otf->mass * otf->c_bfpot));
     }
     DFT_TRY(launch_xconv<T>(A));
-    DFT_TRY(F.inv(s[11], r[R_U]));
+    // P.re += linear part, P *= scale, in the store of the inverse transform
+    PotAddPairStore<T> st{pot, ny, nz, scale};
+    return irfft_yz<T>(s[11], st, nx, ny, nz, 3.0 * nb);
   }
 
-  // pointwise 3: P.re += linear part ; scale
-  if (linear || scale != (T) 1) {
-    T *lin = r[R_U];
+  // pointwise 3 (no linear term): P *= scale
+  if (scale != (T) 1) {
     DFT_TRY(launch_rows(nx, ny, nz, [=] __device__(int x, int y, int z, int i) {
       C p = pot[i];
-      if (linear) p.x += lin[i];
-      if (scale != (T) 1) { p.x *= scale; p.y *= scale; }
+      p.x *= scale; p.y *= scale;
       pot[i] = p;
-    }, nb * 5, "ot_pointwise_3"));
+    }, nb * 4, "ot_pointwise_3"));
   }
   return DFTGPU_OK;
 }
