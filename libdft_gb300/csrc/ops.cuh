@@ -68,6 +68,22 @@ template <class F> int launch_rows(int nx, int ny, int nz, F f, double bytes = 0
   return DFTGPU_OK;
 }
 
+// The same with a register budget for MINB resident 256-thread CTAs per SM:
+// for latency-bound passes with many independent loads per element.
+template <int MINB, class F> __global__ void __launch_bounds__(256, MINB) rows_kernel_b(int ny, int nz, F f) {
+  const int y = blockIdx.x, x = blockIdx.y;
+  const int base = (x * ny + y) * nz;
+  for (int z = threadIdx.x; z < nz; z += blockDim.x) f(x, y, z, base + z);
+}
+template <int MINB, class F>
+int launch_rows_b(int nx, int ny, int nz, F f, double bytes = 0.0, const char *name = "pointwise") {
+  int bd = nz < 256 ? ((nz + 31) / 32) * 32 : 256;
+  ProfScope prof(name, bytes);
+  rows_kernel_b<MINB><<<dim3(ny, nx), bd, 0, rt().stream>>>(ny, nz, f);
+  DFT_CHECK_LAUNCH();
+  return DFTGPU_OK;
+}
+
 // periodic neighbours of (x, y, z) along axis a, by comparison (no division)
 struct Stencil3 {
   int nx, ny, nz;

@@ -387,7 +387,10 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
     T *rst = r[R_RST], *rt = r[R_RT], *J0 = r[R_J0], *J1 = r[R_J1], *J2 = r[R_J2], *h = r[R_H];
     T *v0 = r[R_V0], *v1 = r[R_V1], *v2 = r[R_V2], *A = r[R_A], *Cc = r[R_C], *B0 = r[R_BB0], *B1 = r[R_BB1], *B2 = r[R_BB2];
     T *wo0 = (T *) src.wout[0], *wo1 = (T *) src.wout[1], *wo2 = (T *) src.wout[2];
-    DFT_TRY(launch_rows(nx, ny, nz, [=] __device__(int x, int y, int z, int i) {
+    // FP32: 6 CTAs per SM (42 registers, no spills) keep more of its ~40 loads
+    // per element in flight; the FP64 variant would spill
+    constexpr int kMinBlocks = std::is_same<T, float>::value ? 6 : 1;
+    DFT_TRY(launch_rows_b<kMinBlocks>(nx, ny, nz, [=] __device__(int x, int y, int z, int i) {
       C p = pot[i];
       T hval = 0, wv[3] = { 0, 0, 0 };   // stores last: every load is issued before them
       if (kc) {  // src/ot.c:641-645, 656-657, 673-675 summed over axes
