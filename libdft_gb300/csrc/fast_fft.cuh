@@ -345,7 +345,7 @@ template <int N> constexpr int xconv_smem(int nslice) {
 // cp.async while the first input is loaded and transformed.
 // Requires B | ny/2 so that a CTA's pencils lie on one side of ny/2.
 template <int N, int MODE>
-__global__ void __launch_bounds__(256, MODE == 1 ? 1 : 2) xconv_kernel(const C *__restrict__ tw, const XArgsF A, int multi) {
+__global__ void __launch_bounds__(256, MODE == 1 ? 1 : (MODE == 0 ? 3 : 2)) xconv_kernel(const C *__restrict__ tw, const XArgsF A, int multi) {
   constexpr bool MULTI = MODE == 1;
   constexpr int E = Shape<N>::E, TL = Shape<N>::TL, B = Shape<N>::B, LP = Shape<N>::LP, KXH = N / 2 + 1;
   extern __shared__ __align__(16) unsigned char smraw[];
