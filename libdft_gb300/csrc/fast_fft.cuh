@@ -204,8 +204,8 @@ template <class F> __host__ __device__ constexpr bool split_of(long) { return fa
 // LDS / STS: stage the load / store side through shared memory with a
 // line-fast cooperative loop (used for the transposed side of z passes).
 template <int N, int MODE, int MAP, int LDS, int STS, class Ld, class St>
-__global__ void __launch_bounds__(256) line_kernel(const C *__restrict__ tw, const C *__restrict__ tw2, float sign,
-                                                   const Ld ld, const St st) {
+__device__ __forceinline__ void line_body(const C *__restrict__ tw, const C *__restrict__ tw2, float sign,
+                                          const Ld &ld, const St &st) {
   constexpr int E = Shape<N>::E, TL = Shape<N>::TL, B = Shape<N>::B, LP = Shape<N>::LP;
   __shared__ C sm[B * LP];
   const int a = blockIdx.y, b0 = blockIdx.x * B;
@@ -290,6 +290,19 @@ __global__ void __launch_bounds__(256) line_kernel(const C *__restrict__ tw, con
       }
     }
   }
+}
+
+template <int N, int MODE, int MAP, int LDS, int STS, class Ld, class St>
+__global__ void __launch_bounds__(256) line_kernel(const C *__restrict__ tw, const C *__restrict__ tw2, float sign,
+                                                   const Ld ld, const St st) {
+  line_body<N, MODE, MAP, LDS, STS>(tw, tw2, sign, ld, st);
+}
+// Split loads hold all of a thread's operands (two complex per element) at
+// once; the bound keeps them to 80 registers, 3 CTAs per SM, without spills.
+template <int N, int MODE, int MAP, int LDS, int STS, class Ld, class St>
+__global__ void __launch_bounds__(256, 3) line_kernel_split(const C *__restrict__ tw, const C *__restrict__ tw2,
+                                                            float sign, const Ld ld, const St st) {
+  line_body<N, MODE, MAP, LDS, STS>(tw, tw2, sign, ld, st);
 }
 
 // --------------------------------------------------------------- x pencils

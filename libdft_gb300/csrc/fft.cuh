@@ -437,7 +437,10 @@ int launch_fast_lines(int na, int nb, float sign, const Ld &ld, const St &st) {
   DFT_TRY(get_plan<float>(N, &p1));
   p2.tw = nullptr;
   if (MODE != LINE_C2C) DFT_TRY(get_plan<float>(2 * N, &p2));
-  ff::line_kernel<N, MODE, MAP, LDS, STS, Ld, St><<<dim3(nb / B, na), 256, 0, rt().stream>>>(p1.tw, p2.tw, sign, ld, st);
+  if constexpr (LDS == 0 && ff::split_of<Ld>(0))
+    ff::line_kernel_split<N, MODE, MAP, LDS, STS, Ld, St><<<dim3(nb / B, na), 256, 0, rt().stream>>>(p1.tw, p2.tw, sign, ld, st);
+  else
+    ff::line_kernel<N, MODE, MAP, LDS, STS, Ld, St><<<dim3(nb / B, na), 256, 0, rt().stream>>>(p1.tw, p2.tw, sign, ld, st);
   DFT_CHECK_LAUNCH();
   return DFTGPU_OK;
 }
