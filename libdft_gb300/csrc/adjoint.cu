@@ -328,9 +328,14 @@ template <typename T> __device__ __forceinline__ typename cplx_t<T>::type half_e
 // prefetches its operand lines into L2 before the transform.
 template <typename T> struct AdjLoad {   // D^H g' = exp(conj a) g'
   typedef typename cplx_t<T>::type C;
-  static constexpr bool kSplit = true;
+  static constexpr bool kSplit = true, kAhead = true;
   struct Raw { C g, v; };
   const C *gp; const C *V; int ny, nz; T hr, hi;
+  __device__ void prefetch_lines(int x, int y0, int nl, int) const {
+    const size_t o = ((size_t) x * ny + y0) * nz, n = (size_t) nl * nz * sizeof(C);
+    if (threadIdx.x == 0) prefetch_bulk_l2(gp + o, n);
+    if (threadIdx.x == 32) prefetch_bulk_l2(V + o, n);
+  }
   __device__ Raw fetch(int x, int y, int e) const {
     const size_t i = ((size_t) x * ny + y) * nz + e;
     return Raw{ gp[i], V[i] };

@@ -52,6 +52,12 @@ __device__ __forceinline__ double2 cexp_dev(double2 z) {
 
 // Bring the line holding p into L2 (generic address; no register result).
 __device__ __forceinline__ void prefetch_l2(const void *p) { asm volatile("prefetch.L2 [%0];" ::"l"(p)); }
+// Bring [p, p + bytes) into L2 with one bulk prefetch; skipped unless p and
+// bytes are multiples of 16 (the instruction's requirement).
+__device__ __forceinline__ void prefetch_bulk_l2(const void *p, size_t bytes) {
+  if ((((size_t) p) | bytes) & 15 || bytes == 0 || bytes > 0xffffffffull) return;
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(__cvta_generic_to_global(p)), "r"((unsigned) bytes));
+}
 
 // exp(z) - 1 from expm1 and the half-angle sine (cos y - 1 = -2 sin^2(y/2)),
 // so that a factor near 1 keeps the full relative precision of its

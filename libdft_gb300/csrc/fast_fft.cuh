@@ -199,13 +199,27 @@ enum { MAP_E = 0, MAP_L = 1 };
 // called before the transform for the elements it will store.
 template <class F> __host__ __device__ constexpr auto split_of(int) -> decltype(F::kSplit, bool()) { return F::kSplit; }
 template <class F> __host__ __device__ constexpr bool split_of(long) { return false; }
+// Load functors with kAhead: each CTA prefetches into L2 the input of the CTA
+// `ahead` places after it (one wave of resident CTAs later), whose loads then
+// hit L2 instead of waiting on DRAM.
+template <class F> __host__ __device__ constexpr auto ahead_of(int) -> decltype(F::kAhead, bool()) { return F::kAhead; }
+template <class F> __host__ __device__ constexpr bool ahead_of(long) { return false; }
+template <int N, int MODE, int B, class Ld> __device__ __forceinline__ void prefetch_ahead(const Ld &ld, int ahead) {
+  if constexpr (ahead_of<Ld>(0)) {
+    const int id = blockIdx.y * gridDim.x + blockIdx.x + ahead;
+    if (ahead > 0 && id < (int) (gridDim.x * gridDim.y)) {
+      const int a2 = id / gridDim.x, b2 = (id - a2 * gridDim.x) * B;
+      ld.prefetch_lines(a2, b2, B, MODE == 2 ? N + 1 : N);
+    }
+  }
+}
 
 // MODE 0 C2C, 1 R2C (N = nz/2, post-processed to N+1 outputs), 2 C2R.
 // LDS / STS: stage the load / store side through shared memory with a
 // line-fast cooperative loop (used for the transposed side of z passes).
 template <int N, int MODE, int MAP, int LDS, int STS, class Ld, class St>
 __device__ __forceinline__ void line_body(const C *__restrict__ tw, const C *__restrict__ tw2, float sign,
-                                          const Ld &ld, const St &st) {
+                                          const Ld &ld, const St &st, int ahead) {
   constexpr int E = Shape<N>::E, TL = Shape<N>::TL, B = Shape<N>::B, LP = Shape<N>::LP;
   __shared__ C sm[B * LP];
   const int a = blockIdx.y, b0 = blockIdx.x * B;
@@ -216,11 +230,13 @@ __device__ __forceinline__ void line_body(const C *__restrict__ tw, const C *__r
     typename Ld::Raw raw[E];
 #pragma unroll
     for (int q = 0; q < E; q++) raw[q] = ld.fetch(a, b0 + l, t + TL * q);
+    prefetch_ahead<N, MODE, B>(ld, ahead);
 #pragma unroll
     for (int q = 0; q < E; q++) v[q] = ld.cook(raw[q]);
   } else if constexpr (LDS == 0) {
 #pragma unroll
     for (int q = 0; q < E; q++) v[q] = ld(a, b0 + l, t + TL * q);
+    prefetch_ahead<N, MODE, B>(ld, ahead);
   } else {
     // line-fast cooperative load of the whole tile (C2R: also the Nyquist
     // element N, which lands in the pitch's spare slot), fully unrolled so
@@ -234,6 +250,7 @@ __device__ __forceinline__ void line_body(const C *__restrict__ tw, const C *__r
         sm[sidx(ll, e, LP)] = ld(a, b0 + ll, e);
       }
     }
+    prefetch_ahead<N, MODE, B>(ld, ahead);
     __syncthreads();
 #pragma unroll
     for (int q = 0; q < E; q++) {
@@ -294,15 +311,15 @@ __device__ __forceinline__ void line_body(const C *__restrict__ tw, const C *__r
 
 template <int N, int MODE, int MAP, int LDS, int STS, class Ld, class St>
 __global__ void __launch_bounds__(256) line_kernel(const C *__restrict__ tw, const C *__restrict__ tw2, float sign,
-                                                   const Ld ld, const St st) {
-  line_body<N, MODE, MAP, LDS, STS>(tw, tw2, sign, ld, st);
+                                                   const Ld ld, const St st, int ahead) {
+  line_body<N, MODE, MAP, LDS, STS>(tw, tw2, sign, ld, st, ahead);
 }
 // Split loads hold all of a thread's operands (two complex per element) at
 // once; the bound keeps them to 80 registers, 3 CTAs per SM, without spills.
 template <int N, int MODE, int MAP, int LDS, int STS, class Ld, class St>
 __global__ void __launch_bounds__(256, 3) line_kernel_split(const C *__restrict__ tw, const C *__restrict__ tw2,
-                                                            float sign, const Ld ld, const St st) {
-  line_body<N, MODE, MAP, LDS, STS>(tw, tw2, sign, ld, st);
+                                                            float sign, const Ld ld, const St st, int ahead) {
+  line_body<N, MODE, MAP, LDS, STS>(tw, tw2, sign, ld, st, ahead);
 }
 
 // --------------------------------------------------------------- x pencils

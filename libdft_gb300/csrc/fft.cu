@@ -119,6 +119,15 @@ bool fused_zy_off() {
   return v == 1;
 }
 
+bool prefetch_ahead_on() {
+  static int v = -1;
+  if (v < 0) {
+    const char *e = getenv("DFTGPU_PREFETCH_AHEAD");
+    v = (e && e[0] == '0') ? 0 : 1;
+  }
+  return v == 1;
+}
+
 bool generic_fft_only() {
   static int v = -1;
   if (v < 0) {

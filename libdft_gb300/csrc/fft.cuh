@@ -420,6 +420,20 @@ template <class Kernel> bool SmemOptIn<Kernel>::done = false;
 }  // namespace
 
 bool generic_fft_only();   // DFTGPU_GENERIC_FFT=1 disables the register kernels
+bool prefetch_ahead_on();  // DFTGPU_PREFETCH_AHEAD=0 disables the one-wave-ahead L2 prefetch
+
+// CTAs of a 256-thread kernel resident on the whole GPU at once (the distance
+// of the line kernels' one-wave-ahead prefetch); 0 when prefetching is off.
+template <class K> int resident_ctas(K kernel) {
+  static int n = -1;
+  if (n < 0) {
+    int per_sm = 0;
+    if (!prefetch_ahead_on() || cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 256, 0) != cudaSuccess)
+      per_sm = 0;
+    n = per_sm * rt().num_sms;
+  }
+  return n;
+}
 
 // FP32 power-of-two lengths: register-resident kernel.  EF / EFS: the fast
 // address index of the load / store side is the element (1) or the line (0).
@@ -437,10 +451,13 @@ int launch_fast_lines(int na, int nb, float sign, const Ld &ld, const St &st) {
   DFT_TRY(get_plan<float>(N, &p1));
   p2.tw = nullptr;
   if (MODE != LINE_C2C) DFT_TRY(get_plan<float>(2 * N, &p2));
-  if constexpr (LDS == 0 && ff::split_of<Ld>(0))
-    ff::line_kernel_split<N, MODE, MAP, LDS, STS, Ld, St><<<dim3(nb / B, na), 256, 0, rt().stream>>>(p1.tw, p2.tw, sign, ld, st);
-  else
-    ff::line_kernel<N, MODE, MAP, LDS, STS, Ld, St><<<dim3(nb / B, na), 256, 0, rt().stream>>>(p1.tw, p2.tw, sign, ld, st);
+  if constexpr (LDS == 0 && ff::split_of<Ld>(0)) {
+    auto k = ff::line_kernel_split<N, MODE, MAP, LDS, STS, Ld, St>;
+    k<<<dim3(nb / B, na), 256, 0, rt().stream>>>(p1.tw, p2.tw, sign, ld, st, resident_ctas(k));
+  } else {
+    auto k = ff::line_kernel<N, MODE, MAP, LDS, STS, Ld, St>;
+    k<<<dim3(nb / B, na), 256, 0, rt().stream>>>(p1.tw, p2.tw, sign, ld, st, resident_ctas(k));
+  }
   DFT_CHECK_LAUNCH();
   return DFTGPU_OK;
 }

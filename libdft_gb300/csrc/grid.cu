@@ -219,9 +219,14 @@ template <typename T> int k_axpb(T *p, size_t n, T a, T b) {   // p = a p + b
 // before the transform, so the loads after it do not wait on DRAM.
 template <typename T> struct PhaseLoad {   // psi * exp(-i V dt / 2)
   typedef typename cplx_t<T>::type C;
-  static constexpr bool kSplit = true;
+  static constexpr bool kSplit = true, kAhead = true;
   struct Raw { C p, v; };
   const C *psi; const C *V; int ny, nz; T hr, hi;   // (hr, hi) = dt / 2
+  __device__ void prefetch_lines(int x, int y0, int nl, int) const {
+    const size_t o = ((size_t) x * ny + y0) * nz, n = (size_t) nl * nz * sizeof(C);
+    if (threadIdx.x == 0) prefetch_bulk_l2(psi + o, n);
+    if (threadIdx.x == 32) prefetch_bulk_l2(V + o, n);
+  }
   __device__ Raw fetch(int x, int y, int e) const {
     const size_t i = ((size_t) x * ny + y) * nz + e;
     return Raw{ psi[i], V[i] };

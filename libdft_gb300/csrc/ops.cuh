@@ -179,14 +179,23 @@ template <typename T> struct SpecStoreZ {           // z pass output
     spec[((size_t) k * nx + x) * ny + y] = v;
   }
 };
-template <typename T> struct SpecLoadZ {            // z pass input (inverse)
-  const typename cplx_t<T>::type *spec; int nx, ny;
-  __device__ typename cplx_t<T>::type operator()(int x, int y, int k) const {
+// Load functors with kAhead provide prefetch_lines(a, b0, nl, ne), called by
+// every thread of a CTA of the line kernels: bring the input of lines
+// (a, b0 .. b0+nl-1), elements 0 .. ne-1, into L2 (bulk prefetches).
+template <typename T> struct SpecLoadZ {            // z pass input (inverse); its tiles are one short
+  typedef typename cplx_t<T>::type C;                // run per plane, not prefetched ahead
+  const C *spec; int nx, ny;
+  __device__ C operator()(int x, int y, int k) const {
     return spec[((size_t) k * nx + x) * ny + y];
   }
 };
 template <typename T> struct SpecLineY {            // y pass in place: line (kz, x), element y
+  typedef typename cplx_t<T>::type C;
+  static constexpr bool kAhead = true;
   typename cplx_t<T>::type *spec; int nx, ny;
+  __device__ void prefetch_lines(int kz, int x0, int nl, int) const {     // nl whole lines, contiguous
+    if (threadIdx.x == 0) prefetch_bulk_l2(spec + ((size_t) kz * nx + x0) * ny, (size_t) nl * ny * sizeof(C));
+  }
   __device__ typename cplx_t<T>::type operator()(int kz, int x, int y) const {
     return spec[((size_t) kz * nx + x) * ny + y];
   }
@@ -195,7 +204,11 @@ template <typename T> struct SpecLineY {            // y pass in place: line (kz
   }
 };
 template <typename T> struct RealPairLoad {         // packed (f[2e], f[2e+1]) of a real row
+  static constexpr bool kAhead = true;
   const T *f; int ny, nz;
+  __device__ void prefetch_lines(int x, int y0, int nl, int) const {      // nl whole rows, contiguous
+    if (threadIdx.x == 0) prefetch_bulk_l2(f + ((size_t) x * ny + y0) * nz, (size_t) nl * nz * sizeof(T));
+  }
   __device__ typename cplx_t<T>::type operator()(int x, int y, int e) const {
     const T *row = f + ((size_t) x * ny + y) * nz;
     return mk<T>(row[2 * e], row[2 * e + 1]);
@@ -215,7 +228,11 @@ template <typename T> struct RealPairStore {        // real row <- scale * (re, 
 // the density row is written (2 real fields).
 template <typename T> struct DensityPairLoad {
   typedef typename cplx_t<T>::type C;
+  static constexpr bool kAhead = true;
   const C *psi; T *rho; int ny, nz;
+  __device__ void prefetch_lines(int x, int y0, int nl, int) const {
+    if (threadIdx.x == 0) prefetch_bulk_l2(psi + ((size_t) x * ny + y0) * nz, (size_t) nl * nz * sizeof(C));
+  }
   __device__ C operator()(int x, int y, int e) const {
     const size_t r = ((size_t) x * ny + y) * nz + 2 * e;
     const C a = psi[r], b = psi[r + 1];
