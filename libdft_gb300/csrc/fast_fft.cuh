@@ -230,7 +230,7 @@ __device__ __forceinline__ void line_body(const C *__restrict__ tw, const C *__r
     typename Ld::Raw raw[E];
 #pragma unroll
     for (int q = 0; q < E; q++) raw[q] = ld.fetch(a, b0 + l, t + TL * q);
-    prefetch_ahead<N, MODE, B>(ld, ahead);
+    prefetch_ahead<N, MODE, B>(ld, ahead);   // after the own loads: issued before it, they are not delayed
 #pragma unroll
     for (int q = 0; q < E; q++) v[q] = ld.cook(raw[q]);
   } else if constexpr (LDS == 0) {

@@ -226,20 +226,27 @@ template <typename T> struct RealPairStore {        // real row <- scale * (re, 
 // density grid: the density pass (src/ot.c:320) done by the first z pass of rho.
 // Algorithmic bytes beyond a real-row load: the psi row is twice as wide, and
 // the density row is written (2 real fields).
+// Split (fetch / cook): the density stores could alias psi for the compiler,
+// so without the split every element's psi loads would wait for the previous
+// element's store.
 template <typename T> struct DensityPairLoad {
   typedef typename cplx_t<T>::type C;
-  static constexpr bool kAhead = true;
+  static constexpr bool kAhead = true, kSplit = true;
+  struct Raw { C a, b; T *dst; };
   const C *psi; T *rho; int ny, nz;
   __device__ void prefetch_lines(int x, int y0, int nl, int) const {
     if (threadIdx.x == 0) prefetch_bulk_l2(psi + ((size_t) x * ny + y0) * nz, (size_t) nl * nz * sizeof(C));
   }
-  __device__ C operator()(int x, int y, int e) const {
+  __device__ Raw fetch(int x, int y, int e) const {
     const size_t r = ((size_t) x * ny + y) * nz + 2 * e;
-    const C a = psi[r], b = psi[r + 1];
-    const C d = mk<T>(a.x * a.x + a.y * a.y, b.x * b.x + b.y * b.y);
-    *reinterpret_cast<C *>(rho + r) = d;     // rows hold an even number of values
+    return Raw{ psi[r], psi[r + 1], rho + r };
+  }
+  __device__ C cook(const Raw &w) const {
+    const C d = mk<T>(w.a.x * w.a.x + w.a.y * w.a.y, w.b.x * w.b.x + w.b.y * w.b.y);
+    *reinterpret_cast<C *>(w.dst) = d;     // rows hold an even number of values
     return d;
   }
+  __device__ C operator()(int x, int y, int e) const { return cook(fetch(x, y, e)); }
 };
 // P <- scale * (P + (re, im) added to the real parts of P[2e], P[2e+1]): the
 // last c2r z pass of the potential adds the merged linear part into P and
