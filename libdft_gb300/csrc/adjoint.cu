@@ -360,9 +360,11 @@ template <typename T> struct AdjStore {
   }
   __device__ void operator()(int x, int y, int e, C h) const {
     const size_t i = ((size_t) x * ny + y) * nz + e;
-    const C a = half_exponent<T>(V[i], hr, hi);
-    const C u = mul_cexp(psi[i], a);
-    const C Y = cmulc(psio[i], gp[i]) + cmulc(u, h);          // conj(g') psi' + conj(h) u
+    // operands this kernel never writes through the read-only path (their
+    // loads may move ahead of the previous elements' stores); gp may be gout
+    const C a = half_exponent<T>(__ldg(V + i), hr, hi);
+    const C u = mul_cexp(__ldg(psi + i), a);
+    const C Y = cmulc(__ldg(psio + i), gp[i]) + cmulc(u, h);   // conj(g') psi' + conj(h) u
     // c = (-i dt/2) Y with dt/2 = (dr2, di2): (-i)(dr2 + i di2) = di2 - i dr2
     const C cc = mk<T>(di2 * Y.x + dr2 * Y.y, di2 * Y.y - dr2 * Y.x);
     C gv = gamV[i];

@@ -248,7 +248,7 @@ template <typename T> struct PhaseStore {
   }
   __device__ void operator()(int x, int y, int e, C val) const {
     const size_t i = ((size_t) x * ny + y) * nz + e;
-    C v = V[i];
+    const C v = __ldg(V + i);   // read-only path: the loads may move ahead of the psi stores
     C z = mk<T>(v.x * hi + v.y * hr, -(v.x * hr - v.y * hi));
     psi[i] = mul_cexp(val, z);
   }
