@@ -28,12 +28,22 @@ namespace ff {
 
 typedef float2 C;
 
+// smallest value >= lo that is 8 (mod 16)
+constexpr int pitch_8_mod_16(int lo) { return lo % 16 <= 8 ? lo - lo % 16 + 8 : lo - lo % 16 + 24; }
+
 template <int N> struct Shape {
   static constexpr int E = (N == 64) ? 8 : 16;
   static constexpr int NS = (N == 512) ? 3 : 2;
   static constexpr int TL = N / E;           // threads per line
   static constexpr int B = 256 / TL;         // lines per CTA
-  static constexpr int LP = N + N / 16 + 1;  // padded line pitch in shared memory (odd)
+  // padded line pitch in shared memory: odd (the skew e/16 and an odd pitch
+  // make both thread mappings conflict-free) when a half-warp holds one line
+  // (TL >= 16); when it holds two lines (TL = 8), a pitch = 8 (mod 16) plus
+  // the line offset (l / 2) mod 16 of sidx() puts the two lines' 8-element
+  // windows in opposite halves of the 16 bank pairs while 16 consecutive lines
+  // still start in 16 different ones
+  static constexpr int LP0 = N + N / 16 + 1;
+  static constexpr int LP = TL != 8 ? LP0 : pitch_8_mod_16(LP0 + 15);   // room for the line offset
   static constexpr int SMEM = B * LP * (int) sizeof(C);
   template <int S> __host__ __device__ static constexpr int R() {
     return N == 64 ? 8 : N == 128 ? (S == 0 ? 16 : 8) : N == 256 ? 16 : (S < 2 ? 16 : 2);
@@ -46,7 +56,9 @@ template <int N> struct Shape {
 
 template <int N> constexpr bool supported() { return N == 64 || N == 128 || N == 256 || N == 512; }
 
-__device__ __forceinline__ int sidx(int l, int e, int LP) { return l * LP + e + (e >> 4); }
+__host__ __device__ constexpr int sidx(int l, int e, int LP) {
+  return l * LP + e + (e >> 4) + ((LP & 15) == 8 ? ((l >> 1) & 15) : 0);
+}
 
 // --------------------------------------------------------------- butterflies
 __device__ __forceinline__ C rot(C a, float s) { return make_float2(-s * a.y, s * a.x); }   // * (s i)
