@@ -28,22 +28,25 @@ namespace ff {
 
 typedef float2 C;
 
-// smallest value >= lo that is 8 (mod 16)
-constexpr int pitch_8_mod_16(int lo) { return lo % 16 <= 8 ? lo - lo % 16 + 8 : lo - lo % 16 + 24; }
+// smallest value >= lo that is r (mod 16)
+constexpr int pitch_mod_16(int lo, int r) { return lo % 16 <= r ? lo - lo % 16 + r : lo - lo % 16 + 16 + r; }
 
 template <int N> struct Shape {
   static constexpr int E = (N == 64) ? 8 : 16;
   static constexpr int NS = (N == 512) ? 3 : 2;
   static constexpr int TL = N / E;           // threads per line
   static constexpr int B = 256 / TL;         // lines per CTA
-  // padded line pitch in shared memory: odd (the skew e/16 and an odd pitch
-  // make both thread mappings conflict-free) when a half-warp holds one line
-  // (TL >= 16); when it holds two lines (TL = 8), a pitch = 8 (mod 16) plus
-  // the line offset (l / 2) mod 16 of sidx() puts the two lines' 8-element
-  // windows in opposite halves of the 16 bank pairs while 16 consecutive lines
-  // still start in 16 different ones
+  // padded line pitch in shared memory (8-byte words; 16 bank pairs), chosen
+  // with the skew e/16 of sidx() so that each access pattern of the line
+  // kernels hits 16 different bank pairs per half-warp:
+  //  TL = 16: a half-warp is 16 elements of one line, or 16 lines at one
+  //           element: an odd pitch;
+  //  TL = 8:  two lines x 8 elements, or 16 lines: pitch = 8 (mod 16) plus
+  //           the line offset (l / 2) mod 16 of sidx() (the two lines' windows
+  //           in opposite halves, 16 consecutive lines on 16 bank pairs);
+  //  TL = 32: 8 lines x 2 adjacent elements (B = 8): pitch = 2 (mod 16).
   static constexpr int LP0 = N + N / 16 + 1;
-  static constexpr int LP = TL != 8 ? LP0 : pitch_8_mod_16(LP0 + 15);   // room for the line offset
+  static constexpr int LP = TL == 8 ? pitch_mod_16(LP0 + 15, 8) : TL == 32 ? pitch_mod_16(LP0, 2) : LP0;
   static constexpr int SMEM = B * LP * (int) sizeof(C);
   template <int S> __host__ __device__ static constexpr int R() {
     return N == 64 ? 8 : N == 128 ? (S == 0 ? 16 : 8) : N == 256 ? 16 : (S < 2 ? 16 : 2);
