@@ -383,8 +383,8 @@ template <int N> constexpr int xconv_smem(int nslice) {
 // MODE 1: as 0, plus at most one output with several terms (index `multi`)
 //         accumulated in registers and produced at the end.
 // MODE 2: a single output, the sum of all terms, accumulated in registers;
-//         the next input's loads are issued before the current input's
-//         transform, so two inputs are in flight per thread.
+//         while one input is transformed, the CTA's pencils of the next
+//         input are bulk-prefetched into L2 (128-byte runs, one per thread).
 // The launch parameters are staged in shared memory, and this CTA's slice of
 // every kernel octant (all kx, the B ky of its pencils) is fetched with
 // cp.async while the first input is loaded and transformed.
@@ -413,23 +413,24 @@ __global__ void __launch_bounds__(256, MODE == 1 ? 1 : (MODE == 0 ? 3 : 2)) xcon
   cp_async_commit();
   const size_t plane = (size_t) A.nx * A.ny;
   if constexpr (MODE == 2) {
-    C acc[E], nxt[E];
+    C acc[E], v[E];
 #pragma unroll
     for (int j = 0; j < E; j++) acc[j] = make_float2(0.f, 0.f);
     {
       const C *src = A.src[0] + kz * plane + y;
 #pragma unroll
-      for (int q = 0; q < E; q++) nxt[q] = src[(size_t) (t + TL * q) * A.ny];
+      for (int q = 0; q < E; q++) v[q] = src[(size_t) (t + TL * q) * A.ny];
     }
     __syncthreads();   // sA ready
     for (int in = 0; in < sA.nin; in++) {
-      C v[E];
+      if (in > 0) {
+        const C *src = sA.src[in] + kz * plane + y;
 #pragma unroll
-      for (int q = 0; q < E; q++) v[q] = nxt[q];
-      if (in + 1 < sA.nin) {
-        const C *src = sA.src[in + 1] + kz * plane + y;
-#pragma unroll
-        for (int q = 0; q < E; q++) nxt[q] = src[(size_t) (t + TL * q) * A.ny];
+        for (int q = 0; q < E; q++) v[q] = src[(size_t) (t + TL * q) * A.ny];
+      }
+      if (in + 1 < sA.nin) {   // the next input's pencils of this CTA into L2 while this one is transformed
+        const C *nsrc = sA.src[in + 1] + kz * plane + y0;
+        for (int x = threadIdx.x; x < N; x += 256) prefetch_bulk_l2(nsrc + (size_t) x * A.ny, B * sizeof(C));
       }
       transform<N>(v, t, l, -1.f, tw, sm);
       if (in == 0) {
