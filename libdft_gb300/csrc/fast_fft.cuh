@@ -466,6 +466,10 @@ __global__ void __launch_bounds__(256, MODE == 1 ? 1 : (MODE == 0 ? 3 : 2)) xcon
     C v[E];
 #pragma unroll
     for (int q = 0; q < E; q++) v[q] = src[(size_t) (t + TL * q) * A.ny];
+    if (in + 1 < sA.nin) {   // the next input's pencils of this CTA into L2 (as MODE 2)
+      const C *nsrc = sA.src[in + 1] + kz * plane + y0;
+      for (int x = threadIdx.x; x < N; x += 256) prefetch_bulk_l2(nsrc + (size_t) x * A.ny, B * sizeof(C));
+    }
     transform<N>(v, t, l, -1.f, tw, sm);
     if (in == 0) {
       cp_async_wait_all();
