@@ -359,19 +359,40 @@ __device__ __forceinline__ void cp_async4(void *smem, const void *gmem) {
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::); }
 
-// v * K(kx, ky, kz) for term tm; the kernel value comes from this CTA's slice
-// ks[slot][ix][iy - iylo] of the octant
-__device__ __forceinline__ C kmul(const XArgsF &A, const float *ks, int kxh, int B, int tm, C v, int kx, int ky,
-                                  int iyo) {
+// w[j] (+)= K_tm(kx_j, ky) v[j] for all of a thread's elements (x = the
+// element's final position): the term's kind, coefficient and kernel slice
+// are read once per call and each symmetry kind has its own loop.
+template <int N, bool ACC>
+__device__ __forceinline__ void kmul_all(const XArgsF &A, const float *ks, int tm, const C (&v)[Shape<N>::E],
+                                         C (&w)[Shape<N>::E], int t, int y, int iyo) {
+  constexpr int E = Shape<N>::E, B = Shape<N>::B, KXH = N / 2 + 1;
   const int kind = A.kind[tm];
-  if (kind == 4) return v * A.coef[tm];
-  const int ix = kx <= A.nx / 2 ? kx : A.nx - kx;
-  const float kv = ks[(A.slot[tm] * kxh + ix) * B + iyo] * A.coef[tm];
-  if (kind == 0) return v * kv;
-  float sg = 1.f;
-  if (kind == 1 && kx > A.nx / 2) sg = -1.f;
-  if (kind == 2 && ky > A.ny / 2) sg = -1.f;
-  return make_float2(-sg * kv * v.y, sg * kv * v.x);                   // (i sg kv) v
+  const float coef = A.coef[tm];
+  if (kind == 4) {
+#pragma unroll
+    for (int j = 0; j < E; j++) w[j] = ACC ? w[j] + v[j] * coef : v[j] * coef;
+    return;
+  }
+  const float *kk = ks + A.slot[tm] * KXH * B + iyo;
+  if (kind == 0) {
+#pragma unroll
+    for (int j = 0; j < E; j++) {
+      const int x = final_pos<N>(t, j), ix = x <= N / 2 ? x : N - x;
+      const C r = v[j] * (kk[ix * B] * coef);
+      w[j] = ACC ? w[j] + r : r;
+    }
+    return;
+  }
+  // odd kernels: (i sg kv) v, sg = -1 on the negative-frequency half of the odd axis
+  const float sgy = (kind == 2 && y > A.ny / 2) ? -coef : coef;
+#pragma unroll
+  for (int j = 0; j < E; j++) {
+    const int x = final_pos<N>(t, j), ix = x <= N / 2 ? x : N - x;
+    const float sg = kind == 1 ? (x > N / 2 ? -coef : coef) : sgy;
+    const float kv = kk[ix * B] * sg;
+    const C r = make_float2(-kv * v[j].y, kv * v[j].x);
+    w[j] = ACC ? w[j] + r : r;
+  }
 }
 
 template <int N> constexpr int xconv_smem(int nslice) {
@@ -439,8 +460,7 @@ __global__ void __launch_bounds__(256, MODE == 1 ? 1 : (MODE == 0 ? 3 : 2)) xcon
       }
       for (int tm = 0; tm < sA.nterm[0]; tm++) {
         if (sA.in[tm] != in) continue;
-#pragma unroll
-        for (int j = 0; j < E; j++) acc[j] = acc[j] + kmul(sA, ks, KXH, B, tm, v[j], final_pos<N>(t, j), y, iyo);
+        kmul_all<N, true>(sA, ks, tm, v, acc, t, y, iyo);
       }
     }
     to_input_order<N>(acc);
@@ -476,19 +496,19 @@ __global__ void __launch_bounds__(256, MODE == 1 ? 1 : (MODE == 0 ? 3 : 2)) xcon
       __syncthreads();   // kernel slices visible to all threads
     }
     for (int o = 0; o < sA.nout; o++) {
-      if (MULTI && o == multi) {
-        for (int tm = sA.t0[o]; tm < sA.t0[o] + sA.nterm[o]; tm++) {
-          if (sA.in[tm] != in) continue;
-#pragma unroll
-          for (int j = 0; j < E; j++) acc[j] = acc[j] + kmul(sA, ks, KXH, B, tm, v[j], final_pos<N>(t, j), y, iyo);
+      if constexpr (MULTI) {
+        if (o == multi) {
+          for (int tm = sA.t0[o]; tm < sA.t0[o] + sA.nterm[o]; tm++) {
+            if (sA.in[tm] != in) continue;
+            kmul_all<N, true>(sA, ks, tm, v, acc, t, y, iyo);
+          }
+          continue;
         }
-        continue;
       }
       const int tm = sA.t0[o];
       if (sA.in[tm] != in) continue;
       C w[E];
-#pragma unroll
-      for (int j = 0; j < E; j++) w[j] = kmul(sA, ks, KXH, B, tm, v[j], final_pos<N>(t, j), y, iyo);
+      kmul_all<N, false>(sA, ks, tm, v, w, t, y, iyo);
       to_input_order<N>(w);
       transform<N>(w, t, l, 1.f, tw, sm);
       C *dst = sA.dst[o] + kz * plane + y;
