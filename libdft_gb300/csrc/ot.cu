@@ -252,7 +252,12 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
 
   // real-field slots
   T *r[R_NREAL];   // slots of PotSlot (ot_work.cuh)
-  for (int i = 0; i < R_NREAL; i++) { r[i] = F.r(i); if (!r[i]) return DFTGPU_ERR_NOMEM; }
+  for (int i = 0; i < R_NREAL; i++) {
+    r[i] = nullptr;
+    if (i == R_U) continue;   // not used here: the linear part goes into P in its inverse transform
+    r[i] = F.r(i);
+    if (!r[i]) return DFTGPU_ERR_NOMEM;
+  }
   C *s[12];
   for (int i = 0; i < 12; i++) { s[i] = F.s(i); if (!s[i]) return DFTGPU_ERR_NOMEM; }
 

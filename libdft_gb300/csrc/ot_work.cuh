@@ -12,14 +12,15 @@ namespace dftgpu {
 
 // Real-field slots written by the potential evaluation (potential_t).  After a
 // potential evaluation they hold, for the wave function it was evaluated on:
-// R_U the merged linear part (LJ*rho + w*q + c F*h - m/2 V_j*(rho|v|^2)),
 // R_RB rho_bar, R_RT F*rho, R_A V_j*rho,
 // R_Q (c2 rb + c3 rb^2) rho, R_RST rho_st, R_S0..2 G_a = (d_a rho) rho_st,
 // R_V0..2 the velocity v_a (BF),
 // R_E rho|v|^2, R_B0..2 rho v_a, R_J0..2 J_a = F*G_a,
 // R_C V_j*(rho|v|^2) (only with a clamped backflow potential),
-// R_BB0..2 B_a = V_j*(rho v_a), R_H sum_a (d_a rho) J_a.  Slots from
-// R_NREAL on are free.
+// R_BB0..2 B_a = V_j*(rho v_a), R_H sum_a (d_a rho) J_a.  R_U is not used
+// by the potential (the merged linear part LJ*rho + w*q + c F*h
+// - m/2 V_j*(rho|v|^2) is added into P by its inverse transform); the energy
+// density uses slot 0 as scratch.  Slots from R_NREAL on are free.
 enum PotSlot {
   R_U, R_RB, R_RT, R_A, R_Q, R_RST, R_S0, R_S1, R_S2, R_V0, R_V1, R_V2, R_E,
   R_B0, R_B1, R_B2, R_J0, R_J1, R_J2, R_C, R_BB0, R_BB1, R_BB2, R_H, R_NREAL
