@@ -3,6 +3,9 @@
 
 * 64^3 plain OT, 200 imaginary-time steps of 10 fs with a repulsive Gaussian
   external potential and the norm fixed: GPU FP64 against the FP64 CPU oracle;
+* the 256^3 droplet of the bench (N = 2000, full OT): energy per atom and mu
+  after 2 renormalised imaginary-time steps, GPU FP64 and FP32 against the
+  FP64 CPU oracle;
 * 128^3 full OT (l_g = 1.1 A), 500 real-time steps of 1 fs from a 1 %
   density modulation: energy drift of the FP64 run, FP32 against FP64
   (energy and density);
@@ -68,6 +71,50 @@ def test_cfg0_plain_imaginary_time_matches_oracle(gpu, port):
     assert abs(n / norm0 - 1) < 1e-12
     for o in (ve, P, ot, wp, w):
         o.free()
+
+
+def test_cfg2_droplet_256_energy_and_mu_match_oracle(gpu, port):
+    """256^3, step 0.8 bohr, full OT, He droplet of N = 2000 (the bench's
+    workload, bench.droplet_psi): 2 imaginary-time predict-correct steps of
+    20 fs, each followed by the renormalisation to N.  Energy per atom and mu
+    = (<T> + int rho Re V_OT + int rho V_ext) / N of the GPU in FP64 and FP32
+    against the FP64 oracle.  Kernel sampling with 2..4 substeps on both sides
+    (CPU time of the oracle's kernel generation at 256^3)."""
+    import bench
+    shape, step, nsteps = (256, 256, 256), 0.8, 2
+    psi0 = bench.droplet_psi(256, step)
+    dt = -20j / gpu.AUTOFS
+    dv = step ** 3
+    with Grids(port, shape, step, gpu.HELIUM_MASS) as g:
+        wo, wpo, Po, work = g.wf(psi0), g.wf(), g.cgrid(), g.rgrid()
+        oo = g.ot(9, wo, min_ns=2, max_ns=4)
+        mu0 = port.lib.orc_bulk_chempot(oo, 0.0)
+        port.lib.orc_wf_set_norm(wo, bench.NATOMS)
+        port.lib.orc_wf_normalize(wo)
+        for _ in range(nsteps):
+            port.lib.orc_pc_step(oo, wo, wpo, Po, None, mu0, dt.real, dt.imag)
+            port.lib.orc_wf_normalize(wo)
+        n_ref = port.lib.orc_wf_norm(wo)
+        e_ref = port.lib.orc_total_energy(oo, wo, None, work) / n_ref
+        t_ref = port.lib.orc_wf_kinetic_energy(wo)
+        rho = np.abs(g.get_wf(wo)) ** 2
+        vot = g.potential(oo, wo)
+        mu_ref = (t_ref + np.sum(rho * vot.real) * dv) / n_ref
+    for prec, tol, ntol in ((0, 1e-9, 1e-12), (1, 1e-6, 1e-6)):
+        gpu.set_precision(prec)
+        w, wp, P = gpu.Wf(shape, step), gpu.Wf(shape, step), gpu.CGrid(shape, step)
+        ot = gpu.OT(9, w, min_ns=2, max_ns=4)
+        w.set(psi0)
+        w.norm_target = bench.NATOMS
+        w.normalize()
+        ot.run(w, wp, P, None, ot.bulk_chempot(0.0), dt, nsteps, True)
+        e, n, mu = ot.energy_report(w)
+        for o in (P, ot, wp, w):
+            o.free()
+        gpu.set_precision(0)
+        assert abs(n / n_ref - 1) < ntol         # FP32: the renormalised grid is rounded to FP32
+        assert abs((e / n) / e_ref - 1) < tol, (prec, e / n, e_ref)
+        assert abs(mu / mu_ref - 1) < tol, (prec, mu, mu_ref)
 
 
 def cfg1_psi(gpu, shape, step):
