@@ -57,6 +57,17 @@ def droplet_psi(n=NX, step=STEP, seed=3):
     return psi.astype(np.complex128)
 
 
+def finite_or_null(obj):
+    """NaN / inf (phases a run skipped) as JSON null, so the line is strict JSON."""
+    if isinstance(obj, float):
+        return obj if np.isfinite(obj) else None
+    if isinstance(obj, dict):
+        return {k: finite_or_null(v) for k, v in obj.items()}
+    if isinstance(obj, (list, tuple)):
+        return [finite_or_null(v) for v in obj]
+    return obj
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -381,7 +392,7 @@ def main():
     NX = args.grid
     line = run_reference(args) if args.impl == "reference" else run_gpu(args)
     if line is not None:
-        print(json.dumps(line))
+        print(json.dumps(finite_or_null(line)))
 
 
 if __name__ == "__main__":

@@ -59,10 +59,36 @@ __device__ __forceinline__ void prefetch_bulk_l2(const void *p, size_t bytes) {
   asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(__cvta_generic_to_global(p)), "r"((unsigned) bytes));
 }
 
-// exp(z) - 1 from expm1 and the half-angle sine (cos y - 1 = -2 sin^2(y/2)),
-// so that a factor near 1 keeps the full relative precision of its
-// difference from 1.
+// exp(z) - 1 for |Re z| + |Im z| < 0.25 from the Taylor series of e^x - 1,
+// sin y and cos y - 1 (Horner), each truncated where the next term is below
+// 2e-9 of the result on that interval (e^x - 1 to x^7, sin y to y^7,
+// cos y - 1 to y^8): no range reduction, and cos y - 1 keeps its full relative
+// precision, so |exp(i y)| = 1 to the rounding of y.
+__device__ __forceinline__ float2 cexpm1_small(float2 z) {
+  const float x = z.x, y = z.y, y2 = y * y;
+  float em = fmaf(x, 1.f / 5040.f, 1.f / 720.f);
+  em = fmaf(x, em, 1.f / 120.f);
+  em = fmaf(x, em, 1.f / 24.f);
+  em = fmaf(x, em, 1.f / 6.f);
+  em = fmaf(x, em, 0.5f);
+  em = fmaf(x, em, 1.f);
+  em *= x;                                         // e^x - 1
+  float sy = fmaf(y2, -1.f / 5040.f, 1.f / 120.f);
+  sy = fmaf(y2, sy, -1.f / 6.f);
+  sy = fmaf(y2, sy, 1.f);
+  sy *= y;                                         // sin y
+  float cm = fmaf(y2, 1.f / 40320.f, -1.f / 720.f);
+  cm = fmaf(y2, cm, 1.f / 24.f);
+  cm = fmaf(y2, cm, -0.5f);
+  cm *= y2;                                        // cos y - 1
+  return make_float2(fmaf(em, cm, em + cm), fmaf(em, sy, sy));   // (e^x cos y - 1, e^x sin y)
+}
+
+// exp(z) - 1, so that a factor near 1 keeps the full relative precision of
+// its difference from 1: the polynomials above for small |z|, otherwise
+// expm1 and the half-angle sine (cos y - 1 = -2 sin^2(y/2)).
 __device__ __forceinline__ float2 cexpm1(float2 z) {
+  if (fabsf(z.x) + fabsf(z.y) < 0.25f) return cexpm1_small(z);
   float sh, ch;
   sincosf(0.5f * z.y, &sh, &ch);
   const float em = expm1f(z.x), s2 = 2.f * sh * sh;
@@ -99,7 +125,7 @@ template <typename C> __device__ __forceinline__ C cprod1p(C p, C q) {
 // modes) uses the factor directly, so a damped value keeps its own relative
 // precision.
 __device__ __forceinline__ float2 mul_cexp(float2 a, float2 z) {
-  if (fabsf(z.x) + fabsf(z.y) < 0.25f) return mul_1p(a, cexpm1(z));
+  if (fabsf(z.x) + fabsf(z.y) < 0.25f) return mul_1p(a, cexpm1_small(z));
   return cmul(a, cexp_dev(z));
 }
 __device__ __forceinline__ double2 mul_cexp(double2 a, double2 z) {
