@@ -217,6 +217,8 @@ template <class F> __host__ __device__ constexpr bool split_of(long) { return fa
 // Load functors with kAhead: each CTA prefetches into L2 the input of the CTA
 // `ahead` places after it (one wave of resident CTAs later), whose loads then
 // hit L2 instead of waiting on DRAM.
+template <class F> __host__ __device__ constexpr auto bounded_store_of(int) -> decltype(F::kBoundedStore, bool()) { return F::kBoundedStore; }
+template <class F> __host__ __device__ constexpr bool bounded_store_of(long) { return false; }
 template <class F> __host__ __device__ constexpr auto ahead_of(int) -> decltype(F::kAhead, bool()) { return F::kAhead; }
 template <class F> __host__ __device__ constexpr bool ahead_of(long) { return false; }
 template <int N, int MODE, int B, class Ld> __device__ __forceinline__ void prefetch_ahead(const Ld &ld, int ahead) {
@@ -327,6 +329,14 @@ __device__ __forceinline__ void line_body(const C *__restrict__ tw, const C *__r
 template <int N, int MODE, int MAP, int LDS, int STS, class Ld, class St>
 __global__ void __launch_bounds__(256) line_kernel(const C *__restrict__ tw, const C *__restrict__ tw2, float sign,
                                                    const Ld ld, const St st, int ahead) {
+  line_body<N, MODE, MAP, LDS, STS>(tw, tw2, sign, ld, st, ahead);
+}
+// Passes whose store functor asks for it (kBoundedStore: the inverse phase
+// pass, whose operand loads follow the transform): bounded to 48 registers,
+// 5 CTAs per SM, to hide their latency.
+template <int N, int MODE, int MAP, int LDS, int STS, class Ld, class St>
+__global__ void __launch_bounds__(256, 5) line_kernel_stsplit(const C *__restrict__ tw, const C *__restrict__ tw2,
+                                                              float sign, const Ld ld, const St st, int ahead) {
   line_body<N, MODE, MAP, LDS, STS>(tw, tw2, sign, ld, st, ahead);
 }
 // Split loads hold all of a thread's operands (two complex per element) at

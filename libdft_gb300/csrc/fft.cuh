@@ -454,6 +454,9 @@ int launch_fast_lines(int na, int nb, float sign, const Ld &ld, const St &st) {
   if constexpr (LDS == 0 && ff::split_of<Ld>(0)) {
     auto k = ff::line_kernel_split<N, MODE, MAP, LDS, STS, Ld, St>;
     k<<<dim3(nb / B, na), 256, 0, rt().stream>>>(p1.tw, p2.tw, sign, ld, st, resident_ctas(k));
+  } else if constexpr (STS == 0 && ff::bounded_store_of<St>(0)) {
+    auto k = ff::line_kernel_stsplit<N, MODE, MAP, LDS, STS, Ld, St>;
+    k<<<dim3(nb / B, na), 256, 0, rt().stream>>>(p1.tw, p2.tw, sign, ld, st, resident_ctas(k));
   } else {
     auto k = ff::line_kernel<N, MODE, MAP, LDS, STS, Ld, St>;
     k<<<dim3(nb / B, na), 256, 0, rt().stream>>>(p1.tw, p2.tw, sign, ld, st, resident_ctas(k));

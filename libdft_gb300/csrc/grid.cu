@@ -240,7 +240,7 @@ template <typename T> struct PhaseLoad {   // psi * exp(-i V dt / 2)
 };
 template <typename T> struct PhaseStore {
   typedef typename cplx_t<T>::type C;
-  static constexpr bool kSplit = true;
+  static constexpr bool kSplit = true, kBoundedStore = true;
   C *psi; const C *V; int ny, nz; T hr, hi;
   __device__ void prefetch(int x, int y, int e) const {
     const size_t i = ((size_t) x * ny + y) * nz + e;
