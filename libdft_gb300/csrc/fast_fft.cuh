@@ -300,18 +300,22 @@ __device__ __forceinline__ void line_body(const C *__restrict__ tw, const C *__r
     for (int j = 0; j < E; j++) sm[sidx(l, final_pos<N>(t, j), LP)] = v[j];
     __syncthreads();
     if constexpr (MODE == 1) {
-      // X[k] = (Z[k] + Z*[N-k]) / 2 - (i/2) w^k (Z[k] - Z*[N-k]),  k = 0..N
-      constexpr int TOT = B * (N + 1), IT = (TOT + 255) / 256;
+      // X[k] = (Z[k] + Z*[N-k]) / 2 - (i/2) w^k (Z[k] - Z*[N-k]),  k = 0..N, in
+      // pairs: with sum = Z[k] + Z*[N-k] and tt = w^k (Z[k] - Z*[N-k]),
+      // X[k] = (sum - i tt) / 2 and X[N-k] = conj(sum + i tt) / 2 (w^N = -1),
+      // so one read of Z[k], Z[N-k] gives both outputs (k = 0: X[0] and X[N];
+      // k = N/2 pairs with itself)
+      constexpr int TOT = B * (N / 2 + 1), IT = (TOT + 255) / 256;
 #pragma unroll
       for (int it = 0; it < IT; it++) {
         const int idx = threadIdx.x + it * 256;
         if (idx < TOT) {
           const int ll = idx % B, k = idx / B;
-          const C zk = sm[sidx(ll, k == N ? 0 : k, LP)], zm = sm[sidx(ll, k == 0 ? 0 : N - k, LP)];
+          const C zk = sm[sidx(ll, k, LP)], zm = sm[sidx(ll, k == 0 ? 0 : N - k, LP)];
           const C sum = make_float2(zk.x + zm.x, zk.y - zm.y), dif = make_float2(zk.x - zm.x, zk.y + zm.y);
-          const C w = k == N ? make_float2(-1.f, 0.f) : __ldg(&tw2[k]);
-          const C tt = cmul(dif, w);
+          const C tt = cmul(dif, __ldg(&tw2[k]));
           st(a, b0 + ll, k, make_float2(0.5f * (sum.x + tt.y), 0.5f * (sum.y - tt.x)));
+          if (k != N / 2) st(a, b0 + ll, N - k, make_float2(0.5f * (sum.x - tt.y), -0.5f * (sum.y + tt.x)));
         }
       }
     } else {
