@@ -510,13 +510,18 @@ template <typename T> static int energy_density_t(dft_ot_functional *otf, rgrid 
   C *s[8];
   for (int i = 0; i < 8; i++) { s[i] = F.s(i); if (!s[i]) return DFTGPU_ERR_NOMEM; }
 
+  const bool any = plain || kc || bf;
   if (dens) {
     if (dens != otf->density) DFT_CUDA(cudaMemcpyAsync(rho, dens->value, nb, cudaMemcpyDeviceToDevice, rt().stream));
-  } else {
+    if (!any) return add ? DFTGPU_OK : rfill(edg, 0.0);
+    DFT_TRY(F.fwd(rho, s[0]));
+  } else if (!any) {
     DFT_TRY(density(gwf->grid, otf->density));
+    return add ? DFTGPU_OK : rfill(edg, 0.0);
+  } else {   // rho = |psi|^2 (src/ot-energy.c:44), formed and stored by the first z pass
+    DensityPairLoad<T> ld{psi, rho, ny, nz};
+    DFT_TRY(rfft_zy<T>(ld, s[0], nx, ny, nz, 2.0 * nb));
   }
-  if (!plain && !kc && !bf) return add ? DFTGPU_OK : rfill(edg, 0.0);
-  DFT_TRY(F.fwd(rho, s[0]));
   {
     XConvArgs<T> A; xc_init(A, P); xc_in(A, (const C *) s[0]);
     if (plain) {
