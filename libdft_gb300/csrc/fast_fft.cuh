@@ -5,8 +5,9 @@
 // transform is 2 or 3 Stockham stages with compile-time radices
 //   N = 64: 8 x 8     N = 128: 16 x 8     N = 256: 16 x 16     N = 512: 16 x 16 x 2
 // computed entirely in registers; only the stage boundaries exchange data
-// through shared memory (one store + one load per element, padded so that
-// neither mapping below causes bank conflicts).  The first stage reads
+// through shared memory (one store + one load per element; the line pitch and
+// skew of Shape<N>::LP / sidx() keep both mappings below free of bank
+// conflicts).  The first stage reads
 // element t + TL*q of its line and the last stage produces elements
 // t + TL*j, so loads and stores go straight between HBM and registers:
 //   EFAST mapping (thread t fast within a line): lines contiguous in memory
@@ -17,6 +18,9 @@
 // that side through shared memory with a cooperative line-fast loop.  The
 // forward transform's output layout equals the inverse's input layout, so the
 // x-pencil kernels apply k-space factors in registers between the two.
+// Load / store functors may opt into split loads, store-side L2 prefetch,
+// bounded entry points and a one-wave-ahead bulk L2 prefetch (see the traits
+// before line_body).
 #pragma once
 
 #include <cooperative_groups.h>
