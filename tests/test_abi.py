@@ -74,11 +74,13 @@ def test_init_without_gpu_reports_nodevice(built):
     assert L.dftgpu_last_error() == 7
 
 
-def test_c_dropin_example_compiles_and_links(built, tmp_path):
-    """The libdft-style driver (REAL complex time steps, dft_ot_* calls)
-    compiles as C against include/dftgpu.h and links against libdftgpu.so."""
-    src = os.path.join(ROOT, "libdft_gb300", "examples", "imag_time.c")
-    exe = tmp_path / "imag_time"
+@pytest.mark.parametrize("example", ["imag_time", "moving_bubble"])
+def test_c_dropin_example_compiles_and_links(built, tmp_path, example):
+    """The libdft-style drivers (REAL complex time steps, dft_ot_* calls; the
+    moving-background bubble of examples/gas-bubble/bubble.c) compile as C
+    against include/dftgpu.h and link against libdftgpu.so."""
+    src = os.path.join(ROOT, "libdft_gb300", "examples", example + ".c")
+    exe = tmp_path / example
     subprocess.run(["gcc", "-std=gnu11", "-O2", "-I", os.path.join(ROOT, "include"), src, "-o", str(exe),
                     "-L", os.path.dirname(built), "-ldftgpu", "-lm", "-Wl,-rpath," + os.path.dirname(built)],
                    check=True)
