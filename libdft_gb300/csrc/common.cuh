@@ -187,14 +187,15 @@ int reduce_partials(double **buf, size_t *n);
 // algorithmic bytes (each input read once, each output written once).
 bool prof_on();
 int prof_begin();                                     // returns a record id or -1
-void prof_end(int id, const char *name, double bytes);
+void prof_end(int id, const char *name, double bytes, int kernels = 1);
 
-struct ProfScope {
+struct ProfScope {      // kernels: kernel launches inside the scope
   int id;
   const char *name;
   double bytes;
-  ProfScope(const char *n, double b) : id(prof_on() ? prof_begin() : -1), name(n), bytes(b) {}
-  ~ProfScope() { if (id >= 0) prof_end(id, name, bytes); }
+  int kernels;
+  ProfScope(const char *n, double b, int k = 1) : id(prof_on() ? prof_begin() : -1), name(n), bytes(b), kernels(k) {}
+  ~ProfScope() { if (id >= 0) prof_end(id, name, bytes, kernels); }
 };
 
 inline size_t elem_size(int prec) { return prec == DFTGPU_FP32 ? 4 : 8; }

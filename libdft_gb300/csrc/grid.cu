@@ -85,7 +85,7 @@ int par_streams(cudaStream_t **aux, cudaEvent_t **ev) {
 
 // ------------------------------------------------------------------ profiler
 namespace {
-struct ProfRec { cudaEvent_t a, b; const char *name; double bytes; };
+struct ProfRec { cudaEvent_t a, b; const char *name; double bytes; int kernels; };
 bool g_prof = false;
 std::vector<ProfRec> g_recs;      // records of the current profile window
 std::vector<cudaEvent_t> g_pool;  // spare events
@@ -109,15 +109,17 @@ int prof_begin() {
   r.b = pool_event();
   r.name = nullptr;
   r.bytes = 0;
+  r.kernels = 0;
   cudaEventRecord(r.a, rt().stream);
   g_recs.push_back(r);
   return (int) g_recs.size() - 1;
 }
 
-void prof_end(int id, const char *name, double bytes) {
+void prof_end(int id, const char *name, double bytes, int kernels) {
   ProfRec &r = g_recs[id];
   r.name = name;
   r.bytes = bytes;
+  r.kernels = kernels;
   cudaEventRecord(r.b, rt().stream);
 }
 
@@ -129,7 +131,8 @@ int prof_enable(int on) {
   return DFTGPU_OK;
 }
 
-// JSON {"class": {"launches": n, "ms": t, "bytes": b}, ...}
+// JSON {"class": {"launches": n, "ms": t, "bytes": b}, ...}; launches counts
+// kernel launches (a scope may hold several, e.g. the two-kernel reduction)
 int prof_report(char *buf, size_t len) {
   DFT_CUDA(cudaDeviceSynchronize());
   struct Acc { const char *name; long n; double ms, bytes; };
@@ -140,7 +143,7 @@ int prof_report(char *buf, size_t len) {
     size_t k = 0;
     while (k < acc.size() && strcmp(acc[k].name, r.name)) k++;
     if (k == acc.size()) acc.push_back({r.name, 0, 0.0, 0.0});
-    acc[k].n++;
+    acc[k].n += r.kernels;
     acc[k].ms += ms;
     acc[k].bytes += r.bytes;
   }
@@ -353,8 +356,11 @@ template <typename T> int scale_by_norm_t(cgrid *c, const double *slot, double t
   typedef typename cplx_t<T>::type C;
   C *p = (C *) c->value;
   T *factor = (T *) (reduce_slots() + 48);   // scratch slot, written here and read below on the same stream
-  norm_factor_kernel<T><<<1, 1, 0, rt().stream>>>(slot, target, factor);
-  DFT_CHECK_LAUNCH();
+  {
+    ProfScope prof("reduce_fp64", 0.0);
+    norm_factor_kernel<T><<<1, 1, 0, rt().stream>>>(slot, target, factor);
+    DFT_CHECK_LAUNCH();
+  }
   return launch_each(gsize(c), [=] __device__(size_t i) {
     const T f = *factor;
     C z = p[i];

@@ -154,7 +154,7 @@ template <int NV> __global__ void reduce_final_kernel(const double *partial, dou
 template <int NV, class F> int reduce_dev(size_t n, F f, double *slot, double scale) {
   double *part; size_t np;
   DFT_TRY(reduce_partials(&part, &np));
-  ProfScope prof("reduce_fp64", 0.0);
+  ProfScope prof("reduce_fp64", 0.0, 2);
   reduce_partial_kernel<NV><<<RED_BLOCKS, RED_THREADS, 0, rt().stream>>>(n, f, part);
   DFT_CHECK_LAUNCH();
   reduce_final_kernel<NV><<<1, RED_THREADS, 0, rt().stream>>>(part, slot, scale);
