@@ -46,6 +46,7 @@ extern "C" {
 #define DFTGPU_ERR_NONFINITE    5   /* NaN / Inf detected by an FP64 reduction */
 #define DFTGPU_ERR_UNSUPPORTED  6   /* model / boundary / propagator not provided */
 #define DFTGPU_ERR_NODEVICE     7   /* no CUDA device */
+#define DFTGPU_ERR_IO           8   /* file could not be opened, read or written */
 
 /* precision of newly allocated grids */
 #define DFTGPU_FP64 0
@@ -328,6 +329,84 @@ REAL dft_ot_bulk_chempot2(dft_ot_functional *otf);
 REAL dft_ot_bulk_compressibility(dft_ot_functional *otf, REAL rho);
 REAL dft_ot_bulk_sound_speed(dft_ot_functional *otf, REAL rho);
 REAL dft_ot_bulk_dispersion(dft_ot_functional *otf, REAL *k, REAL rho0);
+REAL dft_ot_bulk_chempot3(dft_ot_functional *otf, REAL rho0);                 /* src/helium-ot-bulk.c:128 */
+/* -1/X(k) of the uniform liquid (src/helium-ot-bulk.c:445); as there, k below
+ * 0.01 bohr^-1 returns 0.01. */
+REAL dft_ot_bulk_istatic(dft_ot_functional *otf, REAL *k, REAL rho0);
+
+/* ------------------------------------------- driver compatibility
+ * Names libdft's example drivers take from libgrid's <grid/grid.h> and
+ * <grid/au.h> and from libdft's <dft/dft.h> besides the entry points above.
+ * include/grid/grid.h, grid/au.h, dft/dft.h and dft/ot.h include this file,
+ * so a driver builds with its own #include lines and -I<repo>/include. */
+#define HBAR           1.0                    /* atomic units */
+#define GRID_AUTOM     0.529177210903E-10     /* bohr -> m (CODATA 2018) */
+#define GRID_AUTOS     2.4188843265857E-17    /* a.u. time -> s */
+#define GRID_AUTOPA    2.9421015697E13        /* a.u. pressure -> Pa */
+#define GRID_AUKB      (1.0 / GRID_AUTOK)     /* Boltzmann constant, hartree / K */
+#define GRID_HZTOCM1   3.33564095198152E-11   /* Hz -> cm^-1 (1 / c in cm/s) */
+#define FMT_R "%le"
+#define FMT_I "%ld"
+
+typedef struct {      /* src/dft.h:55-60 */
+  REAL kx, ky, kz;    /* wave vector */
+  REAL a;             /* relative amplitude */
+  REAL rho;           /* background density */
+} dft_plane_wave;
+
+/* Wall-clock and CPU timer (examples/imag_time/imag_time.c:228,242). */
+typedef struct grid_timer_struct {
+  double wall0, cpu0;
+} grid_timer;
+void grid_timer_start(grid_timer *timer);
+REAL grid_timer_wall_clock_time(grid_timer *timer);   /* seconds since grid_timer_start */
+REAL grid_timer_cpu_time(grid_timer *timer);
+
+/* FFTW planning and host threads (examples/imag_time/imag_time.c:192-194,226):
+ * accepted and ignored -- the GPU transforms need no plans or wisdom and the
+ * host does no grid arithmetic. */
+void grid_set_fftw_flags(INT flags);
+void grid_threads_init(INT threads);
+void grid_fft_read_wisdom(char *file);
+void grid_fft_write_wisdom(char *file);
+
+/* Map callbacks of libdft (src/common.c, src/initial.c) for rgrid_map /
+ * cgrid_map / grid_wf_map: host functions, same arguments and values. */
+REAL dft_common_lj_func(REAL r2, REAL sig, REAL eps);                      /* src/common.c:31 */
+REAL dft_common_lennard_jones(void *arg, REAL x, REAL y, REAL z);          /* src/common.c:53 (dft_common_lj *) */
+REAL dft_common_lennard_jones_smooth(void *arg, REAL x, REAL y, REAL z);   /* src/common.c:104 */
+REAL dft_common_spherical_avg(void *arg, REAL x, REAL y, REAL z);          /* src/common.c:131 (REAL *radius) */
+REAL dft_common_spherical_avg_k(void *arg, REAL kx, REAL ky, REAL kz);     /* src/common.c:173 */
+REAL dft_common_gaussian(void *arg, REAL x, REAL y, REAL z);               /* src/common.c:193 (REAL *inv_width) */
+REAL dft_common_vortex_x(void *param, REAL x, REAL y, REAL z);             /* src/common.c:1240 (REAL *mass) */
+REAL dft_common_vortex_y(void *param, REAL x, REAL y, REAL z);             /* src/common.c:1260 */
+REAL dft_common_vortex_z(void *param, REAL x, REAL y, REAL z);             /* src/common.c:1280 */
+
+/* Grid files.  <base>.grd holds the whole grid (FP64, with its shape, step,
+ * origin and, for complex grids, momentum); <base>.x, .y, .z are text cuts
+ * along each axis through (nx/2, ny/2, nz/2): "coordinate value" lines
+ * (complex: "coordinate re im").  The file names follow libdft's drivers
+ * (examples/imag_time/imag_time.c:248-250, examples/imag_time/Makefile:16);
+ * the .grd layout is this library's own, written out below, because
+ * libgrid's is not part of libdft -- files written by libgrid are refused
+ * (DFTGPU_ERR_UNSUPPORTED).  Reading requires the grid's shape
+ * (DFTGPU_ERR_SIZE otherwise) and sets its values, origin and momentum; an
+ * FP32 grid receives the values rounded to FP32.
+ *   .grd layout, little-endian: char magic[8] = "DFTGPUG1"; int64 kind
+ *   (0 real, 1 complex); int64 nx, ny, nz; double step, x0, y0, z0, kx0,
+ *   ky0, kz0; then nx*ny*nz doubles (complex: re, im pairs) in [x][y][z]
+ *   order. */
+void rgrid_write_grid(char *base, rgrid *grid);            /* examples/imag_time/imag_time.c:248 */
+void cgrid_write_grid(char *base, cgrid *grid);            /* examples/imag_time/imag_time.c:250 */
+void rgrid_read_grid(rgrid *grid, char *base);             /* examples/added_mass_viscosity/added_mass2.c:368 */
+void cgrid_read_grid(cgrid *grid, char *base);             /* examples/added_mass/added_mass.c:111 */
+/* The same on host buffers (nx*ny*nz FP64 values, complex interleaved):
+ * meta = { step, x0, y0, z0, kx0, ky0, kz0 }.  Return a DFTGPU_* code. */
+int dftgpu_grid_file_write(const char *base, int is_complex, INT nx, INT ny, INT nz, const double *meta,
+                           const double *values);
+int dftgpu_grid_file_read(const char *base, int is_complex, INT nx, INT ny, INT nz, double *meta, double *values);
+/* one value of a complex grid (cgrid_value_at_index; indices wrap periodically) */
+int cgrid_value_at_index_re_im(cgrid *grid, INT i, INT j, INT k, REAL *re, REAL *im);
 
 /* ----------------------------------------------- fused step and reports */
 /* One predict-correct step exactly as the libdft dynamics examples write it
@@ -381,6 +460,31 @@ int dftgpu_adjoint_run(dft_ot_functional *otf, wf *gwf, rgrid *vext, double mu0,
 
 #ifndef __cplusplus
 #include <complex.h>
+#include <math.h>
+#include <stdlib.h>
+/* libgrid's math names for REAL = double, as libdft's drivers use them */
+#define SQRT(x) sqrt(x)
+#define EXP(x) exp(x)
+#define POW(x, y) pow(x, y)
+#define FABS(x) fabs(x)
+#define SIN(x) sin(x)
+#define COS(x) cos(x)
+#define TAN(x) tan(x)
+#define TANH(x) tanh(x)
+#define LOG(x) log(x)
+#define ACOS(x) acos(x)
+#define ASIN(x) asin(x)
+#define ATAN(x) atan(x)
+#define ATAN2(y, x) atan2(y, x)
+#define CEXP(x) cexp(x)
+#define CABS(x) cabs(x)
+#define CREAL(x) creal(x)
+#define CIMAG(x) cimag(x)
+#define CARG(x) carg(x)
+#define CONJ(x) conj(x)
+#define CSQRT(x) csqrt(x)
+#define ABS(x) labs(x)
+
 /* REAL complex forms of the libgrid / libdft entry points (C only). */
 void grid_wf_propagate(wf *gwf, cgrid *potential, REAL complex time);
 void grid_wf_propagate_predict(wf *gwf, wf *gwfp, cgrid *potential, REAL complex time);
@@ -391,6 +495,29 @@ void cgrid_multiply(cgrid *grid, REAL complex c);
 void cgrid_constant(cgrid *grid, REAL complex c);
 void cgrid_map(cgrid *grid, REAL complex (*func)(void *arg, REAL x, REAL y, REAL z), void *farg);
 void grid_wf_map(wf *gwf, REAL complex (*func)(void *arg, REAL x, REAL y, REAL z), void *farg);  /* src/helium-ot-bulk.c:331 */
+REAL complex cgrid_value_at_index(cgrid *grid, INT i, INT j, INT k);  /* src/helium-ot-bulk.c:353 */
+
+/* complex map callbacks of libdft (src/common.c, src/initial.c) */
+REAL complex dft_common_cgaussian(void *arg, REAL x, REAL y, REAL z);       /* src/common.c:235 (REAL *inv_width) */
+REAL complex dft_common_planewave(void *arg, REAL x, REAL y, REAL z);       /* src/common.c:1214 (dft_plane_wave *) */
+REAL complex dft_initial_vortex_x_n1(void *na, REAL x, REAL y, REAL z);     /* src/initial.c:31 */
+REAL complex dft_initial_vortex_y_n1(void *na, REAL x, REAL y, REAL z);     /* src/initial.c:51 */
+REAL complex dft_initial_vortex_z_n1(void *na, REAL x, REAL y, REAL z);     /* src/initial.c:71 */
+REAL complex dft_initial_vortex_x_n2(void *na, REAL x, REAL y, REAL z);     /* src/initial.c:91 */
+REAL complex dft_initial_vortex_y_n2(void *na, REAL x, REAL y, REAL z);     /* src/initial.c:112 */
+REAL complex dft_initial_vortex_z_n2(void *na, REAL x, REAL y, REAL z);     /* src/initial.c:133 */
+REAL complex dft_initial_bubble(void *prm, REAL x, REAL y, REAL z);         /* src/initial.c:154 (REAL *radius) */
+
+/* Drivers of libdft built on the entry points above (src/helium-ot-bulk.c):
+ * the period of a small density wave of wave vector k (rounded to the grid)
+ * propagated from the plane wave of amplitude amp, as an energy in hartree
+ * (k is updated to the value used; pred selects predict-correct steps; dir 0,
+ * 1, 2 = x, y, z) -- src/helium-ot-bulk.c:274; and the surface tension of a
+ * slab of the given width relaxed with time step ts -- src/helium-ot-bulk.c:486.
+ * Where the reference calls exit(1) (bad direction, one point along it),
+ * these record DFTGPU_ERR_ARG and return NAN. */
+REAL dft_ot_dispersion(wf *gwf, dft_ot_functional *otf, REAL ts, REAL *k, REAL amp, char pred, char dir);
+REAL dft_ot_bulk_surface_tension(wf *gwf, dft_ot_functional *otf, REAL ts, REAL width);
 #endif
 
 #ifdef __cplusplus

@@ -145,6 +145,17 @@ SIGNATURES = {
     "dftgpu_wf_propagate_vjp": (_i, [_vp, _vp, _d, _d, _vp, _vp, _vp, _vp, _vp]),
     "dftgpu_pc_step_vjp": (_i, [_vp, _vp, _vp, _d, _d, _d, _i, _vp, _vp]),
     "dftgpu_adjoint_run": (_i, [_vp, _vp, _vp, _d, _d, _d, _l, _i, _l, _vp, _dp, _vp, _vp]),
+    "dft_ot_bulk_chempot3": (_d, [_vp, _d]),
+    "dft_ot_bulk_istatic": (_d, [_vp, _dp, _d]),
+    "dft_ot_dispersion": (_d, [_vp, _vp, _d, _dp, _d, C.c_byte, C.c_byte]),
+    "dft_ot_bulk_surface_tension": (_d, [_vp, _vp, _d, _d]),
+    "cgrid_value_at_index_re_im": (_i, [_vp, _l, _l, _l, _dp, _dp]),
+    "rgrid_write_grid": (None, [C.c_char_p, _vp]),
+    "cgrid_write_grid": (None, [C.c_char_p, _vp]),
+    "rgrid_read_grid": (None, [_vp, C.c_char_p]),
+    "cgrid_read_grid": (None, [_vp, C.c_char_p]),
+    "dftgpu_grid_file_write": (_i, [C.c_char_p, _i, _l, _l, _l, _dp, _dp]),
+    "dftgpu_grid_file_read": (_i, [C.c_char_p, _i, _l, _l, _l, _dp, _dp]),
 }
 
 OPTIONAL = set()   # entry points allowed to be absent (none)

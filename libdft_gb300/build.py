@@ -20,8 +20,8 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libdftgpu.so")
 INCLUDE = os.path.join(ROOT, "include")
 
-CU_SOURCES = ["fft.cu", "grid.cu", "ot.cu", "api.cu", "adjoint.cu", "noalloc.cu"]
-C_SOURCES = ["compat.c"]
+CU_SOURCES = ["fft.cu", "grid.cu", "ot.cu", "api.cu", "adjoint.cu", "noalloc.cu", "drivers.cu"]
+C_SOURCES = ["compat.c", "maps.c"]
 
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
@@ -43,7 +43,8 @@ def _run(cmd):
 def build(verbose: bool = False, jobs: int | None = None) -> str:
     os.makedirs(BUILD, exist_ok=True)
     nv = nvcc()
-    common = [ARCH, "-O3", "-lineinfo", "-std=c++17", "--extended-lambda", "-Xcompiler", "-fPIC",
+    # host arithmetic without FMA contraction: the same results on x86 and Arm
+    common = [ARCH, "-O3", "-lineinfo", "-std=c++17", "--extended-lambda", "-Xcompiler", "-fPIC,-ffp-contract=off",
               "-I", INCLUDE, "-I", CSRC]
     if os.environ.get("DFTGPU_PTXAS_VERBOSE"):
         common += ["-Xptxas", "-v"]
@@ -59,7 +60,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
     cc = os.environ.get("CC", "gcc")
     for s in C_SOURCES:
         obj = os.path.join(BUILD, s.replace(".c", ".o"))
-        cmds.append([cc, "-O2", "-fPIC", "-std=gnu11", "-I", INCLUDE, "-c", os.path.join(CSRC, s), "-o", obj])
+        cmds.append([cc, "-O2", "-fPIC", "-ffp-contract=off", "-std=gnu11", "-I", INCLUDE, "-c", os.path.join(CSRC, s), "-o", obj])
         objs.append(obj)
     with cf.ThreadPoolExecutor(max_workers=jobs or min(8, os.cpu_count() or 4)) as ex:
         outs = list(ex.map(_run, cmds))

@@ -192,15 +192,40 @@ void rgrid_map(rgrid *g, rgrid_map_fn func, void *farg) {
   copy_values_in(g->prec, g->value, h.data(), h.size());
 }
 
+// n consecutive values of precision prec from element idx of a device grid,
+// read on the work stream after the work queued on it
+static int read_values(int prec, const void *dev, size_t idx, int n, double *out) {
+  if (prec == DFTGPU_FP32) {
+    float f[2];
+    DFT_CUDA(cudaMemcpyAsync(f, (const float *) dev + idx, n * sizeof(float), cudaMemcpyDeviceToHost, rt().stream));
+    DFT_CUDA(cudaStreamSynchronize(rt().stream));
+    for (int i = 0; i < n; i++) out[i] = f[i];
+  } else {
+    DFT_CUDA(cudaMemcpyAsync(out, (const double *) dev + idx, n * sizeof(double), cudaMemcpyDeviceToHost, rt().stream));
+    DFT_CUDA(cudaStreamSynchronize(rt().stream));
+  }
+  return DFTGPU_OK;
+}
+
+static size_t wrapped_index(INT nx, INT ny, INT nz, INT i, INT j, INT k) {
+  i = ((i % nx) + nx) % nx; j = ((j % ny) + ny) % ny; k = ((k % nz) + nz) % nz;
+  return ((size_t) i * ny + j) * nz + k;
+}
+
 REAL rgrid_value_at_index(rgrid *g, INT i, INT j, INT k) {
-  i = ((i % g->nx) + g->nx) % g->nx; j = ((j % g->ny) + g->ny) % g->ny; k = ((k % g->nz) + g->nz) % g->nz;
-  const size_t idx = ((size_t) i * g->ny + j) * g->nz + k;
+  if (!g) { bad_arg("rgrid_value_at_index: NULL grid"); return NAN; }
   double v = NAN;
-  if (g->prec == DFTGPU_FP32) {
-    float f;
-    if (cudaMemcpy(&f, (float *) g->value + idx, 4, cudaMemcpyDeviceToHost) == cudaSuccess) v = f;
-  } else cudaMemcpy(&v, (double *) g->value + idx, 8, cudaMemcpyDeviceToHost);
+  if (read_values(g->prec, g->value, wrapped_index(g->nx, g->ny, g->nz, i, j, k), 1, &v) != DFTGPU_OK) return NAN;
   return v;
+}
+
+int cgrid_value_at_index_re_im(cgrid *g, INT i, INT j, INT k, REAL *re, REAL *im) {
+  if (!g || !re || !im) return bad_arg("cgrid_value_at_index: NULL argument");
+  double v[2] = { NAN, NAN };
+  const int rc = read_values(g->prec, g->value, 2 * wrapped_index(g->nx, g->ny, g->nz, i, j, k), 2, v);
+  *re = v[0];
+  *im = v[1];
+  return rc;
 }
 
 int rgrid_copy_to_host(rgrid *g, double *host) { return copy_values_out(g->prec, g->value, host, gsize(g)); }
@@ -381,8 +406,15 @@ int dftgpu_wf_propagate_correct(wf *g, cgrid *pot, double dr, double di) { retur
 // 0 K OT parameters and unit conversions (src/ot.c:1026-1036, 1234-1270)
 void dft_ot_init_params(dft_ot_functional *otf, INT model) {
   const double a3 = GRID_AUTOANG * GRID_AUTOANG * GRID_AUTOANG;
-  otf->model = model;
-  otf->beta = otf->rhom = otf->C = 0.0;
+  /* as src/ot.c:1002-1012: the model field is the caller's (dft_ot_alloc sets
+   * it, src/ot.c:81); its high-density bits select the HD parameters */
+  if (otf->model & (DFT_OT_HD | DFT_OT_HD2)) {
+    otf->beta = (40.0 / (GRID_AUTOANG * GRID_AUTOANG * GRID_AUTOANG));
+    otf->rhom = (0.37 * GRID_AUTOANG * GRID_AUTOANG * GRID_AUTOANG);
+    otf->C = 0.1;
+  } else {
+    otf->beta = otf->rhom = otf->C = 0.0;
+  }
   otf->b = -718.99;
   otf->c2 = -2.411857E4;
   otf->c2_exp = 2.0;
@@ -403,7 +435,7 @@ void dft_ot_init_params(dft_ot_functional *otf, INT model) {
   otf->lj_params.sigma = 2.556 / GRID_AUTOANG;
   otf->lj_params.epsilon = 10.22 / GRID_AUTOK;
   otf->lj_params.cval = 0.0;
-  otf->rho_0s = 0.04 * a3;
+  otf->rho_0s = 0.04 * GRID_AUTOANG * GRID_AUTOANG * GRID_AUTOANG;   /* the product order of src/ot.c:1248 */
   otf->alpha_s = 54.31 / a3;
   otf->l_g = 1.0 / GRID_AUTOANG;
   otf->mass = 4.0026 / GRID_AUTOAMU;
@@ -428,6 +460,7 @@ dft_ot_functional *dft_ot_alloc(INT model, wf *gwf, INT min_substeps, INT max_su
   cgrid *c = gwf->grid;
   dft_ot_functional *otf = (dft_ot_functional *) calloc(1, sizeof(dft_ot_functional));
   if (!otf) return nullptr;
+  otf->model = model;
   dft_ot_init_params(otf, model);
   OtPriv *P = new OtPriv();
   P->prec = c->prec;
@@ -597,20 +630,47 @@ REAL dft_ot_bulk_chempot2(dft_ot_functional *o) { return dft_ot_bulk_dEdRho(o, o
 REAL dft_ot_bulk_compressibility(dft_ot_functional *o, REAL rho) { return 1.0 / (rho * dft_ot_bulk_dPdRho(o, rho)); }
 REAL dft_ot_bulk_sound_speed(dft_ot_functional *o, REAL rho) { return 1.0 / sqrt(o->mass * rho * dft_ot_bulk_compressibility(o, rho)); }
 
-REAL dft_ot_bulk_dispersion(dft_ot_functional *o, REAL *kp, REAL rho0) {
-  const double k = *kp;
-  if (rho0 < 0.0 || k < 1E-3) return 0.0;
+REAL dft_ot_bulk_chempot3(dft_ot_functional *o, REAL rho0) { return dft_ot_bulk_dEdRho(o, rho0); }
+
+// Fourier transform of the cored LJ potential at k, by the rectangle rule in
+// x = r / sigma from h / sigma to 1000 in steps of 0.01 (src/helium-ot-bulk.c:382-392)
+static double lj_transform(const dft_ot_functional *o, double k) {
   const double sg = o->lj_params.sigma, ks = k * sg;
   double lj = 0.0;
   for (double x = o->lj_params.h / sg; x < 1E3; x += 1.0E-2) lj += sin(ks * x) * (pow(x, -11.0) - pow(x, -5.0));
-  lj *= 1.0E-2 * 16.0 * M_PI * o->lj_params.epsilon * sg * sg * sg / ks;
+  return lj * (1.0E-2 * 16.0 * M_PI * o->lj_params.epsilon * sg * sg * sg / ks);
+}
+
+// kinetic term kin + rho V_LJ(k) + the correlation terms of the uniform
+// liquid, summed in this order (src/helium-ot-bulk.c:419-422, 456-459)
+static double response_terms(const dft_ot_functional *o, double kin, double k, double rho0) {
   const double kh = k * o->lj_params.h, pi = (3.0 / (kh * kh * kh)) * (sin(kh) - kh * cos(kh));
+  return kin + rho0 * lj_transform(o, k) + o->c2 * (2.0 * pi + pi * pi) * rho0 * rho0 +
+         2.0 * o->c3 * (pi + pi * pi) * rho0 * rho0 * rho0;
+}
+
+// the KC term with prefactor c: c alpha_s rho0 (1 - rho0/rho_0s)^2 exp(-k^2 l_g^2 / 4)
+static double kc_term(const dft_ot_functional *o, double c, double k, double rho0) {
+  const double f = 1.0 - rho0 / o->rho_0s;
+  return c * o->alpha_s * rho0 * f * f * exp(-k * k * o->l_g * o->l_g / 4.0);
+}
+
+REAL dft_ot_bulk_istatic(dft_ot_functional *o, REAL *kp, REAL rho0) {
+  if (rho0 < 0.0) return 0.0;
+  const double k = *kp;
+  if (k < 1E-2) return 1E-2;
+  double chi = response_terms(o, k * k / (4.0 * o->mass), k, rho0);
+  // src/helium-ot-bulk.c:462-463: the KC prefactor is hbar^2 / 2m (no k^2 here)
+  if (o->model & DFT_OT_KC) chi += kc_term(o, -(1.0 / (2.0 * o->mass)), k, rho0);
+  return chi;
+}
+
+REAL dft_ot_bulk_dispersion(dft_ot_functional *o, REAL *kp, REAL rho0) {
+  const double k = *kp;
+  if (rho0 < 0.0 || k < 1E-3) return 0.0;
   const double t = k * k / o->mass;
-  double chi = t / 4.0 + rho0 * lj + o->c2 * (2.0 * pi + pi * pi) * rho0 * rho0 + 2.0 * o->c3 * (pi + pi * pi) * rho0 * rho0 * rho0;
-  if (o->model & DFT_OT_KC) {
-    const double f = 1.0 - rho0 / o->rho_0s;
-    chi += -(t / 2.0) * o->alpha_s * rho0 * f * f * exp(-k * k * o->l_g * o->l_g / 4.0);
-  }
+  double chi = response_terms(o, t / 4.0, k, rho0);
+  if (o->model & DFT_OT_KC) chi += kc_term(o, -(t / 2.0), k, rho0);
   if (o->model & DFT_OT_BACKFLOW) {
     const dft_ot_bf &p = o->bf_params;
     auto vj = [&](double q) {

@@ -44,3 +44,10 @@ void cgrid_map(cgrid *grid, cmap_fn func, void *farg) {
 }
 
 void grid_wf_map(wf *gwf, cmap_fn func, void *farg) { cgrid_map(gwf->grid, func, farg); }
+
+/* cgrid_value_at_index (src/helium-ot-bulk.c:353); NAN + NAN i on error */
+REAL complex cgrid_value_at_index(cgrid *grid, INT i, INT j, INT k) {
+  REAL re = NAN, im = NAN;
+  cgrid_value_at_index_re_im(grid, i, j, k, &re, &im);
+  return re + I * im;
+}

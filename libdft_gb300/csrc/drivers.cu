@@ -1,0 +1,280 @@
+// Host-side parts of libdft's drivers around the time step: grid files
+// (rgrid_write_grid / cgrid_read_grid ...) and the two libdft drivers that
+// run the time step themselves, dft_ot_dispersion and
+// dft_ot_bulk_surface_tension (src/helium-ot-bulk.c:274-369, 486-518).  Both
+// drivers are written on the library's public entry points, so every step they
+// take is the GPU step the rest of the library provides.
+#include <math.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <string>
+#include <vector>
+
+#include "grid_internal.cuh"
+
+using namespace dftgpu;
+
+namespace {
+
+const char kMagic[8] = { 'D', 'F', 'T', 'G', 'P', 'U', 'G', '1' };
+
+struct File {
+  FILE *f;
+  explicit File(const std::string &path, const char *mode) : f(fopen(path.c_str(), mode)) {}
+  ~File() { if (f) fclose(f); }
+  int close() { int rc = f ? fclose(f) : 0; f = nullptr; return rc; }
+};
+
+// "coordinate value" lines along each axis through (nx/2, ny/2, nz/2)
+int write_cuts(const std::string &base, int cplx, const INT n[3], const double *meta, const double *v) {
+  static const char *ext[3] = { ".x", ".y", ".z" };
+  for (int a = 0; a < 3; a++) {
+    File out(base + ext[a], "w");
+    if (!out.f) { set_error(DFTGPU_ERR_IO, "grid file: cannot open %s%s", base.c_str(), ext[a]); return DFTGPU_ERR_IO; }
+    INT at[3] = { n[0] / 2, n[1] / 2, n[2] / 2 };
+    for (INT i = 0; i < n[a]; i++) {
+      at[a] = i;
+      const size_t idx = ((size_t) at[0] * n[1] + at[1]) * n[2] + at[2];
+      const double c = (double) (i - n[a] / 2) * meta[0] - meta[1 + a];
+      if (cplx) fprintf(out.f, "%le %le %le\n", c, v[2 * idx], v[2 * idx + 1]);
+      else fprintf(out.f, "%le %le\n", c, v[idx]);
+    }
+    if (out.close()) { set_error(DFTGPU_ERR_IO, "grid file: write error on %s%s", base.c_str(), ext[a]); return DFTGPU_ERR_IO; }
+  }
+  return DFTGPU_OK;
+}
+
+bool dims_ok(INT nx, INT ny, INT nz) { return nx > 0 && ny > 0 && nz > 0; }
+
+// A driver checks the error state of the void entry points it calls: it
+// sets a pending error aside on entry and puts it back on exit if the driver
+// itself recorded none.
+struct ErrorScope {
+  int saved;
+  ErrorScope() : saved(g_last_error) { g_last_error = 0; }
+  ~ErrorScope() { if (!g_last_error) g_last_error = saved; }
+};
+int pending_error() { return g_last_error; }
+
+}  // namespace
+
+extern "C" {
+
+int dftgpu_grid_file_write(const char *base, int is_complex, INT nx, INT ny, INT nz, const double *meta,
+                           const double *values) {
+  if (!base || !meta || !values || !dims_ok(nx, ny, nz)) {
+    set_error(DFTGPU_ERR_ARG, "dftgpu_grid_file_write: argument");
+    return DFTGPU_ERR_ARG;
+  }
+  const INT n[3] = { nx, ny, nz };
+  const size_t count = (size_t) nx * ny * nz * (is_complex ? 2 : 1);
+  {
+    File out(std::string(base) + ".grd", "wb");
+    if (!out.f) { set_error(DFTGPU_ERR_IO, "grid file: cannot open %s.grd", base); return DFTGPU_ERR_IO; }
+    const int64_t head[4] = { is_complex ? 1 : 0, (int64_t) nx, (int64_t) ny, (int64_t) nz };
+    bool ok = fwrite(kMagic, 1, 8, out.f) == 8 && fwrite(head, sizeof(int64_t), 4, out.f) == 4 &&
+              fwrite(meta, sizeof(double), 7, out.f) == 7 && fwrite(values, sizeof(double), count, out.f) == count;
+    ok = (out.close() == 0) && ok;
+    if (!ok) { set_error(DFTGPU_ERR_IO, "grid file: write error on %s.grd", base); return DFTGPU_ERR_IO; }
+  }
+  return write_cuts(base, is_complex, n, meta, values);
+}
+
+int dftgpu_grid_file_read(const char *base, int is_complex, INT nx, INT ny, INT nz, double *meta, double *values) {
+  if (!base || !meta || !values || !dims_ok(nx, ny, nz)) {
+    set_error(DFTGPU_ERR_ARG, "dftgpu_grid_file_read: argument");
+    return DFTGPU_ERR_ARG;
+  }
+  File in(std::string(base) + ".grd", "rb");
+  if (!in.f) { set_error(DFTGPU_ERR_IO, "grid file: cannot open %s.grd", base); return DFTGPU_ERR_IO; }
+  char magic[8];
+  int64_t head[4];
+  if (fread(magic, 1, 8, in.f) != 8 || memcmp(magic, kMagic, 8) != 0) {
+    set_error(DFTGPU_ERR_UNSUPPORTED, "grid file: %s.grd is not in this library's grid layout", base);
+    return DFTGPU_ERR_UNSUPPORTED;
+  }
+  if (fread(head, sizeof(int64_t), 4, in.f) != 4) { set_error(DFTGPU_ERR_IO, "grid file: %s.grd truncated", base); return DFTGPU_ERR_IO; }
+  if (head[0] != (is_complex ? 1 : 0)) {
+    set_error(DFTGPU_ERR_ARG, "grid file: %s.grd holds a %s grid", base, head[0] ? "complex" : "real");
+    return DFTGPU_ERR_ARG;
+  }
+  if (head[1] != nx || head[2] != ny || head[3] != nz) {
+    set_error(DFTGPU_ERR_SIZE, "grid file: %s.grd is %lldx%lldx%lld, the grid %ldx%ldx%ld", base, (long long) head[1],
+              (long long) head[2], (long long) head[3], (long) nx, (long) ny, (long) nz);
+    return DFTGPU_ERR_SIZE;
+  }
+  const size_t count = (size_t) nx * ny * nz * (is_complex ? 2 : 1);
+  if (fread(meta, sizeof(double), 7, in.f) != 7 || fread(values, sizeof(double), count, in.f) != count) {
+    set_error(DFTGPU_ERR_IO, "grid file: %s.grd truncated", base);
+    return DFTGPU_ERR_IO;
+  }
+  return DFTGPU_OK;
+}
+
+void rgrid_write_grid(char *base, rgrid *g) {
+  if (!g) { set_error(DFTGPU_ERR_ARG, "rgrid_write_grid: NULL grid"); return; }
+  std::vector<double> h(gsize(g));
+  if (rgrid_copy_to_host(g, h.data()) != DFTGPU_OK) return;
+  const double meta[7] = { g->step, g->x0, g->y0, g->z0, 0.0, 0.0, 0.0 };
+  dftgpu_grid_file_write(base, 0, g->nx, g->ny, g->nz, meta, h.data());
+}
+
+void cgrid_write_grid(char *base, cgrid *g) {
+  if (!g) { set_error(DFTGPU_ERR_ARG, "cgrid_write_grid: NULL grid"); return; }
+  std::vector<double> h(2 * gsize(g));
+  if (cgrid_copy_to_host(g, h.data()) != DFTGPU_OK) return;
+  const double meta[7] = { g->step, g->x0, g->y0, g->z0, g->kx0, g->ky0, g->kz0 };
+  dftgpu_grid_file_write(base, 1, g->nx, g->ny, g->nz, meta, h.data());
+}
+
+void rgrid_read_grid(rgrid *g, char *base) {
+  if (!g) { set_error(DFTGPU_ERR_ARG, "rgrid_read_grid: NULL grid"); return; }
+  std::vector<double> h(gsize(g));
+  double meta[7];
+  if (dftgpu_grid_file_read(base, 0, g->nx, g->ny, g->nz, meta, h.data()) != DFTGPU_OK) return;
+  if (rgrid_copy_from_host(g, h.data()) != DFTGPU_OK) return;
+  rgrid_set_origin(g, meta[1], meta[2], meta[3]);
+}
+
+void cgrid_read_grid(cgrid *g, char *base) {
+  if (!g) { set_error(DFTGPU_ERR_ARG, "cgrid_read_grid: NULL grid"); return; }
+  std::vector<double> h(2 * gsize(g));
+  double meta[7];
+  if (dftgpu_grid_file_read(base, 1, g->nx, g->ny, g->nz, meta, h.data()) != DFTGPU_OK) return;
+  if (cgrid_copy_from_host(g, h.data()) != DFTGPU_OK) return;
+  g->x0 = meta[1]; g->y0 = meta[2]; g->z0 = meta[3];
+  cgrid_set_momentum(g, meta[4], meta[5], meta[6]);
+}
+
+// ------------------------------------------------------------ drivers
+
+// sqrt(rho) (1 + a cos(k.r)) as a (re, im) map (dft_common_planewave)
+static void plane_wave_map(void *arg, REAL x, REAL y, REAL z, REAL *re, REAL *im) {
+  const dft_plane_wave *p = (const dft_plane_wave *) arg;
+  const REAL amp = sqrt(p->rho);
+  *re = amp + p->a * amp * cos(p->kx * x + p->ky * y + p->kz * z);
+  *im = 0.0;
+}
+
+// Steps until the density at the grid centre has swung through half a period
+// of the density wave (src/helium-ot-bulk.c:333-355).  libdft loops without
+// limit; this stops after kMaxSteps (1e6) with DFTGPU_ERR_NONFINITE.
+REAL dft_ot_dispersion(wf *gwf, dft_ot_functional *otf, REAL ts, REAL *k, REAL amp, char pred, char dir) {
+  const long kMaxSteps = 1000000;
+  ErrorScope errors;
+  if (!gwf || !otf || !k) { set_error(DFTGPU_ERR_ARG, "dft_ot_dispersion: NULL argument"); return NAN; }
+  cgrid *g = gwf->grid;
+  const INT n[3] = { g->nx, g->ny, g->nz };
+  if (dir < 0 || dir > 2 || n[(int) dir] == 1) {
+    set_error(DFTGPU_ERR_ARG, "dft_ot_dispersion: direction %d is not 0, 1 or 2 with more than one point", (int) dir);
+    return NAN;
+  }
+  // the wave vector rounded to the grid (src/helium-ot-bulk.c:290-324)
+  const REAL dk = 2.0 * M_PI / (((REAL) n[(int) dir]) * g->step);
+  dft_plane_wave wave = { 0.0, 0.0, 0.0, amp, otf->rho0 };
+  const REAL kk = ((REAL) ((INT) (0.5 + *k / dk))) * dk;
+  *k = kk;
+  if (kk == 0.0) return 0.0;
+  (&wave.kx)[(int) dir] = kk;
+
+  const REAL rho0 = otf->rho0, mu0 = dft_ot_bulk_chempot2(otf);
+  wf *gwfp = pred ? grid_wf_clone(gwf, (char *) "gwfp for dft_ot_dispersion") : nullptr;
+  cgrid *pot = cgrid_clone(g, (char *) "potential for dft_ot_dispersion");
+  REAL omega = NAN;
+  if ((pred && !gwfp) || !pot) goto done;
+  cgrid_map_re_im(g, plane_wave_map, &wave);
+  {
+    REAL ival = 0.0;
+    long l;
+    grid_timer timer;
+    for (l = 0; l < kMaxSteps; l++) {
+      grid_timer_start(&timer);
+      cgrid_zero(pot);
+      if (pred) {
+        cgrid_copy(gwfp->grid, g);
+        dft_ot_potential(otf, pot, gwf);
+        cgrid_add_re_im(pot, -mu0, 0.0);
+        dftgpu_wf_propagate_predict(gwf, gwfp, pot, ts, 0.0);
+        dft_ot_potential(otf, pot, gwfp);
+        cgrid_add_re_im(pot, -mu0, 0.0);
+        cgrid_multiply_re_im(pot, 0.5, 0.0);
+        dftgpu_wf_propagate_correct(gwf, pot, ts, 0.0);
+      } else {
+        dft_ot_potential(otf, pot, gwf);
+        dftgpu_wf_propagate(gwf, pot, ts, 0.0);
+      }
+      REAL re, im;
+      if (cgrid_value_at_index_re_im(g, n[0] / 2, n[1] / 2, n[2] / 2, &re, &im) != DFTGPU_OK || pending_error()) goto done;
+      fprintf(stderr, "Iteration %ld - Wall clock time = %le seconds.\n", l, grid_timer_wall_clock_time(&timer));
+      ival += pow(hypot(re, im), 2.0) - rho0;
+      if (!(ival == ival)) { set_error(DFTGPU_ERR_NONFINITE, "dft_ot_dispersion: density at the centre is not finite"); goto done; }
+      if (ival < 0.0) {
+        l--;
+        break;
+      }
+    }
+    if (l >= kMaxSteps) {
+      set_error(DFTGPU_ERR_NONFINITE, "dft_ot_dispersion: no half period within %ld steps", kMaxSteps);
+      goto done;
+    }
+    // src/helium-ot-bulk.c:357-360: 1 / (2 l ts), in K via cm^-1, back to hartree
+    const REAL ts_fs = ts * GRID_AUTOFS;
+    const REAL w = (1.0 / (2.0 * ((REAL) l) * ts_fs / GRID_AUTOFS));
+    omega = (w / GRID_AUTOS) * GRID_HZTOCM1 * 1.439 / GRID_AUTOK;
+  }
+done:
+  if (pot) cgrid_free(pot);
+  if (gwfp) grid_wf_free(gwfp);
+  return omega;
+}
+
+// 1 inside the slab |x| < width / 2, 0 outside (src/helium-ot-bulk.c:471-477)
+static void slab_map(void *arg, REAL x, REAL y, REAL z, REAL *re, REAL *im) {
+  (void) y; (void) z;
+  *re = fabs(x) < *(const REAL *) arg / 2.0 ? 1.0 : 0.0;
+  *im = 0.0;
+}
+
+// Relax a slab of liquid with time step ts until the energy per surface area
+// of its two faces changes by less than 3 % between steps (src/helium-ot-bulk.c:486-518).
+// The slab's width is passed to the map; libdft passes NULL there
+// (src/helium-ot-bulk.c:499), which would read through a null pointer.
+REAL dft_ot_bulk_surface_tension(wf *gwf, dft_ot_functional *otf, REAL ts, REAL width) {
+  const long kMaxSteps = 1000000;
+  ErrorScope errors;
+  if (!gwf || !otf || !otf->density) { set_error(DFTGPU_ERR_ARG, "dft_ot_bulk_surface_tension: NULL argument"); return NAN; }
+  cgrid *g = gwf->grid;
+  const REAL rho0 = otf->rho0, step = g->step, mu0 = dft_ot_bulk_chempot2(otf);
+  cgrid *pot = cgrid_clone(g, (char *) "Surface tension potential");
+  rgrid *density = rgrid_clone(otf->density, (char *) "Surface tension density");
+  REAL stens = NAN;
+  if (pot && density) {
+    cgrid_map_re_im(g, slab_map, &width);
+    cgrid_multiply_re_im(g, sqrt(rho0), 0.0);
+    REAL prev = 1E11;
+    long i;
+    for (i = 1; i <= kMaxSteps; i++) {
+      cgrid_zero(pot);
+      dft_ot_potential(otf, pot, gwf);
+      cgrid_add_re_im(pot, -mu0, 0.0);
+      dftgpu_wf_propagate(gwf, pot, ts, 0.0);
+      dft_ot_energy_density(otf, density, gwf);
+      const REAL e = grid_wf_energy(gwf, nullptr) + rgrid_integral(density);
+      if (pending_error()) { stens = NAN; break; }
+      stens = e / (2.0 * ((REAL) g->ny) * ((REAL) g->nz) * step * step);
+      if (fabs(stens - prev) / stens < 0.03) break;
+      prev = stens;
+    }
+    if (i > kMaxSteps) {
+      set_error(DFTGPU_ERR_NONFINITE, "dft_ot_bulk_surface_tension: not converged within %ld steps", kMaxSteps);
+      stens = NAN;
+    }
+  }
+  if (pot) cgrid_free(pot);
+  if (density) rgrid_free(density);
+  return stens;
+}
+
+}  // extern "C"

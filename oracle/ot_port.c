@@ -70,8 +70,15 @@ REAL complex dft_common_planewave(void *arg, REAL x, REAL y, REAL z) {
  * atomic-unit conversions (src/ot.c:1234-1270). */
 void dft_ot_init_params(dft_ot_functional *otf, INT model) {
   REAL a3 = GRID_AUTOANG * GRID_AUTOANG * GRID_AUTOANG;
-  otf->model = model;
-  otf->beta = otf->rhom = otf->C = 0.0;
+  /* as src/ot.c:1002-1012: the model field is the caller's (dft_ot_alloc sets
+   * it, src/ot.c:81); its high-density bits select the HD parameters */
+  if (otf->model & (DFT_OT_HD | DFT_OT_HD2)) {
+    otf->beta = (40.0 / (GRID_AUTOANG * GRID_AUTOANG * GRID_AUTOANG));
+    otf->rhom = (0.37 * GRID_AUTOANG * GRID_AUTOANG * GRID_AUTOANG);
+    otf->C = 0.1;
+  } else {
+    otf->beta = otf->rhom = otf->C = 0.0;
+  }
   otf->b = -718.99;
   otf->c2 = -2.411857E4;
   otf->c2_exp = 2.0;
@@ -93,7 +100,7 @@ void dft_ot_init_params(dft_ot_functional *otf, INT model) {
   otf->lj_params.sigma = 2.556 / GRID_AUTOANG;
   otf->lj_params.epsilon = 10.22 / GRID_AUTOK;
   otf->lj_params.cval = 0.0;
-  otf->rho_0s = 0.04 * a3;
+  otf->rho_0s = 0.04 * GRID_AUTOANG * GRID_AUTOANG * GRID_AUTOANG;   /* the product order of src/ot.c:1248 */
   otf->alpha_s = 54.31 / a3;
   otf->l_g = 1.0 / GRID_AUTOANG;
   otf->mass = 4.0026 / GRID_AUTOAMU;
@@ -178,6 +185,7 @@ dft_ot_functional *dft_ot_alloc(INT model, wf *gwf, INT min_ns, INT max_ns) {
   }
   dft_ot_functional *otf = (dft_ot_functional *) calloc(1, sizeof(dft_ot_functional));
   if (!otf) return NULL;
+  otf->model = model;
   dft_ot_init_params(otf, model);
 
   /* LJ kernel, rescaled so that its integral is b (src/ot.c:150-161) */

@@ -1,0 +1,213 @@
+"""CPU: what libdft's example drivers need around the time step.
+
+* The map callbacks of libdft's src/common.c and src/initial.c exported by
+  libdftgpu give the same bits as libdft's own build of those files (the
+  reference-built oracle), on a lattice of points and on the core radii.
+* The host-only bulk relations added for the drivers (dft_ot_bulk_istatic,
+  dft_ot_bulk_chempot3) and the semi-analytic dispersion agree with libdft's
+  own build for the three provided models.
+* libdft's example drivers compile UNMODIFIED against include/ (their own
+  #include <grid/grid.h> ... lines) and link against libdftgpu.so.
+* The grid-file layout round-trips and is refused when foreign, truncated or
+  of another shape.
+
+The comparisons with libdft's own code need the reference tree and are
+skipped where it is absent.  No GPU is used.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+from oracle import REF_LIB, Grids, Oracle, ref_available
+
+LIBDIR = os.path.join(ROOT, "libdft_gb300")
+LIB = os.path.join(LIBDIR, "libdftgpu.so")
+INCLUDE = os.path.join(ROOT, "include")
+REF_EXAMPLES = "/root/reference/examples"
+
+needs_ref = pytest.mark.skipif(not ref_available(), reason="reference tree not present")
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not os.path.exists(LIB):
+        from libdft_gb300.build import build
+        build()
+    return C.CDLL(LIB)
+
+
+@pytest.fixture(scope="module")
+def ref():
+    return Oracle("ref")
+
+
+@needs_ref
+def test_map_callbacks_bit_identical_to_libdft(lib, ref, tmp_path):
+    exe = tmp_path / "callback_parity"
+    subprocess.run(["gcc", "-std=gnu11", "-O2", os.path.join(ROOT, "tests", "c", "callback_parity.c"),
+                    "-o", str(exe), "-ldl", "-lm"], check=True)
+    r = subprocess.run([str(exe), LIB, REF_LIB], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "0 differ" in r.stdout and int(r.stdout.split()[1]) > 50000
+
+
+def ot_params(lib, model):
+    import libdft_gb300 as G
+    p = G.OTParams()
+    p.model = model          # dft_ot_alloc sets the model before the parameters (src/ot.c:81,91)
+    lib.dft_ot_init_params.argtypes = [C.c_void_p, C.c_long]
+    lib.dft_ot_init_params(C.byref(p), model)
+    return p
+
+
+@needs_ref
+@pytest.mark.parametrize("model", [0, 1, 8, 9])
+def test_functional_parameters_bit_identical_to_libdft(lib, ref, model):
+    """dft_ot_init_params: every public parameter in atomic units equals the
+    value libdft's own conversion gives (src/ot.c:1002-1270)."""
+    from oracle import PARAM_NAMES
+    p = ot_params(lib, model)
+    with Grids(ref, (8, 8, 8), 1.0, 4.002602 / ref.AUTOAMU) as g:
+        w = g.wf()
+        o = g.ot(model, w)
+        out = np.zeros(len(PARAM_NAMES))
+        ref.lib.orc_ot_params(C.c_void_p(o), out.ctypes.data_as(C.POINTER(C.c_double)))
+    for n, v in zip(PARAM_NAMES, out):
+        assert getattr(p, n) == v, (n, getattr(p, n), v)
+
+
+@needs_ref
+@pytest.mark.parametrize("model", [0, 1, 9])
+def test_bulk_response_matches_libdft(lib, ref, model):
+    p = ot_params(lib, model)
+    R = ref.lib
+    for name in ("dft_ot_bulk_istatic", "dft_ot_bulk_dispersion"):
+        for L in (lib, R):
+            getattr(L, name).restype = C.c_double
+            getattr(L, name).argtypes = [C.c_void_p, C.POINTER(C.c_double), C.c_double]
+    for L in (lib, R):
+        L.dft_ot_bulk_chempot3.restype = C.c_double
+        L.dft_ot_bulk_chempot3.argtypes = [C.c_void_p, C.c_double]
+    with Grids(ref, (8, 8, 8), 1.0, 4.002602 / ref.AUTOAMU) as g:
+        w = g.wf()
+        o = g.ot(model, w)
+        rho0 = p.rho0
+        for k in (0.005, 0.05, 0.3, 1.0, 1.9):
+            for name in ("dft_ot_bulk_istatic", "dft_ot_bulk_dispersion"):
+                ka, kb = C.c_double(k), C.c_double(k)
+                a = getattr(lib, name)(C.byref(p), C.byref(ka), rho0)
+                b = getattr(R, name)(o, C.byref(kb), rho0)
+                assert a == b, (name, model, k, a, b)
+        for rho in (0.5 * rho0, rho0, 1.5 * rho0):
+            assert lib.dft_ot_bulk_chempot3(C.byref(p), rho) == R.dft_ot_bulk_chempot3(o, rho)
+
+
+# libdft example drivers that build against this library as they are
+# (the others use libgrid internals -- wf->cworkspace, otf->workspace1 -- or
+# libgrid functions outside the time step; the design notes list them)
+DRIVERS = ["imag_time/imag_time.c", "dynamics/dynamics.c", "dispersion/dispersion.c",
+           "dispersion/dispersion2.c", "dispersion/dispersion3.c", "dispersion/static-resp.c",
+           "bulk/bulk_properties.c"]
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_EXAMPLES), reason="reference tree not present")
+@pytest.mark.parametrize("driver", DRIVERS)
+def test_libdft_driver_builds_unmodified(lib, tmp_path, driver):
+    src = os.path.join(REF_EXAMPLES, driver)
+    exe = tmp_path / "driver"
+    r = subprocess.run(["gcc", "-std=gnu11", "-O2", "-w", "-I", os.path.dirname(src), "-I", INCLUDE, src,
+                        "-o", str(exe), "-L", LIBDIR, "-ldftgpu", "-lm", "-Wl,-rpath," + LIBDIR],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+
+
+HOST_DRIVERS = ["dispersion/dispersion3.c", "dispersion/static-resp.c"]
+
+
+@needs_ref
+@pytest.mark.parametrize("driver", HOST_DRIVERS)
+def test_host_only_driver_output_identical_to_libdft(lib, ref, tmp_path, driver):
+    """Drivers that need no grid (bulk relations of a functional on the stack)
+    built twice from the same unmodified source -- against this library and
+    against libdft's own build -- print the same bytes.  Both leave
+    otf.model to the caller, who does not set it, so the stack is
+    zero-initialised in both builds to make that read defined."""
+    src = os.path.join(REF_EXAMPLES, driver)
+    inc = tmp_path / "inc"
+    inc.mkdir()
+    os.symlink(os.path.join(os.path.dirname(REF_EXAMPLES), "src"), inc / "dft")
+    os.symlink(os.path.join(ROOT, "oracle", "include", "grid"), inc / "grid")
+    flags = ["gcc", "-std=gnu11", "-O2", "-w", "-ftrivial-auto-var-init=zero"]
+    builds = {
+        "gpu": flags + ["-I", INCLUDE, src, "-o", str(tmp_path / "gpu"), "-L", LIBDIR, "-ldftgpu", "-lm",
+                        "-Wl,-rpath," + LIBDIR],
+        "ref": flags + ["-fgnu89-inline", "-I", str(inc), "-I", os.path.join(os.path.dirname(REF_LIB), "gen"),
+                        src, "-o", str(tmp_path / "ref"), REF_LIB, "-lm", "-fopenmp",
+                        "-Wl,-rpath," + os.path.dirname(REF_LIB)],
+    }
+    out = {}
+    for name, cmd in builds.items():
+        subprocess.run(cmd, check=True)
+        r = subprocess.run([str(tmp_path / name)], capture_output=True, text=True, timeout=300)
+        assert r.returncode == 0, r.stderr[-2000:]
+        out[name] = r.stdout
+    assert out["gpu"] == out["ref"]
+    assert len(out["gpu"].splitlines()) > 50
+
+
+def file_api(lib):
+    lib.dftgpu_grid_file_write.argtypes = [C.c_char_p, C.c_int, C.c_long, C.c_long, C.c_long,
+                                           C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    lib.dftgpu_grid_file_read.argtypes = lib.dftgpu_grid_file_write.argtypes
+    return lib.dftgpu_grid_file_write, lib.dftgpu_grid_file_read
+
+
+def dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+@pytest.mark.parametrize("is_complex", [0, 1])
+def test_grid_file_round_trip_and_cuts(lib, tmp_path, is_complex):
+    write, read = file_api(lib)
+    shape = (6, 4, 10)
+    rng = np.random.default_rng(3)
+    v = rng.standard_normal(shape + ((2,) if is_complex else ()))
+    meta = np.array([0.8, 0.1, -0.2, 0.3, 0.01, 0.02, -0.03])
+    base = str(tmp_path / "wf-output-7").encode()
+    assert write(base, is_complex, *shape, dp(meta), dp(v)) == 0
+    got, gmeta = np.zeros_like(v), np.zeros(7)
+    assert read(base, is_complex, *shape, dp(gmeta), dp(got)) == 0
+    assert np.array_equal(got, v) and np.array_equal(gmeta, meta)
+    # the .x / .y / .z cuts through (nx/2, ny/2, nz/2): coordinate, value(s)
+    c = [n // 2 for n in shape]
+    for a, ext in enumerate("xyz"):
+        rows = np.loadtxt(str(tmp_path / ("wf-output-7." + ext)))
+        idx = list(c)
+        idx[a] = slice(None)
+        want = v[tuple(idx)].reshape(shape[a], -1)
+        coord = (np.arange(shape[a]) - shape[a] // 2) * meta[0] - meta[1 + a]
+        assert np.allclose(rows[:, 0], coord, rtol=1e-6, atol=1e-12)
+        assert np.allclose(rows[:, 1:], want, rtol=1e-6, atol=1e-12)
+
+
+def test_grid_file_refusals(lib, tmp_path):
+    write, read = file_api(lib)
+    lib.dftgpu_last_error.restype = C.c_int
+    shape = (4, 4, 4)
+    v, meta = np.ones(shape), np.array([1.0, 0, 0, 0, 0, 0, 0])
+    base = str(tmp_path / "g").encode()
+    assert write(base, 0, *shape, dp(meta), dp(v)) == 0
+    out, m = np.zeros(shape), np.zeros(7)
+    assert read(base, 0, 4, 4, 6, dp(m), dp(np.zeros((4, 4, 6)))) == 2     # DFTGPU_ERR_SIZE
+    assert read(base, 1, *shape, dp(m), dp(np.zeros(shape + (2,)))) == 1   # DFTGPU_ERR_ARG: real file
+    assert read(str(tmp_path / "missing").encode(), 0, *shape, dp(m), dp(out)) == 8   # DFTGPU_ERR_IO
+    raw = open(tmp_path / "g.grd", "rb").read()
+    open(tmp_path / "t.grd", "wb").write(raw[:-8])
+    assert read(str(tmp_path / "t").encode(), 0, *shape, dp(m), dp(out)) == 8         # truncated
+    open(tmp_path / "f.grd", "wb").write(b"\0" * len(raw))
+    assert read(str(tmp_path / "f").encode(), 0, *shape, dp(m), dp(out)) == 6         # DFTGPU_ERR_UNSUPPORTED
+    assert lib.dftgpu_last_error() == 6
