@@ -354,6 +354,34 @@ typedef struct {      /* src/dft.h:55-60 */
   REAL rho;           /* background density */
 } dft_plane_wave;
 
+/* 1-D potential tables read from "r value" text files (src/dft.h:16-54):
+ * equidistant r from begin in steps of step, length values. */
+#define DFT_MAX_POTENTIAL_POINTS 8192
+typedef struct extpot {
+  REAL points[DFT_MAX_POTENTIAL_POINTS];
+  REAL begin;
+  INT length;
+  REAL step;
+} dft_extpot;
+/* tables along x, y, z, averaging mode (0 none, 1 xy, 2 yz, 3 xz, 4 all),
+ * orientation (theta0, phi0) and origin of the mapped potential */
+typedef struct extpot_set {
+  dft_extpot *x, *y, *z;
+  char average;
+  REAL theta0, phi0;
+  REAL x0, y0, z0;
+} dft_extpot_set;
+/* Read a table (src/common.c:541-576).  Where libdft exits, this records
+ * DFTGPU_ERR_IO (file not readable) or DFTGPU_ERR_ARG (distances decreasing or
+ * not equidistant) and leaves the table as read so far. */
+void dft_common_read_pot(char *file, dft_extpot *pot);
+/* rgrid_map callback of a dft_extpot_set (src/common.c:588-668). */
+REAL dft_common_extpot(void *arg, REAL x, REAL y, REAL z);
+/* Read the three tables and map them onto potential (src/common.c:689-709);
+ * nothing is mapped if a table cannot be read. */
+void dft_common_potential_map(char average, char *filex, char *filey, char *filez, rgrid *potential, REAL theta0,
+                              REAL phi0, REAL x0, REAL y0, REAL z0);
+
 /* Wall-clock and CPU timer (examples/imag_time/imag_time.c:228,242). */
 typedef struct grid_timer_struct {
   double wall0, cpu0;

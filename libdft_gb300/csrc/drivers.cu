@@ -148,6 +148,88 @@ void cgrid_read_grid(cgrid *g, char *base) {
   cgrid_set_momentum(g, meta[4], meta[5], meta[6]);
 }
 
+// ------------------------------------------------------------ potentials from files
+
+// Table of "r value" pairs, equidistant in r (src/common.c:541-576): the
+// first two distances fix begin and step; a later distance more than step/10
+// off its place is refused.
+static int read_pot(const char *file, dft_extpot *pot) {
+  if (!file || !pot) { set_error(DFTGPU_ERR_ARG, "dft_common_read_pot: NULL argument"); return DFTGPU_ERR_ARG; }
+  File in(file, "r");
+  if (!in.f) { set_error(DFTGPU_ERR_IO, "dft_common_read_pot: cannot open %s", file); return DFTGPU_ERR_IO; }
+  double begin = 0.0, step = 0.0, r = 0.0, prev;
+  INT n;
+  int rc = DFTGPU_OK;
+  for (n = 0; n < DFT_MAX_POTENTIAL_POINTS; n++) {
+    prev = r;
+    if (fscanf(in.f, " %le %le", &r, &pot->points[n]) != 2) break;
+    if (n == 0) {
+      begin = r;
+    } else if (n == 1) {
+      step = r - begin;
+      if (step < 0.0) { rc = DFTGPU_ERR_ARG; set_error(rc, "dft_common_read_pot: %s: distances decrease", file); break; }
+    } else if (fabs(r - prev - step) > step / 10.0) {
+      rc = DFTGPU_ERR_ARG;
+      set_error(rc, "dft_common_read_pot: %s: distances not equidistant at line %ld", file, (long) n + 1);
+      break;
+    }
+  }
+  pot->begin = begin;
+  pot->length = n;
+  pot->step = step;
+  return rc;
+}
+
+// value of one table at distance r: the entry below r, the first entry
+// inside the table's start, 0 beyond its end (src/common.c:606-631)
+static double table_at(const dft_extpot *t, double r) {
+  const INT i = (INT) ((r - t->begin) / t->step);
+  if (i < 0) return t->points[0];
+  if (i > t->length - 1) return 0.0;
+  return t->points[i];
+}
+
+// The three tables combined by direction: sin^2(theta) (cos^2(phi) V_x +
+// sin^2(phi) V_y) + cos^2(theta) V_z about the rotated axes, or their
+// averages (src/common.c:633-660)
+static double extpot(const dft_extpot_set *set, double x, double y, double z) {
+  x -= set->x0;
+  y -= set->y0;
+  z -= set->z0;
+  const double r = sqrt(x * x + y * y + z * z);
+  double px = table_at(set->x, r), py = table_at(set->y, r), pz = table_at(set->z, r), tmp;
+  switch (set->average) {
+    case 1: tmp = (px + py) / 2.0; px = py = tmp; break;
+    case 2: tmp = (py + pz) / 2.0; py = pz = tmp; break;
+    case 3: tmp = (px + pz) / 2.0; px = pz = tmp; break;
+    case 4: return (px + py + pz) / 3.0;
+    default: break;
+  }
+  const double theta = acos(z / (r + 1E-3)) - set->theta0, phi = atan(y / (x + 1E-3)) - set->phi0;
+  double st = sin(theta), ct = cos(theta), sp = sin(phi), cp = cos(phi);
+  st *= st; ct *= ct; sp *= sp; cp *= cp;
+  return px * st * cp + py * st * sp + pz * ct;
+}
+
+void dft_common_read_pot(char *file, dft_extpot *pot) { read_pot(file, pot); }
+
+REAL dft_common_extpot(void *arg, REAL x, REAL y, REAL z) { return extpot((const dft_extpot_set *) arg, x, y, z); }
+
+void dft_common_potential_map(char average, char *filex, char *filey, char *filez, rgrid *potential, REAL theta0,
+                              REAL phi0, REAL x0, REAL y0, REAL z0) {
+  if (!potential) { set_error(DFTGPU_ERR_ARG, "dft_common_potential_map: NULL grid"); return; }
+  std::vector<dft_extpot> t(3);
+  dft_extpot_set set = { &t[0], &t[1], &t[2], average, theta0, phi0, x0, y0, z0 };
+  fprintf(stderr, "libdft: Mapping potential file with x = %s, y = %s, z = %s. Average = %d - ", filex ? filex : "",
+          filey ? filey : "", filez ? filez : "", (int) average);
+  if (read_pot(filex, set.x) || read_pot(filey, set.y) || read_pot(filez, set.z)) {
+    fprintf(stderr, "not mapped.\n");
+    return;
+  }
+  rgrid_map(potential, dft_common_extpot, &set);
+  fprintf(stderr, "done.\n");
+}
+
 // ------------------------------------------------------------ drivers
 
 // sqrt(rho) (1 + a cos(k.r)) as a (re, im) map (dft_common_planewave)

@@ -125,6 +125,109 @@ def test_libdft_driver_builds_unmodified(lib, tmp_path, driver):
     assert r.returncode == 0, r.stderr[-3000:]
 
 
+class ExtPot(C.Structure):
+    """dft_extpot (libdft src/dft.h:32-37; include/dftgpu.h)"""
+    _fields_ = [("points", C.c_double * 8192), ("begin", C.c_double), ("length", C.c_long), ("step", C.c_double)]
+
+
+class ExtPotSet(C.Structure):
+    _fields_ = [("x", C.POINTER(ExtPot)), ("y", C.POINTER(ExtPot)), ("z", C.POINTER(ExtPot)), ("average", C.c_char),
+                ("theta0", C.c_double), ("phi0", C.c_double), ("x0", C.c_double), ("y0", C.c_double),
+                ("z0", C.c_double)]
+
+
+def pot_file(path, begin, step, n, seed, jitter=0.0):
+    rng = np.random.default_rng(seed)
+    r = begin + step * np.arange(n) + jitter * rng.standard_normal(n)
+    v = 1e-3 * np.exp(-r / 3.0) * (1 + 0.1 * rng.standard_normal(n))
+    with open(path, "w") as f:
+        for a, b in zip(r, v):
+            f.write("%.9g %.9g\n" % (a, b))
+    return str(path).encode()
+
+
+@needs_ref
+def test_potential_tables_and_map_callback_bit_identical_to_libdft(lib, ref, tmp_path):
+    """dft_common_read_pot and the dft_common_extpot map of
+    dft_common_potential_map (src/common.c:541-709) against libdft's build,
+    for the five averaging modes, with and without rotation and shift."""
+    files = [pot_file(tmp_path / ("p%d.dat" % i), b, s, n, i)
+             for i, (b, s, n) in enumerate([(1.0, 0.05, 400), (0.5, 0.1, 150), (2.0, 0.02, 2049)])]
+    tabs = {}
+    for name, L in (("gpu", lib), ("ref", ref.lib)):
+        L.dft_common_read_pot.argtypes = [C.c_char_p, C.POINTER(ExtPot)]
+        L.dft_common_extpot.restype = C.c_double
+        L.dft_common_extpot.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_double]
+        tabs[name] = [ExtPot() for _ in files]
+        for f, t in zip(files, tabs[name]):
+            L.dft_common_read_pot(f, C.byref(t))
+    for a, b in zip(tabs["gpu"], tabs["ref"]):
+        assert (a.begin, a.length, a.step) == (b.begin, b.length, b.step)
+        assert bytes(a.points) == bytes(b.points)
+    pts = np.random.default_rng(7).uniform(-30, 30, size=(2000, 3))
+    pts[:5] = [[0, 0, 0], [1, 0, 0], [0, 0, 2.5], [-0.001, 0, 0], [0, -3, 0]]
+    for avg in range(5):
+        for orient in ((0.0, 0.0, 0.0, 0.0, 0.0), (0.4, -1.1, 1.5, -2.0, 0.25)):
+            out = []
+            for name, L in (("gpu", lib), ("ref", ref.lib)):
+                t = tabs[name]
+                st = ExtPotSet(C.pointer(t[0]), C.pointer(t[1]), C.pointer(t[2]), bytes([avg]), *orient)
+                out.append(np.array([L.dft_common_extpot(C.byref(st), *p) for p in pts]))
+            assert out[0].tobytes() == out[1].tobytes(), (avg, orient)
+
+
+def extpot_on_grid(lib, files, avg, orient, shape, step):
+    """dft_common_extpot of this library at the rgrid_map points
+    x_i = (i - nx/2) step (origin 0), as a grid"""
+    tabs = [ExtPot() for _ in files]
+    lib.dft_common_read_pot.argtypes = [C.c_char_p, C.POINTER(ExtPot)]
+    lib.dft_common_extpot.restype = C.c_double
+    lib.dft_common_extpot.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_double]
+    for f, t in zip(files, tabs):
+        lib.dft_common_read_pot(f, C.byref(t))
+    st = ExtPotSet(C.pointer(tabs[0]), C.pointer(tabs[1]), C.pointer(tabs[2]), bytes([avg]), *orient)
+    ax = [(np.arange(n) - n // 2) * step for n in shape]
+    out = np.empty(shape)
+    for i, x in enumerate(ax[0]):
+        for j, y in enumerate(ax[1]):
+            for k, z in enumerate(ax[2]):
+                out[i, j, k] = lib.dft_common_extpot(C.byref(st), x, y, z)
+    return out
+
+
+@needs_ref
+def test_libdft_potential_map_equals_callback_on_grid_points(lib, ref, tmp_path):
+    """libdft's own dft_common_potential_map onto its CPU grid gives, point for
+    point, this library's callback at the grid coordinates rgrid_map uses --
+    the values dft_common_potential_map uploads to a device grid."""
+    files = [pot_file(tmp_path / ("q%d.dat" % i), 0.5 + 0.2 * i, 0.05, 600, 10 + i) for i in range(3)]
+    shape, step, orient = (10, 8, 12), 0.9, (0.3, 0.7, 0.5, -1.0, 2.0)
+    R = ref.lib
+    R.dft_common_potential_map.argtypes = [C.c_byte, C.c_char_p, C.c_char_p, C.c_char_p, C.c_void_p] + [C.c_double] * 5
+    for avg in (0, 4):
+        with Grids(ref, shape, step, 1.0) as g:
+            rg = g.rgrid()
+            R.dft_common_potential_map(avg, *files, rg, *orient)
+            want = g.get_r(rg)
+        assert extpot_on_grid(lib, files, avg, orient, shape, step).tobytes() == want.tobytes()
+
+
+def test_potential_table_refusals(lib, tmp_path):
+    lib.dft_common_read_pot.argtypes = [C.c_char_p, C.POINTER(ExtPot)]
+    lib.dftgpu_last_error.restype = C.c_int
+    t = ExtPot()
+    lib.dft_common_read_pot(str(tmp_path / "none.dat").encode(), C.byref(t))
+    assert lib.dftgpu_last_error() == 8                                   # DFTGPU_ERR_IO
+    lib.dft_common_read_pot(pot_file(tmp_path / "j.dat", 1.0, 0.1, 50, 1, jitter=0.03), C.byref(t))
+    assert lib.dftgpu_last_error() == 1                                   # not equidistant
+    with open(tmp_path / "d.dat", "w") as f:
+        f.write("2.0 1.0\n1.0 2.0\n0.0 3.0\n")
+    lib.dft_common_read_pot(str(tmp_path / "d.dat").encode(), C.byref(t))
+    assert lib.dftgpu_last_error() == 1                                   # decreasing
+    lib.dft_common_read_pot(pot_file(tmp_path / "ok.dat", 1.0, 0.1, 50, 2), C.byref(t))
+    assert lib.dftgpu_last_error() == 0 and t.length == 50 and abs(t.step - 0.1) < 1e-8
+
+
 HOST_DRIVERS = ["dispersion/dispersion3.c", "dispersion/static-resp.c"]
 
 

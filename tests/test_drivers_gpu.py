@@ -141,3 +141,20 @@ def test_surface_tension_driver_matches_its_loop(gpu):
     assert st == pytest.approx(ref, rel=1e-12, abs=0)
     for o in (ed, P, ot, w):
         o.free()
+
+
+def test_potential_map_onto_device_grid(gpu, tmp_path):
+    """dft_common_potential_map (src/common.c:689) fills a device grid with the
+    values of its map callback at the grid points (FP64: bit for bit)."""
+    from test_driver_compat import extpot_on_grid, pot_file
+    L = gpu.lib()
+    gpu.set_precision(0)
+    files = [pot_file(tmp_path / ("v%d.dat" % i), 0.5 + 0.2 * i, 0.05, 600, 20 + i) for i in range(3)]
+    shape, step, orient = (10, 8, 12), 0.9, (0.3, 0.7, 0.5, -1.0, 2.0)
+    g = gpu.RGrid(shape, step)
+    L.dft_common_potential_map.argtypes = [C.c_byte, C.c_char_p, C.c_char_p, C.c_char_p, C.c_void_p] + [C.c_double] * 5
+    L.dft_common_potential_map.restype = None
+    L.dft_common_potential_map(0, *files, g.ptr, *orient)
+    assert L.dftgpu_last_error() == 0
+    assert g.get().tobytes() == extpot_on_grid(L, files, 0, orient, shape, step).tobytes()
+    g.free()
