@@ -259,7 +259,9 @@ REAL dft_ot_dispersion(wf *gwf, dft_ot_functional *otf, REAL ts, REAL *k, REAL a
   const REAL kk = ((REAL) ((INT) (0.5 + *k / dk))) * dk;
   *k = kk;
   if (kk == 0.0) return 0.0;
-  (&wave.kx)[(int) dir] = kk;
+  if (dir == 0) wave.kx = kk;
+  else if (dir == 1) wave.ky = kk;
+  else wave.kz = kk;
 
   const REAL rho0 = otf->rho0, mu0 = dft_ot_bulk_chempot2(otf);
   wf *gwfp = pred ? grid_wf_clone(gwf, (char *) "gwfp for dft_ot_dispersion") : nullptr;
