@@ -50,6 +50,12 @@ bool rc_shape(const cgrid *c, const rgrid *r) {
 
 int bad_arg(const char *what) { set_error(DFTGPU_ERR_ARG, "%s", what); return DFTGPU_ERR_ARG; }
 
+// NULL grids / wave functions are refused with DFTGPU_ERR_ARG before any device work
+#define NEED(cond, what, ...)                                 \
+  do {                                                        \
+    if (!(cond)) { bad_arg(what ": NULL argument"); return __VA_ARGS__; } \
+  } while (0)
+
 // Instantiated graph of one predict-correct step, replayed by dftgpu_run when
 // it is called again with the same arguments.  Any free of a grid, wave
 // function or functional bumps g_generation and so invalidates it.
@@ -144,16 +150,16 @@ rgrid *rgrid_clone(rgrid *g, char *id) {
   return c;
 }
 
-void rgrid_set_origin(rgrid *g, REAL x0, REAL y0, REAL z0) { g->x0 = x0; g->y0 = y0; g->z0 = z0; }
-void rgrid_zero(rgrid *g) { rfill(g, 0.0); }
-void rgrid_constant(rgrid *g, REAL c) { rfill(g, c); }
+void rgrid_set_origin(rgrid *g, REAL x0, REAL y0, REAL z0) { NEED(g, "rgrid_set_origin"); g->x0 = x0; g->y0 = y0; g->z0 = z0; }
+void rgrid_zero(rgrid *g) { NEED(g, "rgrid_zero"); rfill(g, 0.0); }
+void rgrid_constant(rgrid *g, REAL c) { NEED(g, "rgrid_constant"); rfill(g, c); }
 void rgrid_copy(rgrid *d, rgrid *s) {
   if (!same_shape(d, s)) { bad_arg("rgrid_copy: shape mismatch"); return; }
   if (cudaMemcpyAsync(d->value, s->value, gsize(s) * elem_size(s->prec), cudaMemcpyDeviceToDevice, rt().stream) != cudaSuccess)
     set_error(DFTGPU_ERR_CUDA, "rgrid_copy");
 }
-void rgrid_add(rgrid *g, REAL c) { raxpb(g, 1.0, c); }
-void rgrid_multiply(rgrid *g, REAL c) { raxpb(g, c, 0.0); }
+void rgrid_add(rgrid *g, REAL c) { NEED(g, "rgrid_add"); raxpb(g, 1.0, c); }
+void rgrid_multiply(rgrid *g, REAL c) { NEED(g, "rgrid_multiply"); raxpb(g, c, 0.0); }
 void rgrid_sum(rgrid *d, rgrid *a, rgrid *b) {
   if (!same_shape(d, a) || !same_shape(d, b)) { bad_arg("rgrid_sum: shape mismatch"); return; }
   rbinary(d, a, b, 0.0, 0);
@@ -171,12 +177,14 @@ void rgrid_add_scaled_product(rgrid *d, REAL c, rgrid *a, rgrid *b) {
   rbinary(d, a, b, c, 3);
 }
 REAL rgrid_integral(rgrid *g) {
+  NEED(g, "rgrid_integral", NAN);
   double v = NAN;
   rintegral(g, &v);
   return v;
 }
 
 void rgrid_map(rgrid *g, rgrid_map_fn func, void *farg) {
+  NEED(g && func, "rgrid_map");
   const INT nx = g->nx, ny = g->ny, nz = g->nz;
   std::vector<double> h(gsize(g));
   for (INT i = 0; i < nx; i++) {
@@ -228,14 +236,16 @@ int cgrid_value_at_index_re_im(cgrid *g, INT i, INT j, INT k, REAL *re, REAL *im
   return rc;
 }
 
-int rgrid_copy_to_host(rgrid *g, double *host) { return copy_values_out(g->prec, g->value, host, gsize(g)); }
-int rgrid_copy_from_host(rgrid *g, const double *host) { return copy_values_in(g->prec, g->value, host, gsize(g)); }
+int rgrid_copy_to_host(rgrid *g, double *host) { NEED(g && host, "rgrid_copy_to_host", DFTGPU_ERR_ARG); return copy_values_out(g->prec, g->value, host, gsize(g)); }
+int rgrid_copy_from_host(rgrid *g, const double *host) { NEED(g && host, "rgrid_copy_from_host", DFTGPU_ERR_ARG); return copy_values_in(g->prec, g->value, host, gsize(g)); }
 int rgrid_copy_to_host_raw(rgrid *g, void *host) {
+  NEED(g && host, "rgrid_copy_to_host_raw", DFTGPU_ERR_ARG);
   DFT_CUDA(cudaMemcpyAsync(host, g->value, gsize(g) * elem_size(g->prec), cudaMemcpyDeviceToHost, rt().stream));
   DFT_CUDA(cudaStreamSynchronize(rt().stream));
   return DFTGPU_OK;
 }
 int rgrid_copy_from_host_raw(rgrid *g, const void *host) {
+  NEED(g && host, "rgrid_copy_from_host_raw", DFTGPU_ERR_ARG);
   DFT_CUDA(cudaMemcpyAsync(g->value, host, gsize(g) * elem_size(g->prec), cudaMemcpyHostToDevice, rt().stream));
   return DFTGPU_OK;
 }
@@ -257,19 +267,20 @@ cgrid *cgrid_clone(cgrid *g, char *id) {
 // (callers: examples/gas-bubble/bubble.c:104,173,
 // examples/added_mass/added_mass.c:78, examples/1d-bubble/bubble-1d.c:136).
 void cgrid_set_momentum(cgrid *g, REAL kx0, REAL ky0, REAL kz0) {
-  if (!g) { bad_arg("cgrid_set_momentum: NULL grid"); return; }
+  NEED(g, "cgrid_set_momentum");
   g->kx0 = kx0; g->ky0 = ky0; g->kz0 = kz0;
 }
-void cgrid_zero(cgrid *g) { cfill(g, 0.0, 0.0); }
-void cgrid_constant_re_im(cgrid *g, REAL re, REAL im) { cfill(g, re, im); }
-void cgrid_add_re_im(cgrid *g, REAL re, REAL im) { cmuladd(g, 1.0, 0.0, re, im); }
-void cgrid_multiply_re_im(cgrid *g, REAL re, REAL im) { cmuladd(g, re, im, 0.0, 0.0); }
+void cgrid_zero(cgrid *g) { NEED(g, "cgrid_zero"); cfill(g, 0.0, 0.0); }
+void cgrid_constant_re_im(cgrid *g, REAL re, REAL im) { NEED(g, "cgrid_constant"); cfill(g, re, im); }
+void cgrid_add_re_im(cgrid *g, REAL re, REAL im) { NEED(g, "cgrid_add"); cmuladd(g, 1.0, 0.0, re, im); }
+void cgrid_multiply_re_im(cgrid *g, REAL re, REAL im) { NEED(g, "cgrid_multiply"); cmuladd(g, re, im, 0.0, 0.0); }
 void cgrid_copy(cgrid *d, cgrid *s) {
   if (!same_shape(d, s)) { bad_arg("cgrid_copy: shape mismatch"); return; }
   if (cudaMemcpyAsync(d->value, s->value, gsize(s) * 2 * elem_size(s->prec), cudaMemcpyDeviceToDevice, rt().stream) != cudaSuccess)
     set_error(DFTGPU_ERR_CUDA, "cgrid_copy");
 }
 void cgrid_map_re_im(cgrid *g, cgrid_map_fn func, void *farg) {
+  NEED(g && func, "cgrid_map");
   const INT nx = g->nx, ny = g->ny, nz = g->nz;
   std::vector<double> h(2 * gsize(g));
   for (INT i = 0; i < nx; i++) {
@@ -285,14 +296,16 @@ void cgrid_map_re_im(cgrid *g, cgrid_map_fn func, void *farg) {
   }
   copy_values_in(g->prec, g->value, h.data(), h.size());
 }
-int cgrid_copy_to_host(cgrid *g, double *host) { return copy_values_out(g->prec, g->value, host, 2 * gsize(g)); }
-int cgrid_copy_from_host(cgrid *g, const double *host) { return copy_values_in(g->prec, g->value, host, 2 * gsize(g)); }
+int cgrid_copy_to_host(cgrid *g, double *host) { NEED(g && host, "cgrid_copy_to_host", DFTGPU_ERR_ARG); return copy_values_out(g->prec, g->value, host, 2 * gsize(g)); }
+int cgrid_copy_from_host(cgrid *g, const double *host) { NEED(g && host, "cgrid_copy_from_host", DFTGPU_ERR_ARG); return copy_values_in(g->prec, g->value, host, 2 * gsize(g)); }
 int cgrid_copy_to_host_raw(cgrid *g, void *host) {
+  NEED(g && host, "cgrid_copy_to_host_raw", DFTGPU_ERR_ARG);
   DFT_CUDA(cudaMemcpyAsync(host, g->value, gsize(g) * 2 * elem_size(g->prec), cudaMemcpyDeviceToHost, rt().stream));
   DFT_CUDA(cudaStreamSynchronize(rt().stream));
   return DFTGPU_OK;
 }
 int cgrid_copy_from_host_raw(cgrid *g, const void *host) {
+  NEED(g && host, "cgrid_copy_from_host_raw", DFTGPU_ERR_ARG);
   DFT_CUDA(cudaMemcpyAsync(g->value, host, gsize(g) * 2 * elem_size(g->prec), cudaMemcpyHostToDevice, rt().stream));
   return DFTGPU_OK;
 }
@@ -341,14 +354,16 @@ void grid_wf_free(wf *g) {
   free(g);
 }
 
-void grid_wf_constant_re_im(wf *g, REAL re, REAL im) { cfill(g->grid, re, im); }
+void grid_wf_constant_re_im(wf *g, REAL re, REAL im) { NEED(g, "grid_wf_constant"); cfill(g->grid, re, im); }
 
 void grid_wf_density(wf *g, rgrid *d) {
+  NEED(g, "grid_wf_density");
   if (!rc_shape(g->grid, d)) { bad_arg("grid_wf_density: shape mismatch"); return; }
   density(g->grid, d);
 }
 
 REAL grid_wf_norm(wf *g) {
+  NEED(g, "grid_wf_norm", NAN);
   double v = NAN;
   double *slot = reduce_slots();
   if (norm_dev(g->grid, slot + 1) != DFTGPU_OK) return NAN;
@@ -359,6 +374,7 @@ REAL grid_wf_norm(wf *g) {
 }
 
 REAL grid_wf_normalize(wf *g) {
+  NEED(g, "grid_wf_normalize", NAN);
   double *slot = reduce_slots();
   if (norm_dev(g->grid, slot + 2) != DFTGPU_OK) return NAN;
   if (scale_by_norm(g->grid, slot + 2, g->norm) != DFTGPU_OK) return NAN;
@@ -370,12 +386,14 @@ REAL grid_wf_normalize(wf *g) {
 }
 
 REAL grid_wf_kinetic_energy(wf *g) {
+  NEED(g, "grid_wf_kinetic_energy", NAN);
   double v = NAN;
   kinetic_energy(g, &v);
   return v;
 }
 
 REAL grid_wf_energy(wf *g, rgrid *pot) {
+  NEED(g, "grid_wf_energy", NAN);
   double e = grid_wf_kinetic_energy(g);
   if (pot) {
     rgrid *d = rgrid_new(g->grid->nx, g->grid->ny, g->grid->nz, g->grid->step, g->grid->prec, "tmp");
@@ -391,16 +409,18 @@ REAL grid_wf_energy(wf *g, rgrid *pot) {
 }
 
 void grid_wf_velocity(wf *g, rgrid *vx, rgrid *vy, rgrid *vz, REAL eps) {
+  NEED(g, "grid_wf_velocity");
   if (!rc_shape(g->grid, vx) || !rc_shape(g->grid, vy) || !rc_shape(g->grid, vz)) { bad_arg("grid_wf_velocity"); return; }
   velocity(g, vx, vy, vz, eps);
 }
 
-int dftgpu_wf_propagate(wf *g, cgrid *pot, double dr, double di) { return propagate(g, g->grid, g->grid, pot, dr, di); }
+int dftgpu_wf_propagate(wf *g, cgrid *pot, double dr, double di) { NEED(g, "propagate", DFTGPU_ERR_ARG); return propagate(g, g->grid, g->grid, pot, dr, di); }
 int dftgpu_wf_propagate_predict(wf *g, wf *gp, cgrid *pot, double dr, double di) {
+  NEED(g, "propagate_predict", DFTGPU_ERR_ARG);
   if (!gp || !same_shape(g->grid, gp->grid)) return bad_arg("propagate_predict: wave function mismatch");
   return propagate(g, gp->grid, g->grid, pot, dr, di);
 }
-int dftgpu_wf_propagate_correct(wf *g, cgrid *pot, double dr, double di) { return propagate(g, g->grid, g->grid, pot, dr, di); }
+int dftgpu_wf_propagate_correct(wf *g, cgrid *pot, double dr, double di) { NEED(g, "propagate_correct", DFTGPU_ERR_ARG); return propagate(g, g->grid, g->grid, pot, dr, di); }
 
 // ------------------------------------------------------------------ OT functional
 // 0 K OT parameters and unit conversions (src/ot.c:1026-1036, 1234-1270)

@@ -85,3 +85,30 @@ def test_c_dropin_example_compiles_and_links(built, tmp_path, example):
                     "-L", os.path.dirname(built), "-ldftgpu", "-lm", "-Wl,-rpath," + os.path.dirname(built)],
                    check=True)
     assert exe.exists()
+
+
+def test_null_arguments_are_refused_without_a_device(built):
+    """The grid and wave-function entry points refuse NULL with DFTGPU_ERR_ARG
+    (libdft would dereference it) before any device work."""
+    import math
+    L = ctypes.CDLL(built)
+    L.dftgpu_last_error.restype = ctypes.c_int
+    buf = (ctypes.c_double * 8)()
+    for name in ("rgrid_copy_to_host", "rgrid_copy_from_host", "cgrid_copy_to_host", "cgrid_copy_from_host",
+                 "rgrid_copy_to_host_raw", "cgrid_copy_to_host_raw"):
+        f = getattr(L, name)
+        f.restype = ctypes.c_int
+        assert f(None, buf) == 1, name
+    for name in ("dftgpu_wf_propagate", "dftgpu_wf_propagate_correct"):
+        f = getattr(L, name)
+        f.restype = ctypes.c_int
+        f.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_double]
+        assert f(None, None, 1.0, 0.0) == 1, name
+    for name in ("grid_wf_norm", "grid_wf_normalize", "grid_wf_kinetic_energy", "rgrid_integral"):
+        f = getattr(L, name)
+        f.restype = ctypes.c_double
+        f.argtypes = [ctypes.c_void_p]
+        assert math.isnan(f(None)) and L.dftgpu_last_error() == 1, name
+    for name in ("rgrid_zero", "cgrid_zero"):
+        getattr(L, name)(None)
+        assert L.dftgpu_last_error() == 1, name
