@@ -77,6 +77,9 @@ template <typename T> int get_plan(int n, FftPlan<T> *plan) {
     void *d = nullptr;
     cudaError_t err = cudaMalloc(&d, sizeof(C) * (size_t) n);
     if (err == cudaSuccess) err = cudaMemcpy(d, h, sizeof(C) * (size_t) n, cudaMemcpyHostToDevice);
+    // the table is complete on the device before any stream (also a
+    // non-blocking one: a caller's, or a parallel branch) reads it
+    if (err == cudaSuccess) err = cudaDeviceSynchronize();
     free(h);
     if (err != cudaSuccess) {
       set_error(DFTGPU_ERR_CUDA, "twiddle table: %s", cudaGetErrorString(err));
