@@ -299,10 +299,8 @@ def run_gpu(args):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": "He droplet N=2000, 256^3, step 0.8 bohr, full OT (KC+BF), imaginary-time "
-                               "predict-correct dt=20 fs, renormalised each step",
-                   "grid": [NX, NX, NX], "model": "OT+KC+BF", "precision": "FP32 bulk, FP64 reductions",
-                   "l2": "inputs larger than L2 (psi 134 MB FP32); no flush", "parallelism": "replicas"},
+        "config": {"workload": workload_name(), "grid": [NX, NX, NX], "model": "OT+KC+BF",
+                   "precision": "FP32 bulk, FP64 reductions", "l2": l2_note(), "parallelism": "replicas"},
         "e2e": {"value": world * ke / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": 2 * N * 4,
                 "d2h_bytes_per_step": 2 * N * 4},
         "adjoint": {"value": world * adj_steps / (ms_adj * 1e-3), "unit": "trajectory steps/s",
@@ -334,9 +332,22 @@ def run_gpu(args):
     return line
 
 
+def workload_name():
+    return ("He droplet N=2000, %d^3, step 0.8 bohr, full OT (KC+BF), imaginary-time predict-correct dt=20 fs, "
+            "renormalised each step" % NX)
+
+
+def l2_note():
+    """whether one wave function (FP32) outruns the 129 MB L2 between steps"""
+    mb = 8 * NX ** 3 / 1e6
+    if mb > 129:
+        return "inputs larger than L2 (psi %.0f MB FP32); no flush" % mb
+    return "psi %.1f MB FP32 fits in L2 (profiling size, not the headline workload); no flush" % mb
+
+
 # ---------------------------------------------------------------------- CPU oracle
 def cpu_baseline(args, steps=1):
-    """The FP64 CPU oracle on the same 256^3 workload, all host cores."""
+    """The FP64 CPU oracle on the same workload, all host cores."""
     from oracle import Grids, Oracle
     o = Oracle("port")
     psi0 = droplet_psi(NX)
@@ -357,8 +368,8 @@ def cpu_baseline(args, steps=1):
             o.lib.orc_wf_normalize(w)
         el = time.perf_counter() - t
     return {"value": steps / el, "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
-            "sample": "%d predict-correct step(s) of the 256^3 full-OT droplet workload, FP64, OpenMP over all "
-                      "host cores (%.1f s)" % (steps, el)}
+            "sample": "%d predict-correct step(s) of the %d^3 full-OT droplet workload, FP64, OpenMP over all "
+                      "host cores (%.1f s)" % (steps, NX, el)}
 
 
 def run_reference(args):
@@ -369,8 +380,7 @@ def run_reference(args):
     return {"impl": "reference", "metric": metric_name(), "value": cb["value"], "unit": "steps/s", "n_gpus": 0,
             "steps": max(1, min(args.steps, 2)), "warmup": 0, "ms_per_step": 1e3 / cb["value"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "He droplet N=2000, 256^3, step 0.8 bohr, full OT (KC+BF), imaginary-time "
-                                   "predict-correct dt=20 fs, renormalised each step", "grid": [NX, NX, NX]},
+            "config": {"workload": workload_name(), "grid": [NX, NX, NX]},
             "cpu_baseline": cb, "e2e": {"value": cb["value"], "unit": "steps/s", "h2d_bytes_per_step": 0,
                                         "d2h_bytes_per_step": 0}}
 
