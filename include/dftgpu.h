@@ -403,6 +403,10 @@ void grid_fft_write_wisdom(char *file);
 REAL dft_common_lj_func(REAL r2, REAL sig, REAL eps);                      /* src/common.c:31 */
 REAL dft_common_lennard_jones(void *arg, REAL x, REAL y, REAL z);          /* src/common.c:53 (dft_common_lj *) */
 REAL dft_common_lennard_jones_smooth(void *arg, REAL x, REAL y, REAL z);   /* src/common.c:104 */
+/* the 1-D forms (integrated over the x-y plane, for grids along z) */
+REAL dft_common_lennard_jones_1d(void *arg, REAL x, REAL y, REAL z);       /* src/common.c:80 */
+REAL dft_common_spherical_avg_1d(void *arg, REAL x, REAL y, REAL z);       /* src/common.c:152 */
+REAL dft_common_gaussian_1d(void *arg, REAL x, REAL y, REAL z);            /* src/common.c:214 */
 REAL dft_common_spherical_avg(void *arg, REAL x, REAL y, REAL z);          /* src/common.c:131 (REAL *radius) */
 REAL dft_common_spherical_avg_k(void *arg, REAL kx, REAL ky, REAL kz);     /* src/common.c:173 */
 REAL dft_common_gaussian(void *arg, REAL x, REAL y, REAL z);               /* src/common.c:193 (REAL *inv_width) */

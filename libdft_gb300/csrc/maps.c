@@ -36,6 +36,17 @@ REAL dft_common_lennard_jones(void *arg, REAL x, REAL y, REAL z) {
   return dft_common_lj_func(r2, p->sigma, p->epsilon);
 }
 
+/* LJ integrated over the plane perpendicular to z, for a 1-D grid along z:
+ * 2 pi eps s^6 (2 s^6 - 5 z^6) / (5 z^10), |z| clamped at h -- src/common.c:80-91 */
+REAL dft_common_lennard_jones_1d(void *arg, REAL x, REAL y, REAL z) {
+  const dft_common_lj *p = (const dft_common_lj *) arg;
+  REAL s6 = pow(p->sigma, 6.0);
+  (void) x; (void) y;
+  z = fabs(z);
+  if (z < p->h) z = p->h;
+  return 2.0 * M_PI * p->epsilon * s6 * (2.0 * s6 - 5.0 * pow(z, 6.0)) / (5.0 * pow(z, 10.0));
+}
+
 /* LJ with the core replaced by U(h) (r/h)^4 -- src/common.c:104-116 */
 REAL dft_common_lennard_jones_smooth(void *arg, REAL x, REAL y, REAL z) {
   const dft_common_lj *p = (const dft_common_lj *) arg;
@@ -49,6 +60,16 @@ REAL dft_common_spherical_avg(void *arg, REAL x, REAL y, REAL z) {
   REAL h = *(const REAL *) arg, h2 = h * h;
   if (x * x + y * y + z * z <= h2) return 3.0 / (4.0 * M_PI * h * h2);
   return 0.0;
+}
+
+/* the sphere's step function integrated over the plane perpendicular to z:
+ * 3 (h^2 - z^2) / (4 h^3) inside |z| <= h -- src/common.c:152-159 */
+REAL dft_common_spherical_avg_1d(void *arg, REAL x, REAL y, REAL z) {
+  REAL h = *(const REAL *) arg, h2 = h * h;
+  (void) x; (void) y;
+  z = fabs(z);
+  if (z > h) return 0.0;
+  return 3.0 * (h2 - z * z) / (4.0 * h2 * h);
 }
 
 /* its Fourier transform 3 (sin(hk) - hk cos(hk)) / (hk)^3, with the
@@ -65,6 +86,14 @@ REAL dft_common_gaussian(void *arg, REAL x, REAL y, REAL z) {
   REAL a = *(const REAL *) arg, c = 0.5 * M_2_SQRTPI * a;
   c = c * c * c;
   return c * exp(-(x * x + y * y + z * z) * a * a);
+}
+
+/* the Gaussian integrated over the plane perpendicular to z:
+ * (a / sqrt(pi)) exp(-a^2 z^2) -- src/common.c:214-220 */
+REAL dft_common_gaussian_1d(void *arg, REAL x, REAL y, REAL z) {
+  REAL a = *(const REAL *) arg, c = 0.5 * M_2_SQRTPI * a;
+  (void) x; (void) y;
+  return c * exp(-z * z * a * a);
 }
 
 /* the same as a complex value -- src/common.c:235-242 */

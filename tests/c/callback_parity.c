@@ -101,6 +101,9 @@ int main(int argc, char **argv) {
   real_cb("dft_common_lennard_jones", &lj);
   real_cb("dft_common_lennard_jones", &lj_core);
   real_cb("dft_common_lennard_jones_smooth", &lj);
+  real_cb("dft_common_lennard_jones_1d", &lj);
+  real_cb("dft_common_spherical_avg_1d", &radius);
+  real_cb("dft_common_gaussian_1d", &inv_width);
   real_cb("dft_common_spherical_avg", &radius);
   real_cb("dft_common_spherical_avg_k", &radius);
   real_cb("dft_common_gaussian", &inv_width);
