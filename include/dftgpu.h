@@ -157,7 +157,16 @@ REAL rgrid_value_outside_periodic(rgrid *grid, INT i, INT j, INT k);
 
 /* ------------------------------------------------------- runtime control */
 /* Select the GPU.  libgrid: cuda_enable(1, NGPUS, gpus)
- * (examples/imag_time/imag_time.c:185-189).  One GPU only: ngpus must be 1. */
+ * (examples/imag_time/imag_time.c:185-189).  One GPU only: ngpus must be 1.
+ * One device per process: call this before allocating any grid and do not
+ * switch devices afterwards.  The FP64 reduction slots and partial sums, the
+ * FFT twiddle tables and the parallel-branch streams are process-global and
+ * are allocated on that device at first use; a functional's and a wave
+ * function's work buffers belong to that object.  Like libgrid's CPU calls,
+ * the library is not reentrant: issue all calls from one host thread, on the
+ * one work stream (dftgpu_set_stream) -- two functionals or wave functions
+ * stepped concurrently on different streams would race on the reduction
+ * slots. */
 void cuda_enable(char value, INT ngpus, int *gpus);
 int dftgpu_init(int device);
 /* Precision for grids allocated from now on (DFTGPU_FP64 / DFTGPU_FP32). */

@@ -654,14 +654,18 @@ __device__ __forceinline__ unsigned long long gtimer() {
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
 }
-// Wait for the completion of phase `parity`; after 0.5 s the wait gives up
-// and records the failure in *fault (read by the host after the launch).
-__device__ __forceinline__ void mbar_wait(unsigned bar, unsigned parity, int *fault) {
-  if (mbar_try_wait(bar, parity)) return;
+// Wait for the completion of phase `parity`; after 0.5 s the wait gives up,
+// records the failure in *fault (read by the host after the launch) and
+// returns false.  A thread whose wait gave up skips its global stores, and
+// every CTA ends with a cluster barrier, so no CTA exits before each peer has
+// passed its own bounded waits.
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity, int *fault) {
+  if (mbar_try_wait(bar, parity)) return true;
   const unsigned long long t0 = gtimer();
   while (!mbar_try_wait(bar, parity)) {
-    if (gtimer() - t0 > 500000000ull) { atomicExch(fault, 1); return; }
+    if (gtimer() - t0 > 500000000ull) { atomicExch(fault, 1); return false; }
   }
+  return true;
 }
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void bulk_g2s(unsigned dst, const void *src, unsigned bytes, unsigned bar) {
@@ -705,7 +709,7 @@ __global__ void __launch_bounds__(256, 2) zy_r2c_kernel(const C *__restrict__ tw
   }
   __syncthreads();
   if (tid < Z::RY) bulk_g2s(su32(a1 + tid * Z::PRW), f + ((size_t) x * NY + rank * Z::RY + tid) * NZ, NZ * 4, bar_ld);
-  mbar_wait(bar_ld, 0, fault);
+  bool ok = mbar_wait(bar_ld, 0, fault);
   {  // z pass of this CTA's rows into the plane [kz][row]
     constexpr int N = Z::NZC, E = Shape<N>::E, TL = Shape<N>::TL, B = Shape<N>::B, LP = Shape<N>::LP;
     const int t = tid % TL, l = tid / TL;
@@ -745,7 +749,7 @@ __global__ void __launch_bounds__(256, 2) zy_r2c_kernel(const C *__restrict__ tw
     bulk_s2c(cl_addr(su32(nq + rank * Z::RY), 0), su32(plt + Z::NZC * Z::RY), Z::RY * 8, cl_addr(bar_in, 0));
   }
   if (tid <= CL) bulk_commit();
-  mbar_wait(bar_in, 0, fault);
+  ok = mbar_wait(bar_in, 0, fault) && ok;
   {  // y pass of this CTA's column lines
     constexpr int N = NY, E = Shape<N>::E, TL = Shape<N>::TL;
     const int t = tid % TL, l = tid / TL, c = rank * Z::KC + l;
@@ -757,7 +761,7 @@ __global__ void __launch_bounds__(256, 2) zy_r2c_kernel(const C *__restrict__ tw
                     : a1[(sr * Z::KC + l) * Z::RY + r];
     }
     transform<N>(v, t, l, -1.f, twy, scr);
-    if (c != 0) {
+    if (c != 0 && ok) {
 #pragma unroll
       for (int j = 0; j < E; j++) spec[((size_t) c * nx + x) * NY + final_pos<N>(t, j)] = v[j];
     }
@@ -767,7 +771,7 @@ __global__ void __launch_bounds__(256, 2) zy_r2c_kernel(const C *__restrict__ tw
         for (int j = 0; j < E; j++) scr[final_pos<N>(t, j)] = v[j];
       }
       __syncthreads();
-      if (l == 0) {
+      if (l == 0 && ok) {
 #pragma unroll
         for (int j = 0; j < E; j++) {
           const int k = final_pos<N>(t, j);
@@ -780,6 +784,7 @@ __global__ void __launch_bounds__(256, 2) zy_r2c_kernel(const C *__restrict__ tw
     }
   }
   if (tid <= CL) bulk_wait_read();   // own outgoing copies have read the plane
+  cluster.sync();                    // no CTA leaves while a peer may still be copying into it
 }
 
 // inverse: spec[kz][x][y] -> real field f[x][y][z] * scale
@@ -815,7 +820,7 @@ __global__ void __launch_bounds__(256, 2) yz_c2r_kernel(const C *__restrict__ tw
   } else if (tid == Z::KC && rank == 0) {
     bulk_g2s(su32(nqs), spec + ((size_t) Z::NZC * nx + x) * NY, NY * 8, bar_ld);
   }
-  mbar_wait(bar_ld, 0, fault);
+  bool ok = mbar_wait(bar_ld, 0, fault);
   {  // y pass of this CTA's column lines into the outgoing blocks
     constexpr int N = NY, E = Shape<N>::E, TL = Shape<N>::TL;
     const int t = tid % TL, l = tid / TL, c = rank * Z::KC + l;
@@ -852,7 +857,7 @@ __global__ void __launch_bounds__(256, 2) yz_c2r_kernel(const C *__restrict__ tw
              cl_addr(bar_in, tid - CL));
   }
   if (tid < 2 * CL) bulk_commit();
-  mbar_wait(bar_in, 0, fault);
+  ok = mbar_wait(bar_in, 0, fault) && ok;
   {  // c2r z pass of this CTA's rows (line-fast), rows stored through shared memory
     constexpr int N = Z::NZC, E = Shape<N>::E, TL = Shape<N>::TL, B = Shape<N>::B, LP = Shape<N>::LP;
     const int t = tid / B, l = tid % B;
@@ -881,12 +886,13 @@ __global__ void __launch_bounds__(256, 2) yz_c2r_kernel(const C *__restrict__ tw
         const int idx = tid + it * 256, e = idx % N, ll = idx / N;
         const C val = scr[sidx(ll, e, LP)];
         C *row = reinterpret_cast<C *>(f + ((size_t) x * NY + rank * Z::RY + rb * B + ll) * NZ);
-        row[e] = make_float2(val.x * scale, val.y * scale);
+        if (ok) row[e] = make_float2(val.x * scale, val.y * scale);
       }
       __syncthreads();
     }
   }
   if (tid < 2 * CL) bulk_wait_read();   // own outgoing copies have read their blocks
+  cluster.sync();                        // no CTA leaves while a peer may still be copying into it
 }
 
 }  // namespace ff

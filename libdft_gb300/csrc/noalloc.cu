@@ -69,14 +69,30 @@ bool radices_for(int n, int *radix, int *nst) {
   return m == 1;
 }
 
-// tw[t] = exp(-2 pi i t / n), evaluated in FP64 and rounded once
+// tw[t] = exp(-2 pi i t / n), evaluated in FP64 and rounded once.  In FP32
+// the pair is the one, among the float pairs within one ulp of (cos, sin),
+// whose x^2 + y^2 is closest to 1 (the rule of the library's own tables):
+// independently rounded pairs leave |w|^2 off 1 by up to 1.2e-7 in a fixed
+// pattern, which drifts the norm of a real-time step.
+__device__ __forceinline__ void round_unit(double c, double s, float2 &w) {
+  const float fx = (float) c, fy = (float) s;
+  const float xs[2] = { fx, nextafterf(fx, c > (double) fx ? 2.f : -2.f) };
+  const float ys[2] = { fy, nextafterf(fy, s > (double) fy ? 2.f : -2.f) };
+  double best = -1.0;
+  for (int a = 0; a < 2; a++)
+    for (int b = 0; b < 2; b++) {
+      const double dev = fabs((double) xs[a] * xs[a] + (double) ys[b] * ys[b] - 1.0);
+      if (best < 0.0 || dev < best) { best = dev; w = make_float2(xs[a], ys[b]); }
+    }
+}
+__device__ __forceinline__ void round_unit(double c, double s, double2 &w) { w = make_double2(c, s); }
+
 template <typename T> __global__ void twiddle_kernel(typename cplx_t<T>::type *tw, int n) {
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
     const int tt = (t <= n / 2) ? t : t - n;
     double s, c;
     sincospi(-2.0 * (double) tt / (double) n, &s, &c);
-    tw[t].x = (T) c;
-    tw[t].y = (T) s;
+    round_unit(c, s, tw[t]);
   }
 }
 
@@ -156,6 +172,14 @@ int propagate_noalloc_t(void *out, const void *in, const void *pot, int nx, int 
   DFT_TRY(choose_tile(nx, ny, sizeof(C), 2, &B, &smem));
   smem = kin_smem(nx, B, sizeof(C));
   K.B = B;
+  int optin = 0, dev = 0;
+  DFT_CUDA(cudaGetDevice(&dev));
+  DFT_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  if (smem > (size_t) optin) {
+    set_error(DFTGPU_ERR_SIZE, "noalloc: kinetic pass for nx=%d needs %zu bytes of shared memory (limit %d)", nx, smem,
+              optin);
+    return DFTGPU_ERR_SIZE;
+  }
   if (smem > 48 * 1024)
     DFT_CUDA(cudaFuncSetAttribute(xkinetic_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
   xkinetic_kernel<T><<<dim3(ny / B, nz), FFT_THREADS, smem, s>>>(K);

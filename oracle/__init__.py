@@ -26,7 +26,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_LIB = os.path.join(HERE, "_build", "liboracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libdft_ref.so")
-REF_TREE = "/root/reference/src"
+# root of the libdft source tree (read in place; LIBDFT_REFERENCE overrides the default)
+REF_ROOT = os.environ.get("LIBDFT_REFERENCE", "/root/reference")
+REF_TREE = os.path.join(REF_ROOT, "src")
 
 # model flags (libdft src/ot.h:37-60)
 DFT_OT_PLAIN = 0

@@ -35,10 +35,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
-from oracle import Oracle, Grids, build  # noqa: E402
+from oracle import REF_ROOT, Oracle, Grids, build  # noqa: E402
 
-EOS_FILE = "/root/reference/examples/bulk/equation_of_state.dat"
-DISPERSION_DIR = "/root/reference/examples/dispersion"
+EOS_FILE = os.path.join(REF_ROOT, "examples", "bulk", "equation_of_state.dat")
+DISPERSION_DIR = os.path.join(REF_ROOT, "examples", "dispersion")
 
 
 def coords(shape, step):

@@ -17,7 +17,10 @@
   minutes per evaluation);
 * 512^3 full OT, a vortex ring of radius 40 bohr: FP32 against FP64 (energy
   and norm by FP64 reductions every 10 steps, the density in the plane
-  through the ring's axis after 40 steps).
+  through the ring's axis after 400 steps);
+* the droplet relaxation at its full length (1000 steps), FP32 against FP64,
+  and the 2-step droplet with libdft's default kernel sampling (4..32
+  substeps) against the oracle.
 """
 import numpy as np
 import pytest
@@ -115,6 +118,87 @@ def test_cfg2_droplet_256_energy_and_mu_match_oracle(gpu, port):
         assert abs(n / n_ref - 1) < ntol         # FP32: the renormalised grid is rounded to FP32
         assert abs((e / n) / e_ref - 1) < tol, (prec, e / n, e_ref)
         assert abs(mu / mu_ref - 1) < tol, (prec, mu, mu_ref)
+
+
+def test_cfg2_droplet_256_default_substeps_match_oracle(gpu, port):
+    """The same 2-step droplet comparison with the kernels sampled as libdft
+    samples them by default (4..32 substeps, src/ot.h DFT_MIN/MAX_SUBSTEPS):
+    energy per atom and mu of the GPU (FP64, FP32) against the FP64 oracle."""
+    import bench
+    shape, step, nsteps = (256, 256, 256), 0.8, 2
+    psi0 = bench.droplet_psi(256, step)
+    dt = -20j / gpu.AUTOFS
+    dv = step ** 3
+    with Grids(port, shape, step, gpu.HELIUM_MASS) as g:
+        wo, wpo, Po, work = g.wf(psi0), g.wf(), g.cgrid(), g.rgrid()
+        oo = g.ot(9, wo, min_ns=4, max_ns=32)
+        mu0 = port.lib.orc_bulk_chempot(oo, 0.0)
+        port.lib.orc_wf_set_norm(wo, bench.NATOMS)
+        port.lib.orc_wf_normalize(wo)
+        for _ in range(nsteps):
+            port.lib.orc_pc_step(oo, wo, wpo, Po, None, mu0, dt.real, dt.imag)
+            port.lib.orc_wf_normalize(wo)
+        n_ref = port.lib.orc_wf_norm(wo)
+        e_ref = port.lib.orc_total_energy(oo, wo, None, work) / n_ref
+        t_ref = port.lib.orc_wf_kinetic_energy(wo)
+        rho = np.abs(g.get_wf(wo)) ** 2
+        vot = g.potential(oo, wo)
+        mu_ref = (t_ref + np.sum(rho * vot.real) * dv) / n_ref
+    for prec, tol in ((0, 1e-9), (1, 1e-6)):
+        gpu.set_precision(prec)
+        w, wp, P = gpu.Wf(shape, step), gpu.Wf(shape, step), gpu.CGrid(shape, step)
+        ot = gpu.OT(9, w)                       # default 4..32 substeps
+        w.set(psi0)
+        w.norm_target = bench.NATOMS
+        w.normalize()
+        ot.run(w, wp, P, None, ot.bulk_chempot(0.0), dt, nsteps, True)
+        e, n, mu = ot.energy_report(w)
+        for o in (P, ot, wp, w):
+            o.free()
+        gpu.set_precision(0)
+        print("cfg2 default substeps prec=%d: rel E/N %.3e, rel mu %.3e" % (prec, abs((e / n) / e_ref - 1),
+                                                                            abs(mu / mu_ref - 1)))
+        assert abs((e / n) / e_ref - 1) < tol, (prec, e / n, e_ref)
+        assert abs(mu / mu_ref - 1) < tol, (prec, mu, mu_ref)
+
+
+def run_droplet(gpu, prec, nsteps):
+    """The bench's droplet (256^3, step 0.8 bohr, full OT, N = 2000) relaxed by
+    nsteps imaginary-time predict-correct steps of 20 fs, renormalised to N
+    after each (examples/imag_time/imag_time.c:224-257); returns E/N, mu and
+    the density."""
+    import bench
+    shape, step = (256, 256, 256), 0.8
+    gpu.set_precision(prec)
+    w, wp, P = gpu.Wf(shape, step), gpu.Wf(shape, step), gpu.CGrid(shape, step)
+    ot = gpu.OT(9, w)
+    w.set(bench.droplet_psi(256, step))
+    w.norm_target = bench.NATOMS
+    w.normalize()
+    ot.run(w, wp, P, None, ot.bulk_chempot(0.0), -20j / gpu.AUTOFS, nsteps, True)
+    e, n, mu = ot.energy_report(w)
+    rho = np.abs(w.get()) ** 2
+    for o in (P, ot, wp, w):
+        o.free()
+    gpu.set_precision(0)
+    return e / n, mu, rho
+
+
+def test_cfg2_droplet_1000_steps_fp32_vs_fp64(gpu):
+    """The full specified relaxation: 1000 imaginary-time steps of 20 fs of the
+    256^3 droplet.  FP32 bulk (FP64 reductions) against the FP64 run: relative
+    error of the energy per atom and of mu <= 1e-6; the density's relative L2
+    error is reported."""
+    e64, mu64, rho64 = run_droplet(gpu, 0, 1000)
+    e32, mu32, rho32 = run_droplet(gpu, 1, 1000)
+    re, rmu = abs(e32 / e64 - 1), abs(mu32 / mu64 - 1)
+    l2 = np.linalg.norm(rho32 - rho64) / np.linalg.norm(rho64)
+    print("cfg2 1000 steps: E/N %.9f K (FP64) %.9f K (FP32) rel %.3e; mu rel %.3e; density L2 %.3e"
+          % (e64 * gpu.AUTOK, e32 * gpu.AUTOK, re, rmu, l2))
+    assert np.isfinite([e32, mu32]).all()
+    assert re < 1e-6, re
+    assert rmu < 1e-6, rmu
+    assert l2 < 1e-4, l2
 
 
 def cfg1_psi(gpu, shape, step):
@@ -257,19 +341,22 @@ def run_ring(gpu, prec, shape, step, nsteps):
 def test_cfg4_vortex_ring_512_fp32(gpu):
     """512^3, step 0.6 bohr, full OT, vortex ring of radius 40 bohr, dt =
     0.5 fs, energy and norm (FP64 reductions) every 10 steps: the FP32 run
-    against the FP64 run of the same 40 steps, and the density in the plane
-    through the ring's axis after them.  (The tanh core is not a stationary
-    profile: over these 20 fs the core relaxes -- the energy of both runs
-    changes by ~2e-4 -- while the ring itself moves by < 0.01 bohr.)"""
-    shape, step, nsteps = (512, 512, 512), 0.6, 40
+    against the FP64 run of the same 400 steps (200 fs), and the density in
+    the plane through the ring's axis after them.  (The tanh core is not a
+    stationary profile: the core relaxes while the ring itself moves slowly.)"""
+    shape, step, nsteps = (512, 512, 512), 0.6, 400
     e32, n32, p32, rho0 = run_ring(gpu, 1, shape, step, nsteps)
     e64, n64, p64, _ = run_ring(gpu, 0, shape, step, nsteps)
+    print("cfg4 400 steps: max rel energy %.3e, max rel norm %.3e, FP64 energy change %.3e"
+          % (np.abs(e32 / e64 - 1).max(), np.abs(n32 / n64 - 1).max(), abs(e64[-1] / e64[0] - 1)))
     assert np.isfinite(e32).all()
-    assert np.abs(e32 / e64 - 1).max() < 2e-6, e32 / e64 - 1
-    assert np.abs(n32 / n64 - 1).max() < 2e-6, n32 / n64 - 1
+    # real time: FP32 rounding accumulates (128^3, 500 steps: 5e-6 in energy)
+    assert np.abs(e32 / e64 - 1).max() < 1e-5, e32 / e64 - 1
+    assert np.abs(n32 / n64 - 1).max() < 1e-5, n32 / n64 - 1
     # the cores are resolved: the density on the core line stays near zero
     x = (np.arange(shape[0]) - shape[0] // 2) * step
     core = np.argmin(np.abs(x - 40.0))
     assert p64[core, shape[2] // 2] < 0.2 * rho0
     err = np.linalg.norm(p32 - p64) / np.linalg.norm(p64)
-    assert err < 1e-5, err
+    print("cfg4 400 steps: density L2 in the axis plane %.3e" % err)
+    assert err < 1e-4, err

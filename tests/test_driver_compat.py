@@ -22,12 +22,12 @@ import numpy as np
 import pytest
 
 from conftest import ROOT
-from oracle import REF_LIB, Grids, Oracle, ref_available
+from oracle import REF_LIB, REF_ROOT, Grids, Oracle, ref_available
 
 LIBDIR = os.path.join(ROOT, "libdft_gb300")
 LIB = os.path.join(LIBDIR, "libdftgpu.so")
 INCLUDE = os.path.join(ROOT, "include")
-REF_EXAMPLES = "/root/reference/examples"
+REF_EXAMPLES = os.path.join(REF_ROOT, "examples")
 
 needs_ref = pytest.mark.skipif(not ref_available(), reason="reference tree not present")
 

@@ -251,6 +251,32 @@ def test_propagate_matches_oracle(gpu, port, prec, shape):
         o.free()
 
 
+@pytest.mark.parametrize("shape", [(24, 20, 30), (64, 96, 32)])
+def test_velocity_matches_oracle(gpu, port, prec, shape):
+    """grid_wf_velocity (the exported entry point, src/ot.c:387-390) against
+    the oracle: v = (hbar/m) Im(psi* D psi) / max(|psi|^2, eps), central
+    differences, with a region of near-zero density so that eps is active."""
+    step = 0.9
+    psi = liquid_psi(shape, step, 13)
+    X, Y, Z = coords(shape, step)
+    psi = psi * np.tanh(np.sqrt(X ** 2 + (Y - 3.0) ** 2 + Z ** 2) / 2.0) ** 3   # a cavity: |psi|^2 -> 0
+    eps = 1e-4 * float(np.max(np.abs(psi) ** 2))
+    with Grids(port, shape, step, gpu.HELIUM_MASS) as g:
+        wo, vx, vy, vz = g.wf(psi), g.rgrid(), g.rgrid(), g.rgrid()
+        port.lib.orc_wf_velocity(wo, vx, vy, vz, eps)
+        ref = [g.get_r(v) for v in (vx, vy, vz)]
+    w = gpu.Wf(shape, step)
+    w.set(psi)
+    out = [gpu.RGrid(shape, step) for _ in range(3)]
+    L = gpu.lib()
+    L.grid_wf_velocity(w.ptr, out[0].ptr, out[1].ptr, out[2].ptr, eps)
+    assert L.dftgpu_last_error() == 0
+    for o, r in zip(out, ref):
+        assert relerr(o.get(), r) < (1e-12 if prec == 0 else 2e-5)
+    for o in out + [w]:
+        o.free()
+
+
 def test_pc_steps_match_reference_plain(gpu, prec):
     fx = golden("plain_16.npz")
     shape, step = tuple(int(s) for s in fx["shape"]), float(fx["step"])

@@ -85,3 +85,55 @@ def test_noalloc_rejects_grids_beyond_the_static_scratch():
     assert rc == 2
     assert "static scratch" in L.dftgpu_last_error_message().decode()
     L.dftgpu_last_error()
+
+
+@pytest.mark.parametrize("prec", [0, 1], ids=["fp64", "fp32"])
+def test_noalloc_in_place_allocates_nothing_and_keeps_the_norm(prec):
+    """psi_out may be psi_in.  After a first call (which looks up the static
+    scratch's address), further calls must not change the device's free
+    memory, and in FP32 the norm after many real-time steps must follow the
+    allocating entry point (both use unit-circle-rounded twiddles)."""
+    import torch
+    import libdft_gb300 as G
+
+    L = G.lib()
+    assert L.dftgpu_init(0) == 0
+    G.set_precision(prec)
+    shape, step, dt = (32, 32, 64), 0.8, 41.3 + 0.0j   # real time: the norm is conserved exactly in exact arithmetic
+    psi, V = _psi_and_potential(shape, step, 5)
+    V = V.real.astype(np.complex128)                   # real potential: unitary step
+    w = G.Wf(shape, step)
+    P = G.CGrid(shape, step)
+    w.set(psi)
+    P.set(V)
+    as_t = lambda a: torch.from_numpy(np.ascontiguousarray(a).view(np.float64).astype(
+        np.float64 if prec == 0 else np.float32)).to("cuda")
+    buf, pot = as_t(psi), as_t(V)
+    nx, ny, nz = shape
+    call = lambda: L.dftgpu_wf_propagate_noalloc(buf.data_ptr(), buf.data_ptr(), pot.data_ptr(), nx, ny, nz, step,
+                                                 G.HELIUM_MASS, dt.real, dt.imag, prec, None)
+    assert call() == 0, L.dftgpu_last_error_message()
+    w.propagate(P, dt)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    nsteps = 200
+    for _ in range(nsteps - 1):
+        assert call() == 0, L.dftgpu_last_error_message()
+        w.propagate(P, dt)
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+    got = buf.double().cpu().numpy().view(np.complex128).reshape(shape)
+    ref = w.get()
+    n0 = np.sum(np.abs(psi) ** 2)
+    drift_new = abs(np.sum(np.abs(got) ** 2) / n0 - 1.0)
+    drift_ref = abs(np.sum(np.abs(ref) ** 2) / n0 - 1.0)
+    # FP32: the drift stays within a small multiple of the allocating path's
+    # (a twiddle table with a biased |w|^2 drifts steadily every step);
+    # FP64: round-off only
+    bound = 2e-12 if prec == 0 else max(3.0 * drift_ref, 2e-6)
+    assert drift_new < bound, (drift_new, drift_ref)
+    err = np.abs(got - ref).max() / np.abs(ref).max()
+    assert err < (1e-9 if prec == 0 else 2e-4), err
+    w.free()
+    P.free()
+    G.set_precision(0)
