@@ -261,6 +261,23 @@ int dftgpu_wf_propagate(wf *gwf, cgrid *potential, double dt_re, double dt_im);
 int dftgpu_wf_propagate_predict(wf *gwf, wf *gwfp, cgrid *potential, double dt_re, double dt_im);
 int dftgpu_wf_propagate_correct(wf *gwf, cgrid *potential, double dt_re, double dt_im);
 
+/* Absorbing boundary (libgrid; examples/gas-bubble/bubble.c:149-157,
+ * examples/1d-bubble/bubble-1d.c:192): the layer of grid points outside
+ * [lx, hx) x [ly, hy) x [lz, hz) absorbs, with a weight lambda that rises
+ * linearly from 0 at the layer's inner edge to 1 at the grid's edge.  Set on
+ * gwf and, when given, gwfp.  From then on the predict / correct steps of that
+ * wave function (grid_wf_propagate_predict / _correct, dftgpu_pc_step,
+ * dftgpu_run) add -i amp lambda (|psi|^2 / rho0 - 1), evaluated from the step's
+ * input, to their potential, which drives the density in the layer towards
+ * rho0.  libgrid's own arithmetic is not in the reference tree: this form is
+ * this library's.  The adjoint entry points refuse a wave function that has a
+ * boundary (DFTGPU_ERR_UNSUPPORTED). */
+void grid_wf_boundary(wf *gwf, wf *gwfp, REAL amp, REAL rho0, INT lx, INT hx, INT ly, INT hy, INT lz, INT hz);
+/* potential += -i amp lambda (|psi|^2 / rho0 - 1) over gwf's absorbing layer
+ * (examples/1d-bubble/bubble-1d.c:222; single-step callers, whose
+ * grid_wf_propagate does not add it). */
+void grid_wf_absorb_potential(wf *gwf, cgrid *potential, REAL amp, REAL rho0);
+
 /* Allocation-free form of dftgpu_wf_propagate (no counterpart in the
  * reference: libgrid allocates its own work grids).  For callers that may not
  * call cudaMalloc -- code running inside someone else's stream capture, hosts

@@ -99,6 +99,8 @@ SIGNATURES = {
     "grid_wf_energy": (_d, [_vp, _vp]),
     "grid_wf_kinetic_energy": (_d, [_vp]),
     "grid_wf_velocity": (None, [_vp, _vp, _vp, _vp, _d]),
+    "grid_wf_boundary": (None, [_vp, _vp, _d, _d, _l, _l, _l, _l, _l, _l]),
+    "grid_wf_absorb_potential": (None, [_vp, _vp, _d, _d]),
     "dftgpu_wf_propagate": (_i, [_vp, _vp, _d, _d]),
     "dftgpu_wf_propagate_predict": (_i, [_vp, _vp, _vp, _d, _d]),
     "dftgpu_wf_propagate_correct": (_i, [_vp, _vp, _d, _d]),

@@ -53,6 +53,10 @@ static int ot_vjp_t(dft_ot_functional *otf, wf *gwf, const typename cplx_t<T>::t
     set_error(DFTGPU_ERR_UNSUPPORTED, "adjoint: backflow clamps / weight are not differentiated");
     return DFTGPU_ERR_UNSUPPORTED;
   }
+  if (hd_model(otf)) {
+    set_error(DFTGPU_ERR_UNSUPPORTED, "adjoint: the high-density terms (HD, HD2) are not differentiated");
+    return DFTGPU_ERR_UNSUPPORTED;
+  }
   // forward intermediates for this psi (potential into scratch)
   cgrid *c = gwf->grid;
   if (!fresh) {
@@ -576,6 +580,21 @@ bool fits_r(dft_ot_functional *otf, const rgrid *r) {
   return r && P && r->nx == P->nx && r->ny == P->ny && r->nz == P->nz && r->prec == P->prec;
 }
 
+// While an adjoint entry point runs, the potential evaluations keep every
+// intermediate in its work slot (the VJP reads them), i.e. they do not use
+// the fused producer passes that keep some of them in registers only.
+// The high-density terms and the absorbing boundary are not differentiated:
+// refused before any work.
+int hd_refused(dft_ot_functional *otf, wf *gwf = nullptr) {
+  if (gwf && ((WfPriv *) gwf->priv)->abs.on) {
+    set_error(DFTGPU_ERR_UNSUPPORTED, "adjoint: the absorbing boundary is not differentiated");
+    return DFTGPU_ERR_UNSUPPORTED;
+  }
+  if (!hd_model(otf)) return DFTGPU_OK;
+  set_error(DFTGPU_ERR_UNSUPPORTED, "adjoint: the high-density terms (HD, HD2) are not differentiated");
+  return DFTGPU_ERR_UNSUPPORTED;
+}
+
 }  // namespace
 
 extern "C" {
@@ -583,6 +602,7 @@ extern "C" {
 int dftgpu_ot_potential_vjp(dft_ot_functional *otf, wf *gwf, cgrid *cot, cgrid *grad_psi) {
   if (!otf || !gwf || !fits(otf, gwf->grid) || !fits(otf, cot) || !fits(otf, grad_psi))
     return adj_arg("dftgpu_ot_potential_vjp: grid mismatch");
+  DFT_TRY(hd_refused(otf));
   return ot_vjp(otf, gwf, cot, 1.0, grad_psi, 0);
 }
 
@@ -602,6 +622,7 @@ int dftgpu_pc_step_vjp(dft_ot_functional *otf, wf *gwf, rgrid *vext, double mu0,
   if (!otf || !gwf || !fits(otf, gwf->grid) || !fits(otf, cot)) return adj_arg("dftgpu_pc_step_vjp: grid mismatch");
   if ((vext && !fits_r(otf, vext)) || (grad_vext && !fits_r(otf, grad_vext)))
     return adj_arg("dftgpu_pc_step_vjp: vext mismatch");
+  DFT_TRY(hd_refused(otf, gwf));
   AdjWork *W = work_get((OtPriv *) otf->priv, gwf);
   if (!W) return DFTGPU_ERR_NOMEM;
   DFT_TRY(ccopy(W->wk->grid, gwf->grid));
@@ -616,6 +637,7 @@ int dftgpu_adjoint_run(dft_ot_functional *otf, wf *gwf, rgrid *vext, double mu0,
   if ((vext && !fits_r(otf, vext)) || (grad_vext && !fits_r(otf, grad_vext)) || (grad_psi0 && !fits(otf, grad_psi0)))
     return adj_arg("dftgpu_adjoint_run: grid mismatch");
   if (nsteps < 0) return adj_arg("dftgpu_adjoint_run: nsteps < 0");
+  DFT_TRY(hd_refused(otf, gwf));
   AdjWork *W = work_get((OtPriv *) otf->priv, gwf);
   if (!W) return DFTGPU_ERR_NOMEM;
   const bool f32 = gwf->grid->prec == DFTGPU_FP32;

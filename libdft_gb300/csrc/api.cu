@@ -349,9 +349,56 @@ wf *grid_wf_clone(wf *g, char *id) {
 void grid_wf_free(wf *g) {
   if (!g) return;
   WfPriv *p = (WfPriv *) g->priv;
-  if (p) { dev_free(p->spec); delete p; }
+  if (p) {
+    dev_free(p->spec);
+    if (p->vtot) { dev_free(p->vtot->value); free(p->vtot); }
+    delete p;
+  }
   cgrid_free(g->grid);
   free(g);
+}
+
+// Absorbing boundary (libgrid; call sites examples/gas-bubble/bubble.c:149-157,
+// examples/1d-bubble/bubble-1d.c:192,222).  libgrid's arithmetic is not in the
+// reference tree; the form here is this library's (AbsBoundary in
+// grid_internal.cuh): outside [lx, hx) x [ly, hy) x [lz, hz) the weight lambda
+// rises linearly to 1 at the grid's edge, and the absorbing potential is
+// -i amp lambda (|psi|^2 / rho0 - 1), which drives the density there towards
+// rho0.  grid_wf_propagate_predict / _correct (and dftgpu_pc_step /
+// dftgpu_run) add it, evaluated from the step's input, to the potential of
+// the wave function that has the boundary; grid_wf_propagate does not (a
+// single-step caller adds it with grid_wf_absorb_potential).
+static int set_boundary(wf *g, REAL amp, REAL rho0, const INT lo[3], const INT hi[3]) {
+  const INT n[3] = { g->grid->nx, g->grid->ny, g->grid->nz };
+  for (int a = 0; a < 3; a++)
+    if (lo[a] < 0 || hi[a] > n[a] || lo[a] > hi[a]) return bad_arg("grid_wf_boundary: layer outside the grid");
+  if (!(rho0 > 0.0)) return bad_arg("grid_wf_boundary: rho0 must be positive");
+  AbsBoundary &b = ((WfPriv *) g->priv)->abs;
+  b.on = 1;
+  b.amp = amp;
+  b.rho0 = rho0;
+  for (int a = 0; a < 3; a++) { b.lo[a] = (int) lo[a]; b.hi[a] = (int) hi[a]; }
+  g_generation++;   // a captured step graph of this wave function is stale
+  return DFTGPU_OK;
+}
+
+void grid_wf_boundary(wf *gwf, wf *gwfp, REAL amp, REAL rho0, INT lx, INT hx, INT ly, INT hy, INT lz, INT hz) {
+  NEED(gwf, "grid_wf_boundary");
+  const INT lo[3] = { lx, ly, lz }, hi[3] = { hx, hy, hz };
+  if (set_boundary(gwf, amp, rho0, lo, hi)) return;
+  if (gwfp) set_boundary(gwfp, amp, rho0, lo, hi);
+}
+
+void grid_wf_absorb_potential(wf *gwf, cgrid *potential, REAL amp, REAL rho0) {
+  NEED(gwf && potential, "grid_wf_absorb_potential");
+  if (!same_shape(gwf->grid, potential) || potential->prec != gwf->grid->prec) {
+    bad_arg("grid_wf_absorb_potential: grid mismatch");
+    return;
+  }
+  const AbsBoundary &b = ((WfPriv *) gwf->priv)->abs;
+  if (!b.on) { bad_arg("grid_wf_absorb_potential: no absorbing boundary set (grid_wf_boundary)"); return; }
+  if (!(rho0 > 0.0)) { bad_arg("grid_wf_absorb_potential: rho0 must be positive"); return; }
+  absorb_add(potential, potential, gwf->grid, b, amp, rho0);
 }
 
 void grid_wf_constant_re_im(wf *g, REAL re, REAL im) { NEED(g, "grid_wf_constant"); cfill(g->grid, re, im); }
@@ -418,9 +465,9 @@ int dftgpu_wf_propagate(wf *g, cgrid *pot, double dr, double di) { NEED(g, "prop
 int dftgpu_wf_propagate_predict(wf *g, wf *gp, cgrid *pot, double dr, double di) {
   NEED(g, "propagate_predict", DFTGPU_ERR_ARG);
   if (!gp || !same_shape(g->grid, gp->grid)) return bad_arg("propagate_predict: wave function mismatch");
-  return propagate(g, gp->grid, g->grid, pot, dr, di);
+  return propagate_pc(g, gp->grid, g->grid, pot, dr, di);
 }
-int dftgpu_wf_propagate_correct(wf *g, cgrid *pot, double dr, double di) { NEED(g, "propagate_correct", DFTGPU_ERR_ARG); return propagate(g, g->grid, g->grid, pot, dr, di); }
+int dftgpu_wf_propagate_correct(wf *g, cgrid *pot, double dr, double di) { NEED(g, "propagate_correct", DFTGPU_ERR_ARG); return propagate_pc(g, g->grid, g->grid, pot, dr, di); }
 
 // ------------------------------------------------------------------ OT functional
 // 0 K OT parameters and unit conversions (src/ot.c:1026-1036, 1234-1270)
@@ -473,8 +520,8 @@ void dft_ot_init_params(dft_ot_functional *otf, INT model) {
 
 dft_ot_functional *dft_ot_alloc(INT model, wf *gwf, INT min_substeps, INT max_substeps) {
   if (!gwf) { bad_arg("dft_ot_alloc: NULL wave function"); return nullptr; }
-  if (model & ~((INT) (DFT_OT_KC | DFT_OT_BACKFLOW))) {
-    set_error(DFTGPU_ERR_UNSUPPORTED, "dft_ot_alloc: model %ld outside {PLAIN, KC, BACKFLOW}", (long) model);
+  if (model & ~((INT) (DFT_OT_KC | DFT_OT_HD | DFT_OT_HD2 | DFT_OT_BACKFLOW))) {
+    set_error(DFTGPU_ERR_UNSUPPORTED, "dft_ot_alloc: model %ld outside {PLAIN, KC, HD, HD2, BACKFLOW}", (long) model);
     return nullptr;
   }
   cgrid *c = gwf->grid;
@@ -707,10 +754,10 @@ REAL dft_ot_bulk_dispersion(dft_ot_functional *o, REAL *kp, REAL rho0) {
 static int pc_step_impl(dft_ot_functional *otf, wf *gwf, wf *gwfp, cgrid *P, rgrid *vext, double mu0, double dr, double di) {
   // P = Vext + V_OT[psi] - mu0   (the fills and shifts run inside the potential's pointwise passes)
   DFT_TRY(ot_potential_ex(otf, P, gwf, 1, vext, -mu0, 1.0));
-  DFT_TRY(propagate(gwf, gwfp->grid, gwf->grid, P, dr, di));
+  DFT_TRY(propagate_pc(gwf, gwfp->grid, gwf->grid, P, dr, di));
   // P = (P + Vext + V_OT[psi_p] - mu0) / 2
   DFT_TRY(ot_potential_ex(otf, P, gwfp, 0, vext, -mu0, 0.5));
-  return propagate(gwf, gwf->grid, gwf->grid, P, dr, di);
+  return propagate_pc(gwf, gwf->grid, gwf->grid, P, dr, di);
 }
 
 static int check_step_args(dft_ot_functional *otf, wf *gwf, wf *gwfp, cgrid *P, rgrid *vext) {

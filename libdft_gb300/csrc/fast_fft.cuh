@@ -24,6 +24,7 @@
 #pragma once
 
 #include <cooperative_groups.h>
+#include <cuda.h>
 
 #include "common.cuh"
 
@@ -208,6 +209,81 @@ template <int N> __device__ __forceinline__ void to_input_order(C (&v)[Shape<N>:
   for (int q = 0; q < E; q++) v[q] = t[q];
 }
 
+// --------------------------------------------------------------- asynchronous copies
+__device__ __forceinline__ unsigned su32(const void *p) { return (unsigned) __cvta_generic_to_shared(p); }
+__device__ __forceinline__ unsigned cl_addr(unsigned a, unsigned rank) {   // shared::cluster address in CTA rank
+  unsigned r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ void mbar_init(unsigned bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void mbar_expect_tx(unsigned bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ unsigned long long gtimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// Wait for the completion of phase `parity`; after 0.5 s the wait gives up,
+// records the failure in *fault (read by the host after the launch) and
+// returns false.  A thread whose wait gave up skips its global stores, and
+// every CTA ends with a cluster barrier, so no CTA exits before each peer has
+// passed its own bounded waits.
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity, int *fault) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = gtimer();
+  while (!mbar_try_wait(bar, parity)) {
+    if (gtimer() - t0 > 500000000ull) { atomicExch(fault, 1); return false; }
+  }
+  return true;
+}
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void bulk_g2s(unsigned dst, const void *src, unsigned bytes, unsigned bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+               ::"r"(dst), "l"(src), "r"(bytes), "r"(bar)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_s2c(unsigned dst, unsigned src, unsigned bytes, unsigned bar) {
+  asm volatile("cp.async.bulk.shared::cluster.shared::cta.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+               ::"r"(dst), "r"(src), "r"(bytes), "r"(bar)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+
+// TMA (cp.async.bulk.tensor) of one 3-D box of a tensor map: load into shared
+// memory completing on an mbarrier, store from shared memory as a bulk group.
+// The tensor map is a __grid_constant__ kernel parameter (its generic address).
+__device__ __forceinline__ void tma_load_3d(unsigned dst, const void *tmap, int c0, int c1, int c2, unsigned bar) {
+  asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+               ::"r"(dst), "l"(tmap), "r"(c0), "r"(c1), "r"(c2), "r"(bar)
+               : "memory");
+}
+__device__ __forceinline__ void tma_store_3d(const void *tmap, int c0, int c1, int c2, unsigned src) {
+  asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%1, %2, %3}], [%4];"
+               ::"l"(tmap), "r"(c0), "r"(c1), "r"(c2), "r"(src)
+               : "memory");
+}
+// Byte offset of 8-byte element (row, col) of a box stored with the 128-byte
+// swizzle (16 elements per 128-byte row; the 16-byte chunk index is XORed
+// with the row index mod 8; the box starts on a 1024-byte boundary).
+__device__ __forceinline__ int swz128(int row, int col) {
+  return row * 128 + ((((col >> 1) ^ (row & 7)) << 4) | ((col & 1) << 3));
+}
+
 // --------------------------------------------------------------- line pass
 enum { MAP_E = 0, MAP_L = 1 };
 
@@ -235,17 +311,48 @@ template <int N, int MODE, int B, class Ld> __device__ __forceinline__ void pref
   }
 }
 
+// TMA staging of the transposed side of a z pass: the [kz][x][y] tile of a
+// CTA (its B lines, the N or N+1 kz values) moves as B/16 boxes {16 y, 1 x,
+// rows kz} of a 3-D tensor map over the spectral buffer, with the 128-byte
+// swizzle; each box starts on a 1024-byte boundary of shared memory.
+struct alignas(64) TmaMaps {
+  CUtensorMap load, store;   // the staged load / store side (the unused one is not read)
+};
+template <int N, int MODE> struct TmaTile {
+  static constexpr int ROWS = MODE == 0 ? N : N + 1;           // kz values of the tile
+  static constexpr int NBOX = Shape<N>::B / 16;
+  static constexpr int BOXB = ((ROWS * 128 + 1023) / 1024) * 1024;
+  static constexpr int BYTES = NBOX * BOXB;
+  static constexpr bool OK = ROWS <= 256 && Shape<N>::B % 16 == 0;
+};
+// Shared memory of a line pass: the transform's exchange buffer, which also
+// holds the TMA boxes (1024-byte aligned) when TMA is on.
+template <int N, int MODE, int TMA> struct LineSmem {
+  static constexpr int XB = Shape<N>::B * Shape<N>::LP * (int) sizeof(C);
+  static constexpr int TB = TMA ? TmaTile<N, MODE>::BYTES : 0;
+  static constexpr int BYTES = (XB > TB ? XB : TB) + (TMA ? 1024 : 0);
+};
+
 // MODE 0 C2C, 1 R2C (N = nz/2, post-processed to N+1 outputs), 2 C2R.
 // LDS / STS: stage the load / store side through shared memory with a
 // line-fast cooperative loop (used for the transposed side of z passes).
-template <int N, int MODE, int MAP, int LDS, int STS, class Ld, class St>
+// TMA: the staged side moves by TMA instead (tensor maps in tm, bounded wait
+// recorded in *fault; a thread whose wait gave up skips its global stores).
+template <int N, int MODE, int MAP, int LDS, int STS, int TMA, class Ld, class St>
 __device__ __forceinline__ void line_body(const C *__restrict__ tw, const C *__restrict__ tw2, float sign,
-                                          const Ld &ld, const St &st, int ahead) {
+                                          const Ld &ld, const St &st, int ahead, const TmaMaps *tm, int *fault) {
   constexpr int E = Shape<N>::E, TL = Shape<N>::TL, B = Shape<N>::B, LP = Shape<N>::LP;
-  __shared__ C sm[B * LP];
+  typedef TmaTile<N, MODE> TT;
+  static_assert(!TMA || TT::OK, "TMA tile");
+  __shared__ __align__(16) unsigned char smraw[LineSmem<N, MODE, TMA>::BYTES];
+  __shared__ unsigned long long tbar;
+  unsigned char *smb = smraw;
+  if constexpr (TMA) smb += (1024 - (su32(smraw) & 1023)) & 1023;
+  C *sm = reinterpret_cast<C *>(smb);
   const int a = blockIdx.y, b0 = blockIdx.x * B;
   const int t = MAP == MAP_E ? threadIdx.x % TL : threadIdx.x / B;
   const int l = MAP == MAP_E ? threadIdx.x / TL : threadIdx.x % B;
+  bool ok = true;
   C v[E];
   if constexpr (LDS == 0 && split_of<Ld>(0)) {
     typename Ld::Raw raw[E];
@@ -259,26 +366,48 @@ __device__ __forceinline__ void line_body(const C *__restrict__ tw, const C *__r
     for (int q = 0; q < E; q++) v[q] = ld(a, b0 + l, t + TL * q);
     prefetch_ahead<N, MODE, B>(ld, ahead);
   } else {
-    // line-fast cooperative load of the whole tile (C2R: also the Nyquist
-    // element N, which lands in the pitch's spare slot), fully unrolled so
-    // that every load is in flight before the first shared-memory store
-    constexpr int NE = MODE == 2 ? N + 1 : N, TOT = B * NE, IT = (TOT + 255) / 256;
-#pragma unroll
-    for (int it = 0; it < IT; it++) {
-      const int idx = threadIdx.x + it * 256;
-      if (TOT % 256 == 0 || idx < TOT) {
-        const int ll = idx % B, e = idx / B;
-        sm[sidx(ll, e, LP)] = ld(a, b0 + ll, e);
+    if constexpr (TMA) {
+      // the tile's boxes by TMA (one thread), completion on an mbarrier
+      const unsigned sb = su32(smb), mb = su32(&tbar);
+      if (threadIdx.x == 0) {
+        mbar_init(mb, 1);
+        fence_mbar_init();
       }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        mbar_expect_tx(mb, TT::NBOX * TT::ROWS * 128);
+#pragma unroll
+        for (int h = 0; h < TT::NBOX; h++) tma_load_3d(sb + h * TT::BOXB, &tm->load, b0 + 16 * h, a, 0, mb);
+      }
+      ok = mbar_wait(mb, 0, fault);
+      prefetch_ahead<N, MODE, B>(ld, ahead);
+    } else {
+      // line-fast cooperative load of the whole tile (C2R: also the Nyquist
+      // element N, which lands in the pitch's spare slot), fully unrolled so
+      // that every load is in flight before the first shared-memory store
+      constexpr int NE = MODE == 2 ? N + 1 : N, TOT = B * NE, IT = (TOT + 255) / 256;
+#pragma unroll
+      for (int it = 0; it < IT; it++) {
+        const int idx = threadIdx.x + it * 256;
+        if (TOT % 256 == 0 || idx < TOT) {
+          const int ll = idx % B, e = idx / B;
+          sm[sidx(ll, e, LP)] = ld(a, b0 + ll, e);
+        }
+      }
+      prefetch_ahead<N, MODE, B>(ld, ahead);
+      __syncthreads();
     }
-    prefetch_ahead<N, MODE, B>(ld, ahead);
-    __syncthreads();
+    // element e of this thread's line from the staged tile
+    auto staged = [&](int e) -> C {
+      if constexpr (TMA) return *reinterpret_cast<const C *>(smb + (l >> 4) * TT::BOXB + swz128(e, l & 15));
+      else return sm[sidx(l, e, LP)];
+    };
 #pragma unroll
     for (int q = 0; q < E; q++) {
       const int e = t + TL * q;
       if constexpr (MODE == 2) {
         // Z[k] = (X[k] + X*[N-k]) + i w^-k (X[k] - X*[N-k]),  w = exp(-2 pi i / 2N)
-        C xk = sm[sidx(l, e, LP)], xm = sm[sidx(l, N - e, LP)];
+        C xk = staged(e), xm = staged(N - e);
         if (e == 0) { xk.y = 0.f; xm.y = 0.f; }
         const C sum = make_float2(xk.x + xm.x, xk.y - xm.y), dif = make_float2(xk.x - xm.x, xk.y + xm.y);
         C w = __ldg(&tw2[e]);
@@ -286,7 +415,7 @@ __device__ __forceinline__ void line_body(const C *__restrict__ tw, const C *__r
         const C tt = cmul(dif, w);
         v[q] = make_float2(sum.x - tt.y, sum.y + tt.x);
       } else {
-        v[q] = sm[sidx(l, e, LP)];
+        v[q] = staged(e);
       }
     }
     __syncthreads();
@@ -297,13 +426,55 @@ __device__ __forceinline__ void line_body(const C *__restrict__ tw, const C *__r
   }
   transform<N>(v, t, l, sign, tw, sm);
   if constexpr (STS == 0) {
+    if (ok) {
 #pragma unroll
-    for (int j = 0; j < E; j++) st(a, b0 + l, final_pos<N>(t, j), v[j]);
+      for (int j = 0; j < E; j++) st(a, b0 + l, final_pos<N>(t, j), v[j]);
+    }
   } else {
 #pragma unroll
     for (int j = 0; j < E; j++) sm[sidx(l, final_pos<N>(t, j), LP)] = v[j];
     __syncthreads();
-    if constexpr (MODE == 1) {
+    if constexpr (TMA) {
+      // the output tile in registers first (the boxes overlay the exchange
+      // buffer), then into the swizzled boxes and out by TMA
+      constexpr int TOT = MODE == 1 ? B * (N / 2 + 1) : B * N, IT = (TOT + 255) / 256;
+      C xa[IT], xb[IT];
+#pragma unroll
+      for (int it = 0; it < IT; it++) {
+        const int idx = threadIdx.x + it * 256;
+        if (idx < TOT) {
+          const int ll = idx % B, k = idx / B;
+          if constexpr (MODE == 1) {
+            const C zk = sm[sidx(ll, k, LP)], zm = sm[sidx(ll, k == 0 ? 0 : N - k, LP)];
+            const C sum = make_float2(zk.x + zm.x, zk.y - zm.y), dif = make_float2(zk.x - zm.x, zk.y + zm.y);
+            const C tt = cmul(dif, __ldg(&tw2[k]));
+            xa[it] = make_float2(0.5f * (sum.x + tt.y), 0.5f * (sum.y - tt.x));
+            xb[it] = make_float2(0.5f * (sum.x - tt.y), -0.5f * (sum.y + tt.x));
+          } else {
+            xa[it] = sm[sidx(ll, k, LP)];
+          }
+        }
+      }
+      __syncthreads();
+#pragma unroll
+      for (int it = 0; it < IT; it++) {
+        const int idx = threadIdx.x + it * 256;
+        if (idx < TOT) {
+          const int ll = idx % B, k = idx / B;
+          unsigned char *box = smb + (ll >> 4) * TT::BOXB;
+          *reinterpret_cast<C *>(box + swz128(k, ll & 15)) = xa[it];
+          if (MODE == 1 && k != N / 2) *reinterpret_cast<C *>(box + swz128(N - k, ll & 15)) = xb[it];
+        }
+      }
+      fence_proxy_async();   // the generic-proxy writes above, visible to the TMA store
+      __syncthreads();
+      if (threadIdx.x == 0) {
+#pragma unroll
+        for (int h = 0; h < TT::NBOX; h++) tma_store_3d(&tm->store, b0 + 16 * h, a, 0, su32(smb) + h * TT::BOXB);
+        bulk_commit();
+        bulk_wait_read();   // the boxes have been read before the CTA's shared memory is released
+      }
+    } else if constexpr (MODE == 1) {
       // X[k] = (Z[k] + Z*[N-k]) / 2 - (i/2) w^k (Z[k] - Z*[N-k]),  k = 0..N, in
       // pairs: with sum = Z[k] + Z*[N-k] and tt = w^k (Z[k] - Z*[N-k]),
       // X[k] = (sum - i tt) / 2 and X[N-k] = conj(sum + i tt) / 2 (w^N = -1),
@@ -334,25 +505,28 @@ __device__ __forceinline__ void line_body(const C *__restrict__ tw, const C *__r
   }
 }
 
-template <int N, int MODE, int MAP, int LDS, int STS, class Ld, class St>
+template <int N, int MODE, int MAP, int LDS, int STS, int TMA, class Ld, class St>
 __global__ void __launch_bounds__(256) line_kernel(const C *__restrict__ tw, const C *__restrict__ tw2, float sign,
-                                                   const Ld ld, const St st, int ahead) {
-  line_body<N, MODE, MAP, LDS, STS>(tw, tw2, sign, ld, st, ahead);
+                                                   const Ld ld, const St st, int ahead,
+                                                   const __grid_constant__ TmaMaps tm, int *fault) {
+  line_body<N, MODE, MAP, LDS, STS, TMA>(tw, tw2, sign, ld, st, ahead, &tm, fault);
 }
 // Passes whose store functor asks for it (kBoundedStore: the inverse phase
 // pass, whose operand loads follow the transform): bounded to 48 registers,
 // 5 CTAs per SM, to hide their latency.
-template <int N, int MODE, int MAP, int LDS, int STS, class Ld, class St>
+template <int N, int MODE, int MAP, int LDS, int STS, int TMA, class Ld, class St>
 __global__ void __launch_bounds__(256, 5) line_kernel_stsplit(const C *__restrict__ tw, const C *__restrict__ tw2,
-                                                              float sign, const Ld ld, const St st, int ahead) {
-  line_body<N, MODE, MAP, LDS, STS>(tw, tw2, sign, ld, st, ahead);
+                                                              float sign, const Ld ld, const St st, int ahead,
+                                                              const __grid_constant__ TmaMaps tm, int *fault) {
+  line_body<N, MODE, MAP, LDS, STS, TMA>(tw, tw2, sign, ld, st, ahead, &tm, fault);
 }
 // Split loads hold all of a thread's operands (two complex per element) at
 // once; the bound keeps them to 80 registers, 3 CTAs per SM, without spills.
-template <int N, int MODE, int MAP, int LDS, int STS, class Ld, class St>
+template <int N, int MODE, int MAP, int LDS, int STS, int TMA, class Ld, class St>
 __global__ void __launch_bounds__(256, 3) line_kernel_split(const C *__restrict__ tw, const C *__restrict__ tw2,
-                                                            float sign, const Ld ld, const St st, int ahead) {
-  line_body<N, MODE, MAP, LDS, STS>(tw, tw2, sign, ld, st, ahead);
+                                                            float sign, const Ld ld, const St st, int ahead,
+                                                            const __grid_constant__ TmaMaps tm, int *fault) {
+  line_body<N, MODE, MAP, LDS, STS, TMA>(tw, tw2, sign, ld, st, ahead, &tm, fault);
 }
 
 // --------------------------------------------------------------- x pencils
@@ -591,6 +765,57 @@ __global__ void __launch_bounds__(256) xkinetic_kernel(const C *__restrict__ tw,
   for (int j = 0; j < E; j++) base[(size_t) final_pos<N>(t, j) * ny] = v[j];
 }
 
+// --------------------------------------------------------------- factorised kinetic passes
+// exp(cdt |k - k0|^2) is a product of one factor per axis, and the 3-D DFT is
+// the product of the three 1-D DFTs, so F^-1 K F = prod_a (F_a^-1 K_a F_a):
+// the kinetic step of the split-operator propagator runs as one pass per axis,
+// each a line FFT, the factor exp(cdt (k_a - k0_a)^2) / n_a applied as
+// v + v f (f = exp(.) - 1, tabulated per CTA in shared memory), and the
+// inverse line FFT.  Every pass reads and writes the wave function in its own
+// [x][y][z] layout (no transposed spectra): z rows (element-fast), y and x
+// lines strided with B consecutive z per CTA (line-fast).  The potential
+// half steps are the load functor of the z pass and the store functor of the
+// x pass.  Bounds: MINB CTAs per SM (split load / bounded store variants).
+template <int N, int MAP, int MINB, class Ld, class St>
+__global__ void __launch_bounds__(256, MINB) line_kin_kernel(const C *__restrict__ tw, float2 cdt, float inv_n, float dk,
+                                                             float k0, const Ld ld, const St st, int ahead) {
+  constexpr int E = Shape<N>::E, TL = Shape<N>::TL, B = Shape<N>::B, LP = Shape<N>::LP;
+  __shared__ C sm[B * LP];
+  __shared__ C fk[N];   // exp(cdt (k - k0)^2) - 1
+  const int a = blockIdx.y, b0 = blockIdx.x * B;
+  const int t = MAP == MAP_E ? threadIdx.x % TL : threadIdx.x / B;
+  const int l = MAP == MAP_E ? threadIdx.x / TL : threadIdx.x % B;
+  C v[E];
+  if constexpr (split_of<Ld>(0)) {
+    typename Ld::Raw raw[E];
+#pragma unroll
+    for (int q = 0; q < E; q++) raw[q] = ld.fetch(a, b0 + l, t + TL * q);
+    prefetch_ahead<N, 0, B>(ld, ahead);
+#pragma unroll
+    for (int q = 0; q < E; q++) v[q] = ld.cook(raw[q]);
+  } else {
+#pragma unroll
+    for (int q = 0; q < E; q++) v[q] = ld(a, b0 + l, t + TL * q);
+    prefetch_ahead<N, 0, B>(ld, ahead);
+  }
+  for (int e = threadIdx.x; e < N; e += 256) {
+    const float k = (float) (e < (N + 1) / 2 ? e : e - N) * dk - k0;
+    fk[e] = cexpm1(make_float2(cdt.x * (k * k), cdt.y * (k * k)));
+  }
+  if constexpr (split_of<St>(0)) {
+#pragma unroll
+    for (int j = 0; j < E; j++) st.prefetch(a, b0 + l, final_pos<N>(t, j));
+  }
+  transform<N>(v, t, l, -1.f, tw, sm);
+  __syncthreads();      // fk complete (the transform's own barriers precede its last stage)
+#pragma unroll
+  for (int j = 0; j < E; j++) v[j] = mul_1p(make_float2(v[j].x * inv_n, v[j].y * inv_n), fk[final_pos<N>(t, j)]);
+  to_input_order<N>(v);
+  transform<N>(v, t, l, 1.f, tw, sm);
+#pragma unroll
+  for (int j = 0; j < E; j++) st(a, b0 + l, final_pos<N>(t, j), v[j]);
+}
+
 // --------------------------------------------------------------- fused z + y plane passes
 // The z and y passes of a real field's 3-D transform done by one cluster of
 // CL CTAs per x plane, so the half spectrum crosses HBM once instead of
@@ -627,59 +852,6 @@ template <int NY, int NZ, int CL> struct ZYPlane {
   static_assert(NZC % 16 == 0 && NY % 16 == 0, "staged pitches stay 16-byte multiples");
 };
 
-__device__ __forceinline__ unsigned su32(const void *p) { return (unsigned) __cvta_generic_to_shared(p); }
-__device__ __forceinline__ unsigned cl_addr(unsigned a, unsigned rank) {   // shared::cluster address in CTA rank
-  unsigned r;
-  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
-  return r;
-}
-__device__ __forceinline__ void mbar_init(unsigned bar, unsigned count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
-__device__ __forceinline__ void mbar_expect_tx(unsigned bar, unsigned bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned parity) {
-  unsigned ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(bar), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-__device__ __forceinline__ unsigned long long gtimer() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-// Wait for the completion of phase `parity`; after 0.5 s the wait gives up,
-// records the failure in *fault (read by the host after the launch) and
-// returns false.  A thread whose wait gave up skips its global stores, and
-// every CTA ends with a cluster barrier, so no CTA exits before each peer has
-// passed its own bounded waits.
-__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity, int *fault) {
-  if (mbar_try_wait(bar, parity)) return true;
-  const unsigned long long t0 = gtimer();
-  while (!mbar_try_wait(bar, parity)) {
-    if (gtimer() - t0 > 500000000ull) { atomicExch(fault, 1); return false; }
-  }
-  return true;
-}
-__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-__device__ __forceinline__ void bulk_g2s(unsigned dst, const void *src, unsigned bytes, unsigned bar) {
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-               ::"r"(dst), "l"(src), "r"(bytes), "r"(bar)
-               : "memory");
-}
-__device__ __forceinline__ void bulk_s2c(unsigned dst, unsigned src, unsigned bytes, unsigned bar) {
-  asm volatile("cp.async.bulk.shared::cluster.shared::cta.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-               ::"r"(dst), "r"(src), "r"(bytes), "r"(bar)
-               : "memory");
-}
-__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
 
 // forward: real field f[x][y][z] -> spec[kz][x][y], kz = 0..NZC
 template <int NY, int NZ, int CL>

@@ -6,6 +6,8 @@
 #include <mutex>
 #include <utility>
 
+#include <cudaTypedefs.h>
+
 #include "fft.cuh"
 #include "ops.cuh"
 
@@ -129,6 +131,57 @@ bool prefetch_ahead_on() {
     v = (e && e[0] == '0') ? 0 : 1;
   }
   return v == 1;
+}
+
+bool factorised_propagation() {
+  static int v = -1;
+  if (v < 0) {
+    const char *e = getenv("DFTGPU_FACTORISED_PROP");
+    v = (e && e[0] == '1') ? 1 : 0;
+  }
+  return v == 1;
+}
+
+namespace {
+int g_tma = -1;
+}
+bool tma_on() {
+  if (g_tma < 0) {
+    const char *e = getenv("DFTGPU_TMA");
+    g_tma = (e && e[0] == '0') ? 0 : 1;
+  }
+  return g_tma == 1;
+}
+void tma_disable() { g_tma = 0; }
+
+namespace {
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+}
+
+int encode_spec_map(CUtensorMap *map, const void *spec, int nx, int ny, int rows) {
+  if (!g_encode) {
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn) {
+      cudaGetLastError();
+      set_error(DFTGPU_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+      return DFTGPU_ERR_CUDA;
+    }
+    g_encode = (PFN_cuTensorMapEncodeTiled_v12000) fn;
+  }
+  // [rows][nx][ny] of 8-byte elements; box {16 y, 1 x, rows}: 128-byte rows
+  const cuuint64_t dims[3] = { (cuuint64_t) ny, (cuuint64_t) nx, (cuuint64_t) rows };
+  const cuuint64_t strides[2] = { (cuuint64_t) ny * 8, (cuuint64_t) nx * ny * 8 };
+  const cuuint32_t box[3] = { 16, 1, (cuuint32_t) rows }, estr[3] = { 1, 1, 1 };
+  const CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, const_cast<void *>(spec), dims, strides, box, estr,
+                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    set_error(DFTGPU_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d) for a %d x %d x %d spectrum", (int) r, rows, nx, ny);
+    return DFTGPU_ERR_CUDA;
+  }
+  return DFTGPU_OK;
 }
 
 bool generic_fft_only() {
@@ -323,7 +376,7 @@ template int launch_xkinetic<double>(KinArgs<double> &);
 // ------------------------------------------------------------------ fused z + y passes
 namespace {
 
-int *g_zy_fault = nullptr;   // set by a fused kernel whose barrier wait gave up
+int *g_zy_fault = nullptr;   // set by a kernel whose wait on an asynchronous copy gave up
 
 template <int NY, int NZ, int CL, bool FWD, class Kern, class... Args>
 int launch_zy_cluster(Kern kfn, int nx, Args... args) {
@@ -333,10 +386,7 @@ int launch_zy_cluster(Kern kfn, int nx, Args... args) {
     DFT_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, Z::SMEM));
     attr_done = true;
   }
-  if (!g_zy_fault) {
-    DFT_CUDA(cudaMalloc(&g_zy_fault, sizeof(int)));
-    DFT_CUDA(cudaMemset(g_zy_fault, 0, sizeof(int)));
-  }
+  if (!async_fault_flag()) return DFTGPU_ERR_CUDA;
   FftPlan<float> pz, p2, py;
   DFT_TRY(get_plan<float>(Z::NZC, &pz));
   DFT_TRY(get_plan<float>(NZ, &p2));
@@ -373,13 +423,25 @@ bool fused_shape(int ny, int nz) {
 
 }  // namespace
 
+int *async_fault_flag() {
+  if (!g_zy_fault) {
+    if (cudaMalloc(&g_zy_fault, sizeof(int)) != cudaSuccess || cudaMemset(g_zy_fault, 0, sizeof(int)) != cudaSuccess) {
+      cudaGetLastError();
+      g_zy_fault = nullptr;
+      set_error(DFTGPU_ERR_CUDA, "asynchronous-copy fault flag");
+      return nullptr;
+    }
+  }
+  return g_zy_fault;
+}
+
 int fused_zy_fault() {
   if (!g_zy_fault) return DFTGPU_OK;
   int v = 0;
   DFT_CUDA(cudaMemcpy(&v, g_zy_fault, sizeof(int), cudaMemcpyDeviceToHost));
   if (v) {
     cudaMemset(g_zy_fault, 0, sizeof(int));
-    set_error(DFTGPU_ERR_CUDA, "fused plane pass: a barrier wait timed out");
+    set_error(DFTGPU_ERR_CUDA, "a wait on an asynchronous copy (TMA or fused plane pass) timed out");
     return DFTGPU_ERR_CUDA;
   }
   return DFTGPU_OK;

@@ -19,6 +19,8 @@
 // FP64 on the host and rounded once to the bulk precision.
 #pragma once
 
+#include <string.h>
+
 #include <type_traits>
 
 #include "common.cuh"
@@ -421,6 +423,7 @@ template <class Kernel> bool SmemOptIn<Kernel>::done = false;
 
 bool generic_fft_only();   // DFTGPU_GENERIC_FFT=1 disables the register kernels
 bool prefetch_ahead_on();  // DFTGPU_PREFETCH_AHEAD=0 disables the one-wave-ahead L2 prefetch
+bool factorised_propagation();  // DFTGPU_FACTORISED_PROP=1: FP32 propagation by one kinetic pass per axis
 
 // CTAs of a 256-thread kernel resident on the whole GPU at once (the distance
 // of the line kernels' one-wave-ahead prefetch); 0 when prefetching is off.
@@ -433,6 +436,37 @@ template <class K> int resident_ctas(K kernel) {
     n = per_sm * rt().num_sms;
   }
   return n;
+}
+
+// TMA for the transposed side of the z passes (DFTGPU_TMA=0 turns it off)
+bool tma_on();
+void tma_disable();
+// Tensor map over a spectral buffer [rows][nx][ny] of complex FP32 values
+// (8-byte elements) with boxes {16 y, 1 x, rows} and the 128-byte swizzle.
+int encode_spec_map(CUtensorMap *map, const void *spec, int nx, int ny, int rows);
+// Device flag set by a kernel whose bounded wait on an asynchronous copy gave
+// up (read and cleared by dftgpu_synchronize and the device-to-host copies).
+int *async_fault_flag();
+
+// Functors of the spectral layout [kz][x][y] used by z passes (kSpecZ: members
+// spec, nx, ny), whose staged side may move by TMA.
+template <class F> __host__ __device__ constexpr auto spec_z_of(int) -> decltype(F::kSpecZ, bool()) { return F::kSpecZ; }
+template <class F> __host__ __device__ constexpr bool spec_z_of(long) { return false; }
+
+template <int N, int MODE, int MAP, int LDS, int STS, int TMA, class Ld, class St>
+void launch_line_kernel(int na, int nb, const float2 *tw, const float2 *tw2, float sign, const Ld &ld, const St &st,
+                        const ff::TmaMaps &tm, int *fault) {
+  constexpr int B = ff::Shape<N>::B;
+  if constexpr (LDS == 0 && ff::split_of<Ld>(0)) {
+    auto k = ff::line_kernel_split<N, MODE, MAP, LDS, STS, TMA, Ld, St>;
+    k<<<dim3(nb / B, na), 256, 0, rt().stream>>>(tw, tw2, sign, ld, st, resident_ctas(k), tm, fault);
+  } else if constexpr (STS == 0 && ff::bounded_store_of<St>(0)) {
+    auto k = ff::line_kernel_stsplit<N, MODE, MAP, LDS, STS, TMA, Ld, St>;
+    k<<<dim3(nb / B, na), 256, 0, rt().stream>>>(tw, tw2, sign, ld, st, resident_ctas(k), tm, fault);
+  } else {
+    auto k = ff::line_kernel<N, MODE, MAP, LDS, STS, TMA, Ld, St>;
+    k<<<dim3(nb / B, na), 256, 0, rt().stream>>>(tw, tw2, sign, ld, st, resident_ctas(k), tm, fault);
+  }
 }
 
 // FP32 power-of-two lengths: register-resident kernel.  EF / EFS: the fast
@@ -451,18 +485,63 @@ int launch_fast_lines(int na, int nb, float sign, const Ld &ld, const St &st) {
   DFT_TRY(get_plan<float>(N, &p1));
   p2.tw = nullptr;
   if (MODE != LINE_C2C) DFT_TRY(get_plan<float>(2 * N, &p2));
-  if constexpr (LDS == 0 && ff::split_of<Ld>(0)) {
-    auto k = ff::line_kernel_split<N, MODE, MAP, LDS, STS, Ld, St>;
-    k<<<dim3(nb / B, na), 256, 0, rt().stream>>>(p1.tw, p2.tw, sign, ld, st, resident_ctas(k));
-  } else if constexpr (STS == 0 && ff::bounded_store_of<St>(0)) {
-    auto k = ff::line_kernel_stsplit<N, MODE, MAP, LDS, STS, Ld, St>;
-    k<<<dim3(nb / B, na), 256, 0, rt().stream>>>(p1.tw, p2.tw, sign, ld, st, resident_ctas(k));
-  } else {
-    auto k = ff::line_kernel<N, MODE, MAP, LDS, STS, Ld, St>;
-    k<<<dim3(nb / B, na), 256, 0, rt().stream>>>(p1.tw, p2.tw, sign, ld, st, resident_ctas(k));
+  ff::TmaMaps tm;
+  memset(&tm, 0, sizeof(tm));
+  constexpr bool TMA_LD = LDS && spec_z_of<Ld>(0) && ff::TmaTile<N, MODE>::OK;
+  constexpr bool TMA_ST = STS && spec_z_of<St>(0) && ff::TmaTile<N, MODE>::OK;
+  if constexpr (TMA_LD || TMA_ST) {
+    if (tma_on()) {
+      constexpr int ROWS = ff::TmaTile<N, MODE>::ROWS;
+      int rc = DFTGPU_OK;
+      if constexpr (TMA_LD) rc = encode_spec_map(&tm.load, ld.spec, ld.nx, ld.ny, ROWS);
+      if constexpr (TMA_ST) if (!rc) rc = encode_spec_map(&tm.store, st.spec, st.nx, st.ny, ROWS);
+      int *fault = rc ? nullptr : async_fault_flag();
+      if (fault) {
+        launch_line_kernel<N, MODE, MAP, LDS, STS, 1>(na, nb, p1.tw, p2.tw, sign, ld, st, tm, fault);
+        DFT_CHECK_LAUNCH();
+        return DFTGPU_OK;
+      }
+      tma_disable();   // no tensor maps here: the load / store loops from now on
+      g_last_error = 0;   // the encode failure is not the caller's error
+    }
   }
+  launch_line_kernel<N, MODE, MAP, LDS, STS, 0>(na, nb, p1.tw, p2.tw, sign, ld, st, tm, nullptr);
   DFT_CHECK_LAUNCH();
   return DFTGPU_OK;
+}
+
+// One factorised kinetic pass (ff::line_kin_kernel) over na x nb lines of
+// length N: line-fast (MAP_L) when the lines are strided with consecutive
+// lines adjacent, element-fast (MAP_E) for contiguous rows.  Returns -1 when
+// the shape does not fit (nb not a multiple of the CTA's line count).
+template <int N, int MAP, class Ld, class St>
+int launch_kin_lines(int na, int nb, float2 cdt, float inv_n, float dk, float k0, const Ld &ld, const St &st) {
+  constexpr int B = ff::Shape<N>::B;
+  if (nb % B) return -1;
+  FftPlan<float> p;
+  DFT_TRY(get_plan<float>(N, &p));
+  // two transforms and the factor table: rows bounded to 80 registers (3 CTAs
+  // per SM); strided lines keep a runtime-stride address per element and get
+  // 128 (2 CTAs per SM) so that they do not spill
+  auto k = ff::line_kin_kernel<N, MAP, (MAP == ff::MAP_E || !ff::bounded_store_of<St>(0)) ? 3 : 2, Ld, St>;
+  k<<<dim3(nb / B, na), 256, 0, rt().stream>>>(p.tw, cdt, inv_n, dk, k0, ld, st, resident_ctas(k));
+  DFT_CHECK_LAUNCH();
+  return DFTGPU_OK;
+}
+
+template <int MAP, class Ld, class St>
+int launch_kin_pass(int n, int na, int nb, float2 cdt, float dk, float k0, const Ld &ld, const St &st, const char *name,
+                    double bytes) {
+  if (generic_fft_only()) return -1;
+  if (n != 64 && n != 128 && n != 256 && n != 512) return -1;
+  ProfScope prof(name, bytes);
+  const float inv_n = 1.f / (float) n;
+  switch (n) {
+    case 64: return launch_kin_lines<64, MAP>(na, nb, cdt, inv_n, dk, k0, ld, st);
+    case 128: return launch_kin_lines<128, MAP>(na, nb, cdt, inv_n, dk, k0, ld, st);
+    case 256: return launch_kin_lines<256, MAP>(na, nb, cdt, inv_n, dk, k0, ld, st);
+    default: return launch_kin_lines<512, MAP>(na, nb, cdt, inv_n, dk, k0, ld, st);
+  }
 }
 
 // extra_bytes: algorithmic bytes read / written by the fused functors beyond

@@ -188,12 +188,16 @@ void *dev_alloc(size_t bytes) {
 
 void dev_free(void *p) { if (p) cudaFree(p); }
 
+// Grid dimensions: 2^a 3^b 5^c in [2, FFT_MAX_N]; x and y may be odd (libdft's
+// largest production grid is 729 x 384 x 384, examples/gas-bubble/config.h:56),
+// z must be even (real fields are transformed as packed pairs along z).
 int check_dims(INT nx, INT ny, INT nz) {
   INT d[3] = { nx, ny, nz };
   for (int i = 0; i < 3; i++) {
     INT m = d[i];
-    if (m < 2 || m > FFT_MAX_N || (m & 1)) {
-      set_error(DFTGPU_ERR_SIZE, "grid dimension %ld must be even and in [2, %d]", (long) m, FFT_MAX_N);
+    if (m < 2 || m > FFT_MAX_N || (i == 2 && (m & 1))) {
+      set_error(DFTGPU_ERR_SIZE, "grid dimension %ld must be in [2, %d]%s", (long) m, FFT_MAX_N,
+                i == 2 ? " and even along z" : "");
       return DFTGPU_ERR_SIZE;
     }
     while (m % 2 == 0) m /= 2;
@@ -257,10 +261,94 @@ template <typename T> struct PhaseStore {
   }
 };
 
+// Functors of the factorised kinetic passes (FP32 register FFTs): the wave
+// function stays in its [x][y][z] layout; (a, b, e) = (x, y, z) for the z
+// rows, (x, z, y) for the y lines and (y, z, x) for the x lines.
+struct RowStoreF {   // z rows
+  float2 *f; int ny, nz;
+  __device__ void operator()(int x, int y, int z, float2 v) const { f[((size_t) x * ny + y) * nz + z] = v; }
+};
+// (32-bit element offsets: grids of up to 2^31 points; a 64-bit address per
+// element of a strided line costs two registers each across the transform)
+struct LineYF {      // y lines, B consecutive z per CTA
+  static constexpr bool kAhead = true;
+  float2 *f; int ny, nz;
+  __device__ void prefetch_lines(int x, int z0, int nl, int ne) const {   // one run of nl values per y
+    for (int y = threadIdx.x; y < ne; y += blockDim.x) prefetch_bulk_l2(f + ((unsigned) (x * ny + y) * (unsigned) nz + z0), (size_t) nl * sizeof(float2));
+  }
+  __device__ float2 operator()(int x, int z, int y) const { return f[(unsigned) (x * ny + y) * (unsigned) nz + z]; }
+  __device__ void operator()(int x, int z, int y, float2 v) const { f[(unsigned) (x * ny + y) * (unsigned) nz + z] = v; }
+};
+struct LineXF {      // x lines, B consecutive z per CTA
+  static constexpr bool kAhead = true;
+  const float2 *f; int nx, ny, nz;
+  __device__ void prefetch_lines(int y, int z0, int nl, int ne) const {   // one run of nl values per x
+    for (int x = threadIdx.x; x < ne; x += blockDim.x) prefetch_bulk_l2(f + ((unsigned) (x * ny + y) * (unsigned) nz + z0), (size_t) nl * sizeof(float2));
+  }
+  __device__ float2 operator()(int y, int z, int x) const { return f[(unsigned) (x * ny + y) * (unsigned) nz + z]; }
+};
+struct PhaseStoreXF {   // x lines: psi <- v exp(-i V dt / 2)
+  static constexpr bool kSplit = true, kBoundedStore = true;
+  float2 *psi; const float2 *V; int ny, nz; float hr, hi;
+  __device__ void prefetch(int y, int z, int x) const {
+    const unsigned i = (unsigned) (x * ny + y) * (unsigned) nz + z;
+    if ((i & 3) == 0) prefetch_l2(V + i);   // one per 32-byte sector
+  }
+  __device__ void operator()(int y, int z, int x, float2 val) const {
+    const unsigned i = (unsigned) (x * ny + y) * (unsigned) nz + z;
+    const float2 v = __ldg(V + i);
+    psi[i] = mul_cexp(val, make_float2(v.x * hi + v.y * hr, -(v.x * hr - v.y * hi)));
+  }
+};
+
+// The factorised kinetic passes fit when every axis is a register-FFT length
+// and each pass's line count is a multiple of its CTA's lines.
+static bool kin_fits(int nx, int ny, int nz) {
+  auto ok = [](int n) { return n == 64 || n == 128 || n == 256 || n == 512; };
+  auto lines = [](int n) { return n == 64 ? 32 : 256 / (n / 16); };   // ff::Shape<n>::B
+  return !generic_fft_only() && ok(nx) && ok(ny) && ok(nz) && ny % lines(nz) == 0 && nz % lines(ny) == 0 &&
+         nz % lines(nx) == 0;
+}
+
+// dst = S(V, dt) src in three passes (FP32, register-FFT lengths):
+//   z: rows of src times exp(-i V dt/2), FFT_z, exp(cdt (kz - kz0)^2)/nz, FFT_z^-1 -> dst
+//   y: FFT_y, exp(cdt (ky - ky0)^2)/ny, FFT_y^-1 (in place)
+//   x: FFT_x, exp(cdt (kx - kx0)^2)/nx, FFT_x^-1, times exp(-i V dt/2) (in place)
+// The same operator as the five-pass form below (F^-1 K F factorises per
+// axis); it moves the wave function through HBM three times instead of five,
+// but its strided y and x passes (128-byte runs, every run in another DRAM
+// page) run at 2.6-3.4 TB/s against 5-6.7 for the contiguous passes of the
+// five-pass form: 317 against 300 us per propagation at 256^3, so it is
+// opt-in (DFTGPU_FACTORISED_PROP=1).
+static int strang_factorised(wf *g, cgrid *dst, cgrid *src, cgrid *V, double dr, double di) {
+  const int nx = (int) src->nx, ny = (int) src->ny, nz = (int) src->nz;
+  const double m = g->mass, step = src->step;
+  const cgrid *mg = g->grid;   // moving-background momentum of the wave function
+  const float2 cdt = make_float2((float) (di / (2.0 * m)), (float) (-dr / (2.0 * m)));   // -i dt / 2m
+  const float hr = (float) (0.5 * dr), hi = (float) (0.5 * di);
+  const double nb = (double) nx * ny * nz * sizeof(float2);
+  float2 *out = (float2 *) dst->value;
+  const float2 *pot = (const float2 *) V->value;
+  PhaseLoad<float> ld{(const float2 *) src->value, pot, ny, nz, hr, hi};
+  RowStoreF sz{out, ny, nz};
+  DFT_TRY(launch_kin_pass<ff::MAP_E>(nz, nx, ny, cdt, (float) (2.0 * M_PI / (nz * step)), (float) mg->kz0, ld, sz,
+                                     "prop_kin_z", 3.0 * nb));
+  LineYF ly{out, ny, nz};
+  DFT_TRY(launch_kin_pass<ff::MAP_L>(ny, nx, nz, cdt, (float) (2.0 * M_PI / (ny * step)), (float) mg->ky0, ly, ly,
+                                     "prop_kin_y", 2.0 * nb));
+  LineXF lx{out, nx, ny, nz};
+  PhaseStoreXF sx{out, pot, ny, nz, hr, hi};
+  return launch_kin_pass<ff::MAP_L>(nx, ny, nz, cdt, (float) (2.0 * M_PI / (nx * step)), (float) mg->kx0, lx, sx,
+                                    "prop_kin_x", 3.0 * nb);
+}
+
 // dst = S(V, dt) src, through the wave function's spectral scratch buffer
 template <typename T> int strang(wf *g, cgrid *dst, cgrid *src, cgrid *V, double dr, double di) {
   typedef typename cplx_t<T>::type C;
   const int nx = (int) src->nx, ny = (int) src->ny, nz = (int) src->nz;
+  if constexpr (std::is_same<T, float>::value) {
+    if (factorised_propagation() && kin_fits(nx, ny, nz)) return strang_factorised(g, dst, src, V, dr, di);
+  }
   C *spec = (C *) wf_spec(g);
   if (!spec) return DFTGPU_ERR_NOMEM;
   const T hr = (T) (0.5 * dr), hi = (T) (0.5 * di);
@@ -287,6 +375,55 @@ int propagate(wf *g, cgrid *dst, cgrid *src, cgrid *V, double dr, double di) {
     return DFTGPU_ERR_ARG;
   }
   return src->prec == DFTGPU_FP32 ? strang<float>(g, dst, src, V, dr, di) : strang<double>(g, dst, src, V, dr, di);
+}
+
+// ------------------------------------------------------------------ absorbing boundary
+// weight of the boundary layer along one axis: (l - i) / l below l, (i - h + 1) / (n - h) from h on
+__device__ __forceinline__ double abs_ramp(int i, int l, int h, int n) {
+  if (i < l) return (double) (l - i) / (double) l;
+  if (i >= h) return (double) (i - h + 1) / (double) (n - h);
+  return 0.0;
+}
+
+template <typename T> static int absorb_add_t(cgrid *dst, const cgrid *pot, const cgrid *psi, const AbsBoundary &b,
+                                              double amp, double rho0) {
+  typedef typename cplx_t<T>::type C;
+  C *d = (C *) dst->value;
+  const C *p = (const C *) pot->value, *w = (const C *) psi->value;
+  const int nx = (int) psi->nx, ny = (int) psi->ny, nz = (int) psi->nz;
+  const int lx = b.lo[0], hx = b.hi[0], ly = b.lo[1], hy = b.hi[1], lz = b.lo[2], hz = b.hi[2];
+  const double irho = 1.0 / rho0;
+  return launch_rows(nx, ny, nz, [=] __device__(int x, int y, int z, int i) {
+    double lam = abs_ramp(x, lx, hx, nx);
+    lam = fmax(lam, abs_ramp(y, ly, hy, ny));
+    lam = fmax(lam, abs_ramp(z, lz, hz, nz));
+    C v = p[i];
+    if (lam > 0.0) {
+      const C a = w[i];
+      v.y -= (T) (amp * lam * (((double) a.x * a.x + (double) a.y * a.y) * irho - 1.0));
+    }
+    d[i] = v;
+  }, 5.0 * gsize(psi) * sizeof(T), "absorb");
+}
+
+int absorb_add(cgrid *dst, const cgrid *pot, const cgrid *psi, const AbsBoundary &b, double amp, double rho0) {
+  return psi->prec == DFTGPU_FP32 ? absorb_add_t<float>(dst, pot, psi, b, amp, rho0)
+                                  : absorb_add_t<double>(dst, pot, psi, b, amp, rho0);
+}
+
+int propagate_pc(wf *g, cgrid *dst, cgrid *src, cgrid *V, double dr, double di) {
+  WfPriv *p = (WfPriv *) g->priv;
+  if (!p || !p->abs.on) return propagate(g, dst, src, V, dr, di);
+  if (!p->vtot) {
+    const cgrid *c = g->grid;
+    p->vtot = (cgrid *) calloc(1, sizeof(cgrid));
+    if (!p->vtot) return DFTGPU_ERR_NOMEM;
+    *p->vtot = *c;
+    p->vtot->value = dev_alloc(gsize(c) * 2 * elem_size(c->prec));
+    if (!p->vtot->value) { free(p->vtot); p->vtot = nullptr; return DFTGPU_ERR_NOMEM; }
+  }
+  DFT_TRY(absorb_add(p->vtot, V, src, p->abs, p->abs.amp, p->abs.rho0));
+  return propagate(g, dst, src, p->vtot, dr, di);
 }
 
 // ------------------------------------------------------------------ spectra of psi
@@ -327,17 +464,22 @@ int kinetic_energy(wf *g, double *out) {
 
 // sum |psi|^2 dV: each reduction item is a run of 8 consecutive values summed
 // in the grid's precision (FP32: within 8 ulps of the run's sum), runs are
-// accumulated in FP64 -- one FP64 add per 8 values instead of per value.
-// Grid sizes are products of three even numbers, so 8 divides the count.
+// accumulated in FP64 -- one FP64 add per 8 values instead of per value.  The
+// last run is short when 8 does not divide the count (odd x and y sizes).
 template <typename T> int norm_dev_t(cgrid *c, double *slot) {
   typedef typename cplx_t<T>::type C;
   const C *p = (const C *) c->value;
   const double dv = c->step * c->step * c->step;
-  return reduce_dev<1>(gsize(c) / 8, [=] __device__(size_t r, double *v) {
+  const size_t n = gsize(c), runs = (n + 7) / 8;
+  return reduce_dev<1>(runs, [=] __device__(size_t r, double *v) {
     const C *q = p + 8 * r;
     T s = (T) 0;
+    if (8 * r + 8 <= n) {
 #pragma unroll
-    for (int k = 0; k < 8; k++) { const C z = q[k]; s += z.x * z.x + z.y * z.y; }
+      for (int k = 0; k < 8; k++) { const C z = q[k]; s += z.x * z.x + z.y * z.y; }
+    } else {
+      for (size_t k = 0; 8 * r + k < n; k++) { const C z = q[k]; s += z.x * z.x + z.y * z.y; }
+    }
     v[0] = (double) s;
   }, slot, dv);
 }

@@ -8,9 +8,28 @@ namespace dftgpu {
 inline size_t gsize(const rgrid *g) { return (size_t) g->nx * g->ny * g->nz; }
 inline size_t gsize(const cgrid *g) { return (size_t) g->nx * g->ny * g->nz; }
 
+// Absorbing boundary of a wave function (grid_wf_boundary): the layer outside
+// [lx, hx) x [ly, hy) x [lz, hz) (grid indices) with the weight
+// lambda = max over the axes of the linear ramp from 0 at the inner edge to 1
+// at the grid's edge, and the potential -i amp lambda (|psi|^2 / rho0 - 1).
+struct AbsBoundary {
+  int on = 0;
+  double amp = 0, rho0 = 0;
+  int lo[3] = { 0, 0, 0 }, hi[3] = { 0, 0, 0 };
+};
+
 struct WfPriv {
   void *spec = nullptr;        // nx*ny*nz complex spectral scratch
+  AbsBoundary abs;
+  cgrid *vtot = nullptr;       // potential plus the absorbing term (predict-correct steps)
 };
+
+// dst = pot + (-i) amp lambda (|psi|^2 / rho0 - 1) over the boundary layer
+// (dst may be pot); grid.cu
+int absorb_add(cgrid *dst, const cgrid *pot, const cgrid *psi, const AbsBoundary &b, double amp, double rho0);
+// The predict / correct propagation: S(V + V_abs(src)) when the wave function
+// has an absorbing boundary, else S(V)
+int propagate_pc(wf *g, cgrid *dst, cgrid *src, cgrid *V, double dr, double di);
 
 void *dev_alloc(size_t bytes);
 void dev_free(void *p);

@@ -174,6 +174,7 @@ template <int NV, class F> int reduce_host(size_t n, F f, double *out, double sc
 // ---------------------------------------------------------------- functors
 // Spectral layout [kz][x][y]; real / complex grids [x][y][z].
 template <typename T> struct SpecStoreZ {           // z pass output
+  static constexpr bool kSpecZ = true;
   typename cplx_t<T>::type *spec; int nx, ny;
   __device__ void operator()(int x, int y, int k, typename cplx_t<T>::type v) const {
     spec[((size_t) k * nx + x) * ny + y] = v;
@@ -184,6 +185,7 @@ template <typename T> struct SpecStoreZ {           // z pass output
 // (a, b0 .. b0+nl-1), elements 0 .. ne-1, into L2 (bulk prefetches).
 template <typename T> struct SpecLoadZ {            // z pass input (inverse); its tiles are one short
   typedef typename cplx_t<T>::type C;                // run per plane, not prefetched ahead
+  static constexpr bool kSpecZ = true;
   const C *spec; int nx, ny;
   __device__ C operator()(int x, int y, int k) const {
     return spec[((size_t) k * nx + x) * ny + y];

@@ -128,15 +128,26 @@ static int rfft3_fp64(const double *f, double2 *spec, const OtPriv *P) {
   return launch_lines<double, LINE_C2C, 0, 0>(P->nx, P->nz / 2 + 1, P->ny, -1.0, io, io);
 }
 
-// octant [kz][kx][ky] of the (re or im) spectrum, times (-1)^(kx+ky+kz) * scale
+// Octant [kz][kx][ky] of the (re or im) kernel spectrum, times scale.  The
+// kernel was sampled about index c = n/2 of each axis (x_i = (i - n/2) step);
+// the kernel about index 0 has the spectrum S(k) exp(2 pi i k c / n) per axis,
+// which is the sign (-1)^k for even n and a rotation for odd n.
 template <typename T> static int extract_octant(const double2 *spec, T *oct, const OtPriv *P, int imag, double scale) {
-  const int nx = P->nx, ny = P->ny, kxh = nx / 2 + 1, kyh = ny / 2 + 1, kzh = P->nz / 2 + 1;
+  const int nx = P->nx, ny = P->ny, nz = P->nz, kxh = nx / 2 + 1, kyh = ny / 2 + 1, kzh = nz / 2 + 1;
   return launch_each((size_t) kzh * kxh * kyh, [=] __device__(size_t i) {
     const int iy = (int) (i % kyh), ix = (int) ((i / kyh) % kxh), iz = (int) (i / ((size_t) kxh * kyh));
-    const double2 v = spec[((size_t) iz * nx + ix) * ny + iy];
-    double val = imag ? v.y : v.x;
-    if ((ix + iy + iz) & 1) val = -val;
-    oct[i] = (T) (val * scale);
+    double2 v = spec[((size_t) iz * nx + ix) * ny + iy];
+    const int k[3] = { ix, iy, iz }, n[3] = { nx, ny, nz };
+    for (int a = 0; a < 3; a++) {
+      if (!(n[a] & 1)) {
+        if (k[a] & 1) v = make_double2(-v.x, -v.y);
+      } else {   // exp(2 pi i k c / n), c = (n - 1) / 2, reduced modulo n
+        double s, c;
+        sincospi(2.0 * (double) (((long) k[a] * (n[a] / 2)) % n[a]) / (double) n[a], &s, &c);
+        v = make_double2(v.x * c - v.y * s, v.x * s + v.y * c);
+      }
+    }
+    oct[i] = (T) ((imag ? v.y : v.x) * scale);
   });
 }
 
@@ -163,8 +174,8 @@ int ot_generate_kernels(dft_ot_functional *otf, int min_ns, int max_ns) {
       if (which == 0) {
         ShapeLJ s{otf->lj_params.h, otf->lj_params.sigma, otf->lj_params.epsilon, otf->lj_params.cval};
         rc = adaptive_map(f, P, min_ns, max_ns, tol, s);
-      } else {
-        ShapeSA s{otf->lj_params.h};
+      } else {   // HD2: radius 1.065 h (src/ot.c:164-166, PRB 72, 214522)
+        ShapeSA s{(otf->model & DFT_OT_HD2) ? otf->lj_params.h * 1.065 : otf->lj_params.h};
         rc = adaptive_map(f, P, min_ns, max_ns, tol, s);
       }
       if (rc) goto done;
@@ -236,9 +247,14 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
   const bool lj = src.terms & POT_LJ, loc = src.terms & POT_LOCAL;
   const bool kc = (src.terms & POT_KC) && (otf->model & DFT_OT_KC);
   const bool bf = (src.terms & POT_BF) && (otf->model & DFT_OT_BACKFLOW);
-  // the backflow real part is merged into the linear part unless it is clamped
+  // high-density models: the Barranco penalty (a local term) and the
+  // backflow's cut-off density rho G(rho) (src/ot.c:374-378, 843-982)
+  const bool hd = hd_model(otf), hdp = hd && (src.terms & POT_HD), bfhd = bf && hd;
+  const HdPar<T> hp = hd_par<T>(otf);
+  // the backflow real part is merged into the linear part unless it is
+  // clamped or multiplied by d(rho G)/drho
   const bool clampp = otf->max_bfpot < (10000.0 / GRID_AUTOK);
-  const bool cmerge = bf && !clampp;
+  const bool cmerge = bf && !clampp && !bfhd;
   const Stencil3 S{nx, ny, nz};
   C *pot = (C *) Pg->value;
   const C *psi = gwf ? (const C *) gwf->grid->value : nullptr;
@@ -258,8 +274,8 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
     r[i] = F.r(i);
     if (!r[i]) return DFTGPU_ERR_NOMEM;
   }
-  C *s[12];
-  for (int i = 0; i < 12; i++) { s[i] = F.s(i); if (!s[i]) return DFTGPU_ERR_NOMEM; }
+  C *s[OT_MAX_SPEC];
+  for (int i = 0; i < OT_MAX_SPEC; i++) { s[i] = F.s(i); if (!s[i]) return DFTGPU_ERR_NOMEM; }
 
   if (src.dens) {
     if (src.dens != otf->density->value)
@@ -269,6 +285,14 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
     DensityPairLoad<T> ld{psi, rho, ny, nz};
     DFT_TRY(rfft_zy<T>(ld, s[0], nx, ny, nz, 2.0 * nb));
   }
+  // HD backflow: A = V_j * (rho G) (src/ot.c:843-849) convolves the cut-off density, s10
+  const C *sA = s[0];
+  if (bfhd) {
+    T *rg = r[R_RG];
+    DFT_TRY(launch_each((size_t) nx * ny * nz, [=] __device__(size_t i) { rg[i] = hp.rg(rho[i]); }, 2.0 * nb, "ot_hd_density"));
+    DFT_TRY(F.fwd(rg, s[10]));
+    sA = s[10];
+  }
 
   // x pass 1: one input, kernels SA (+F) (+V_j); rho^ stays in s0.  The
   // derivative kernels dF_a are the central-difference gradient of the
@@ -276,9 +300,10 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
   // dF_a*rho and sum_a dF_a*G_a are taken as stencils of F*rho and J_a.
   if (loc || kc || bf) {
     XConvArgs<T> A; xc_init(A, P); xc_in(A, (const C *) s[0]);
+    if (bfhd) xc_in(A, sA);
     if (loc) { xc_out(A, s[2]); xc_term(A, 0, F.k(OT_SA), KER_EVEN, (T) 1); }
     if (kc) { xc_out(A, s[3]); xc_term(A, 0, F.k(OT_F), KER_EVEN, (T) 1); }
-    if (bf) { xc_out(A, s[7]); xc_term(A, 0, F.k(OT_VJ), KER_EVEN, (T) 1); }
+    if (bf) { xc_out(A, s[7]); xc_term(A, bfhd ? 1 : 0, F.k(OT_VJ), KER_EVEN, (T) 1); }
     DFT_TRY(launch_xconv<T>(A));
     C *sp[3]; T *dst[3]; int n = 0;
     if (loc) { sp[n] = s[2]; dst[n++] = r[R_RB]; }
@@ -334,16 +359,18 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
       // src/ot.c:557-567 (the LJ term src/ot.c:530 is in the merged linear part)
       p.x += add;
       if (loc) p.x += (c2 / (T) 2) * (b * b) + (c3 / (T) 3) * (b * b * b);
+      if (hdp) p.x += hp.vhd(rh);   // Barranco penalty src/ot.c:374-378, 815-819
       pot[i] = p;
       if (loc) q[i] = (c2 * b + c3 * (b * b)) * rh;
       if (kc) {  // src/ot.c:608-612, 632-637
         rst[i] = st;
         s0[i] = dr[0] * st; s1[i] = dr[1] * st; s2[i] = dr[2] * st;
       }
-      if (bf) {  // C, B_a inputs src/ot.c:852-888
+      if (bf) {  // C, B_a inputs src/ot.c:852-888 (HD: the cut-off density rho G)
+        const T rb_ = bfhd ? hp.rg(rh) : rh;
         v0[i] = va[0]; v1[i] = va[1]; v2[i] = va[2];
-        e[i] = (va[2] * va[2] + va[1] * va[1] + va[0] * va[0]) * rh;
-        b0[i] = va[0] * rh; b1[i] = va[1] * rh; b2[i] = va[2] * rh;
+        e[i] = (va[2] * va[2] + va[1] * va[1] + va[0] * va[0]) * rb_;
+        b0[i] = va[0] * rb_; b1[i] = va[1] * rb_; b2[i] = va[2] * rb_;
       }
     }, nb * (5 + (kc ? 5 : 0) + (bf ? 9 : 0)), "ot_pointwise_1"));
   }
@@ -388,8 +415,8 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
   if (kc || bf) {
     const T c = (T) (otf->alpha_s / (2.0 * otf->mass)), hm = (T) (-0.5 * otf->mass), cbf = (T) otf->c_bfpot;
     const T pcap = (T) otf->max_bfpot, inv2h = (T) (1.0 / (2.0 * P->step));
-    const T eps = (T) otf->div_epsilon;
-    T *rst = r[R_RST], *rt = r[R_RT], *J0 = r[R_J0], *J1 = r[R_J1], *J2 = r[R_J2], *h = r[R_H];
+    const T eps = (T) otf->div_epsilon, irs = (T) (1.0 / otf->rho_0s);
+    T *rt = r[R_RT], *J0 = r[R_J0], *J1 = r[R_J1], *J2 = r[R_J2], *h = r[R_H];
     T *v0 = r[R_V0], *v1 = r[R_V1], *v2 = r[R_V2], *A = r[R_A], *Cc = r[R_C], *B0 = r[R_BB0], *B1 = r[R_BB1], *B2 = r[R_BB2];
     T *wo0 = (T *) src.wout[0], *wo1 = (T *) src.wout[1], *wo2 = (T *) src.wout[2];
     // FP32: 6 CTAs per SM (42 registers, no spills) keep more of its ~40 loads
@@ -408,7 +435,8 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
           t1 += (Ja[a][ip] - Ja[a][im]) * inv2h;         // dF_a * G_a = D_a J_a
           jd += ja * ((rt[ip] - rt[im]) * inv2h);        // J_a (dF_a * rho) = J_a D_a (F*rho)
         }
-        p.x += c * rst[i] * t1 - c * jd;
+        const T st = (T) 1 - rt[i] * irs;   // rho_st (src/ot.c:608-612)
+        p.x += c * st * t1 - c * jd;
         hval = hv;
       }
       if (bf) {
@@ -418,10 +446,14 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
         T vv = 0, vb = 0;
         for (int k = 0; k < 3; k++) { vv += va[k][i] * va[k][i]; vb += va[k][i] * Ba[k][i]; }
         T re = hm * (a * vv - (T) 2 * vb);
-        if (clampp) re = clampv<T>(re + hm * Cc[i], pcap);
+        if (!cmerge) re += hm * Cc[i];
+        if (bfhd) re *= hp.drg(rho[i]);       // d(rho G)/drho  src/ot.c:907-908
+        if (clampp) re = clampv<T>(re, pcap);
         p.x += re * cbf;
-        // imaginary part src/ot.c:924-990 with w_a = v_a A - B_a (src/ot.c:924-931)
+        // imaginary part src/ot.c:924-990 with w_a = v_a A - B_a (src/ot.c:924-931);
+        // HD: the gradient of rho G, and G times the gradient of w_a (src/ot.c:934-982)
         T rr = rho[i];
+        const T gw = bfhd ? hp.g(rr) : (T) 1;
         if (rr < eps) rr = eps;
         T im = 0;
         for (int k = 0; k < 3; k++) {
@@ -429,7 +461,8 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
           const T w = va[k][i] * a - Ba[k][i];
           wv[k] = w;
           const T wp = va[k][ip] * A[ip] - Ba[k][ip], wm = va[k][imm] * A[imm] - Ba[k][imm];
-          im += (T) 0.5 * (((rho[ip] - rho[imm]) * inv2h) / rr) * w + (T) 0.5 * ((wp - wm) * inv2h);
+          const T dr = bfhd ? hp.rg(rho[ip]) - hp.rg(rho[imm]) : rho[ip] - rho[imm];
+          im += (T) 0.5 * ((dr * inv2h) / rr) * w + (T) 0.5 * ((wp - wm) * inv2h) * gw;
         }
         if (clampp) im = clampv<T>(im, pcap);
         p.y += im * cbf;
@@ -437,7 +470,7 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
       if (kc) h[i] = hval;
       if (bf && wo0) { wo0[i] = wv[0]; wo1[i] = wv[1]; wo2[i] = wv[2]; }   // src/ot.c:924-931
       pot[i] = p;
-    }, nb * (2 + (kc ? 7 : 0) + (bf ? (clampp ? 9 : 8) : 0)), "ot_pointwise_2"));
+    }, nb * (2 + (kc ? 6 : 0) + (bf ? (cmerge ? 8 : 9) : 0)), "ot_pointwise_2"));
   }
 
   // merged linear part (one inverse transform):
@@ -501,16 +534,20 @@ template <typename T> static int energy_density_t(dft_ot_functional *otf, rgrid 
   const double nb = (double) nx * ny * nz * sizeof(T);   // bytes of one real field
   const bool plain = terms & (POT_LJ | POT_LOCAL);
   const bool kc = (terms & POT_KC) && (otf->model & DFT_OT_KC), bf = (terms & POT_BF) && (otf->model & DFT_OT_BACKFLOW);
+  // high-density models: Barranco's energy with the plain part
+  // (src/ot-energy.c:96-99), the backflow with rho G(rho) (src/ot-energy.c:221-227)
+  const bool hd = hd_model(otf), hde = hd && (terms & POT_HD), bfhd = bf && hd;
+  const HdPar<T> hp = hd_par<T>(otf);
   const Stencil3 S{nx, ny, nz};
   const C *psi = (const C *) gwf->grid->value;
   T *rho = (T *) otf->density->value, *ed = (T *) edg->value;
-  enum { R_U, R_RB, R_RT, R_A, R_RST, R_S0, R_S1, R_S2, R_V0, R_V1, R_V2, R_E, R_B0, R_B1, R_B2, R_NREAL };
+  enum { R_U, R_RB, R_RT, R_A, R_RST, R_S0, R_S1, R_S2, R_V0, R_V1, R_V2, R_E, R_B0, R_B1, R_B2, R_RG, R_NREAL };
   T *r[R_NREAL];
   for (int i = 0; i < R_NREAL; i++) { r[i] = F.r(i); if (!r[i]) return DFTGPU_ERR_NOMEM; }
-  C *s[8];
-  for (int i = 0; i < 8; i++) { s[i] = F.s(i); if (!s[i]) return DFTGPU_ERR_NOMEM; }
+  C *s[9];
+  for (int i = 0; i < 9; i++) { s[i] = F.s(i); if (!s[i]) return DFTGPU_ERR_NOMEM; }
 
-  const bool any = plain || kc || bf;
+  const bool any = plain || kc || bf || hde;
   if (dens) {
     if (dens != otf->density) DFT_CUDA(cudaMemcpyAsync(rho, dens->value, nb, cudaMemcpyDeviceToDevice, rt().stream));
     if (!any) return add ? DFTGPU_OK : rfill(edg, 0.0);
@@ -522,14 +559,21 @@ template <typename T> static int energy_density_t(dft_ot_functional *otf, rgrid 
     DensityPairLoad<T> ld{psi, rho, ny, nz};
     DFT_TRY(rfft_zy<T>(ld, s[0], nx, ny, nz, 2.0 * nb));
   }
-  {
+  T *rg = r[R_RG];   // the backflow's density: rho G(rho) (HD) or rho
+  if (bfhd) {
+    DFT_TRY(launch_each((size_t) nx * ny * nz, [=] __device__(size_t i) { rg[i] = hp.rg(rho[i]); }, 2.0 * nb, "ot_hd_density"));
+    DFT_TRY(F.fwd(rg, s[8]));
+  }
+  const T *rbf = bfhd ? rg : rho;
+  if (plain || kc || bf) {
     XConvArgs<T> A; xc_init(A, P); xc_in(A, (const C *) s[0]);
+    if (bfhd) xc_in(A, (const C *) s[8]);
     if (plain) {
       xc_out(A, s[1]); xc_term(A, 0, F.k(OT_LJ), KER_EVEN, (T) 1);
       xc_out(A, s[2]); xc_term(A, 0, F.k(OT_SA), KER_EVEN, (T) 1);
     }
     if (kc) { xc_out(A, s[3]); xc_term(A, 0, F.k(OT_F), KER_EVEN, (T) 1); }
-    if (bf) { xc_out(A, s[4]); xc_term(A, 0, F.k(OT_VJ), KER_EVEN, (T) 1); }
+    if (bf) { xc_out(A, s[4]); xc_term(A, bfhd ? 1 : 0, F.k(OT_VJ), KER_EVEN, (T) 1); }
     DFT_TRY(launch_xconv<T>(A));
     if (plain) {
       DFT_TRY(F.inv(s[1], r[R_U]));
@@ -551,6 +595,7 @@ template <typename T> static int energy_density_t(dft_ot_functional *otf, rgrid 
         const T b = rb[i];
         acc += (T) 0.5 * rh * u[i] + (c2 / (T) 2) * ((b * b) * rh) + (c3 / (T) 3) * ((b * b * b) * rh);
       }
+      if (hde) acc += hp.ehd(rh);   // src/ot-energy.c:96-99
       if (kc) {  // src/ot-energy.c:144-161
         const T st = rt[i] * (-irs) + (T) 1;
         rst[i] = st;
@@ -572,10 +617,10 @@ template <typename T> static int energy_density_t(dft_ot_functional *otf, rgrid 
           va[a] = g0 * (pz.x * d.y - pz.y * d.x);
         }
         v0[i] = va[0]; v1[i] = va[1]; v2[i] = va[2];
-        const T vv = va[0] * va[0] + va[1] * va[1] + va[2] * va[2];
-        acc += -(cm / (T) 4) * (A[i] * vv * rh);
-        e[i] = rh * vv;
-        b0[i] = rh * va[0]; b1[i] = rh * va[1]; b2[i] = rh * va[2];
+        const T vv = va[0] * va[0] + va[1] * va[1] + va[2] * va[2], rhb = rbf[i];
+        acc += -(cm / (T) 4) * (A[i] * vv * rhb);
+        e[i] = rhb * vv;
+        b0[i] = rhb * va[0]; b1[i] = rhb * va[1]; b2[i] = rhb * va[2];
       }
       ed[i] = acc;
     }, nb * (4 + (kc ? 5 : 0) + (bf ? 10 : 0)), "ed_pointwise_1"));
@@ -614,10 +659,11 @@ template <typename T> static int energy_density_t(dft_ot_functional *otf, rgrid 
         }
       }
       if (bf) {  // src/ot-energy.c:253-287
-        acc += (cm / (T) 2) * (B0[i] * rh * v0[i]);
-        acc += (cm / (T) 2) * (B1[i] * rh * v1[i]);
-        acc += (cm / (T) 2) * (B2[i] * rh * v2[i]);
-        acc += -(cm / (T) 4) * (cc[i] * rh);
+        const T rhb = rbf[i];
+        acc += (cm / (T) 2) * (B0[i] * rhb * v0[i]);
+        acc += (cm / (T) 2) * (B1[i] * rhb * v1[i]);
+        acc += (cm / (T) 2) * (B2[i] * rhb * v2[i]);
+        acc += -(cm / (T) 4) * (cc[i] * rhb);
       }
       ed[i] = acc;
     }, nb * (3 + (kc ? 5 : 0) + (bf ? 8 : 0)), "ed_pointwise_2"));

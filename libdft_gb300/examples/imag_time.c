@@ -7,9 +7,11 @@
  * sqrt(rho0) (1 - exp(-r^2 / (2 * 5^2))), predict-correct imaginary-time
  * steps of 10 fs with the particle number held at its initial value.
  * The loop body is the one libdft's examples use
- * (examples/imag_time/imag_time.c:231-239).
+ * (examples/imag_time/imag_time.c:231-239).  With "hd" the functional is the
+ * one that example allocates, DFT_OT_PLAIN | DFT_OT_KC | DFT_OT_HD
+ * (examples/imag_time/imag_time.c:204).
  *
- *   usage: imag_time [steps] [fp32]
+ *   usage: imag_time [steps] [fp32|fp64] [hd]
  */
 #include <math.h>
 #include <stdio.h>
@@ -43,7 +45,8 @@ int main(int argc, char **argv) {
   wf *gwf = grid_wf_alloc(NX, NY, NZ, STEP, DFT_HELIUM_MASS, WF_PERIODIC_BOUNDARY, WF_2ND_ORDER_FFT, "gwf");
   if (!gwf) { fprintf(stderr, "grid_wf_alloc: %s\n", dftgpu_last_error_message()); return 1; }
   wf *gwfp = grid_wf_clone(gwf, "gwfp");
-  dft_ot_functional *otf = dft_ot_alloc(DFT_OT_PLAIN, gwf, DFT_MIN_SUBSTEPS, DFT_MAX_SUBSTEPS);
+  const INT model = (argc > 3 && !strcmp(argv[3], "hd")) ? (DFT_OT_PLAIN | DFT_OT_KC | DFT_OT_HD) : DFT_OT_PLAIN;
+  dft_ot_functional *otf = dft_ot_alloc(model, gwf, DFT_MIN_SUBSTEPS, DFT_MAX_SUBSTEPS);
   if (!otf) { fprintf(stderr, "dft_ot_alloc: %s\n", dftgpu_last_error_message()); return 1; }
   REAL rho0 = dft_ot_bulk_density_pressurized(otf, 0.0);
   REAL mu0 = dft_ot_bulk_chempot_pressurized(otf, 0.0);

@@ -83,6 +83,8 @@ class Oracle:
             "orc_wf_density": (None, [_vp, _vp]),
             "orc_wf_velocity": (None, [_vp, _vp, _vp, _vp, _d]),
             "orc_wf_set_momentum": (None, [_vp, _d, _d, _d]),
+            "orc_wf_boundary": (None, [_vp, _vp, _d, _d, _l, _l, _l, _l, _l, _l]),
+            "orc_wf_absorb_potential": (None, [_vp, _vp, _d, _d]),
             "orc_cgrid_new": (_vp, [_l, _l, _l, _d]),
             "orc_cgrid_free": (None, [_vp]),
             "orc_cgrid_set": (None, [_vp, _dp]),

@@ -242,12 +242,6 @@ static void not_restated(const char *name) {
   abort();
 }
 
-void grid_func1_operate_one_product(rgrid *d, rgrid *a, rgrid *b, REAL x, REAL y) { (void) d; (void) a; (void) b; (void) x; (void) y; not_restated("grid_func1_operate_one_product"); }
-void grid_func2_operate_one(rgrid *d, rgrid *s, REAL x, REAL y) { (void) d; (void) s; (void) x; (void) y; not_restated("grid_func2_operate_one"); }
-void grid_func2_operate_one_product(rgrid *d, rgrid *a, rgrid *b, REAL x, REAL y) { (void) d; (void) a; (void) b; (void) x; (void) y; not_restated("grid_func2_operate_one_product"); }
-void grid_func3_operate_one_product(rgrid *d, rgrid *a, rgrid *b, REAL x, REAL y) { (void) d; (void) a; (void) b; (void) x; (void) y; not_restated("grid_func3_operate_one_product"); }
-void grid_func4_operate_one(rgrid *d, rgrid *s, REAL x, REAL y, REAL z) { (void) d; (void) s; (void) x; (void) y; (void) z; not_restated("grid_func4_operate_one"); }
-void grid_func5_operate_one(rgrid *d, rgrid *s, REAL x, REAL y, REAL z) { (void) d; (void) s; (void) x; (void) y; (void) z; not_restated("grid_func5_operate_one"); }
 void grid_func6a_operate_one(rgrid *d, rgrid *s, REAL x, REAL y, REAL z) { (void) d; (void) s; (void) x; (void) y; (void) z; not_restated("grid_func6a_operate_one"); }
 void grid_func6b_operate_one(rgrid *d, rgrid *s, REAL x, REAL y, REAL z) { (void) d; (void) s; (void) x; (void) y; (void) z; not_restated("grid_func6b_operate_one"); }
 void grid_spline_ypp(REAL *x, REAL *y, INT n, REAL yp1, REAL ypn, REAL *y2) { (void) x; (void) y; (void) n; (void) yp1; (void) ypn; (void) y2; not_restated("grid_spline_ypp"); }
@@ -295,6 +289,39 @@ void rgrid_zero(rgrid *g) { memset(g->value, 0, sizeof(REAL) * (size_t) (g->nx *
 #define RAT(g) ((g)->value[ij * (g)->nz2 + k])
 
 void rgrid_constant(rgrid *g, REAL c) { RLOOP(g) RAT(g) = c; }
+
+/* High-density terms (libgrid grid_func1..5; not in the reference tree).
+ * Restated from the published functional -- a documented choice, parity is
+ * unpinned at this boundary:
+ *   Barranco et al., PRB 72, 214522 (2005) (cited at src/ot.h:142-146):
+ *     E_HD(rho) = C rho [1 + tanh(beta (rho - rho_m))]                   (func5)
+ *     V_HD(rho) = dE_HD/drho = C [1 + tanh(t)] + C beta rho sech^2(t),
+ *                 t = beta (rho - rho_m)                                  (func4)
+ *   backflow density cut-off (src/ot.c:1234-1236): rho -> rho G(rho),
+ *     G(rho) = [1 - tanh(xi (rho - rho_bf))] / 2  (1 below rho_bf, 0 above),
+ *     func1 = G, func2 = rho G, func3 = d(rho G)/drho = G + rho G'. */
+static REAL hd_sech2(REAL t) { REAL c = cosh(t); return 1.0 / (c * c); }   /* 0 once cosh overflows */
+static REAL bf_cut(REAL r, REAL xi, REAL rbf) { return 0.5 * (1.0 - tanh(xi * (r - rbf))); }
+static REAL bf_cut_d(REAL r, REAL xi, REAL rbf) { return -0.5 * xi * hd_sech2(xi * (r - rbf)); }
+
+void grid_func1_operate_one_product(rgrid *d, rgrid *a, rgrid *b, REAL xi, REAL rbf) {
+  RLOOP(d) RAT(d) = RAT(a) * bf_cut(RAT(b), xi, rbf);
+}
+void grid_func2_operate_one(rgrid *d, rgrid *s, REAL xi, REAL rbf) {
+  RLOOP(d) { REAL r = RAT(s); RAT(d) = r * bf_cut(r, xi, rbf); }
+}
+void grid_func2_operate_one_product(rgrid *d, rgrid *a, rgrid *b, REAL xi, REAL rbf) {
+  RLOOP(d) { REAL r = RAT(b); RAT(d) = RAT(a) * (r * bf_cut(r, xi, rbf)); }
+}
+void grid_func3_operate_one_product(rgrid *d, rgrid *a, rgrid *b, REAL xi, REAL rbf) {
+  RLOOP(d) { REAL r = RAT(b); RAT(d) = RAT(a) * (bf_cut(r, xi, rbf) + r * bf_cut_d(r, xi, rbf)); }
+}
+void grid_func4_operate_one(rgrid *d, rgrid *s, REAL beta, REAL rhom, REAL C) {
+  RLOOP(d) { REAL r = RAT(s), t = beta * (r - rhom); RAT(d) = C * (1.0 + tanh(t)) + C * beta * r * hd_sech2(t); }
+}
+void grid_func5_operate_one(rgrid *d, rgrid *s, REAL beta, REAL rhom, REAL C) {
+  RLOOP(d) { REAL r = RAT(s); RAT(d) = C * r * (1.0 + tanh(beta * (r - rhom))); }
+}
 void rgrid_copy(rgrid *dst, rgrid *src) { memcpy(dst->value, src->value, sizeof(REAL) * (size_t) (src->nx * src->ny * src->nz2)); }
 void rgrid_sum(rgrid *d, rgrid *a, rgrid *b) { RLOOP(d) RAT(d) = RAT(a) + RAT(b); }
 void rgrid_difference(rgrid *d, rgrid *a, rgrid *b) { RLOOP(d) RAT(d) = RAT(a) - RAT(b); }
@@ -503,16 +530,27 @@ void rgrid_inverse_fft_norm2(rgrid *g) {
   rgrid_scale_real(g, g->step * g->step * g->step / (REAL) (g->nx * g->ny * g->nz));
 }
 
+/* Product of two spectra times the centring phase: the kernel operand was
+ * sampled about index c = n/2 of each axis (x_i = (i - n/2) step), and the
+ * kernel about index 0 has the spectrum times exp(2 pi i k c / n) per axis --
+ * the sign (-1)^k for even n, a rotation for odd n (odd x and y sizes). */
+static REAL complex centring_phase(INT k, INT n) {
+  if (!(n & 1)) return (k & 1) ? -1.0 : 1.0;
+  const REAL ang = 2.0 * M_PI * (REAL) ((k * (n / 2)) % n) / (REAL) n;
+  return cos(ang) + I * sin(ang);
+}
+
 void rgrid_fft_convolute(rgrid *d, rgrid *a, rgrid *b) {
   INT nx = d->nx, ny = d->ny, nzh = d->nz / 2 + 1;
   REAL complex *cd = (REAL complex *) d->value, *ca = (REAL complex *) a->value, *cb = (REAL complex *) b->value;
 #pragma omp parallel for schedule(static)
   for (INT ij = 0; ij < nx * ny; ij++) {
     INT i = ij / ny, j = ij % ny;
+    REAL complex pxy = centring_phase(i, nx) * centring_phase(j, ny);
     for (INT k = 0; k < nzh; k++) {
       INT idx = ij * nzh + k;
-      REAL complex v = ca[idx] * cb[idx];
-      cd[idx] = ((i + j + k) & 1) ? -v : v;
+      REAL complex v = ca[idx] * cb[idx] * pxy;
+      cd[idx] = (k & 1) ? -v : v;
     }
   }
 }
@@ -850,9 +888,77 @@ static void strang_step(wf *g, cgrid *dst, cgrid *src, cgrid *pot, REAL complex 
   apply_potential_half(dst, dst, pot, dt);
 }
 
+/* Absorbing boundary (libgrid grid_wf_boundary / grid_wf_absorb_potential,
+ * call sites examples/gas-bubble/bubble.c:149-157, examples/1d-bubble/
+ * bubble-1d.c:192,222).  libgrid's arithmetic is not in the reference tree;
+ * the restatement (a documented choice, shared with the GPU library): the
+ * layer outside [lx, hx) x [ly, hy) x [lz, hz) has the weight
+ * lambda = max over the axes of (l - i) / l below l and (i - h + 1) / (n - h)
+ * from h on, and the absorbing potential is -i amp lambda (|psi|^2 / rho0 - 1).
+ * Predict / correct steps of a wave function with a boundary add it,
+ * evaluated from the step's input, to their potential; grid_wf_propagate does
+ * not (single-step callers add it with grid_wf_absorb_potential). */
+static REAL abs_ramp(INT i, INT l, INT h, INT n) {
+  if (i < l) return (REAL) (l - i) / (REAL) l;
+  if (i >= h) return (REAL) (i - h + 1) / (REAL) (n - h);
+  return 0.0;
+}
+
+void grid_wf_boundary(wf *gwf, wf *gwfp, REAL amp, REAL rho0, INT lx, INT hx, INT ly, INT hy, INT lz, INT hz) {
+  wf *w[2] = { gwf, gwfp };
+  for (int n = 0; n < 2; n++) {
+    if (!w[n]) continue;
+    w[n]->abs_on = 1;
+    w[n]->abs_amp = amp;
+    w[n]->abs_rho0 = rho0;
+    w[n]->abs_lo[0] = lx; w[n]->abs_hi[0] = hx;
+    w[n]->abs_lo[1] = ly; w[n]->abs_hi[1] = hy;
+    w[n]->abs_lo[2] = lz; w[n]->abs_hi[2] = hz;
+  }
+}
+
+/* dst = pot - i amp lambda (|psi|^2 / rho0 - 1) (dst may be pot) */
+static void absorb_add(wf *g, cgrid *dst, const cgrid *pot, REAL amp, REAL rho0) {
+  cgrid *c = g->grid;
+  INT nx = c->nx, ny = c->ny, nz = c->nz;
+#pragma omp parallel for schedule(static)
+  for (INT ij = 0; ij < nx * ny; ij++) {
+    INT i = ij / ny, j = ij % ny;
+    REAL lij = abs_ramp(i, g->abs_lo[0], g->abs_hi[0], nx);
+    REAL ly = abs_ramp(j, g->abs_lo[1], g->abs_hi[1], ny);
+    if (ly > lij) lij = ly;
+    for (INT k = 0; k < nz; k++) {
+      REAL lam = abs_ramp(k, g->abs_lo[2], g->abs_hi[2], nz);
+      if (lij > lam) lam = lij;
+      REAL complex v = pot->value[ij * nz + k];
+      if (lam > 0.0) {
+        REAL complex a = c->value[ij * nz + k];
+        v -= I * amp * lam * ((creal(a) * creal(a) + cimag(a) * cimag(a)) / rho0 - 1.0);
+      }
+      dst->value[ij * nz + k] = v;
+    }
+  }
+}
+
+void grid_wf_absorb_potential(wf *gwf, cgrid *potential, REAL amp, REAL rho0) {
+  if (!gwf->abs_on) {
+    fprintf(stderr, "oracle: grid_wf_absorb_potential without grid_wf_boundary.\n");
+    abort();
+  }
+  absorb_add(gwf, potential, potential, amp, rho0);
+}
+
+static void strang_step_pc(wf *g, cgrid *dst, cgrid *src, cgrid *pot, REAL complex dt) {
+  if (!g->abs_on) { strang_step(g, dst, src, pot, dt); return; }
+  cgrid *v = cgrid_clone(pot, "absorbing potential");
+  absorb_add(g, v, pot, g->abs_amp, g->abs_rho0);
+  strang_step(g, dst, src, v, dt);
+  cgrid_free(v);
+}
+
 void grid_wf_propagate(wf *g, cgrid *pot, REAL complex dt) { strang_step(g, g->grid, g->grid, pot, dt); }
-void grid_wf_propagate_predict(wf *g, wf *gp, cgrid *pot, REAL complex dt) { strang_step(g, gp->grid, g->grid, pot, dt); }
-void grid_wf_propagate_correct(wf *g, cgrid *pot, REAL complex dt) { strang_step(g, g->grid, g->grid, pot, dt); }
+void grid_wf_propagate_predict(wf *g, wf *gp, cgrid *pot, REAL complex dt) { strang_step_pc(g, gp->grid, g->grid, pot, dt); }
+void grid_wf_propagate_correct(wf *g, cgrid *pot, REAL complex dt) { strang_step_pc(g, g->grid, g->grid, pot, dt); }
 
 void grid_wf_propagate_potential(wf *g, REAL complex dt, cgrid *pot, REAL cons) {
   INT n = CN(g->grid);

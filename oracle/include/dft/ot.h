@@ -26,8 +26,9 @@
 #define DFT_ZERO       2097152
 #define DFT_GP2        4194304
 
-/* Models the oracle restates: the 0 K OT functional with optional KC and BF. */
-#define ORACLE_SUPPORTED_MODELS (DFT_OT_KC | DFT_OT_BACKFLOW)
+/* Models the oracle restates: the 0 K OT functional with optional KC, BF and
+ * the high-density terms (HD, HD2). */
+#define ORACLE_SUPPORTED_MODELS (DFT_OT_KC | DFT_OT_HD | DFT_OT_HD2 | DFT_OT_BACKFLOW)
 
 #define DFT_HELIUM_MASS (4.002602 / GRID_AUTOAMU)
 #define DFT_MIN_SUBSTEPS 4

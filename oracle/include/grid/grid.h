@@ -18,9 +18,10 @@
  *  - rgrid_fft / cgrid_fft: unnormalised forward DFT, exp(-2 pi i k.n/N);
  *    rgrid_inverse_fft_norm: scaled 1/N; rgrid_inverse_fft_norm2: scaled
  *    step^3/N (the convolution normalisation implied by src/ot.c:160,181);
- *  - rgrid_fft_convolute: product of two spectra times (-1)^(i+j+k), the
- *    phase that moves a kernel sampled about the grid centre to index 0
- *    (exact for even grid dimensions, the only ones supported);
+ *  - rgrid_fft_convolute: product of two spectra times the phase that moves
+ *    a kernel sampled about index n/2 of each axis to index 0:
+ *    exp(2 pi i k (n/2) / n) per axis, i.e. (-1)^(i+j+k) for even sizes and a
+ *    rotation for odd x / y sizes;
  *  - finite differences: second-order central, periodic;
  *  - rgrid_adaptive_map: cell average over s^3 cell-centred sub-points,
  *    s = min_ns, 2 min_ns, ... <= max_ns, stopping when two successive
@@ -107,6 +108,10 @@ typedef struct wf_struct {
   char boundary;
   char propagator;
   cgrid *cworkspace;         /* scratch for propagation / kinetic energy */
+  /* absorbing boundary (grid_wf_boundary): layer outside [lo, hi) per axis */
+  int abs_on;
+  REAL abs_amp, abs_rho0;
+  INT abs_lo[3], abs_hi[3];
 } wf;
 
 typedef struct grid_timer_struct {
@@ -226,6 +231,8 @@ void grid_wf_propagate_kinetic_fft(wf *gwf, REAL complex time);
 /* libgrid routines that libdft's non-hot code references (HD / thermal
  * functionals, spline and file-driven potentials).  Not restated: they print
  * an error and abort if called. */
+void grid_wf_boundary(wf *gwf, wf *gwfp, REAL amp, REAL rho0, INT lx, INT hx, INT ly, INT hy, INT lz, INT hz);
+void grid_wf_absorb_potential(wf *gwf, cgrid *potential, REAL amp, REAL rho0);
 void grid_func1_operate_one_product(rgrid *dst, rgrid *a, rgrid *b, REAL xi, REAL rhobf);
 void grid_func2_operate_one(rgrid *dst, rgrid *src, REAL xi, REAL rhobf);
 void grid_func2_operate_one_product(rgrid *dst, rgrid *a, rgrid *b, REAL xi, REAL rhobf);

@@ -7,8 +7,10 @@
  * backflow (BF) on 3-D grids: parameters, kernel generation, potential,
  * energy density and the bulk (uniform-liquid) relations.  The arithmetic is
  * organised as a few fused per-point loops around FFT convolutions; every
- * term cites the reference line it restates.  Unsupported models (HD, HD2,
- * thermal, GP, DR, 1-D) are rejected with an error message.
+ * term cites the reference line it restates.  The high-density terms (HD,
+ * HD2) use the shim's restatement of libgrid's grid_func1..5 (grid_shim.c).
+ * Unsupported models (thermal, GP, DR, 1-D) are rejected with an error
+ * message.
  */
 #include <string.h>
 #include "grid/grid.h"
@@ -157,7 +159,7 @@ static inline REAL fd(const rgrid *s, INT i, INT j, INT k, int axis) {
 
 static int check_model(INT model, const char *who) {
   if (model & ~((INT) ORACLE_SUPPORTED_MODELS)) {
-    fprintf(stderr, "oracle: %s: model " FMT_I " is outside the restated subset (OT 0 K, KC, BF).\n", who, model);
+    fprintf(stderr, "oracle: %s: model " FMT_I " is outside the restated subset (OT 0 K, KC, HD, BF).\n", who, model);
     return 0;
   }
   return 1;
@@ -194,8 +196,8 @@ dft_ot_functional *dft_ot_alloc(INT model, wf *gwf, INT min_ns, INT max_ns) {
   rgrid_fft(otf->lennard_jones);
   rgrid_fft_multiply(otf->lennard_jones, otf->b / (step * step * step * creal(rgrid_cvalue_at_index(otf->lennard_jones, 0, 0, 0))));
 
-  /* spherical average of radius h, integral 1 (src/ot.c:164-181) */
-  radius = otf->lj_params.h;
+  /* spherical average of radius h (HD2: 1.065 h), integral 1 (src/ot.c:164-181) */
+  radius = (model & DFT_OT_HD2) ? otf->lj_params.h * 1.065 : otf->lj_params.h;
   otf->spherical_avg = new_grid(gwf, "OT SA");
   rgrid_adaptive_map(otf->spherical_avg, dft_common_spherical_avg, &radius, min_ns, max_ns, tol);
   rgrid_fft(otf->spherical_avg);
@@ -290,7 +292,10 @@ static void kc_potential(dft_ot_functional *otf, cgrid *P, rgrid *rho, rgrid *rk
   }
 }
 
-/* BF potential (src/ot.c:380-400 and 840-991); rk = FFT(rho). */
+/* BF potential (src/ot.c:380-400 and 840-991); rk = FFT(rho).  With HD / HD2
+ * the backflow sees the cut-off density rho G(rho) (src/ot.c:843-886) and its
+ * real part is multiplied by d(rho G)/drho (src/ot.c:907-908), the imaginary
+ * part's gradients by G (src/ot.c:934-982). */
 static void bf_potential(dft_ot_functional *otf, cgrid *P, wf *gwf, rgrid *rho, rgrid *rk) {
   rgrid *vx = otf->workspace2, *vy = otf->workspace3, *vz = otf->workspace4;
   rgrid *A = otf->workspace5, *C = otf->workspace6, *Bx = otf->workspace7, *By = otf->workspace8, *Bz = otf->workspace9;
@@ -299,16 +304,32 @@ static void bf_potential(dft_ot_functional *otf, cgrid *P, wf *gwf, rgrid *rho, 
   REAL m = otf->mass, cap = otf->max_veloc, bcap = otf->max_bfpot, eps = otf->div_epsilon;
   int clamp_v = otf->max_veloc < (999.0 / GRID_AUTOMPS);
   int clamp_p = otf->max_bfpot < (10000.0 / GRID_AUTOK);
+  int hd = (otf->model & (DFT_OT_HD | DFT_OT_HD2)) != 0;
+  rgrid *rt = rho, *gfac = NULL, *dfac = NULL;                 /* rho G, G, d(rho G)/drho */
 
   grid_wf_velocity(gwf, vx, vy, vz, otf->div_epsilon);       /* src/ot.c:390 */
   if (clamp_v)                                                 /* src/ot.c:391-395 */
     for (int a = 0; a < 3; a++) rgrid_threshold_clear(v[a], v[a], cap, -cap, cap, -cap);
 
-  convolve(A, rk, otf->backflow_pot);                          /* A = V_j * rho   src/ot.c:842-849 */
+  if (hd) {
+    rt = rgrid_clone(rho, "rho G");
+    gfac = rgrid_clone(rho, "G");
+    dfac = rgrid_clone(rho, "d(rho G)");
+    rgrid_constant(gfac, 1.0);
+    rgrid_constant(dfac, 1.0);
+    grid_func2_operate_one(rt, rho, otf->xi, otf->rhobf);
+    grid_func1_operate_one_product(gfac, gfac, rho, otf->xi, otf->rhobf);
+    grid_func3_operate_one_product(dfac, dfac, rho, otf->xi, otf->rhobf);
+    rgrid_copy(A, rt);
+    rgrid_fft(A);
+    rgrid_fft_convolute(A, A, otf->backflow_pot);              /* A = V_j * (rho G)  src/ot.c:843-849 */
+    rgrid_inverse_fft_norm2(A);
+  } else
+    convolve(A, rk, otf->backflow_pot);                        /* A = V_j * rho   src/ot.c:842-849 */
 #pragma omp parallel for schedule(static)
   for (INT ij = 0; ij < NRM(rho); ij++)
     for (INT k = 0; k < nz; k++) {
-      REAL r = V(rho, ij, k), x = V(vx, ij, k), y = V(vy, ij, k), z = V(vz, ij, k);
+      REAL r = V(rt, ij, k), x = V(vx, ij, k), y = V(vy, ij, k), z = V(vz, ij, k);
       V(C, ij, k) = (z * z + y * y + x * x) * r;               /* rho |v|^2   src/ot.c:852-860 */
       V(Bx, ij, k) = x * r;                                    /* rho v_a     src/ot.c:871,879,888 */
       V(By, ij, k) = y * r;
@@ -328,6 +349,7 @@ static void bf_potential(dft_ot_functional *otf, cgrid *P, wf *gwf, rgrid *rho, 
     for (INT k = 0; k < nz; k++) {
       REAL x = V(vx, ij, k), y = V(vy, ij, k), z = V(vz, ij, k), a = V(A, ij, k);
       REAL re = -0.5 * m * (a * (z * z + y * y + x * x) - 2.0 * (x * V(Bx, ij, k) + y * V(By, ij, k) + z * V(Bz, ij, k)) + V(C, ij, k));
+      if (hd) re *= V(dfac, ij, k);
       if (clamp_p) { if (re > bcap) re = bcap; else if (re < -bcap) re = -bcap; }
       re *= otf->c_bfpot;
       P->value[ij * nz + k] += re;
@@ -342,12 +364,17 @@ static void bf_potential(dft_ot_functional *otf, cgrid *P, wf *gwf, rgrid *rho, 
     for (INT k = 0; k < nz; k++) {
       REAL r = V(rho, ij, k), im = 0.0;
       if (r < eps) r = eps;
-      for (int a = 0; a < 3; a++) im += 0.5 * (fd(rho, i, j, k, a) / r) * V(v[a], ij, k);
-      for (int a = 0; a < 3; a++) im += 0.5 * fd(v[a], i, j, k, a);
+      for (int a = 0; a < 3; a++) im += 0.5 * (fd(rt, i, j, k, a) / r) * V(v[a], ij, k);
+      for (int a = 0; a < 3; a++) im += 0.5 * fd(v[a], i, j, k, a) * (hd ? V(gfac, ij, k) : 1.0);
       if (clamp_p) { if (im > bcap) im = bcap; else if (im < -bcap) im = -bcap; }
       im *= otf->c_bfpot;
       P->value[ij * nz + k] += I * im;
     }
+  }
+  if (hd) {
+    rgrid_free(rt);
+    rgrid_free(gfac);
+    rgrid_free(dfac);
   }
 }
 
@@ -378,6 +405,10 @@ void dft_ot_potential(dft_ot_functional *otf, cgrid *P, wf *gwf) {
   grid_add_real_to_complex_re(P, q);
 
   if (otf->model & DFT_OT_KC) kc_potential(otf, P, rho, rk);
+  if (otf->model & (DFT_OT_HD | DFT_OT_HD2)) {                 /* Barranco penalty  src/ot.c:374-378, 815-819 */
+    grid_func4_operate_one(q, rho, otf->beta, otf->rhom, otf->C);
+    grid_add_real_to_complex_re(P, q);
+  }
   if (otf->model & DFT_OT_BACKFLOW) bf_potential(otf, P, gwf, rho, rk);
 }
 
@@ -404,6 +435,10 @@ void dft_ot_energy_density(dft_ot_functional *otf, rgrid *ed, wf *gwf) {
       REAL r = V(rho, ij, k), b = V(rb, ij, k);
       V(ed, ij, k) = 0.5 * r * V(u, ij, k) + (c2 / 2.0) * (ipow(b, e2) * r) + (c3 / 3.0) * (ipow(b, e3) * r);
     }
+  if (otf->model & (DFT_OT_HD | DFT_OT_HD2)) {                 /* Barranco  src/ot-energy.c:96-99 */
+    grid_func5_operate_one(u, rho, otf->beta, otf->rhom, otf->C);
+    rgrid_sum(ed, ed, u);
+  }
 
   if (otf->model & DFT_OT_KC) {
     /* -(alpha_s / 4m) sum_a g_a rho_st [F * (g_a rho_st)]  (src/ot-energy.c:144-190) */
@@ -431,12 +466,25 @@ void dft_ot_energy_density(dft_ot_functional *otf, rgrid *ed, wf *gwf) {
   }
 
   if (otf->model & DFT_OT_BACKFLOW) {
-    /* (src/ot-energy.c:221-287) */
+    /* (src/ot-energy.c:221-287); with HD / HD2 every density of the backflow
+     * energy is the cut-off density rho G(rho) (src/ot-energy.c:221-227) */
     rgrid *vx = otf->workspace2, *vy = otf->workspace3, *vz = otf->workspace4, *t = otf->workspace5;
     rgrid *v[3] = { vx, vy, vz };
     REAL cm = otf->c_bfpot * otf->mass;
+    int hd = (otf->model & (DFT_OT_HD | DFT_OT_HD2)) != 0;
+    rgrid *rho_in = rho;
+    if (hd) {
+      rho = rgrid_clone(rho_in, "rho G");
+      grid_func2_operate_one(rho, rho_in, otf->xi, otf->rhobf);
+    }
     grid_wf_velocity(gwf, vx, vy, vz, DFT_EPS);
-    convolve(t, rk, otf->backflow_pot);
+    if (hd) {
+      rgrid_copy(t, rho);
+      rgrid_fft(t);
+      rgrid_fft_convolute(t, t, otf->backflow_pot);
+      rgrid_inverse_fft_norm2(t);
+    } else
+      convolve(t, rk, otf->backflow_pot);
 #pragma omp parallel for schedule(static)
     for (INT ij = 0; ij < NRM(rho); ij++)
       for (INT k = 0; k < nz; k++) {
@@ -466,6 +514,10 @@ void dft_ot_energy_density(dft_ot_functional *otf, rgrid *ed, wf *gwf) {
 #pragma omp parallel for schedule(static)
     for (INT ij = 0; ij < NRM(rho); ij++)
       for (INT k = 0; k < nz; k++) V(ed, ij, k) += -(cm / 4.0) * (V(t, ij, k) * V(rho, ij, k));
+    if (hd) {
+      rgrid_free(rho);
+      rho = rho_in;
+    }
   }
   (void) nx;
 }

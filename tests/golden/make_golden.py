@@ -201,8 +201,70 @@ def terms():
     print("terms.npz written to", HERE)
 
 
+def compressed_psi(shape, step, rho0, seed):
+    """A liquid compressed to ~15 rho0 (0.33 A^-3) at the centre: it crosses the
+    backflow cut-off density (0.033 A^-3) and reaches the range of the
+    high-density penalty (rho_m = 0.37 A^-3); with a phase (non-zero velocity)."""
+    rng = np.random.default_rng(seed)
+    X, Y, Z = coords(shape, step)
+    bump = np.exp(-(X ** 2 + Y ** 2 + Z ** 2) / (2 * 1.5 ** 2))
+    rho = rho0 * (1 + 0.2 * rng.random(shape)) * (1 + 14.0 * bump)
+    phase = 0.3 * np.sin(2 * np.pi * X / (shape[0] * step)) + 0.2 * rng.random(shape)
+    return (np.sqrt(rho) * np.exp(1j * phase)).astype(np.complex128)
+
+
+def hd():
+    """hd.npz (python tests/golden/make_golden.py hd): the high-density models
+    from libdft's own ot.c / ot-energy.c over the shim's grid_func1..5."""
+    build("ref")
+    o = Oracle("ref")
+    assert o.lib.orc_kind() == 2
+    mass = 4.002602 / o.AUTOAMU
+    L = o.lib
+    shape, step = (16, 18, 20), 0.8
+    out = dict(shape=shape, step=step)
+    rho0 = 0.0218360 * o.AUTOANG ** 3
+    psi = compressed_psi(shape, step, rho0, 3)
+    out["psi"] = psi
+    for model in (2, 11, 13):
+        with Grids(o, shape, step, mass) as g:
+            w = g.wf(psi)
+            otf = g.ot(model, w)
+            out["P_%d" % model] = g.potential(otf, w)
+            out["ed_%d" % model] = g.energy_density(otf, w)
+            if model == 11:
+                mu0 = L.orc_bulk_chempot(otf, 0.0)
+                wp, Pc = g.wf(), g.cgrid()
+                dt = 0.2 / o.AUTOFS + 0j
+                for _ in range(2):
+                    L.orc_pc_step(otf, w, wp, Pc, None, mu0, dt.real, dt.imag)
+                out["psi2_11"], out["mu0"], out["dt"] = g.get_wf(w), mu0, dt
+                g.set_wf(w, psi)
+                rho_g, v = g.rgrid(), [g.rgrid() for _ in range(3)]
+                L.orc_wf_density(w, rho_g)
+                p = g.params(otf)
+                L.orc_wf_velocity(w, v[0], v[1], v[2], p["div_epsilon"])
+                vel = np.stack([g.get_r(x) for x in v])
+                out["vel"] = vel
+                P = g.cgrid(0.0)
+                L.orc_ref_potential2(otf, P, rho_g, v[0], v[1], v[2])
+                out["P2_11"], out["w2_11"] = g.get_c(P), np.stack([g.get_r(x) for x in v])
+                for x, val in zip(v, vel):
+                    g.set_r(x, val)
+                P = g.cgrid(0.0)
+                L.orc_ref_backflow(otf, P, rho_g, v[0], v[1], v[2])
+                out["Pbf_11"], out["wbf_11"] = g.get_c(P), np.stack([g.get_r(x) for x in v])
+                ed = g.rgrid(0.0)
+                L.orc_ref_energy_density_bf(otf, ed, w, rho_g)
+                out["edbf_11"] = g.get_r(ed)
+    np.savez_compressed(os.path.join(HERE, "hd.npz"), **out)
+    print("hd.npz written to", HERE)
+
+
 if __name__ == "__main__":
     if sys.argv[1:] == ["terms"]:
         terms()
+    elif sys.argv[1:] == ["hd"]:
+        hd()
     else:
         main()

@@ -356,3 +356,92 @@ def test_adjoint_rejects_clamped_backflow_and_bad_args(gpu, fp64):
         ot.potential_vjp(w, cot, other)
     for o in (other, g, cot, ot, w):
         o.free()
+
+
+def _gaussians(theta, X, Y, Z, autok):
+    """V = sum_g a_g exp(-((x - cx_g)^2 + y^2 + (z - cz_g)^2) / (2 w_g^2)), theta = (a [K], w, cx, cz) x 4,
+    and dV/dtheta for every parameter."""
+    V = np.zeros(X.shape)
+    dV = []
+    for a, wd, cx, cz in np.asarray(theta).reshape(4, 4):
+        r2 = (X - cx) ** 2 + Y ** 2 + (Z - cz) ** 2
+        e = np.exp(-r2 / (2 * wd ** 2)) / autok
+        V += a * e
+        dV += [e, a * e * r2 / wd ** 3, a * e * (X - cx) / wd ** 2, a * e * (Z - cz) / wd ** 2]
+    return V, dV
+
+
+def test_gaussian_parameter_gradient_matches_oracle_finite_differences(gpu, port):
+    """The 16-parameter external potential of the adjoint workload (4 Gaussians,
+    amplitude ~U(5, 50) K, width ~U(2, 6) bohr, centre ~U(-10, 10) bohr in x and
+    z, seed 11) on the full-OT liquid with a 1 % density wave (l_g = 1.1 A),
+    64^3, step 0.8 bohr, 40 real-time steps of 1 fs; J = int (rho_T -
+    rho_target)^2 dV with rho_target the initial density shifted 2 bohr along z.
+    Every parameter's derivative by central differences (h = 1e-4 relative) of
+    the FP64 CPU oracle's trajectory, against the GPU adjoint in FP64 and FP32."""
+    shape, step, nsteps = (64, 64, 64), 0.8, 40
+    dt = 1.0 / gpu.AUTOFS
+    lg = 1.1 / gpu.AUTOANG
+    X, Y, Z = coords(shape, step)
+    rho0 = 0.0218360 * gpu.AUTOANG ** 3
+    phase = np.random.default_rng(7).uniform(0, 2 * np.pi)
+    psi = np.sqrt(rho0 * (1 + 0.01 * np.cos(2 * np.pi * X / (32 * step) + phase))).astype(complex)
+    rho = np.abs(psi) ** 2
+    kz = 2 * np.pi * np.fft.fftfreq(shape[2], d=step)
+    rho_t = np.real(np.fft.ifft(np.fft.fft(rho, axis=2) * np.exp(-1j * kz * 2.0), axis=2))
+    rng = np.random.default_rng(11)
+    theta0 = np.stack([rng.uniform(5, 50, 4), rng.uniform(2, 6, 4), rng.uniform(-10, 10, 4),
+                       rng.uniform(-10, 10, 4)], 1).ravel()
+    V0, dVs = _gaussians(theta0, X, Y, Z, gpu.AUTOK)
+    dv = step ** 3
+
+    with Grids(port, shape, step, gpu.HELIUM_MASS) as g:
+        wo, wpo, Po, vo = g.wf(psi), g.wf(), g.cgrid(), g.rgrid()
+        oo = g.ot(9, wo, lg_bohr=lg)
+        mu0 = port.lib.orc_bulk_chempot(oo, 0.0)
+
+        def J_oracle(th):
+            g.set_r(vo, _gaussians(th, X, Y, Z, gpu.AUTOK)[0])
+            g.set_wf(wo, psi)
+            for _ in range(nsteps):
+                port.lib.orc_pc_step(oo, wo, wpo, Po, vo, mu0, dt, 0.0)
+            return float(np.sum((np.abs(g.get_wf(wo)) ** 2 - rho_t) ** 2) * dv)
+
+        J_ref = J_oracle(theta0)
+        fd = np.zeros(16)
+        for k in range(16):
+            e = np.zeros(16)
+            e[k] = 1e-4 * abs(theta0[k])
+            fd[k] = (J_oracle(theta0 + e) - J_oracle(theta0 - e)) / (2 * e[k])
+
+    grads = {}
+    for prec in (0, 1):
+        gpu.set_precision(prec)
+        w = gpu.Wf(shape, step)
+        ot = gpu.OT(9, w, lg_bohr=lg)
+        vext, rt, gv = gpu.RGrid(shape, step), gpu.RGrid(shape, step), gpu.RGrid(shape, step)
+        vext.set(V0)
+        rt.set(rho_t)
+        w.set(psi)
+        J = ot.adjoint_run(w, vext, mu0, dt, nsteps, False, rt, gv, checkpoint_every=7)
+        G = gv.get()
+        grads[prec] = (J, np.array([np.sum(G * d) for d in dVs]))
+        for o in (gv, rt, vext, ot, w):
+            o.free()
+    gpu.set_precision(0)
+    # FP64: every component within 1e-4 of its finite difference (components
+    # below 1e-3 of the gradient's norm relative to that), the vector within
+    # 1e-6.  FP32 bulk is outside the 1e-4 gradient target: its forward
+    # trajectory alone moves J by ~2e-4 over these 40 real-time steps, and
+    # the gradient is held to 5e-3 of its norm.
+    scale = np.linalg.norm(fd)
+    for prec, tol_J, tol_norm, tol_comp in ((0, 1e-9, 1e-6, 1e-4), (1, 1e-3, 5e-3, None)):
+        J, an = grads[prec]
+        err_norm = np.linalg.norm(an - fd) / scale
+        err_comp = np.max(np.abs(an - fd) / np.maximum(np.abs(fd), 1e-3 * scale))
+        print("16-parameter gradient prec=%d: J rel %.2e, |g - fd| / |fd| = %.2e, max component rel %.2e"
+              % (prec, abs(J / J_ref - 1), err_norm, err_comp))
+        assert abs(J / J_ref - 1) < tol_J
+        assert err_norm < tol_norm, (prec, err_norm)
+        if tol_comp is not None:
+            assert err_comp < tol_comp, (prec, err_comp)

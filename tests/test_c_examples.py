@@ -33,9 +33,12 @@ def run(exe, *args):
     return r.stdout, nums
 
 
+@pytest.mark.parametrize("model", ["plain", "hd"])
 @pytest.mark.parametrize("prec", ["fp64", "fp32"])
-def test_imag_time_driver_runs(gpu, tmp_path, prec):
-    out, nums = run(build(tmp_path, "imag_time"), 20, prec)
+def test_imag_time_driver_runs(gpu, tmp_path, prec, model):
+    """"hd": the functional libdft's imag_time example allocates,
+    DFT_OT_PLAIN | DFT_OT_KC | DFT_OT_HD (examples/imag_time/imag_time.c:204)."""
+    out, nums = run(build(tmp_path, "imag_time"), 20, prec, model)
     assert nums["N"] > 0 and abs(nums["E"]) < 1e12, out
 
 

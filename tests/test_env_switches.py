@@ -1,6 +1,7 @@
 """Switches that change how the work is scheduled but not what is computed:
-DFTGPU_PREFETCH_AHEAD=0 (no one-wave-ahead L2 prefetch in the line passes)
-and DFTGPU_STREAMS=1 (no parallel graph branches).  The selections are read
+DFTGPU_PREFETCH_AHEAD=0 (no one-wave-ahead L2 prefetch in the line passes),
+DFTGPU_STREAMS=1 (no parallel graph branches) and DFTGPU_TMA=0 (the z passes'
+transposed side staged by load / store loops instead of TMA boxes).  The selections are read
 once per process, so the switched side runs in a child process; potentials
 and predict-correct steps must be bitwise equal to the default run's."""
 import json
@@ -15,7 +16,7 @@ from conftest import ROOT, liquid_psi
 
 pytestmark = pytest.mark.gpu
 
-CASES = [((64, 64, 64), 0.8, 9, 1), ((32, 24, 40), 0.9, 9, 0)]   # shape, step, model, precision
+CASES = [((64, 64, 64), 0.8, 9, 1), ((32, 24, 40), 0.9, 9, 0), ((32, 64, 256), 0.7, 9, 1)]   # shape, step, model, precision
 
 CHILD = r"""
 import json, sys
@@ -61,7 +62,7 @@ def run_here(gpu, shape, step, model, prec):
     return p, psi
 
 
-@pytest.mark.parametrize("env", [{"DFTGPU_PREFETCH_AHEAD": "0"}, {"DFTGPU_STREAMS": "1"}])
+@pytest.mark.parametrize("env", [{"DFTGPU_PREFETCH_AHEAD": "0"}, {"DFTGPU_STREAMS": "1"}, {"DFTGPU_TMA": "0"}])
 def test_scheduling_switches_do_not_change_results(gpu, tmp_path, env):
     r = subprocess.run([sys.executable, "-c", CHILD, ROOT, json.dumps(CASES), str(tmp_path)],
                        env=dict(os.environ, **env), capture_output=True, text=True, timeout=600)

@@ -92,7 +92,12 @@ def test_potential_and_energy_density_match_reference(gpu, prec, fixture):
                                               ((96, 80, 128), 0.8, 9), ((64, 64, 64), 0.8, 9),
                                               ((128, 64, 80), 0.8, 9), ((64, 128, 128), 0.8, 1),
                                               ((16, 256, 256), 0.8, 9), ((4, 512, 512), 0.5, 0),
-                                              ((2, 4, 6), 1.0, 9), ((1024, 6, 4), 0.6, 9), ((6, 4, 1024), 0.6, 9)])
+                                              ((2, 4, 6), 1.0, 9), ((1024, 6, 4), 0.6, 9), ((6, 4, 1024), 0.6, 9),
+                                              # odd x / y sizes (2^a 3^b 5^c; libdft's 729 x 384 x 384 grid,
+                                              # examples/gas-bubble/config.h:56): kernels rotated by
+                                              # exp(2 pi i k c / n) instead of the sign (-1)^k
+                                              ((9, 10, 8), 0.8, 9), ((15, 9, 12), 0.9, 9), ((27, 25, 16), 0.8, 9),
+                                              ((45, 3, 10), 0.8, 1), ((243, 16, 16), 0.8, 9)])
 def test_potential_vs_oracle_live(gpu, port, prec, shape, step, model):
     psi = liquid_psi(shape, step, 3)
     ns = (2, 4) if np.prod(shape) > 200000 else (4, 32)      # coarser kernel sampling on big grids (CPU time)
@@ -220,7 +225,7 @@ def test_uniform_liquid_potential_is_chemical_potential(gpu, prec, model):
 
 
 @pytest.mark.parametrize("shape", [(24, 20, 30), (128, 128, 128), (64, 96, 160),
-                                   (2, 6, 4), (1024, 4, 6), (6, 4, 1024), (4, 1024, 2)])
+                                   (2, 6, 4), (1024, 4, 6), (6, 4, 1024), (4, 1024, 2), (9, 15, 10), (27, 5, 8)])
 def test_propagate_matches_oracle(gpu, port, prec, shape):
     step = 0.9
     rng = np.random.default_rng(9)
@@ -235,7 +240,7 @@ def test_propagate_matches_oracle(gpu, port, prec, shape):
             ref.append(g.get_wf(wo))
         wp = g.wf()
         port.lib.orc_predict(wo, wp, Po, 10.0, -1.0)
-        refp, refk = g.get_wf(wp), port.lib.orc_wf_kinetic_energy(wo)
+        refp, refk, refn = g.get_wf(wp), port.lib.orc_wf_kinetic_energy(wo), port.lib.orc_wf_norm(wo)
     w = gpu.Wf(shape, step)
     P = gpu.CGrid(shape, step)
     w.set(psi)
@@ -247,6 +252,7 @@ def test_propagate_matches_oracle(gpu, port, prec, shape):
     w.predict(wp, P, 10.0 - 1.0j)
     assert relerr(wp.get(), refp) < TOL[prec] * 3
     assert abs(w.kinetic_energy() / refk - 1) < TOL[prec] * 3
+    assert abs(w.norm() / refn - 1) < TOL[prec] * 3        # FP64 runs of 8 (and a short last run)
     for o in (wp, P, w):
         o.free()
 
@@ -359,14 +365,16 @@ def test_energy_report_matches_oracle(gpu, port, prec):
 
 def test_errors_are_reported(gpu):
     L = gpu.lib()
-    assert not L.grid_wf_alloc(17, 16, 16, 1.0, 7000.0, 3, 1, b"odd")      # odd size
+    assert not L.grid_wf_alloc(17, 16, 16, 1.0, 7000.0, 3, 1, b"prime17")  # factor 17
+    assert L.dftgpu_last_error() == 2
+    assert not L.grid_wf_alloc(16, 16, 15, 1.0, 7000.0, 3, 1, b"oddz")     # odd z (packed real rows)
     assert L.dftgpu_last_error() == 2
     assert not L.grid_wf_alloc(14, 16, 16, 1.0, 7000.0, 3, 1, b"prime7")   # factor 7
     assert L.dftgpu_last_error() == 2
     assert not L.grid_wf_alloc(16, 16, 16, 1.0, 7000.0, 1, 1, b"dirichlet")
     assert L.dftgpu_last_error() == 6
     w = gpu.Wf((16, 16, 16), 1.0)
-    assert not L.dft_ot_alloc(2, w.ptr, 4, 32)                             # DFT_OT_HD
+    assert not L.dft_ot_alloc(32, w.ptr, 4, 32)                            # DFT_OT_T400MK (thermal)
     assert L.dftgpu_last_error() == 6
     psi = np.ones((16, 16, 16), dtype=complex)
     psi[3, 4, 5] = np.nan

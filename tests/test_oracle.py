@@ -158,3 +158,71 @@ def test_reference_build_live_vs_port_odd_sizes(shape):
             out.append((g.potential(otf, w), g.energy_density(otf, w)))
     assert relerr(out[0][0], out[1][0]) < 1e-12
     assert relerr(out[0][1], out[1][1]) < 1e-12
+
+
+def hd_psi(o, shape, step, seed=5):
+    """A liquid whose density rises to ~0.33 A^-3 at a compressed core: it
+    crosses the backflow cut-off density (0.033 A^-3) and reaches the range
+    where the high-density penalty (rho_m = 0.37 A^-3) acts; with a phase."""
+    rng = np.random.default_rng(seed)
+    rho0 = 0.0218360 * o.AUTOANG ** 3
+    ax = [(np.arange(n) - n // 2) * step for n in shape]
+    X, Y, Z = np.meshgrid(*ax, indexing="ij")
+    bump = np.exp(-(X ** 2 + Y ** 2 + Z ** 2) / (2 * 1.5 ** 2))
+    rho = rho0 * (1 + 0.2 * rng.random(shape)) * (1 + 14.0 * bump)
+    return np.sqrt(rho) * np.exp(0.3j * np.sin(2 * np.pi * X / (shape[0] * step)) + 0.2j * rng.random(shape))
+
+
+@pytest.mark.skipif(not ref_available(), reason="reference tree not present")
+@pytest.mark.parametrize("model", [2, 4, 10, 11, 13])
+def test_reference_build_live_vs_port_high_density(model):
+    """HD / HD2 models (Barranco penalty, backflow density cut-off, HD2's
+    wider spherical average): the restatement against libdft's own ot.c and
+    ot-energy.c (src/ot.c:164-166, 374-378, 815-819, 843-982;
+    src/ot-energy.c:96-99, 221-287) compiled on the same shim."""
+    ref, prt = Oracle("ref"), Oracle("port")
+    shape = (16, 18, 20)
+    out = []
+    for o in (ref, prt):
+        with Grids(o, shape, 0.8, 4.002602 / o.AUTOAMU) as g:
+            w = g.wf(hd_psi(o, shape, 0.8))
+            otf = g.ot(model, w)
+            out.append((g.potential(otf, w), g.energy_density(otf, w)))
+    assert relerr(out[0][0].real, out[1][0].real) < 1e-12
+    if np.abs(out[0][0].imag).max() > 0:
+        assert relerr(out[0][0].imag, out[1][0].imag) < 1e-11
+    assert relerr(out[0][1], out[1][1]) < 1e-12
+
+
+@pytest.mark.parametrize("model", [2, 4])
+def test_high_density_potential_is_the_energy_derivative(port, model):
+    """Without kinetic correlation and backflow the OT energy is a functional
+    of rho alone and the potential is its derivative: sum V drho dV = dE for a
+    small density change (central difference), in a region where the
+    high-density penalty is large.  (libdft's kinetic-correlation potential,
+    src/ot.c:604-797, is not the exact derivative of its kinetic-correlation
+    energy, src/ot-energy.c:123-191, on strongly varying densities -- 7 % on
+    this one -- so models with KC are left out.)"""
+    shape, step = (16, 16, 16), 0.8
+    psi = hd_psi(port, shape, step)
+    rng = np.random.default_rng(9)
+    ax = [(np.arange(n) - n // 2) * step for n in shape]
+    X, Y, Z = np.meshgrid(*ax, indexing="ij")
+    drho = np.exp(-((X - 0.5) ** 2 + Y ** 2 + (Z + 0.4) ** 2) / (2 * 1.2 ** 2)) * (1 + 0.1 * rng.random(shape))
+    with Grids(port, shape, step, 4.002602 / port.AUTOAMU) as g:
+        w = g.wf(np.abs(psi))
+        otf = g.ot(model, w)
+
+        def energy(p):
+            g.set_wf(w, p)
+            return float(np.sum(g.energy_density(otf, w)) * step ** 3)
+
+        rho = np.abs(psi) ** 2
+        h = 1e-4 * rho.max()
+        e_p = energy(np.sqrt(rho + h * drho))
+        e_m = energy(np.sqrt(rho - h * drho))
+        g.set_wf(w, np.sqrt(rho))
+        V = g.potential(otf, w).real
+    fd = (e_p - e_m) / (2 * h)
+    an = float(np.sum(V * drho) * step ** 3)
+    assert abs(fd / an - 1) < 1e-6, (fd, an)
