@@ -10,7 +10,7 @@ number renormalised to N after every step.  One "step" is one
 predict-correct step: two OT potential evaluations and two split-operator
 propagations.  --workload selects the specification's other cases (cfg0:
 64^3 plain OT with an external potential; cfg1: 128^3 real time; cfg4: the
-512^3 vortex ring); --grid overrides the grid size (profiling of smaller
+512^3 vortex ring); --grid overrides the grid size, N or NXxNYxNZ (profiling of smaller
 cases).  Data are synthetic; at 256^3 and above every input (psi: 134 MB in
 FP32 at 256^3) is larger than L2, so no L2 flush is needed between steps.
 
@@ -41,20 +41,26 @@ RHO0 = 0.0218360 * AUTOANG ** 3       # bulk liquid density at P = 0 (bohr^-3)
 NATOMS = 2000.0
 
 
-def droplet_psi(n=256, step=0.8, seed=3):
-    rho0 = RHO0
-    R = (3.0 * NATOMS / (4.0 * np.pi * rho0)) ** (1.0 / 3.0)
-    ax = (np.arange(n) - n // 2) * step
-    r = np.sqrt(ax[:, None, None] ** 2 + ax[None, :, None] ** 2 + ax[None, None, :] ** 2)
-    rho = 0.5 * rho0 * (1.0 - np.tanh((r - R) / 1.5))
-    rng = np.random.default_rng(seed)
-    psi = np.sqrt(rho) * (1.0 + 1e-3 * rng.standard_normal((n, n, n)))
-    return psi.astype(np.complex128)
+def _shape(n):
+    """a grid size: N (cubic) or (nx, ny, nz)"""
+    return tuple(n) if isinstance(n, (tuple, list)) else (n, n, n)
 
 
 def _centred(n, step):
-    ax = (np.arange(n) - n // 2) * step
-    return ax[:, None, None], ax[None, :, None], ax[None, None, :]
+    nx, ny, nz = _shape(n)
+    return ((np.arange(nx) - nx // 2) * step)[:, None, None], ((np.arange(ny) - ny // 2) * step)[None, :, None], \
+        ((np.arange(nz) - nz // 2) * step)[None, None, :]
+
+
+def droplet_psi(n=256, step=0.8, seed=3):
+    rho0 = RHO0
+    R = (3.0 * NATOMS / (4.0 * np.pi * rho0)) ** (1.0 / 3.0)
+    X, Y, Z = _centred(n, step)
+    r = np.sqrt(X ** 2 + Y ** 2 + Z ** 2)
+    rho = 0.5 * rho0 * (1.0 - np.tanh((r - R) / 1.5))
+    rng = np.random.default_rng(seed)
+    psi = np.sqrt(rho) * (1.0 + 1e-3 * rng.standard_normal(_shape(n)))
+    return psi.astype(np.complex128)
 
 
 def bubble_psi(n, step):
@@ -62,20 +68,20 @@ def bubble_psi(n, step):
     X, Y, Z = _centred(n, step)
     r2 = X ** 2 + Y ** 2 + Z ** 2
     rng = np.random.default_rng(42)
-    return (np.sqrt(RHO0) * (1 - np.exp(-r2 / (2 * 5.0 ** 2))) * (1 + 1e-3 * rng.standard_normal((n, n, n)))).astype(complex)
+    return (np.sqrt(RHO0) * (1 - np.exp(-r2 / (2 * 5.0 ** 2))) * (1 + 1e-3 * rng.standard_normal(_shape(n)))).astype(complex)
 
 
 def gaussian_vext(n, step):
     """10 K exp(-r^2 / (2 * 3^2)) at the grid centre."""
     X, Y, Z = _centred(n, step)
-    return 10.0 / AUTOK * np.exp(-(X ** 2 + Y ** 2 + Z ** 2) / (2 * 3.0 ** 2)) * np.ones((n, n, n))
+    return 10.0 / AUTOK * np.exp(-(X ** 2 + Y ** 2 + Z ** 2) / (2 * 3.0 ** 2)) * np.ones(_shape(n))
 
 
 def wave_psi(n, step):
     """rho0 (1 + 0.01 cos(2 pi x / (32 step) + phi)), phi ~ U(0, 2 pi) from seed 7."""
     X, _, _ = _centred(n, step)
     phase = np.random.default_rng(7).uniform(0, 2 * np.pi)
-    return (np.sqrt(RHO0 * (1 + 0.01 * np.cos(2 * np.pi * X / (32 * step) + phase))) * np.ones((n, n, n))).astype(complex)
+    return (np.sqrt(RHO0 * (1 + 0.01 * np.cos(2 * np.pi * X / (32 * step) + phase))) * np.ones(_shape(n))).astype(complex)
 
 
 def ring_psi(n, step, R=40.0, core=1.0):
@@ -108,7 +114,16 @@ def set_workload(name, grid=None):
     global W
     W = dict(WORKLOADS[name], name=name)
     if grid:
-        W["n"] = grid
+        W["n"] = grid if isinstance(grid, int) or len(grid) != 1 else grid[0]
+
+
+def shape():
+    return _shape(W["n"])
+
+
+def npoints():
+    nx, ny, nz = shape()
+    return nx * ny * nz
 
 
 def metric_name():
@@ -203,19 +218,18 @@ class Setup:
 
     def __init__(self, G, prec, psi0, vext0, norm):
         G.set_precision(prec)
-        n, step = W["n"], W["step"]
-        shape = (n, n, n)
-        self.w, self.wp = G.Wf(shape, step), G.Wf(shape, step)
+        step, shp = W["step"], shape()
+        self.w, self.wp = G.Wf(shp, step), G.Wf(shp, step)
         lg = W["lg"] / AUTOANG if W["lg"] else None
         self.ot = G.OT(W["model"], self.w, lg_bohr=lg)
         self.w.set(psi0)
         if norm is not None:
             self.w.norm_target = norm
             self.w.normalize()
-        self.P = G.CGrid(shape, step)
+        self.P = G.CGrid(shp, step)
         self.vext = None
         if vext0 is not None:
-            self.vext = G.RGrid(shape, step)
+            self.vext = G.RGrid(shp, step)
             self.vext.set(vext0)
         self.mu0 = self.ot.bulk_chempot(0.0)
 
@@ -272,12 +286,11 @@ def time_adjoint(G, torch, S, nsteps, every):
     """dJ/dVext and dJ/dpsi_0 of J = int (|psi_T|^2 - rho_t)^2 dV over nsteps
     steps (forward sweep, checkpoints every `every` steps, reverse sweep
     recomputing each segment), timed with CUDA events on the library's stream."""
-    n, step = W["n"], W["step"]
-    shape = (n, n, n)
+    step, shp = W["step"], shape()
     psi = S.w.get()
-    vext, rt, gv = G.RGrid(shape, step), G.RGrid(shape, step), G.RGrid(shape, step)
-    gp = G.CGrid(shape, step)
-    vext.set(np.zeros(shape))
+    vext, rt, gv = G.RGrid(shp, step), G.RGrid(shp, step), G.RGrid(shp, step)
+    gp = G.CGrid(shp, step)
+    vext.set(np.zeros(shp))
     rt.set(np.abs(psi) ** 2 * 1.01)
     S.ot.adjoint_run(S.w, vext, S.mu0, dt_au(), 2, W["renorm"], rt, gv, gp, checkpoint_every=every)   # allocations
     S.w.set(psi)
@@ -299,7 +312,7 @@ def model_bytes():
     """Algorithmic bytes of one FP32 step: (4 T + 28) N P, T = 3-D real transforms per potential
     (plain 5, + KC 24, full 34), P = 4 bytes."""
     T = {0: 5, 1: 24, 8: 15, 9: 34}[W["model"]]
-    return (4 * T + 28) * W["n"] ** 3 * 4
+    return (4 * T + 28) * npoints() * 4
 
 
 def run_gpu(args):
@@ -319,7 +332,7 @@ def run_gpu(args):
     psi0, vext0, norm = initial_state()
     K, Wu = args.steps, args.warmup
     n = W["n"]
-    N = n ** 3
+    N = npoints()
 
     # ---- FP32-bulk headline
     S = Setup(G, G.FP32, psi0, vext0, norm)
@@ -405,7 +418,7 @@ def run_gpu(args):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": workload_name(), "grid": [n, n, n], "model": model_name(),
+        "config": {"workload": workload_name(), "grid": list(shape()), "model": model_name(),
                    "precision": "FP32 bulk, FP64 reductions", "l2": l2_note(), "parallelism": "replicas"},
         "e2e": {"value": world * ke / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": 2 * N * 4,
                 "d2h_bytes_per_step": 2 * N * 4},
@@ -452,13 +465,14 @@ def model_name():
 
 
 def workload_name():
-    n = W["n"]
-    return "%s: %s, %d^3, step %g bohr" % (W["name"], W["what"], n, W["step"])
+    nx, ny, nz = shape()
+    g = "%d^3" % nx if nx == ny == nz else "%dx%dx%d" % (nx, ny, nz)
+    return "%s: %s, %s, step %g bohr" % (W["name"], W["what"], g, W["step"])
 
 
 def l2_note():
     """whether one wave function (FP32) outruns the 129 MB L2 between steps"""
-    mb = 8 * W["n"] ** 3 / 1e6
+    mb = 8 * npoints() / 1e6
     if mb > 129:
         return "inputs larger than L2 (psi %.0f MB FP32); no flush" % mb
     return "psi %.1f MB FP32 fits in L2 (smaller than the headline workload); no flush" % mb
@@ -471,9 +485,9 @@ def cpu_baseline(warmup=1, steps=5):
     from oracle import Grids, Oracle
     o = Oracle("port")
     psi0, vext0, norm = initial_state()
-    n, step = W["n"], W["step"]
+    step = W["step"]
     mass = 4.002602 / o.AUTOAMU
-    with Grids(o, (n, n, n), step, mass) as g:
+    with Grids(o, shape(), step, mass) as g:
         w = g.wf(psi0)
         vext = g.rgrid(vext0) if vext0 is not None else None
         # kernels sampled with one sub-point per cell: the step's cost does not
@@ -499,8 +513,8 @@ def cpu_baseline(warmup=1, steps=5):
             one()
         el = time.perf_counter() - t
     return {"value": steps / el, "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
-            "sample": "%d warm-up + %d timed predict-correct step(s) of the %s workload (%d^3), FP64, OpenMP over "
-                      "all host cores (%.1f s timed)" % (warmup, steps, W["name"], n, el)}
+            "sample": "%d warm-up + %d timed predict-correct step(s) of the %s workload (%s), FP64, OpenMP over "
+                      "all host cores (%.1f s timed)" % (warmup, steps, W["name"], "x".join(map(str, shape())), el)}
 
 
 def run_reference(args):
@@ -515,7 +529,7 @@ def run_reference(args):
     return {"impl": "reference", "metric": metric_name(), "value": cb["value"], "unit": "steps/s", "n_gpus": 0,
             "steps": steps, "warmup": warm, "ms_per_step": 1e3 / cb["value"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": workload_name(), "grid": [W["n"]] * 3},
+            "config": {"workload": workload_name(), "grid": list(shape())},
             "cpu_baseline": cb, "e2e": {"value": cb["value"], "unit": "steps/s", "h2d_bytes_per_step": 0,
                                         "d2h_bytes_per_step": 0}}
 
@@ -530,12 +544,13 @@ def main():
     ap.add_argument("--acc-steps", type=int, default=20)
     ap.add_argument("--cpu-steps", type=int, default=5, help="timed steps of the CPU baseline (after 1 warm-up)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--grid", type=int, default=0, help="grid points per axis (default: the workload's)")
+    ap.add_argument("--grid", default="", help="grid size N (cubic) or NXxNYxNZ (default: the workload's)")
     ap.add_argument("--fp32-only", action="store_true", help="skip the FP64 and accuracy phases (profiling runs)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    set_workload(args.workload, args.grid or None)
+    grid = tuple(int(v) for v in args.grid.lower().split("x")) if args.grid else None
+    set_workload(args.workload, grid)
     line = run_reference(args) if args.impl == "reference" else run_gpu(args)
     if line is not None:
         print(json.dumps(finite_or_null(line)))

@@ -487,8 +487,11 @@ int launch_fast_lines(int na, int nb, float sign, const Ld &ld, const St &st) {
   if (MODE != LINE_C2C) DFT_TRY(get_plan<float>(2 * N, &p2));
   ff::TmaMaps tm;
   memset(&tm, 0, sizeof(tm));
+  // TMA on the spectral side of the z passes: loads of the c2r / c2c passes,
+  // stores of the c2c passes.  The r2c passes keep their store loop: with a
+  // TMA store the 256^3 step ran at the same rate (235.4 against 236.6 steps/s).
   constexpr bool TMA_LD = LDS && spec_z_of<Ld>(0) && ff::TmaTile<N, MODE>::OK;
-  constexpr bool TMA_ST = STS && spec_z_of<St>(0) && ff::TmaTile<N, MODE>::OK;
+  constexpr bool TMA_ST = STS && MODE == LINE_C2C && spec_z_of<St>(0) && ff::TmaTile<N, MODE>::OK;
   if constexpr (TMA_LD || TMA_ST) {
     if (tma_on()) {
       constexpr int ROWS = ff::TmaTile<N, MODE>::ROWS;
