@@ -104,7 +104,8 @@ static int ot_vjp_t(dft_ot_functional *otf, wf *gwf, const typename cplx_t<T>::t
   {
     const T c2 = (T) otf->c2, c3 = (T) otf->c3, ck = (T) (otf->alpha_s / (2.0 * otf->mass));
     T *gr = r[A_GR], *wg = r[A_WG], *gm = r[A_GAM], *X = r[A_X], *loc = r[A_LOC], *Y = r[A_Y];
-    T *rb = r[R_RB], *rst = r[R_RST], *rt = r[R_RT], *dz = r[A_Z0];
+    T *rb = r[R_RB], *rt = r[R_RT], *dz = r[A_Z0];
+    const T irs = (T) (1.0 / otf->rho_0s);
     T *L0 = r[A_LJ0], *L1 = r[A_LJ1], *L2 = r[A_LJ2];
     T *J0 = r[R_J0], *J1 = r[R_J1], *J2 = r[R_J2];
     DFT_TRY(launch_rows(nx, ny, nz, [=] __device__(int x, int y, int z, int i) {
@@ -112,7 +113,7 @@ static int ot_vjp_t(dft_ot_functional *otf, wf *gwf, const typename cplx_t<T>::t
       X[i] = ga * q1 + w * (c2 + (T) 2 * c3 * b) * rho[i];
       loc[i] = w * q1;
       if (kc) {
-        Y[i] = ga * rst[i];
+        Y[i] = ga * ((T) 1 - rt[i] * irs);   // rho_st as the potential forms it
         const T *Ja[3] = { J0, J1, J2 };
         T *La[3] = { L0, L1, L2 };
         T dv = 0;
@@ -152,7 +153,8 @@ static int ot_vjp_t(dft_ot_functional *otf, wf *gwf, const typename cplx_t<T>::t
     // pointwise 2: Q_a = dF_a*Y = D_a (F*Y) ; lG_a = -c Q_a + F*lJ_a ; lg_a = c Gam J_a + lG_a rho_st ;
     //              lst = c gamma sum_a D_a J_a + sum lG_a g_a
     {
-      T *gr = r[A_GR], *gm = r[A_GAM], *rst = r[R_RST], *lst = r[A_LST], *fy = r[A_Q0];
+      T *gr = r[A_GR], *gm = r[A_GAM], *rt = r[R_RT], *lst = r[A_LST], *fy = r[A_Q0];
+      const T irs = (T) (1.0 / otf->rho_0s);
       T *F0 = r[A_FLJ0], *F1 = r[A_FLJ1], *F2 = r[A_FLJ2];
       T *J0 = r[R_J0], *J1 = r[R_J1], *J2 = r[R_J2], *G0 = r[A_LG0], *G1 = r[A_LG1], *G2 = r[A_LG2];
       DFT_TRY(launch_rows(nx, ny, nz, [=] __device__(int x, int y, int z, int i) {
@@ -163,7 +165,7 @@ static int ot_vjp_t(dft_ot_functional *otf, wf *gwf, const typename cplx_t<T>::t
           int ip, im; S.nb(x, y, z, i, a, ip, im);
           const T ga_ = (rho[ip] - rho[im]) * inv2h;
           const T lG = -ck * ((fy[ip] - fy[im]) * inv2h) + Fa[a][i];
-          Ga[a][i] = ck * gm[i] * Ja[a][i] + lG * rst[i];
+          Ga[a][i] = ck * gm[i] * Ja[a][i] + lG * ((T) 1 - rt[i] * irs);
           acc += lG * ga_;
           t1 += (Ja[a][ip] - Ja[a][im]) * inv2h;
         }
@@ -580,9 +582,8 @@ bool fits_r(dft_ot_functional *otf, const rgrid *r) {
   return r && P && r->nx == P->nx && r->ny == P->ny && r->nz == P->nz && r->prec == P->prec;
 }
 
-// While an adjoint entry point runs, the potential evaluations keep every
-// intermediate in its work slot (the VJP reads them), i.e. they do not use
-// the fused producer passes that keep some of them in registers only.
+// The potential evaluations leave every intermediate the VJP reads in its
+// work slot (rho_st excepted, which the VJP recomputes from F*rho).
 // The high-density terms and the absorbing boundary are not differentiated:
 // refused before any work.
 int hd_refused(dft_ot_functional *otf, wf *gwf = nullptr) {

@@ -142,6 +142,15 @@ bool factorised_propagation() {
   return v == 1;
 }
 
+bool march_on() {
+  static int v = -1;
+  if (v < 0) {
+    const char *e = getenv("DFTGPU_MARCH");
+    v = (e && e[0] == '0') ? 0 : 1;
+  }
+  return v == 1;
+}
+
 namespace {
 int g_tma = -1;
 }

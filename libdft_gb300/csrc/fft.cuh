@@ -424,6 +424,7 @@ template <class Kernel> bool SmemOptIn<Kernel>::done = false;
 bool generic_fft_only();   // DFTGPU_GENERIC_FFT=1 disables the register kernels
 bool prefetch_ahead_on();  // DFTGPU_PREFETCH_AHEAD=0 disables the one-wave-ahead L2 prefetch
 bool factorised_propagation();  // DFTGPU_FACTORISED_PROP=1: FP32 propagation by one kinetic pass per axis
+bool march_on();  // DFTGPU_MARCH=0: the second OT pointwise pass one CTA per row instead of x-marching
 
 // CTAs of a 256-thread kernel resident on the whole GPU at once (the distance
 // of the line kernels' one-wave-ahead prefetch); 0 when prefetching is off.

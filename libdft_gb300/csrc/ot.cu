@@ -20,6 +20,7 @@
 #include <string.h>
 
 #include "grid_internal.cuh"
+#include "ot_march.cuh"
 #include "ot_work.cuh"
 
 namespace dftgpu {
@@ -315,7 +316,7 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
   // pointwise 1
   {
     const T c2 = (T) otf->c2, c3 = (T) otf->c3, irs = (T) (1.0 / otf->rho_0s);
-    T *rb = r[R_RB], *rt = r[R_RT], *q = r[R_Q], *rst = r[R_RST];
+    T *rb = r[R_RB], *rt = r[R_RT], *q = r[R_Q];
     T *s0 = r[R_S0], *s1 = r[R_S1], *s2 = r[R_S2];
     T *v0 = r[R_V0], *v1 = r[R_V1], *v2 = r[R_V2], *e = r[R_E], *b0 = r[R_B0], *b1 = r[R_B1], *b2 = r[R_B2];
     const T inv2h = (T) (1.0 / (2.0 * P->step));
@@ -362,8 +363,7 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
       if (hdp) p.x += hp.vhd(rh);   // Barranco penalty src/ot.c:374-378, 815-819
       pot[i] = p;
       if (loc) q[i] = (c2 * b + c3 * (b * b)) * rh;
-      if (kc) {  // src/ot.c:608-612, 632-637
-        rst[i] = st;
+      if (kc) {  // src/ot.c:608-612, 632-637 (rho_st itself is recomputed from rt where needed)
         s0[i] = dr[0] * st; s1[i] = dr[1] * st; s2[i] = dr[2] * st;
       }
       if (bf) {  // C, B_a inputs src/ot.c:852-888 (HD: the cut-off density rho G)
@@ -372,7 +372,7 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
         e[i] = (va[2] * va[2] + va[1] * va[1] + va[0] * va[0]) * rb_;
         b0[i] = va[0] * rb_; b1[i] = va[1] * rb_; b2[i] = va[2] * rb_;
       }
-    }, nb * (5 + (kc ? 5 : 0) + (bf ? 9 : 0)), "ot_pointwise_1"));
+    }, nb * (5 + (kc ? 4 : 0) + (bf ? 9 : 0)), "ot_pointwise_1"));
   }
 
   // forward transforms of the produced fields (independent: parallel branches)
@@ -419,10 +419,26 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
     T *rt = r[R_RT], *J0 = r[R_J0], *J1 = r[R_J1], *J2 = r[R_J2], *h = r[R_H];
     T *v0 = r[R_V0], *v1 = r[R_V1], *v2 = r[R_V2], *A = r[R_A], *Cc = r[R_C], *B0 = r[R_BB0], *B1 = r[R_BB1], *B2 = r[R_BB2];
     T *wo0 = (T *) src.wout[0], *wo1 = (T *) src.wout[1], *wo2 = (T *) src.wout[2];
-    // FP32: 6 CTAs per SM (42 registers, no spills) keep more of its ~40 loads
-    // per element in flight; the FP64 variant would spill
+    const double pw2_bytes = nb * (2 + (kc ? 6 : 0) + (bf ? (cmerge ? 8 : 9) : 0));
+    bool marched = false;
+    if constexpr (std::is_same<T, float>::value) {   // x-marching form (ot_march.cuh)
+      if (march_on() && march2_fits(nx, ny, nz)) {
+        March2Args M;
+        M.pot = pot; M.rho = rho; M.rt = rt; M.J0 = J0; M.J1 = J1; M.J2 = J2;
+        M.v0 = v0; M.v1 = v1; M.v2 = v2; M.A = A; M.Cc = Cc; M.B0 = B0; M.B1 = B1; M.B2 = B2;
+        M.h = h; M.wo0 = wo0; M.wo1 = wo1; M.wo2 = wo2;
+        M.nx = nx; M.ny = ny; M.nz = nz; M.lx = 0;
+        M.c = c; M.hm = hm; M.cbf = cbf; M.pcap = pcap; M.inv2h = inv2h; M.eps = eps; M.irs = irs;
+        M.cmerge = cmerge; M.bfhd = bfhd; M.clampp = clampp; M.hp = hp;
+        ProfScope prof("ot_pointwise_2", pw2_bytes);
+        DFT_TRY(launch_march2(M, kc, bf));
+        marched = true;
+      }
+    }
+    // per-row form.  FP32: 6 CTAs per SM (42 registers, no spills) keep more
+    // of its ~40 loads per element in flight; the FP64 variant would spill
     constexpr int kMinBlocks = std::is_same<T, float>::value ? 6 : 1;
-    DFT_TRY(launch_rows_b<kMinBlocks>(nx, ny, nz, [=] __device__(int x, int y, int z, int i) {
+    if (!marched) DFT_TRY(launch_rows_b<kMinBlocks>(nx, ny, nz, [=] __device__(int x, int y, int z, int i) {
       C p = pot[i];
       T hval = 0, wv[3] = { 0, 0, 0 };   // stores last: every load is issued before them
       if (kc) {  // src/ot.c:641-645, 656-657, 673-675 summed over axes
@@ -470,7 +486,7 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
       if (kc) h[i] = hval;
       if (bf && wo0) { wo0[i] = wv[0]; wo1[i] = wv[1]; wo2[i] = wv[2]; }   // src/ot.c:924-931
       pot[i] = p;
-    }, nb * (2 + (kc ? 6 : 0) + (bf ? (cmerge ? 8 : 9) : 0)), "ot_pointwise_2"));
+    }, pw2_bytes, "ot_pointwise_2"));
   }
 
   // merged linear part (one inverse transform):

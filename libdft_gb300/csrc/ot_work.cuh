@@ -13,7 +13,8 @@ namespace dftgpu {
 // Real-field slots written by the potential evaluation (potential_t).  After a
 // potential evaluation they hold, for the wave function it was evaluated on:
 // R_RB rho_bar, R_RT F*rho, R_A V_j*rho,
-// R_Q (c2 rb + c3 rb^2) rho, R_RST rho_st, R_S0..2 G_a = (d_a rho) rho_st,
+// R_Q (c2 rb + c3 rb^2) rho, R_RST rho_st (energy density only: the potential and
+// its adjoint recompute rho_st = 1 - R_RT / rho_0s), R_S0..2 G_a = (d_a rho) rho_st,
 // R_V0..2 the velocity v_a (BF),
 // R_E rho|v|^2, R_B0..2 rho v_a, R_J0..2 J_a = F*G_a,
 // R_C V_j*(rho|v|^2) (only with a clamped backflow potential),

@@ -8,8 +8,8 @@ functional (PRB 72, 214522) in the library and, independently, in the oracle's
 shim.  The fixtures (tests/golden/hd.npz, `make_golden.py hd`) are libdft's own
 ot.c / ot-energy.c compiled over that shim, on a liquid compressed to ~15 rho0
 at its centre, so that the density crosses the backflow cut-off and reaches
-the penalty's range.  Live cases compare with the oracle restatement on grids
-whose FP32 potential runs through the producer z passes."""
+the penalty's range.  Live cases compare with the oracle restatement, on a
+grid whose second pointwise pass runs in its x-marching form."""
 import numpy as np
 import pytest
 
@@ -105,10 +105,10 @@ def test_hd_steps_and_term_entry_points_match_reference(gpu, prec):
 
 
 @pytest.mark.parametrize("model", [11, 13])
-def test_hd_live_vs_oracle_on_producer_pass_grids(gpu, port, prec, model):
-    """(16, 32, 128): nz / 2 = 64, so the FP32 potential runs through the
-    producer z passes (Barranco penalty in the local-correlation pass, the cut-off
-    density in the backflow pass)."""
+def test_hd_live_vs_oracle_marching_grid(gpu, port, prec, model):
+    """(16, 32, 128): nz = 128 and an even ny, so the FP32 potential's second
+    pointwise pass (the backflow with the cut-off density rho G and its
+    derivative) runs in its x-marching form."""
     shape, step = (16, 32, 128), 0.6
     psi = compressed_psi(gpu, shape, step, 8)
     with Grids(port, shape, step, gpu.HELIUM_MASS) as g:
