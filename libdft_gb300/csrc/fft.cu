@@ -23,15 +23,24 @@ std::map<std::pair<int, int>, PlanEntry> g_plans;   // (n, sizeof(T)) -> plan
 std::mutex g_plan_mu;
 
 int factorize(int n, int *radix, int *nst) {
-  int m = n, k = 0;
-  while (m % 8 == 0 && m > 8) { radix[k++] = 8; m /= 8; }
-  // finish the power-of-two part with one 8, 4 or 2
-  if (m % 8 == 0) { radix[k++] = 8; m /= 8; }
-  if (m % 4 == 0) { radix[k++] = 4; m /= 4; }
-  if (m % 2 == 0) { radix[k++] = 2; m /= 2; }
-  while (m % 3 == 0) { radix[k++] = 3; m /= 3; }
-  while (m % 5 == 0) { radix[k++] = 5; m /= 5; }
-  if (m != 1 || k > FFT_MAX_STAGES) return DFTGPU_ERR_SIZE;
+  int m = n, k = 0, a = 0, b = 0, c = 0;
+  while (m % 2 == 0) { m /= 2; a++; }
+  while (m % 3 == 0) { m /= 3; b++; }
+  while (m % 5 == 0) { m /= 5; c++; }
+  if (m != 1) return DFTGPU_ERR_SIZE;
+  // few stages: radix 16 for the power of two, one 8 / 4 / 2 for its rest;
+  // 15 = 3 x 5 and 9 = 3 x 3 for the odd part; a rest of 2 or 4 merged with
+  // a rest of 3 (6, 12) or 2 with a 5 (10)
+  while (a >= 4) { radix[k++] = 16; a -= 4; }
+  int r2 = 1 << a;
+  while (b >= 1 && c >= 1) { radix[k++] = 15; b--; c--; }
+  while (b >= 2) { radix[k++] = 9; b -= 2; }
+  if ((r2 == 2 || r2 == 4) && b == 1) { radix[k++] = 3 * r2; r2 = 1; b = 0; }
+  else if (r2 == 2 && c >= 1) { radix[k++] = 10; r2 = 1; c--; }
+  if (r2 > 1) radix[k++] = r2;
+  if (b == 1) radix[k++] = 3;
+  while (c-- > 0) radix[k++] = 5;
+  if (k > FFT_MAX_STAGES) return DFTGPU_ERR_SIZE;
   *nst = k;
   return DFTGPU_OK;
 }

@@ -10,9 +10,10 @@
 // row of length nz into nz/2 complex values (even + i odd), one FFT of length
 // nz/2 and a twiddle post-processing step; the inverse does the reverse.
 //
-// Every line pass stages a tile of B lines in shared memory as [n][B+1]
-// (element-major, padded), runs a Stockham autosort FFT with radices
-// {8,4,2,3,5} (ping-pong buffers) and streams the tile back.  Loads and
+// The generic line pass (any 2^a 3^b 5^c length, and all of FP64) stages a
+// tile of B lines in shared memory as [n][B+1] (element-major, padded), runs
+// a Stockham autosort FFT with radices {16, 15, 12, 10, 9, 8, 6, 5, 4, 3, 2}
+// (ping-pong buffers) and streams the tile back.  Loads and
 // stores go through functors, which is where pointwise producers (|psi|^2,
 // products of fields, phase factors) and consumers (accumulate into the
 // potential) are fused.  Twiddles come from per-length tables computed in
@@ -46,9 +47,44 @@ template <typename T> int get_plan(int n, FftPlan<T> *plan);
 template <typename C, typename T>
 __device__ __forceinline__ void dft2(C &a, C &b) { C t = a; a = t + b; b = t - b; }
 
+// v * exp(s i 2 pi m / R) given (cos, sin) of 2 pi m / R
+template <typename C, typename T> __device__ __forceinline__ C rot_cs(C v, T c, T sn, T s) {
+  const T si = s * sn;
+  C r; r.x = v.x * c - v.y * si; r.y = v.x * si + v.y * c;
+  return r;
+}
+
+template <int R, typename C, typename T> __device__ __forceinline__ void small_dft(C *u, T s);
+
+// Prime-factor radix R = R1 R2 (gcd 1, Good-Thomas): input n = (A1 n1 + A2 n2)
+// mod R, output k = (K1 k1 + K2 k2) mod R with K1 = 1 (mod R1), 0 (mod R2)
+// and K2 = 0 (mod R1), 1 (mod R2); no twiddles between the two layers.
+template <int R1, int R2, int A1, int A2, int K1, int K2, typename C, typename T>
+__device__ __forceinline__ void pfa_dft(C *u, T s) {
+  constexpr int R = R1 * R2;
+  C y[R2][R1];
+#pragma unroll
+  for (int n2 = 0; n2 < R2; n2++) {
+#pragma unroll
+    for (int n1 = 0; n1 < R1; n1++) y[n2][n1] = u[(A1 * n1 + A2 * n2) % R];
+    small_dft<R1, C, T>(y[n2], s);
+  }
+#pragma unroll
+  for (int k1 = 0; k1 < R1; k1++) {
+    C z[R2];
+#pragma unroll
+    for (int n2 = 0; n2 < R2; n2++) z[n2] = y[n2][k1];
+    small_dft<R2, C, T>(z, s);
+#pragma unroll
+    for (int k2 = 0; k2 < R2; k2++) u[(K1 * k1 + K2 * k2) % R] = z[k2];
+  }
+}
+
+// R-point DFT in place, natural order; s = -1 forward, +1 inverse.
+// Radices 2, 3, 4, 5, 8 directly; 16 and 9 as 4 x 4 and 3 x 3 with their
+// internal twiddles; 6, 10, 12, 15 as prime-factor pairs.
 template <int R, typename C, typename T>
 __device__ __forceinline__ void small_dft(C *u, T s) {
-  // s = -1 forward, +1 inverse
   if constexpr (R == 2) {
     dft2<C, T>(u[0], u[1]);
   } else if constexpr (R == 3) {
@@ -102,10 +138,65 @@ __device__ __forceinline__ void small_dft(C *u, T s) {
     u[5] = g0 - k0;
     u[3] = g1 + imul<C, T>(k1, s);
     u[7] = g1 - imul<C, T>(k1, s);
+  } else if constexpr (R == 16) {
+    // 4 x 4: 4-point DFTs over n1 of x[4 n1 + n2], twiddles W16^(n2 k1),
+    // 4-point DFTs over n2; X[k1 + 4 k2]
+    const T c1 = (T) 0.923879532511286756128, s1 = (T) 0.382683432365089771728, h = (T) 0.707106781186547524401;
+    C y[4][4];
+#pragma unroll
+    for (int n2 = 0; n2 < 4; n2++) {
+#pragma unroll
+      for (int n1 = 0; n1 < 4; n1++) y[n2][n1] = u[4 * n1 + n2];
+      small_dft<4, C, T>(y[n2], s);
+    }
+    y[1][1] = rot_cs<C, T>(y[1][1], c1, s1, s); y[1][2] = rot_cs<C, T>(y[1][2], h, h, s);
+    y[1][3] = rot_cs<C, T>(y[1][3], s1, c1, s);
+    y[2][1] = rot_cs<C, T>(y[2][1], h, h, s); y[2][2] = imul<C, T>(y[2][2], s);
+    y[2][3] = rot_cs<C, T>(y[2][3], -h, h, s);
+    y[3][1] = rot_cs<C, T>(y[3][1], s1, c1, s); y[3][2] = rot_cs<C, T>(y[3][2], -h, h, s);
+    y[3][3] = rot_cs<C, T>(y[3][3], -c1, -s1, s);
+#pragma unroll
+    for (int k1 = 0; k1 < 4; k1++) {
+      C z[4] = { y[0][k1], y[1][k1], y[2][k1], y[3][k1] };
+      small_dft<4, C, T>(z, s);
+#pragma unroll
+      for (int k2 = 0; k2 < 4; k2++) u[k1 + 4 * k2] = z[k2];
+    }
+  } else if constexpr (R == 9) {
+    // 3 x 3 with twiddles W9^(n2 k1): (n2, k1) = (1,1), (1,2), (2,1): m = 1, 2; (2,2): m = 4
+    const T ca = (T) 0.766044443118978035202, sa = (T) 0.642787609686539326323;
+    const T cb = (T) 0.173648177666930348852, sb = (T) 0.984807753012208059367;
+    const T cd = (T) -0.939692620785908384054, sd = (T) 0.342020143325668733044;
+    C y[3][3];
+#pragma unroll
+    for (int n2 = 0; n2 < 3; n2++) {
+#pragma unroll
+      for (int n1 = 0; n1 < 3; n1++) y[n2][n1] = u[3 * n1 + n2];
+      small_dft<3, C, T>(y[n2], s);
+    }
+    y[1][1] = rot_cs<C, T>(y[1][1], ca, sa, s); y[1][2] = rot_cs<C, T>(y[1][2], cb, sb, s);
+    y[2][1] = rot_cs<C, T>(y[2][1], cb, sb, s); y[2][2] = rot_cs<C, T>(y[2][2], cd, sd, s);
+#pragma unroll
+    for (int k1 = 0; k1 < 3; k1++) {
+      C z[3] = { y[0][k1], y[1][k1], y[2][k1] };
+      small_dft<3, C, T>(z, s);
+#pragma unroll
+      for (int k2 = 0; k2 < 3; k2++) u[k1 + 3 * k2] = z[k2];
+    }
+  } else if constexpr (R == 6) {
+    pfa_dft<2, 3, 3, 2, 3, 4, C, T>(u, s);
+  } else if constexpr (R == 10) {
+    pfa_dft<2, 5, 5, 2, 5, 6, C, T>(u, s);
+  } else if constexpr (R == 12) {
+    pfa_dft<4, 3, 3, 4, 9, 4, C, T>(u, s);
+  } else if constexpr (R == 15) {
+    pfa_dft<3, 5, 5, 3, 10, 6, C, T>(u, s);
   }
 }
 
 // One radix-R Stockham stage over a tile of B lines in [n][ldb] layout.
+// B divides blockDim.x: thread t works on line t % B, butterflies
+// t / B + j blockDim.x / B (no division per element).
 template <int R, typename T>
 __device__ __forceinline__ void stockham_stage(const typename cplx_t<T>::type *__restrict__ in,
                                                typename cplx_t<T>::type *__restrict__ out,
@@ -113,14 +204,15 @@ __device__ __forceinline__ void stockham_stage(const typename cplx_t<T>::type *_
                                                const typename cplx_t<T>::type *__restrict__ tw, T s) {
   typedef typename cplx_t<T>::type C;
   const int nR = n / R, twstep = n / (p * R);
-  for (int idx = threadIdx.x; idx < nR * B; idx += blockDim.x) {
-    const int l = idx % B, i = idx / B, k = i % p;
+  const int l = threadIdx.x % B, istep = blockDim.x / B;
+  for (int i = threadIdx.x / B; i < nR; i += istep) {
+    const int k = i % p;
     C u[R];
 #pragma unroll
     for (int q = 0; q < R; q++) {
       C v = in[(i + q * nR) * ldb + l];
       if (q > 0 && k > 0) {
-        C w = __ldg(&tw[(q * k * twstep) % n]);
+        C w = __ldg(&tw[q * k * twstep]);   // q k twstep < R p n / (p R) = n
         w.y *= -s;   // tw holds exp(-i...); inverse (s=+1) uses the conjugate
         v = cmul(v, w);
       }
@@ -144,11 +236,17 @@ __device__ __forceinline__ typename cplx_t<T>::type *tile_fft(typename cplx_t<T>
   for (int st = 0; st < pl.nst; st++) {
     const int R = pl.radix[st];
     switch (R) {
+      case 16: stockham_stage<16, T>(in, out, pl.n, B, ldb, p, pl.tw, s); break;
       case 8: stockham_stage<8, T>(in, out, pl.n, B, ldb, p, pl.tw, s); break;
       case 4: stockham_stage<4, T>(in, out, pl.n, B, ldb, p, pl.tw, s); break;
       case 2: stockham_stage<2, T>(in, out, pl.n, B, ldb, p, pl.tw, s); break;
       case 3: stockham_stage<3, T>(in, out, pl.n, B, ldb, p, pl.tw, s); break;
-      default: stockham_stage<5, T>(in, out, pl.n, B, ldb, p, pl.tw, s); break;
+      case 5: stockham_stage<5, T>(in, out, pl.n, B, ldb, p, pl.tw, s); break;
+      case 6: stockham_stage<6, T>(in, out, pl.n, B, ldb, p, pl.tw, s); break;
+      case 9: stockham_stage<9, T>(in, out, pl.n, B, ldb, p, pl.tw, s); break;
+      case 10: stockham_stage<10, T>(in, out, pl.n, B, ldb, p, pl.tw, s); break;
+      case 12: stockham_stage<12, T>(in, out, pl.n, B, ldb, p, pl.tw, s); break;
+      default: stockham_stage<15, T>(in, out, pl.n, B, ldb, p, pl.tw, s); break;
     }
     __syncthreads();
     p *= R;
@@ -170,6 +268,46 @@ template <typename T> struct LineArgs {
   int e_fast_store;      // 1: the store functor's fast address index is the element
 };
 
+// Visits the (line l, element e) pairs of this thread, e < n: element-fast
+// (each line in turn, elements across the threads) or line-fast (thread t
+// on line t % B, elements t / B + j blockDim.x / B); in batches of U whose
+// fetches are all issued before the first put, so that U global loads per
+// thread are in flight together.
+template <int U, class Fetch, class Put>
+__device__ __forceinline__ void batched_tile(int efast, int n, int B, Fetch fetch, Put put) {
+  typedef decltype(fetch(0, 0)) R;
+  const int tid = threadIdx.x, nth = blockDim.x;
+  if (efast) {
+    for (int e = tid; e < n; e += nth)
+      for (int l0 = 0; l0 < B; l0 += U) {
+        R r[U];
+#pragma unroll
+        for (int u = 0; u < U; u++)
+          if (l0 + u < B) r[u] = fetch(l0 + u, e);
+#pragma unroll
+        for (int u = 0; u < U; u++)
+          if (l0 + u < B) put(l0 + u, e, r[u]);
+      }
+  } else {
+    const int l = tid % B, est = nth / B;
+    for (int e0 = tid / B; e0 < n; e0 += U * est) {
+      R r[U];
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const int e = e0 + u * est;
+        if (e < n) r[u] = fetch(l, e);
+      }
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const int e = e0 + u * est;
+        if (e < n) put(l, e, r[u]);
+      }
+    }
+  }
+}
+
+template <typename C> struct CPair { C a, b; };
+
 // Line (a, b) = (blockIdx.y, blockIdx.x * B + l), element e.
 //   LINE_C2C: X = FFT(ld(a,b,e)), st(a,b,e,X[e]) for e < n
 //   LINE_R2C: z = ld(a,b,e) (packed even/odd reals), st(a,b,k,X[k]) for k <= n
@@ -182,28 +320,29 @@ __global__ void __launch_bounds__(FFT_THREADS) line_fft_kernel(const LineArgs<T>
   C *buf0 = reinterpret_cast<C *>(smem_raw);
   C *buf1 = buf0 + n * ldb;
   const int a = blockIdx.y, b0 = blockIdx.x * B;
+  // element-fast side: each line in turn, elements across the threads;
+  // line-fast side: thread t on line t % B, elements t / B + j (blockDim / B)
+  const int tid = threadIdx.x, nth = blockDim.x, lt = tid % B, et0 = tid / B, est = nth / B;
+  (void) lt; (void) et0; (void) est;
 
   // ---- load
   if (MODE == LINE_C2R) {
     // Z[k] = (X[k] + X*[n-k]) + i w^{-k} (X[k] - X*[n-k]),  w = exp(-2 pi i / 2n)
-    for (int idx = threadIdx.x; idx < n * B; idx += blockDim.x) {
-      int k, l;
-      if (args.e_fast) { k = idx % n; l = idx / n; } else { l = idx % B; k = idx / B; }
-      C xk = ld(a, b0 + l, k), xm = ld(a, b0 + l, n - k);
-      if (k == 0) { xk.y = (T) 0; xm.y = (T) 0; }   // DC / Nyquist are real
-      C sum = xk + conjc(xm), dif = xk - conjc(xm);
-      C w = __ldg(&args.tw2[k]);
-      w.y = -w.y;                                    // w^{-k}
-      C t = cmul(dif, w);
-      C z; z.x = sum.x - t.y; z.y = sum.y + t.x;     // sum + i t
-      buf0[k * ldb + l] = z;
-    }
+    batched_tile<4>(args.e_fast, n, B,
+        [&](int l, int k) { return CPair<C>{ ld(a, b0 + l, k), ld(a, b0 + l, n - k) }; },
+        [&](int l, int k, CPair<C> x) {
+          C xk = x.a, xm = x.b;
+          if (k == 0) { xk.y = (T) 0; xm.y = (T) 0; }   // DC / Nyquist are real
+          C sum = xk + conjc(xm), dif = xk - conjc(xm);
+          C w = __ldg(&args.tw2[k]);
+          w.y = -w.y;                                    // w^{-k}
+          C t = cmul(dif, w);
+          C z; z.x = sum.x - t.y; z.y = sum.y + t.x;     // sum + i t
+          buf0[k * ldb + l] = z;
+        });
   } else {
-    for (int idx = threadIdx.x; idx < n * B; idx += blockDim.x) {
-      int e, l;
-      if (args.e_fast) { e = idx % n; l = idx / n; } else { l = idx % B; e = idx / B; }
-      buf0[e * ldb + l] = ld(a, b0 + l, e);
-    }
+    batched_tile<8>(args.e_fast, n, B, [&](int l, int e) { return ld(a, b0 + l, e); },
+                    [&](int l, int e, C v) { buf0[e * ldb + l] = v; });
   }
   __syncthreads();
 
@@ -212,10 +351,7 @@ __global__ void __launch_bounds__(FFT_THREADS) line_fft_kernel(const LineArgs<T>
   // ---- store
   if (MODE == LINE_R2C) {
     // X[k] = (Z[k] + Z*[n-k]) / 2 - (i/2) w^k (Z[k] - Z*[n-k]),  k = 0..n
-    const int cnt = (n + 1) * B;
-    for (int idx = threadIdx.x; idx < cnt; idx += blockDim.x) {
-      int k, l;
-      if (args.e_fast_store) { k = idx % (n + 1); l = idx / (n + 1); } else { l = idx % B; k = idx / B; }
+    auto one = [&](int k, int l) {
       C zk = res[(k == n ? 0 : k) * ldb + l];
       C zm = res[(k == 0 ? 0 : n - k) * ldb + l];
       C sum = zk + conjc(zm), dif = zk - conjc(zm);
@@ -224,12 +360,19 @@ __global__ void __launch_bounds__(FFT_THREADS) line_fft_kernel(const LineArgs<T>
       C t = cmul(dif, w);
       C x; x.x = (T) 0.5 * (sum.x + t.y); x.y = (T) 0.5 * (sum.y - t.x);   // (sum - i t)/2
       st(a, b0 + l, k, x);
+    };
+    if (args.e_fast_store) {
+      for (int l = 0; l < B; l++)
+        for (int k = tid; k <= n; k += nth) one(k, l);
+    } else {
+      for (int k = et0; k <= n; k += est) one(k, lt);
     }
   } else {
-    for (int idx = threadIdx.x; idx < n * B; idx += blockDim.x) {
-      int e, l;
-      if (args.e_fast_store) { e = idx % n; l = idx / n; } else { l = idx % B; e = idx / B; }
-      st(a, b0 + l, e, res[e * ldb + l]);
+    if (args.e_fast_store) {
+      for (int l = 0; l < B; l++)
+        for (int e = tid; e < n; e += nth) st(a, b0 + l, e, res[e * ldb + l]);
+    } else {
+      for (int e = et0; e < n; e += est) st(a, b0 + lt, e, res[e * ldb + lt]);
     }
   }
 }
@@ -293,39 +436,50 @@ __global__ void __launch_bounds__(FFT_THREADS) xconv_kernel(const XConvArgs<T> A
   C *scr0 = bufs + A.nin * tile, *scr1 = scr0 + tile;
   const int kz = blockIdx.y, y0 = blockIdx.x * B;
   const size_t plane = (size_t) A.nx * A.ny;
+  const int l = threadIdx.x % B, e0 = threadIdx.x / B, est = blockDim.x / B;   // thread: one pencil
 
-  for (int in = 0; in < A.nin; in++) {
+  for (int in = 0; in < A.nin; in++) {   // forward transforms, each into its own tile
     const C *src = A.src[in] + kz * plane + y0;
-    for (int idx = threadIdx.x; idx < n * B; idx += blockDim.x) {
-      const int l = idx % B, e = idx / B;
-      scr0[e * ldb + l] = src[(size_t) e * A.ny + l];
+    C *tin = bufs + in * tile;
+    batched_tile<8>(0, n, B, [&](int ll, int e) { return src[(size_t) e * A.ny + ll]; },
+                    [&](int ll, int e, C v) { tin[e * ldb + ll] = v; });
+    __syncthreads();
+    C *r = tile_fft<T>(tin, scr0, A.plan, B, ldb, (T) -1);
+    if (r != tin) {   // an odd number of stages ends in the scratch tile
+      for (int idx = threadIdx.x; idx < tile; idx += blockDim.x) tin[idx] = r[idx];
+      __syncthreads();
     }
-    __syncthreads();
-    C *r = tile_fft<T>(scr0, scr1, A.plan, B, ldb, (T) -1);
-    C *dst = bufs + in * tile;
-    for (int idx = threadIdx.x; idx < tile; idx += blockDim.x) dst[idx] = r[idx];
-    __syncthreads();
   }
 
   for (int o = 0; o < A.nout; o++) {
     const XOut<T> &out = A.out[o];
-    for (int idx = threadIdx.x; idx < n * B; idx += blockDim.x) {
-      const int l = idx % B, e = idx / B;
-      C acc = mk<T>((T) 0, (T) 0);
+    constexpr int U = 4;   // U elements per batch: their kernel values loaded together
+    for (int eb = e0; eb < n; eb += U * est) {
+      C acc[U];
+#pragma unroll
+      for (int u = 0; u < U; u++) acc[u] = mk<T>((T) 0, (T) 0);
       for (int t = out.t0; t < out.t0 + out.nt; t++) {
         const XTerm<T> &tm = A.term[t];
-        acc = acc + apply_kernel<T>(tm, bufs[tm.in * tile + e * ldb + l], e, y0 + l, kz, A);
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+          const int e = eb + u * est;
+          if (e < n) acc[u] = acc[u] + apply_kernel<T>(tm, bufs[tm.in * tile + e * ldb + l], e, y0 + l, kz, A);
+        }
       }
-      scr0[e * ldb + l] = acc;
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const int e = eb + u * est;
+        if (e < n) scr0[e * ldb + l] = acc[u];
+      }
     }
     __syncthreads();
     C *r = tile_fft<T>(scr0, scr1, A.plan, B, ldb, (T) 1);
     C *dst = out.dst + kz * plane + y0;
-    for (int idx = threadIdx.x; idx < n * B; idx += blockDim.x) {
-      const int l = idx % B, e = idx / B;
-      C v = r[e * ldb + l];
-      if (out.accumulate) v = v + dst[(size_t) e * A.ny + l];
-      dst[(size_t) e * A.ny + l] = v;
+    if (out.accumulate) {
+      batched_tile<8>(0, n, B, [&](int ll, int e) { return dst[(size_t) e * A.ny + ll]; },
+                      [&](int ll, int e, C v) { dst[(size_t) e * A.ny + ll] = v + r[e * ldb + ll]; });
+    } else {
+      for (int e = e0; e < n; e += est) dst[(size_t) e * A.ny + l] = r[e * ldb + l];
     }
     __syncthreads();
   }

@@ -95,18 +95,29 @@ def run_case(G, shape, step, model, clamp, pot2):
 
 
 def test_marching_pass_matches_per_row_pass(gpu, tmp_path):
+    """Potentials and w_a within 1e-6 of the per-row form.  After the three
+    steps the two FP32 wave functions may part by more where the potential
+    is large (the compressed liquid of the high-density cases: V dt of
+    hundreds of radians turns one-ulp differences of V into phase
+    differences of 1e-4): there they agree within twice the per-row form's
+    own distance from the FP64 run (FP64 takes the per-row form)."""
     r = subprocess.run([sys.executable, "-c", CHILD, ROOT, json.dumps(CASES), str(tmp_path)],
                        env=dict(os.environ, DFTGPU_MARCH="0"), capture_output=True, text=True, timeout=900)
     assert r.returncode == 0 and "ok" in r.stdout, r.stderr[-2000:]
-    gpu.set_precision(1)
     try:
         for k, case in enumerate(CASES):
+            gpu.set_precision(0)
+            ref64 = run_case(gpu, *case)
+            gpu.set_precision(1)
             got = run_case(gpu, *case)
             for j, a in enumerate(got):
                 ref = np.load(tmp_path / ("case%d_%d.npy" % (k, j)))
                 err = relerr(a, ref)
-                print("case %s output %d: rel. difference %.2e" % (case, j, err))
-                assert err < 1e-6, (case, j, err)
+                tol = 1e-6
+                if j == len(got) - 1:
+                    tol = max(tol, 2 * relerr(ref, ref64[j]))
+                print("case %s output %d: rel. difference %.2e (tolerance %.1e)" % (case, j, err, tol))
+                assert err < tol, (case, j, err, tol)
     finally:
         gpu.set_precision(0)
 
