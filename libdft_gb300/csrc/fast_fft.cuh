@@ -36,9 +36,12 @@ typedef float2 C;
 // smallest value >= lo that is r (mod 16)
 constexpr int pitch_mod_16(int lo, int r) { return lo % 16 <= r ? lo - lo % 16 + r : lo - lo % 16 + 16 + r; }
 
+// Lengths 3 * 2^k (96, 192, 384) hold 12 elements per thread (radix 12 =
+// 4 x 3 first, then 4 and 2); the powers of two 16 (8 for N = 64).
 template <int N> struct Shape {
-  static constexpr int E = (N == 64) ? 8 : 16;
-  static constexpr int NS = (N == 512) ? 3 : 2;
+  static constexpr bool THREE = N % 3 == 0;
+  static constexpr int E = THREE ? 12 : (N == 64) ? 8 : 16;
+  static constexpr int NS = (N == 512 || N == 96 || N == 192) ? 3 : (N == 384) ? 4 : 2;
   static constexpr int TL = N / E;           // threads per line
   static constexpr int B = 256 / TL;         // lines per CTA
   // padded line pitch in shared memory (8-byte words; 16 bank pairs), chosen
@@ -54,7 +57,12 @@ template <int N> struct Shape {
   static constexpr int LP = TL == 8 ? pitch_mod_16(LP0 + 15, 8) : TL == 32 ? pitch_mod_16(LP0, 2) : LP0;
   static constexpr int SMEM = B * LP * (int) sizeof(C);
   template <int S> __host__ __device__ static constexpr int R() {
-    return N == 64 ? 8 : N == 128 ? (S == 0 ? 16 : 8) : N == 256 ? 16 : (S < 2 ? 16 : 2);
+    // the first stage takes all E elements of a thread (one butterfly): the
+    // loads fill slot q with element t + TL q, the first stage's input order
+    if constexpr (N == 96) return S == 0 ? 12 : S == 1 ? 4 : 2;
+    else if constexpr (N == 192) return S == 0 ? 12 : 4;
+    else if constexpr (N == 384) return S == 0 ? 12 : S < 3 ? 4 : 2;
+    else return N == 64 ? 8 : N == 128 ? (S == 0 ? 16 : 8) : N == 256 ? 16 : (S < 2 ? 16 : 2);
   }
   template <int S> __host__ __device__ static constexpr int P() {   // product of the radices before stage S
     if constexpr (S == 0) return 1;
@@ -62,7 +70,9 @@ template <int N> struct Shape {
   }
 };
 
-template <int N> constexpr bool supported() { return N == 64 || N == 128 || N == 256 || N == 512; }
+template <int N> constexpr bool supported() {
+  return N == 64 || N == 128 || N == 256 || N == 512 || N == 96 || N == 192 || N == 384;
+}
 
 __host__ __device__ constexpr int sidx(int l, int e, int LP) {
   return l * LP + e + (e >> 4) + ((LP & 15) == 8 ? ((l >> 1) & 15) : 0);
@@ -128,9 +138,39 @@ __device__ __forceinline__ void bf16(C *u, float s) {
   for (int i = 0; i < 16; i++) u[i] = t[i];
 }
 
+__device__ __forceinline__ void bf3(C *u, float s) {
+  const float s3 = 0.86602540378443864676f;
+  const C a = u[0], b = u[1], c = u[2];
+  const C m = a - (b + c) * 0.5f, d = (b - c) * s3;
+  u[0] = a + b + c;
+  u[1] = m + rot(d, s);
+  u[2] = m - rot(d, s);
+}
+
+// 12 = 4 x 3 by the prime-factor map: input (3 n1 + 4 n2) mod 12, output
+// (9 k1 + 4 k2) mod 12, no twiddles between the layers
+__device__ __forceinline__ void bf12(C *u, float s) {
+  C y[3][4];
+#pragma unroll
+  for (int n2 = 0; n2 < 3; n2++) {
+#pragma unroll
+    for (int n1 = 0; n1 < 4; n1++) y[n2][n1] = u[(3 * n1 + 4 * n2) % 12];
+    bf4(y[n2][0], y[n2][1], y[n2][2], y[n2][3], s);
+  }
+#pragma unroll
+  for (int k1 = 0; k1 < 4; k1++) {
+    C z[3] = { y[0][k1], y[1][k1], y[2][k1] };
+    bf3(z, s);
+#pragma unroll
+    for (int k2 = 0; k2 < 3; k2++) u[(9 * k1 + 4 * k2) % 12] = z[k2];
+  }
+}
+
 template <int R> __device__ __forceinline__ void bfR(C *u, float s) {
   if constexpr (R == 2) bf2(u);
+  else if constexpr (R == 4) bf4(u[0], u[1], u[2], u[3], s);
   else if constexpr (R == 8) bf8(u, s);
+  else if constexpr (R == 12) bf12(u, s);
   else bf16(u, s);
 }
 

@@ -22,6 +22,21 @@ struct PlanEntry {
 std::map<std::pair<int, int>, PlanEntry> g_plans;   // (n, sizeof(T)) -> plan
 std::mutex g_plan_mu;
 
+// FP64: radices up to 8 (the FP64 kernels compile for those only)
+int factorize_small(int n, int *radix, int *nst) {
+  int m = n, k = 0;
+  while (m % 8 == 0 && m > 8) { radix[k++] = 8; m /= 8; }
+  if (m % 8 == 0) { radix[k++] = 8; m /= 8; }
+  if (m % 4 == 0) { radix[k++] = 4; m /= 4; }
+  if (m % 2 == 0) { radix[k++] = 2; m /= 2; }
+  while (m % 3 == 0) { radix[k++] = 3; m /= 3; }
+  while (m % 5 == 0) { radix[k++] = 5; m /= 5; }
+  if (m != 1 || k > FFT_MAX_STAGES) return DFTGPU_ERR_SIZE;
+  *nst = k;
+  return DFTGPU_OK;
+}
+
+// FP32
 int factorize(int n, int *radix, int *nst) {
   int m = n, k = 0, a = 0, b = 0, c = 0;
   while (m % 2 == 0) { m /= 2; a++; }
@@ -48,8 +63,8 @@ int factorize(int n, int *radix, int *nst) {
 
 template <typename T> int get_plan(int n, FftPlan<T> *plan) {
   typedef typename cplx_t<T>::type C;
-  if (n < 1 || n > 2 * FFT_MAX_N) {
-    set_error(DFTGPU_ERR_SIZE, "FFT length %d outside [1, %d]", n, 2 * FFT_MAX_N);
+  if (n < 1 || n > FFT_MAX_LINE) {
+    set_error(DFTGPU_ERR_SIZE, "FFT length %d outside [1, %d]", n, FFT_MAX_LINE);
     return DFTGPU_ERR_SIZE;
   }
   std::lock_guard<std::mutex> lock(g_plan_mu);
@@ -58,7 +73,7 @@ template <typename T> int get_plan(int n, FftPlan<T> *plan) {
   if (it == g_plans.end()) {
     PlanEntry e;
     if (n == 1) { e.nst = 0; }
-    else if (factorize(n, e.radix, &e.nst) != DFTGPU_OK) {
+    else if ((sizeof(T) == 4 ? factorize(n, e.radix, &e.nst) : factorize_small(n, e.radix, &e.nst)) != DFTGPU_OK) {
       set_error(DFTGPU_ERR_SIZE, "FFT length %d is not of the form 2^a 3^b 5^c", n);
       return DFTGPU_ERR_SIZE;
     }
@@ -109,14 +124,15 @@ template <typename T> int get_plan(int n, FftPlan<T> *plan) {
 template int get_plan<float>(int, FftPlan<float> *);
 template int get_plan<double>(int, FftPlan<double> *);
 
-int choose_tile(int n, int nb, size_t cplx_bytes, int nbufs, int *B, size_t *smem) {
+int choose_tile(int n, int nb, size_t cplx_bytes, int nbufs, int *B, size_t *smem, bool partial) {
   const size_t budget = 113 * 1024, hard = 225 * 1024;
   const int cand[5] = { 16, 8, 4, 2, 1 };
   for (int pass = 0; pass < 2; pass++) {
     for (int c = 0; c < 5; c++) {
       int b = cand[c];
-      if (nb % b) continue;
-      size_t s = (size_t) nbufs * (size_t) n * (size_t) (b + 1) * cplx_bytes;
+      if (nb % b && !partial) continue;
+      if (b > nb && b > 1) continue;
+      size_t s = (size_t) nbufs * (size_t) n * (size_t) tile_pitch(b) * cplx_bytes;
       if (s <= (pass == 0 ? budget : hard)) { *B = b; *smem = s; return DFTGPU_OK; }
     }
   }
@@ -312,6 +328,9 @@ template <typename T> int launch_xconv(XConvArgs<T> &A) {
         case 128: rc = fast_xconv<128>(A); break;
         case 256: rc = fast_xconv<256>(A); break;
         case 512: rc = fast_xconv<512>(A); break;
+        case 96: rc = fast_xconv<96>(A); break;
+        case 192: rc = fast_xconv<192>(A); break;
+        case 384: rc = fast_xconv<384>(A); break;
         default: break;
       }
       if (rc >= 0) return rc;
@@ -360,6 +379,9 @@ template <typename T> int launch_xkinetic(KinArgs<T> &A) {
         case 128: rc = fast_xkinetic<128>(A); break;
         case 256: rc = fast_xkinetic<256>(A); break;
         case 512: rc = fast_xkinetic<512>(A); break;
+        case 96: rc = fast_xkinetic<96>(A); break;
+        case 192: rc = fast_xkinetic<192>(A); break;
+        case 384: rc = fast_xkinetic<384>(A); break;
         default: break;
       }
       if (rc >= 0) return rc;

@@ -12,8 +12,8 @@
 //
 // The generic line pass (any 2^a 3^b 5^c length, and all of FP64) stages a
 // tile of B lines in shared memory as [n][B+1] (element-major, padded), runs
-// a Stockham autosort FFT with radices {16, 15, 12, 10, 9, 8, 6, 5, 4, 3, 2}
-// (ping-pong buffers) and streams the tile back.  Loads and
+// a Stockham autosort FFT (ping-pong buffers; radices {16, 15, 12, 10, 9, 8,
+// 6, 5, 4, 3, 2} in FP32, {8, 5, 4, 3, 2} in FP64) and streams the tile back.  Loads and
 // stores go through functors, which is where pointwise producers (|psi|^2,
 // products of fields, phase factors) and consumers (accumulate into the
 // potential) are fused.  Twiddles come from per-length tables computed in
@@ -31,7 +31,8 @@ namespace dftgpu {
 
 constexpr int FFT_THREADS = 256;
 constexpr int FFT_MAX_STAGES = 16;
-constexpr int FFT_MAX_N = 1024;
+constexpr int FFT_MAX_N = 1024;      // grid dimension (3-D grids)
+constexpr int FFT_MAX_LINE = 4096;   // z of a 1-D grid (nx = ny = 1); transform lengths up to this
 
 template <typename T> struct FftPlan {
   int n;                       // transform length
@@ -235,18 +236,26 @@ __device__ __forceinline__ typename cplx_t<T>::type *tile_fft(typename cplx_t<T>
   int p = 1;
   for (int st = 0; st < pl.nst; st++) {
     const int R = pl.radix[st];
+    // FP64 plans use radices up to 8 only (the larger ones would raise the
+    // kernels' register count, and FP64 occupancy with it, for every length)
     switch (R) {
-      case 16: stockham_stage<16, T>(in, out, pl.n, B, ldb, p, pl.tw, s); break;
       case 8: stockham_stage<8, T>(in, out, pl.n, B, ldb, p, pl.tw, s); break;
       case 4: stockham_stage<4, T>(in, out, pl.n, B, ldb, p, pl.tw, s); break;
       case 2: stockham_stage<2, T>(in, out, pl.n, B, ldb, p, pl.tw, s); break;
       case 3: stockham_stage<3, T>(in, out, pl.n, B, ldb, p, pl.tw, s); break;
       case 5: stockham_stage<5, T>(in, out, pl.n, B, ldb, p, pl.tw, s); break;
-      case 6: stockham_stage<6, T>(in, out, pl.n, B, ldb, p, pl.tw, s); break;
-      case 9: stockham_stage<9, T>(in, out, pl.n, B, ldb, p, pl.tw, s); break;
-      case 10: stockham_stage<10, T>(in, out, pl.n, B, ldb, p, pl.tw, s); break;
-      case 12: stockham_stage<12, T>(in, out, pl.n, B, ldb, p, pl.tw, s); break;
-      default: stockham_stage<15, T>(in, out, pl.n, B, ldb, p, pl.tw, s); break;
+      default:
+        if constexpr (sizeof(T) == 4) {
+          switch (R) {
+            case 16: stockham_stage<16, T>(in, out, pl.n, B, ldb, p, pl.tw, s); break;
+            case 6: stockham_stage<6, T>(in, out, pl.n, B, ldb, p, pl.tw, s); break;
+            case 9: stockham_stage<9, T>(in, out, pl.n, B, ldb, p, pl.tw, s); break;
+            case 10: stockham_stage<10, T>(in, out, pl.n, B, ldb, p, pl.tw, s); break;
+            case 12: stockham_stage<12, T>(in, out, pl.n, B, ldb, p, pl.tw, s); break;
+            default: stockham_stage<15, T>(in, out, pl.n, B, ldb, p, pl.tw, s); break;
+          }
+        }
+        break;
     }
     __syncthreads();
     p *= R;
@@ -267,6 +276,10 @@ template <typename T> struct LineArgs {
   int e_fast;            // 1: the load functor's fast address index is the element
   int e_fast_store;      // 1: the store functor's fast address index is the element
 };
+
+// Element pitch of a tile of B lines: padded against bank conflicts between
+// lines; a single line (long lines of 1-D grids) needs no padding.
+__host__ __device__ __forceinline__ int tile_pitch(int B) { return B == 1 ? 1 : B + 1; }
 
 // Visits the (line l, element e) pairs of this thread, e < n: element-fast
 // (each line in turn, elements across the threads) or line-fast (thread t
@@ -316,7 +329,7 @@ template <typename T, int MODE, class Ld, class St>
 __global__ void __launch_bounds__(FFT_THREADS) line_fft_kernel(const LineArgs<T> args, const Ld ld, const St st) {
   typedef typename cplx_t<T>::type C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int n = args.plan.n, B = args.B, ldb = B + 1;
+  const int n = args.plan.n, B = args.B, ldb = tile_pitch(B);
   C *buf0 = reinterpret_cast<C *>(smem_raw);
   C *buf1 = buf0 + n * ldb;
   const int a = blockIdx.y, b0 = blockIdx.x * B;
@@ -324,12 +337,19 @@ __global__ void __launch_bounds__(FFT_THREADS) line_fft_kernel(const LineArgs<T>
   // line-fast side: thread t on line t % B, elements t / B + j (blockDim / B)
   const int tid = threadIdx.x, nth = blockDim.x, lt = tid % B, et0 = tid / B, est = nth / B;
   (void) lt; (void) et0; (void) est;
+  // the last tile may be partial (B need not divide nb): its missing lines
+  // are transformed as zeros and not stored
+  const int nb = args.nb;
+  const C zero = mk<T>((T) 0, (T) 0);
 
   // ---- load
   if (MODE == LINE_C2R) {
     // Z[k] = (X[k] + X*[n-k]) + i w^{-k} (X[k] - X*[n-k]),  w = exp(-2 pi i / 2n)
-    batched_tile<4>(args.e_fast, n, B,
-        [&](int l, int k) { return CPair<C>{ ld(a, b0 + l, k), ld(a, b0 + l, n - k) }; },
+    batched_tile<sizeof(T) == 4 ? 4 : 2>(args.e_fast, n, B,
+        [&](int l, int k) {
+          if (b0 + l >= nb) return CPair<C>{ zero, zero };
+          return CPair<C>{ ld(a, b0 + l, k), ld(a, b0 + l, n - k) };
+        },
         [&](int l, int k, CPair<C> x) {
           C xk = x.a, xm = x.b;
           if (k == 0) { xk.y = (T) 0; xm.y = (T) 0; }   // DC / Nyquist are real
@@ -341,8 +361,8 @@ __global__ void __launch_bounds__(FFT_THREADS) line_fft_kernel(const LineArgs<T>
           buf0[k * ldb + l] = z;
         });
   } else {
-    batched_tile<8>(args.e_fast, n, B, [&](int l, int e) { return ld(a, b0 + l, e); },
-                    [&](int l, int e, C v) { buf0[e * ldb + l] = v; });
+    batched_tile<sizeof(T) == 4 ? 8 : 4>(args.e_fast, n, B, [&](int l, int e) { return b0 + l < nb ? ld(a, b0 + l, e) : zero; },
+                                         [&](int l, int e, C v) { buf0[e * ldb + l] = v; });
   }
   __syncthreads();
 
@@ -359,7 +379,7 @@ __global__ void __launch_bounds__(FFT_THREADS) line_fft_kernel(const LineArgs<T>
       if (k == n) { w.x = (T) -1; w.y = (T) 0; }
       C t = cmul(dif, w);
       C x; x.x = (T) 0.5 * (sum.x + t.y); x.y = (T) 0.5 * (sum.y - t.x);   // (sum - i t)/2
-      st(a, b0 + l, k, x);
+      if (b0 + l < nb) st(a, b0 + l, k, x);
     };
     if (args.e_fast_store) {
       for (int l = 0; l < B; l++)
@@ -370,9 +390,11 @@ __global__ void __launch_bounds__(FFT_THREADS) line_fft_kernel(const LineArgs<T>
   } else {
     if (args.e_fast_store) {
       for (int l = 0; l < B; l++)
-        for (int e = tid; e < n; e += nth) st(a, b0 + l, e, res[e * ldb + l]);
+        if (b0 + l < nb)
+          for (int e = tid; e < n; e += nth) st(a, b0 + l, e, res[e * ldb + l]);
     } else {
-      for (int e = et0; e < n; e += est) st(a, b0 + lt, e, res[e * ldb + lt]);
+      if (b0 + lt < nb)
+        for (int e = et0; e < n; e += est) st(a, b0 + lt, e, res[e * ldb + lt]);
     }
   }
 }
@@ -431,7 +453,7 @@ template <typename T>
 __global__ void __launch_bounds__(FFT_THREADS) xconv_kernel(const XConvArgs<T> A) {
   typedef typename cplx_t<T>::type C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int n = A.plan.n, B = A.B, ldb = B + 1, tile = n * ldb;
+  const int n = A.plan.n, B = A.B, ldb = tile_pitch(B), tile = n * ldb;   // as choose_tile
   C *bufs = reinterpret_cast<C *>(smem_raw);
   C *scr0 = bufs + A.nin * tile, *scr1 = scr0 + tile;
   const int kz = blockIdx.y, y0 = blockIdx.x * B;
@@ -441,8 +463,8 @@ __global__ void __launch_bounds__(FFT_THREADS) xconv_kernel(const XConvArgs<T> A
   for (int in = 0; in < A.nin; in++) {   // forward transforms, each into its own tile
     const C *src = A.src[in] + kz * plane + y0;
     C *tin = bufs + in * tile;
-    batched_tile<8>(0, n, B, [&](int ll, int e) { return src[(size_t) e * A.ny + ll]; },
-                    [&](int ll, int e, C v) { tin[e * ldb + ll] = v; });
+    batched_tile<sizeof(T) == 4 ? 8 : 4>(0, n, B, [&](int ll, int e) { return src[(size_t) e * A.ny + ll]; },
+                                         [&](int ll, int e, C v) { tin[e * ldb + ll] = v; });
     __syncthreads();
     C *r = tile_fft<T>(tin, scr0, A.plan, B, ldb, (T) -1);
     if (r != tin) {   // an odd number of stages ends in the scratch tile
@@ -453,7 +475,7 @@ __global__ void __launch_bounds__(FFT_THREADS) xconv_kernel(const XConvArgs<T> A
 
   for (int o = 0; o < A.nout; o++) {
     const XOut<T> &out = A.out[o];
-    constexpr int U = 4;   // U elements per batch: their kernel values loaded together
+    constexpr int U = sizeof(T) == 4 ? 4 : 2;   // elements per batch: their kernel values loaded together
     for (int eb = e0; eb < n; eb += U * est) {
       C acc[U];
 #pragma unroll
@@ -476,8 +498,8 @@ __global__ void __launch_bounds__(FFT_THREADS) xconv_kernel(const XConvArgs<T> A
     C *r = tile_fft<T>(scr0, scr1, A.plan, B, ldb, (T) 1);
     C *dst = out.dst + kz * plane + y0;
     if (out.accumulate) {
-      batched_tile<8>(0, n, B, [&](int ll, int e) { return dst[(size_t) e * A.ny + ll]; },
-                      [&](int ll, int e, C v) { dst[(size_t) e * A.ny + ll] = v + r[e * ldb + ll]; });
+      batched_tile<sizeof(T) == 4 ? 8 : 4>(0, n, B, [&](int ll, int e) { return dst[(size_t) e * A.ny + ll]; },
+                                           [&](int ll, int e, C v) { dst[(size_t) e * A.ny + ll] = v + r[e * ldb + ll]; });
     } else {
       for (int e = e0; e < n; e += est) dst[(size_t) e * A.ny + l] = r[e * ldb + l];
     }
@@ -564,7 +586,8 @@ __global__ void __launch_bounds__(FFT_THREADS) xkinetic_kernel(const KinArgs<T> 
 }
 
 // ------------------------------------------------------------ launch helpers
-int choose_tile(int n, int nb, size_t cplx_bytes, int nbufs, int *B, size_t *smem);
+// partial: B need not divide nb (the kernel skips the missing lines of the last tile)
+int choose_tile(int n, int nb, size_t cplx_bytes, int nbufs, int *B, size_t *smem, bool partial = false);
 
 // "Opt-in shared memory already requested" flag per kernel instantiation.
 // It lives in an anonymous namespace so that every translation unit keeps its
@@ -719,6 +742,9 @@ int launch_lines(int n_fft, int na, int nb, T sign, const Ld &ld, const St &st, 
         case 128: rc = launch_fast_lines<128, MODE, EF, EFS>(na, nb, sign, ld, st); break;
         case 256: rc = launch_fast_lines<256, MODE, EF, EFS>(na, nb, sign, ld, st); break;
         case 512: rc = launch_fast_lines<512, MODE, EF, EFS>(na, nb, sign, ld, st); break;
+        case 96: rc = launch_fast_lines<96, MODE, EF, EFS>(na, nb, sign, ld, st); break;
+        case 192: rc = launch_fast_lines<192, MODE, EF, EFS>(na, nb, sign, ld, st); break;
+        case 384: rc = launch_fast_lines<384, MODE, EF, EFS>(na, nb, sign, ld, st); break;
         default: break;
       }
       if (rc >= 0) return rc;
@@ -737,7 +763,7 @@ int launch_lines(int n_fft, int na, int nb, T sign, const Ld &ld, const St &st, 
     args.tw2 = p2.tw;
   }
   int B; size_t smem;
-  DFT_TRY(choose_tile(n_fft, nb, sizeof(C), 2, &B, &smem));
+  DFT_TRY(choose_tile(n_fft, nb, sizeof(C), 2, &B, &smem, true));
   args.B = B;
   auto kfn = line_fft_kernel<T, MODE, Ld, St>;
   typedef SmemOptIn<LineArgs<T> (*)(Ld *, St *, int (*)[MODE + 1])> Flag;
@@ -749,7 +775,7 @@ int launch_lines(int n_fft, int na, int nb, T sign, const Ld &ld, const St &st, 
     set_error(DFTGPU_ERR_SIZE, "line FFT n=%d needs %zu bytes of shared memory", n_fft, smem);
     return DFTGPU_ERR_SIZE;
   }
-  dim3 grid(nb / B, na);
+  dim3 grid((nb + B - 1) / B, na);
   kfn<<<grid, FFT_THREADS, smem, rt().stream>>>(args, ld, st);
   DFT_CHECK_LAUNCH();
   return DFTGPU_OK;

@@ -190,14 +190,19 @@ void dev_free(void *p) { if (p) cudaFree(p); }
 
 // Grid dimensions: 2^a 3^b 5^c in [2, FFT_MAX_N]; x and y may be odd (libdft's
 // largest production grid is 729 x 384 x 384, examples/gas-bubble/config.h:56),
-// z must be even (real fields are transformed as packed pairs along z).
+// z must be even (real fields are transformed as packed pairs along z).  A 1-D
+// grid, nx = ny = 1 (libdft's 1-D effective model, src/ot.c:133-217; its
+// driver examples/1d-bubble/bubble-1d.c:25 runs nz = 4096), takes nz up to
+// FFT_MAX_LINE.
 int check_dims(INT nx, INT ny, INT nz) {
+  const bool one_d = nx == 1 && ny == 1;
   INT d[3] = { nx, ny, nz };
   for (int i = 0; i < 3; i++) {
     INT m = d[i];
-    if (m < 2 || m > FFT_MAX_N || (i == 2 && (m & 1))) {
-      set_error(DFTGPU_ERR_SIZE, "grid dimension %ld must be in [2, %d]%s", (long) m, FFT_MAX_N,
-                i == 2 ? " and even along z" : "");
+    const INT lo = one_d && i < 2 ? 1 : 2, hi = one_d ? FFT_MAX_LINE : FFT_MAX_N;
+    if (m < lo || m > hi || (i == 2 && (m & 1))) {
+      set_error(DFTGPU_ERR_SIZE, "grid dimension %ld must be in [2, %d] (nz up to %d with nx = ny = 1)%s", (long) m,
+                FFT_MAX_N, FFT_MAX_LINE, i == 2 ? " and even along z" : "");
       return DFTGPU_ERR_SIZE;
     }
     while (m % 2 == 0) m /= 2;

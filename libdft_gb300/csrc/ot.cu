@@ -57,6 +57,40 @@ struct ShapeBF {
   }
 };
 
+// 1-D effective kernels of a grid with nx = ny = 1 (libdft's DFT_OT_1D branch,
+// src/ot.c:133-217, src/ot.h:146), integrated over the x-y plane: LJ with the
+// core |z| < h evaluated at h (src/common.c:80-91), the sphere's
+// cross-section (src/common.c:152-158), the Gaussian's line density
+// (src/common.c:214-220), the backflow kernel (src/ot-private.h:29-41)
+struct ShapeLJ1D {
+  double h, sig, eps;
+  __device__ double operator()(double, double, double z) const {
+    const double s6 = pow(sig, 6.0);
+    double a = fabs(z);
+    if (a < h) a = h;
+    return 2.0 * M_PI * eps * s6 * (2.0 * s6 - 5.0 * pow(a, 6.0)) / (5.0 * pow(a, 10.0));
+  }
+};
+struct ShapeSA1D {
+  double h;
+  __device__ double operator()(double, double, double z) const {
+    const double a = fabs(z);
+    return a > h ? 0.0 : 3.0 * (h * h - a * a) / (4.0 * h * h * h);
+  }
+};
+struct ShapeGauss1D {
+  double iw;
+  __device__ double operator()(double, double, double z) const { return iw / sqrt(M_PI) * exp(-z * z * iw * iw); }
+};
+struct ShapeBF1D {
+  double g11, g12, g21, g22, a1, a2;
+  __device__ double operator()(double, double, double z) const {
+    const double z2 = z * z;
+    return M_PI * ((g11 + g12 * (1.0 + a1 * z2) / a1) * exp(-a1 * z2) / a1 +
+                   (g21 + g22 * (1.0 + a2 * z2) / a2) * exp(-a2 * z2) / a2);
+  }
+};
+
 template <class S>
 __device__ double cell_average(const S &f, double x, double y, double z, double step, int ns) {
   double sum = 0.0;
@@ -157,7 +191,10 @@ int ot_generate_kernels(dft_ot_functional *otf, int min_ns, int max_ns) {
   const size_t n = (size_t) P->nx * P->ny * P->nz;
   const size_t nspec = (size_t) (P->nz / 2 + 1) * P->nx * P->ny;
   const double tol = 0.01 / GRID_AUTOK;
-  const double dv = P->step * P->step * P->step, inv_n = 1.0 / (double) n;
+  // the convolution measure: the volume element, or on a 1-D grid (nx = ny = 1)
+  // the line element dz, its kernels being integrated over the x-y plane
+  const bool one_d = P->nx == 1 && P->ny == 1;
+  const double dv = one_d ? P->step : P->step * P->step * P->step, inv_n = 1.0 / (double) n;
   double *f = (double *) dev_alloc(n * sizeof(double));
   double *g = (double *) dev_alloc(n * sizeof(double));
   double2 *spec = (double2 *) dev_alloc(nspec * sizeof(double2));
@@ -172,28 +209,34 @@ int ot_generate_kernels(dft_ot_functional *otf, int min_ns, int max_ns) {
   {
     // LJ with integral b (src/ot.c:150-161), spherical average with integral 1 (src/ot.c:164-181)
     for (int which = 0; which < 2; which++) {
-      if (which == 0) {
+      const double radius = (otf->model & DFT_OT_HD2) ? otf->lj_params.h * 1.065 : otf->lj_params.h;
+      if (which == 0 && one_d) {
+        rc = adaptive_map(f, P, min_ns, max_ns, tol, ShapeLJ1D{otf->lj_params.h, otf->lj_params.sigma, otf->lj_params.epsilon});
+      } else if (which == 0) {
         ShapeLJ s{otf->lj_params.h, otf->lj_params.sigma, otf->lj_params.epsilon, otf->lj_params.cval};
         rc = adaptive_map(f, P, min_ns, max_ns, tol, s);
+      } else if (one_d) {
+        rc = adaptive_map(f, P, min_ns, max_ns, tol, ShapeSA1D{radius});
       } else {   // HD2: radius 1.065 h (src/ot.c:164-166, PRB 72, 214522)
-        ShapeSA s{(otf->model & DFT_OT_HD2) ? otf->lj_params.h * 1.065 : otf->lj_params.h};
-        rc = adaptive_map(f, P, min_ns, max_ns, tol, s);
+        rc = adaptive_map(f, P, min_ns, max_ns, tol, ShapeSA{radius});
       }
       if (rc) goto done;
       if ((rc = rfft3_fp64(f, spec, P))) goto done;
       double2 k0;
       if (cudaMemcpyAsync(&k0, spec, sizeof(k0), cudaMemcpyDeviceToHost, rt().stream) != cudaSuccess ||
           cudaStreamSynchronize(rt().stream) != cudaSuccess) { rc = DFTGPU_ERR_CUDA; goto done; }
+      // 1-D kernels are not rescaled to their integrals (src/ot.c:159-160, 180-181)
       const double target = which == 0 ? otf->b : 1.0;
-      const double scale = target / (dv * k0.x) * dv * inv_n;
+      const double scale = one_d ? dv * inv_n : target / (dv * k0.x) * dv * inv_n;
       rc = P->prec == DFTGPU_FP32 ? extract_octant<float>(spec, (float *) P->ker[which], P, 0, scale)
                                   : extract_octant<double>(spec, (double *) P->ker[which], P, 0, scale);
       if (rc) goto done;
     }
     if (otf->model & DFT_OT_KC) {
       // Gaussian F and its central-difference gradient (src/ot.c:184-200)
-      ShapeGauss s{1.0 / otf->l_g};
-      if ((rc = adaptive_map(f, P, min_ns, max_ns, tol, s))) goto done;
+      rc = one_d ? adaptive_map(f, P, min_ns, max_ns, tol, ShapeGauss1D{1.0 / otf->l_g})
+                 : adaptive_map(f, P, min_ns, max_ns, tol, ShapeGauss{1.0 / otf->l_g});
+      if (rc) goto done;
       for (int which = 2; which < 6; which++) {
         const double *src = f;
         if (which > 2) { if ((rc = fd_field(f, g, P, which - 3))) goto done; src = g; }
@@ -206,8 +249,9 @@ int ot_generate_kernels(dft_ot_functional *otf, int min_ns, int max_ns) {
     if (otf->model & DFT_OT_BACKFLOW) {
       // V_j (src/ot.c:207-217)
       const dft_ot_bf &b = otf->bf_params;
-      ShapeBF s{b.g11, b.g12, b.g21, b.g22, b.a1, b.a2};
-      if ((rc = adaptive_map(f, P, min_ns, max_ns, tol, s))) goto done;
+      rc = one_d ? adaptive_map(f, P, min_ns, max_ns, tol, ShapeBF1D{b.g11, b.g12, b.g21, b.g22, b.a1, b.a2})
+                 : adaptive_map(f, P, min_ns, max_ns, tol, ShapeBF{b.g11, b.g12, b.g21, b.g22, b.a1, b.a2});
+      if (rc) goto done;
       if ((rc = rfft3_fp64(f, spec, P))) goto done;
       rc = P->prec == DFTGPU_FP32 ? extract_octant<float>(spec, (float *) P->ker[6], P, 0, dv * inv_n)
                                   : extract_octant<double>(spec, (double *) P->ker[6], P, 0, dv * inv_n);

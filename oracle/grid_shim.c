@@ -525,9 +525,15 @@ void rgrid_inverse_fft_norm(rgrid *g) {
   rgrid_scale_real(g, 1.0 / (REAL) (g->nx * g->ny * g->nz));
 }
 
+/* Inverse transform of a convolution, times the volume element over N.  A
+ * grid with one point across x and y (libdft's 1-D effective model, whose
+ * kernels are already integrated over the x-y plane, src/ot.c:133-217) takes
+ * the line element dz = step instead of step^3: this is the measure under
+ * which the uniform liquid keeps its bulk chemical potential. */
 void rgrid_inverse_fft_norm2(rgrid *g) {
   rgrid_inverse_fft(g);
-  rgrid_scale_real(g, g->step * g->step * g->step / (REAL) (g->nx * g->ny * g->nz));
+  const REAL dv = (g->nx == 1 && g->ny == 1) ? g->step : g->step * g->step * g->step;
+  rgrid_scale_real(g, dv / (REAL) (g->nx * g->ny * g->nz));
 }
 
 /* Product of two spectra times the centring phase: the kernel operand was

@@ -9,7 +9,7 @@
  * organised as a few fused per-point loops around FFT convolutions; every
  * term cites the reference line it restates.  The high-density terms (HD,
  * HD2) use the shim's restatement of libgrid's grid_func1..5 (grid_shim.c).
- * Unsupported models (thermal, GP, DR, 1-D) are rejected with an error
+ * Unsupported models (thermal, GP, DR) are rejected with an error
  * message.
  */
 #include <string.h>
@@ -55,6 +55,42 @@ REAL dft_ot_backflow_pot(void *arg, REAL x, REAL y, REAL z) {
   const dft_ot_bf *p = (const dft_ot_bf *) arg;
   REAL r2 = x * x + y * y + z * z;
   return (p->g11 + p->g12 * r2) * exp(-p->a1 * r2) + (p->g21 + p->g22 * r2) * exp(-p->a2 * r2);
+}
+
+/* 1-D effective kernels of a grid with nx = ny = 1, already integrated over
+ * the x-y plane (src/ot.c:133-217 with DFT_OT_1D, src/ot.h:146): LJ with the
+ * core |z| < h evaluated at h (src/common.c:80-91), the sphere's cross-section
+ * (src/common.c:152-158), the Gaussian's line density (src/common.c:214-220),
+ * and the backflow kernel integrated over the plane (src/ot-private.h:29-41). */
+REAL dft_common_lennard_jones_1d(void *arg, REAL x, REAL y, REAL z) {
+  const dft_common_lj *p = (const dft_common_lj *) arg;
+  REAL s6 = pow(p->sigma, 6.0);
+  (void) x; (void) y;
+  z = fabs(z);
+  if (z < p->h) z = p->h;
+  return 2.0 * M_PI * p->epsilon * s6 * (2.0 * s6 - 5.0 * pow(z, 6.0)) / (5.0 * pow(z, 10.0));
+}
+
+REAL dft_common_spherical_avg_1d(void *arg, REAL x, REAL y, REAL z) {
+  REAL h = *(const REAL *) arg, h2 = h * h;
+  (void) x; (void) y;
+  z = fabs(z);
+  if (z > h) return 0.0;
+  return 3.0 * (h2 - z * z) / (4.0 * h2 * h);
+}
+
+REAL dft_common_gaussian_1d(void *arg, REAL x, REAL y, REAL z) {
+  REAL iw = *(const REAL *) arg;
+  (void) x; (void) y;
+  return iw / sqrt(M_PI) * exp(-z * z * iw * iw);
+}
+
+REAL dft_ot_backflow_pot_1d(void *arg, REAL x, REAL y, REAL z) {
+  const dft_ot_bf *p = (const dft_ot_bf *) arg;
+  REAL z2 = z * z;
+  (void) x; (void) y;
+  return M_PI * ((p->g11 + p->g12 * (1.0 + p->a1 * z2) / p->a1) * exp(-p->a1 * z2) / p->a1
+               + (p->g21 + p->g22 * (1.0 + p->a2 * z2) / p->a2) * exp(-p->a2 * z2) / p->a2);
 }
 
 /* sqrt(rho) (1 + a cos(k.r)) (src/common.c:1214-1224). */
@@ -180,11 +216,8 @@ dft_ot_functional *dft_ot_alloc(INT model, wf *gwf, INT min_ns, INT max_ns) {
   cgrid *c = gwf->grid;
   REAL step = c->step, tol = 0.01 / GRID_AUTOK, radius, iw;
 
+  const int one_d = c->nx == 1 && c->ny == 1;   /* the 1-D effective model (src/ot.c:133-217) */
   if (!check_model(model, "dft_ot_alloc")) return NULL;
-  if (c->nx == 1 && c->ny == 1) {
-    fprintf(stderr, "oracle: the 1-D effective model is not restated.\n");
-    return NULL;
-  }
   dft_ot_functional *otf = (dft_ot_functional *) calloc(1, sizeof(dft_ot_functional));
   if (!otf) return NULL;
   otf->model = model;
@@ -192,16 +225,20 @@ dft_ot_functional *dft_ot_alloc(INT model, wf *gwf, INT min_ns, INT max_ns) {
 
   /* LJ kernel, rescaled so that its integral is b (src/ot.c:150-161) */
   otf->lennard_jones = new_grid(gwf, "OT LJ");
-  rgrid_adaptive_map(otf->lennard_jones, dft_common_lennard_jones, &otf->lj_params, min_ns, max_ns, tol);
+  rgrid_adaptive_map(otf->lennard_jones, one_d ? dft_common_lennard_jones_1d : dft_common_lennard_jones,
+                     &otf->lj_params, min_ns, max_ns, tol);
   rgrid_fft(otf->lennard_jones);
-  rgrid_fft_multiply(otf->lennard_jones, otf->b / (step * step * step * creal(rgrid_cvalue_at_index(otf->lennard_jones, 0, 0, 0))));
+  if (!one_d)   /* the 1-D kernels are not rescaled (src/ot.c:159-160, 180-181) */
+    rgrid_fft_multiply(otf->lennard_jones, otf->b / (step * step * step * creal(rgrid_cvalue_at_index(otf->lennard_jones, 0, 0, 0))));
 
   /* spherical average of radius h (HD2: 1.065 h), integral 1 (src/ot.c:164-181) */
   radius = (model & DFT_OT_HD2) ? otf->lj_params.h * 1.065 : otf->lj_params.h;
   otf->spherical_avg = new_grid(gwf, "OT SA");
-  rgrid_adaptive_map(otf->spherical_avg, dft_common_spherical_avg, &radius, min_ns, max_ns, tol);
+  rgrid_adaptive_map(otf->spherical_avg, one_d ? dft_common_spherical_avg_1d : dft_common_spherical_avg, &radius,
+                     min_ns, max_ns, tol);
   rgrid_fft(otf->spherical_avg);
-  rgrid_fft_multiply(otf->spherical_avg, 1.0 / (step * step * step * creal(rgrid_cvalue_at_index(otf->spherical_avg, 0, 0, 0))));
+  if (!one_d)
+    rgrid_fft_multiply(otf->spherical_avg, 1.0 / (step * step * step * creal(rgrid_cvalue_at_index(otf->spherical_avg, 0, 0, 0))));
 
   /* KC Gaussian F and its finite-difference gradient (src/ot.c:184-200) */
   if (model & DFT_OT_KC) {
@@ -210,7 +247,7 @@ dft_ot_functional *dft_ot_alloc(INT model, wf *gwf, INT min_ns, INT max_ns) {
     otf->gaussian_x_tf = new_grid(gwf, "OT dF/dx");
     otf->gaussian_y_tf = new_grid(gwf, "OT dF/dy");
     otf->gaussian_z_tf = new_grid(gwf, "OT dF/dz");
-    rgrid_adaptive_map(otf->gaussian_tf, dft_common_gaussian, &iw, min_ns, max_ns, tol);
+    rgrid_adaptive_map(otf->gaussian_tf, one_d ? dft_common_gaussian_1d : dft_common_gaussian, &iw, min_ns, max_ns, tol);
     rgrid_gradient(otf->gaussian_tf, otf->gaussian_x_tf, otf->gaussian_y_tf, otf->gaussian_z_tf);
     rgrid_fft(otf->gaussian_x_tf);
     rgrid_fft(otf->gaussian_y_tf);
@@ -221,7 +258,8 @@ dft_ot_functional *dft_ot_alloc(INT model, wf *gwf, INT min_ns, INT max_ns) {
   /* backflow kernel V_j (src/ot.c:207-217) */
   if (model & DFT_OT_BACKFLOW) {
     otf->backflow_pot = new_grid(gwf, "OT Vj");
-    rgrid_adaptive_map(otf->backflow_pot, dft_ot_backflow_pot, &otf->bf_params, min_ns, max_ns, tol);
+    rgrid_adaptive_map(otf->backflow_pot, one_d ? dft_ot_backflow_pot_1d : dft_ot_backflow_pot, &otf->bf_params,
+                       min_ns, max_ns, tol);
     rgrid_fft(otf->backflow_pot);
   }
 

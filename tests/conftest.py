@@ -59,3 +59,12 @@ def liquid_psi(shape, step, seed, amp=0.1):
                   + 0.5 * amp * np.sin(4 * np.pi * Z / L[2]))
     phase = 0.4 * np.sin(2 * np.pi * X / L[0]) + 0.3 * np.cos(2 * np.pi * (Y / L[1] + Z / L[2]))
     return (np.sqrt(rho) * np.exp(1j * phase) * (1 + 1e-3 * rng.standard_normal(shape))).astype(np.complex128)
+
+
+def line_psi(o, n, step, seed=5):
+    """a liquid column along z with a density wave and a phase (1-D grid, nx = ny = 1)"""
+    rng = np.random.default_rng(seed)
+    rho0 = 0.0218360 * o.AUTOANG ** 3
+    z = (np.arange(n) - n // 2) * step
+    rho = rho0 * (1 + 0.3 * np.cos(2 * np.pi * z / (n * step)) + 0.05 * rng.random(n))
+    return (np.sqrt(rho) * np.exp(0.4j * np.sin(2 * np.pi * z / (n * step)))).reshape(1, 1, n)

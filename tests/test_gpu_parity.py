@@ -29,7 +29,11 @@ def prec(request, gpu):
                                    (8, 16, 512), (64, 256, 32), (128, 128, 128), (96, 120, 160),
                                    (16, 256, 256), (6, 512, 512),
                                    # smallest and largest axes (2 and 1024: generic kernels in FP32 too)
-                                   (2, 4, 6), (4, 6, 2), (1024, 8, 4), (4, 6, 1024), (8, 1024, 2)])
+                                   (2, 4, 6), (4, 6, 2), (1024, 8, 4), (4, 6, 1024), (8, 1024, 2),
+                                   # 3 * 2^k lengths (96, 192, 384: register-resident in FP32), an odd
+                                   # axis of 729 (partial tiles of the generic y pass) and 240 / 120
+                                   (96, 64, 384), (192, 96, 192), (384, 16, 192), (32, 384, 96),
+                                   (729, 8, 6), (9, 729, 4), (240, 16, 240)])
 def test_rfft_spectrum(gpu, prec, shape):
     rng = np.random.default_rng(1)
     f = rng.standard_normal(shape)
@@ -97,7 +101,11 @@ def test_potential_and_energy_density_match_reference(gpu, prec, fixture):
                                               # examples/gas-bubble/config.h:56): kernels rotated by
                                               # exp(2 pi i k c / n) instead of the sign (-1)^k
                                               ((9, 10, 8), 0.8, 9), ((15, 9, 12), 0.9, 9), ((27, 25, 16), 0.8, 9),
-                                              ((45, 3, 10), 0.8, 1), ((243, 16, 16), 0.8, 9)])
+                                              ((45, 3, 10), 0.8, 1), ((243, 16, 16), 0.8, 9),
+                                              # 3 * 2^k lengths on the register-resident FP32 path: z passes
+                                              # of 192 (nz = 384), y pass 96, x convolutions 192 / 96 / 384
+                                              ((16, 96, 384), 0.8, 9), ((192, 32, 32), 0.8, 9),
+                                              ((96, 64, 96), 0.8, 1), ((384, 16, 16), 0.6, 8)])
 def test_potential_vs_oracle_live(gpu, port, prec, shape, step, model):
     psi = liquid_psi(shape, step, 3)
     ns = (2, 4) if np.prod(shape) > 200000 else (4, 32)      # coarser kernel sampling on big grids (CPU time)
@@ -225,7 +233,8 @@ def test_uniform_liquid_potential_is_chemical_potential(gpu, prec, model):
 
 
 @pytest.mark.parametrize("shape", [(24, 20, 30), (128, 128, 128), (64, 96, 160),
-                                   (2, 6, 4), (1024, 4, 6), (6, 4, 1024), (4, 1024, 2), (9, 15, 10), (27, 5, 8)])
+                                   (2, 6, 4), (1024, 4, 6), (6, 4, 1024), (4, 1024, 2), (9, 15, 10), (27, 5, 8),
+                                   (96, 48, 384), (384, 8, 12), (27, 96, 192)])
 def test_propagate_matches_oracle(gpu, port, prec, shape):
     step = 0.9
     rng = np.random.default_rng(9)

@@ -10,7 +10,7 @@ common.c and helium-ot-bulk.c (golden/*.npz, see make_golden.py).
 import numpy as np
 import pytest
 
-from conftest import golden, relerr
+from conftest import golden, line_psi, relerr
 from oracle import Grids, Oracle, ref_available
 
 
@@ -226,3 +226,41 @@ def test_high_density_potential_is_the_energy_derivative(port, model):
     fd = (e_p - e_m) / (2 * h)
     an = float(np.sum(V * drho) * step ** 3)
     assert abs(fd / an - 1) < 1e-6, (fd, an)
+
+
+@pytest.mark.skipif(not ref_available(), reason="reference tree not present")
+@pytest.mark.parametrize("model", [0, 1, 8, 9, 11])
+def test_reference_build_live_vs_port_one_d(model):
+    """The 1-D effective model (nx = ny = 1; src/ot.c:133-217 with DFT_OT_1D,
+    src/ot.h:146): libdft's own 1-D kernels (src/common.c:80-91, 152-158,
+    214-220; src/ot-private.h:29-41), unrescaled, against the restatement."""
+    ref, prt = Oracle("ref"), Oracle("port")
+    out = []
+    for o in (ref, prt):
+        with Grids(o, (1, 1, 96), 0.8, 4.002602 / o.AUTOAMU) as g:
+            w = g.wf(line_psi(o, 96, 0.8))
+            otf = g.ot(model, w)
+            out.append((g.potential(otf, w), g.energy_density(otf, w)))
+    assert relerr(out[0][0].real, out[1][0].real) < 1e-12
+    if np.abs(out[0][0].imag).max() > 0:
+        assert relerr(out[0][0].imag, out[1][0].imag) < 1e-11
+    assert relerr(out[0][1], out[1][1]) < 1e-12
+
+
+@pytest.mark.parametrize("model", [0, 9])
+def test_one_d_uniform_liquid_is_near_the_bulk_chemical_potential(port, model):
+    """The 1-D kernels are not rescaled to their integrals: with the line
+    element dz as the convolution measure the uniform liquid's potential is the
+    bulk chemical potential up to the 1-D LJ's core (|z| < h taken at h),
+    which moves it by 1.1 %; with the volume element step^3 it would be off by
+    the factor step^2."""
+    shape = (1, 1, 64)
+    with Grids(port, shape, 0.9, 4.002602 / port.AUTOAMU) as g:
+        w = g.wf(np.ones(shape))
+        otf = g.ot(model, w)
+        rho0 = port.lib.orc_bulk_density(otf, 0.0)
+        g.set_wf(w, np.full(shape, np.sqrt(rho0), dtype=complex))
+        P = g.potential(otf, w)
+        mu = port.lib.orc_bulk_dEdRho(otf, rho0)
+    assert np.ptp(P.real) < 1e-12 * abs(mu)
+    assert abs(P.real.mean() / mu - 1) < 0.02
