@@ -29,7 +29,7 @@ typedef struct {
   REAL complex *tw;           /* tw[t] = exp(-2 pi i t / n) */
 } fft_plan;
 
-#define NPLANS 32
+#define NPLANS 512   /* distinct lengths in one process (a test session visits many) */
 static fft_plan plans[NPLANS];
 static int nplans = 0;
 
