@@ -463,7 +463,7 @@ __global__ void __launch_bounds__(FFT_THREADS) xconv_kernel(const XConvArgs<T> A
   for (int in = 0; in < A.nin; in++) {   // forward transforms, each into its own tile
     const C *src = A.src[in] + kz * plane + y0;
     C *tin = bufs + in * tile;
-    batched_tile<sizeof(T) == 4 ? 8 : 4>(0, n, B, [&](int ll, int e) { return src[(size_t) e * A.ny + ll]; },
+    batched_tile<sizeof(T) == 4 ? 8 : 1>(0, n, B, [&](int ll, int e) { return src[(size_t) e * A.ny + ll]; },
                                          [&](int ll, int e, C v) { tin[e * ldb + ll] = v; });
     __syncthreads();
     C *r = tile_fft<T>(tin, scr0, A.plan, B, ldb, (T) -1);
@@ -475,7 +475,7 @@ __global__ void __launch_bounds__(FFT_THREADS) xconv_kernel(const XConvArgs<T> A
 
   for (int o = 0; o < A.nout; o++) {
     const XOut<T> &out = A.out[o];
-    constexpr int U = sizeof(T) == 4 ? 4 : 2;   // elements per batch: their kernel values loaded together
+    constexpr int U = sizeof(T) == 4 ? 4 : 1;   // elements per batch (FP32): their kernel values loaded together
     for (int eb = e0; eb < n; eb += U * est) {
       C acc[U];
 #pragma unroll
@@ -498,7 +498,7 @@ __global__ void __launch_bounds__(FFT_THREADS) xconv_kernel(const XConvArgs<T> A
     C *r = tile_fft<T>(scr0, scr1, A.plan, B, ldb, (T) 1);
     C *dst = out.dst + kz * plane + y0;
     if (out.accumulate) {
-      batched_tile<sizeof(T) == 4 ? 8 : 4>(0, n, B, [&](int ll, int e) { return dst[(size_t) e * A.ny + ll]; },
+      batched_tile<sizeof(T) == 4 ? 8 : 1>(0, n, B, [&](int ll, int e) { return dst[(size_t) e * A.ny + ll]; },
                                            [&](int ll, int e, C v) { dst[(size_t) e * A.ny + ll] = v + r[e * ldb + ll]; });
     } else {
       for (int e = e0; e < n; e += est) dst[(size_t) e * A.ny + l] = r[e * ldb + l];
