@@ -345,7 +345,7 @@ __global__ void __launch_bounds__(FFT_THREADS) line_fft_kernel(const LineArgs<T>
   // ---- load
   if (MODE == LINE_C2R) {
     // Z[k] = (X[k] + X*[n-k]) + i w^{-k} (X[k] - X*[n-k]),  w = exp(-2 pi i / 2n)
-    batched_tile<sizeof(T) == 4 ? 4 : 2>(args.e_fast, n, B,
+    batched_tile<sizeof(T) == 4 ? 4 : 1>(args.e_fast, n, B,
         [&](int l, int k) {
           if (b0 + l >= nb) return CPair<C>{ zero, zero };
           return CPair<C>{ ld(a, b0 + l, k), ld(a, b0 + l, n - k) };
@@ -361,7 +361,7 @@ __global__ void __launch_bounds__(FFT_THREADS) line_fft_kernel(const LineArgs<T>
           buf0[k * ldb + l] = z;
         });
   } else {
-    batched_tile<sizeof(T) == 4 ? 8 : 4>(args.e_fast, n, B, [&](int l, int e) { return b0 + l < nb ? ld(a, b0 + l, e) : zero; },
+    batched_tile<sizeof(T) == 4 ? 8 : 1>(args.e_fast, n, B, [&](int l, int e) { return b0 + l < nb ? ld(a, b0 + l, e) : zero; },
                                          [&](int l, int e, C v) { buf0[e * ldb + l] = v; });
   }
   __syncthreads();

@@ -34,9 +34,14 @@ struct March2Args {
   HdPar<float> hp;
 };
 
+// Resident CTAs per SM the kernel is compiled for (per 256 threads): 3 for the
+// full model (80 registers, no spills; unbounded it took 124 and ran 2), 4 for
+// one term (56-64 registers)
+constexpr int march2_minb(int nt, bool kc, bool bf) { return nt >= 512 ? 1 : (kc && bf ? 3 : 4) * (256 / nt); }
+
 // NT threads = nz; TY rows per CTA; KC / BF: the terms present
 template <int NT, int TY, bool KC, bool BF>
-__global__ void __launch_bounds__(NT, NT >= 512 ? 1 : 2048 / NT / 4) march2_kernel(const March2Args a) {
+__global__ void __launch_bounds__(NT, march2_minb(NT, KC, BF)) march2_kernel(const March2Args a) {
   static_assert(KC || BF, "one of the terms");
   // z-exchange plane, double-buffered: rho, F*rho, J_z, w_z of each row
   __shared__ float zx[2][4][TY][NT];
