@@ -286,20 +286,40 @@ __host__ __device__ __forceinline__ int tile_pitch(int B) { return B == 1 ? 1 : 
 // on line t % B, elements t / B + j blockDim.x / B); in batches of U whose
 // fetches are all issued before the first put, so that U global loads per
 // thread are in flight together.
+// Element-fast mapping of the threads over a tile's (line, element) pairs:
+// lines shorter than the CTA take several lines per pass (thread t on line
+// t / n + j lpp, element t % n), so that no thread idles for n < blockDim.
+struct EFastMap {
+  int l0, lstep, e0, estep;
+  __device__ __forceinline__ EFastMap(int n) {
+    const int tid = threadIdx.x, nth = blockDim.x;
+    if (n < nth) {
+      lstep = nth / n;
+      l0 = tid / n;
+      e0 = tid - l0 * n;
+      estep = n;
+      if (l0 >= lstep) l0 = 1 << 30;   // the threads past lstep * n have no pair
+    } else {
+      l0 = 0; lstep = 1; e0 = tid; estep = nth;
+    }
+  }
+};
+
 template <int U, class Fetch, class Put>
 __device__ __forceinline__ void batched_tile(int efast, int n, int B, Fetch fetch, Put put) {
   typedef decltype(fetch(0, 0)) R;
   const int tid = threadIdx.x, nth = blockDim.x;
   if (efast) {
-    for (int e = tid; e < n; e += nth)
-      for (int l0 = 0; l0 < B; l0 += U) {
+    const EFastMap m(n);
+    for (int e = m.e0; e < n; e += m.estep)
+      for (int l0 = m.l0; l0 < B; l0 += U * m.lstep) {
         R r[U];
 #pragma unroll
         for (int u = 0; u < U; u++)
-          if (l0 + u < B) r[u] = fetch(l0 + u, e);
+          if (l0 + u * m.lstep < B) r[u] = fetch(l0 + u * m.lstep, e);
 #pragma unroll
         for (int u = 0; u < U; u++)
-          if (l0 + u < B) put(l0 + u, e, r[u]);
+          if (l0 + u * m.lstep < B) put(l0 + u * m.lstep, e, r[u]);
       }
   } else {
     const int l = tid % B, est = nth / B;
@@ -382,16 +402,18 @@ __global__ void __launch_bounds__(FFT_THREADS) line_fft_kernel(const LineArgs<T>
       if (b0 + l < nb) st(a, b0 + l, k, x);
     };
     if (args.e_fast_store) {
-      for (int l = 0; l < B; l++)
-        for (int k = tid; k <= n; k += nth) one(k, l);
+      const EFastMap m(n + 1);
+      for (int k = m.e0; k <= n; k += m.estep)
+        for (int l = m.l0; l < B; l += m.lstep) one(k, l);
     } else {
       for (int k = et0; k <= n; k += est) one(k, lt);
     }
   } else {
     if (args.e_fast_store) {
-      for (int l = 0; l < B; l++)
-        if (b0 + l < nb)
-          for (int e = tid; e < n; e += nth) st(a, b0 + l, e, res[e * ldb + l]);
+      const EFastMap m(n);
+      for (int e = m.e0; e < n; e += m.estep)
+        for (int l = m.l0; l < B; l += m.lstep)
+          if (b0 + l < nb) st(a, b0 + l, e, res[e * ldb + l]);
     } else {
       if (b0 + lt < nb)
         for (int e = et0; e < n; e += est) st(a, b0 + lt, e, res[e * ldb + lt]);
