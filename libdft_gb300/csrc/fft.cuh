@@ -196,8 +196,11 @@ __device__ __forceinline__ void small_dft(C *u, T s) {
 }
 
 // One radix-R Stockham stage over a tile of B lines in [n][ldb] layout.
-// B divides blockDim.x: thread t works on line t % B, butterflies
-// t / B + j blockDim.x / B (no division per element).
+// FP32: thread t on line t % B, butterflies t / B + j blockDim.x / B; FP64:
+// butterfly (line, index) = (idx % B, idx / B) for idx = t + j blockDim.x,
+// twiddle index mod n.  Each form is the faster one for its precision: the
+// first took the FP32 2.3.5 steps from 94 to 119 steps/s at 240^3, the
+// second the FP64 256^3 step from 99 to 91 ms.
 template <int R, typename T>
 __device__ __forceinline__ void stockham_stage(const typename cplx_t<T>::type *__restrict__ in,
                                                typename cplx_t<T>::type *__restrict__ out,
@@ -205,15 +208,13 @@ __device__ __forceinline__ void stockham_stage(const typename cplx_t<T>::type *_
                                                const typename cplx_t<T>::type *__restrict__ tw, T s) {
   typedef typename cplx_t<T>::type C;
   const int nR = n / R, twstep = n / (p * R);
-  const int l = threadIdx.x % B, istep = blockDim.x / B;
-  for (int i = threadIdx.x / B; i < nR; i += istep) {
-    const int k = i % p;
+  auto butterfly = [&](int l, int i, int k, int tq) {
     C u[R];
 #pragma unroll
     for (int q = 0; q < R; q++) {
       C v = in[(i + q * nR) * ldb + l];
       if (q > 0 && k > 0) {
-        C w = __ldg(&tw[q * k * twstep]);   // q k twstep < R p n / (p R) = n
+        C w = __ldg(&tw[tq ? (q * k * twstep) % n : q * k * twstep]);   // q k twstep < n
         w.y *= -s;   // tw holds exp(-i...); inverse (s=+1) uses the conjugate
         v = cmul(v, w);
       }
@@ -223,6 +224,15 @@ __device__ __forceinline__ void stockham_stage(const typename cplx_t<T>::type *_
     const int j = (i - k) * R + k;
 #pragma unroll
     for (int q = 0; q < R; q++) out[(j + q * p) * ldb + l] = u[q];
+  };
+  if constexpr (sizeof(T) == 4) {
+    const int l = threadIdx.x % B, istep = blockDim.x / B;
+    for (int i = threadIdx.x / B; i < nR; i += istep) butterfly(l, i, i % p, 0);
+  } else {
+    for (int idx = threadIdx.x; idx < nR * B; idx += blockDim.x) {
+      const int l = idx % B, i = idx / B;
+      butterfly(l, i, i % p, 1);
+    }
   }
 }
 
