@@ -243,7 +243,11 @@ void grid_add_real_to_complex_im(cgrid *dst, rgrid *src);
 
 /* -------------------------------------------------------- wave functions
  * libgrid wf API as called by libdft and its examples. */
-/* grid_wf_alloc (imag_time.c:197): periodic boundary + WF_2ND_ORDER_FFT only. */
+/* grid_wf_alloc (imag_time.c:197): periodic boundary + WF_2ND_ORDER_FFT only.
+ * Dimensions 2^a 3^b 5^c in [2, 1024], x and y may be odd, z even; a 1-D grid
+ * (nx = ny = 1, examples/1d-bubble/bubble-1d.c:126) takes nz up to 4096 and the
+ * OT functional's 1-D effective model (src/ot.c:133-217).  Other sizes return
+ * NULL with DFTGPU_ERR_SIZE (the same rule for rgrid_alloc / cgrid_alloc). */
 wf *grid_wf_alloc(INT nx, INT ny, INT nz, REAL step, REAL mass, char boundary, char propagator, char *id);
 wf *grid_wf_clone(wf *gwf, char *id);                     /* imag_time.c:201 */
 void grid_wf_free(wf *gwf);
