@@ -211,17 +211,17 @@ template <typename T> struct RealPairLoad {         // packed (f[2e], f[2e+1]) o
   __device__ void prefetch_lines(int x, int y0, int nl, int) const {      // nl whole rows, contiguous
     if (threadIdx.x == 0) prefetch_bulk_l2(f + ((size_t) x * ny + y0) * nz, (size_t) nl * nz * sizeof(T));
   }
+  // one vector access per pair: rows start on a multiple of nz (even) values
   __device__ typename cplx_t<T>::type operator()(int x, int y, int e) const {
     const T *row = f + ((size_t) x * ny + y) * nz;
-    return mk<T>(row[2 * e], row[2 * e + 1]);
+    return *reinterpret_cast<const typename cplx_t<T>::type *>(row + 2 * e);
   }
 };
 template <typename T> struct RealPairStore {        // real row <- scale * (re, im)
   T *f; int ny, nz; T scale;
   __device__ void operator()(int x, int y, int e, typename cplx_t<T>::type v) const {
     T *row = f + ((size_t) x * ny + y) * nz;
-    row[2 * e] = v.x * scale;
-    row[2 * e + 1] = v.y * scale;
+    *reinterpret_cast<typename cplx_t<T>::type *>(row + 2 * e) = mk<T>(v.x * scale, v.y * scale);
   }
 };
 // (|psi[2e]|^2, |psi[2e+1]|^2) of a wave-function row, also stored into the
@@ -241,7 +241,12 @@ template <typename T> struct DensityPairLoad {
   }
   __device__ Raw fetch(int x, int y, int e) const {
     const size_t r = ((size_t) x * ny + y) * nz + 2 * e;
-    return Raw{ psi[r], psi[r + 1], rho + r };
+    if constexpr (std::is_same<T, float>::value) {   // the pair as one 16-byte load (r even)
+      const float4 q = *reinterpret_cast<const float4 *>(psi + r);
+      return Raw{ make_float2(q.x, q.y), make_float2(q.z, q.w), rho + r };
+    } else {
+      return Raw{ psi[r], psi[r + 1], rho + r };
+    }
   }
   __device__ C cook(const Raw &w) const {
     const C d = mk<T>(w.a.x * w.a.x + w.a.y * w.a.y, w.b.x * w.b.x + w.b.y * w.b.y);
@@ -264,11 +269,18 @@ template <typename T> struct PotAddPairStore {
   }
   __device__ void operator()(int x, int y, int e, C v) const {
     const size_t r = ((size_t) x * ny + y) * nz + 2 * e;
-    C p0 = pot[r], p1 = pot[r + 1];
-    p0.x += v.x;
-    p1.x += v.y;
-    pot[r] = mk<T>(p0.x * scale, p0.y * scale);
-    pot[r + 1] = mk<T>(p1.x * scale, p1.y * scale);
+    if constexpr (std::is_same<T, float>::value) {   // the pair as one 16-byte access (r even)
+      float4 q = *reinterpret_cast<const float4 *>(pot + r);
+      q.x += v.x;
+      q.z += v.y;
+      *reinterpret_cast<float4 *>(pot + r) = make_float4(q.x * scale, q.y * scale, q.z * scale, q.w * scale);
+    } else {
+      C p0 = pot[r], p1 = pot[r + 1];
+      p0.x += v.x;
+      p1.x += v.y;
+      pot[r] = mk<T>(p0.x * scale, p0.y * scale);
+      pot[r + 1] = mk<T>(p1.x * scale, p1.y * scale);
+    }
   }
 };
 template <typename T> struct CplxLoad {
