@@ -211,20 +211,24 @@ template <int N, int S> __host__ __device__ constexpr int in_pos(int t, int slot
 }
 
 // Full transform in registers: on entry v[q] = x[t + TL q]; on exit v[slot]
-// = X[out_pos<N, NS-1>(t, slot)], which is t + TL * j(slot).
-template <int N, int S = 0>
+// = X[out_pos<N, NS-1>(t, slot)], which is t + TL * j(slot).  A line's
+// exchange touches only its own row of sm, so when its TL threads are lanes
+// of one warp (WARP: the element-fast mapping, t = threadIdx % TL) the
+// exchange needs a warp barrier only; otherwise the CTA barrier.
+template <int N, int S = 0, bool WARP = false>
 __device__ __forceinline__ void transform(C (&v)[Shape<N>::E], int t, int l, float s, const C *__restrict__ tw,
                                           C *__restrict__ sm) {
   constexpr int E = Shape<N>::E, LP = Shape<N>::LP;
+  static_assert(!WARP || 32 % Shape<N>::TL == 0, "a line within one warp");
   stage<N, S>(v, t, s, tw);
   if constexpr (S + 1 < Shape<N>::NS) {
 #pragma unroll
     for (int j = 0; j < E; j++) sm[sidx(l, out_pos<N, S>(t, j), LP)] = v[j];
-    __syncthreads();
+    if constexpr (WARP) __syncwarp(); else __syncthreads();
 #pragma unroll
     for (int j = 0; j < E; j++) v[j] = sm[sidx(l, in_pos<N, S + 1>(t, j), LP)];
-    __syncthreads();
-    transform<N, S + 1>(v, t, l, s, tw, sm);
+    if constexpr (WARP) __syncwarp(); else __syncthreads();
+    transform<N, S + 1, WARP>(v, t, l, s, tw, sm);
   }
 }
 
@@ -464,7 +468,7 @@ __device__ __forceinline__ void line_body(const C *__restrict__ tw, const C *__r
 #pragma unroll
     for (int j = 0; j < E; j++) st.prefetch(a, b0 + l, final_pos<N>(t, j));
   }
-  transform<N>(v, t, l, sign, tw, sm);
+  transform<N, 0, MAP == MAP_E>(v, t, l, sign, tw, sm);
   if constexpr (STS == 0) {
     if (ok) {
 #pragma unroll
