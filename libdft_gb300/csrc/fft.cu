@@ -338,7 +338,7 @@ template <typename T> int launch_xconv(XConvArgs<T> &A) {
   }
   DFT_TRY(get_plan<T>(A.nx, &A.plan));
   int B; size_t smem;
-  DFT_TRY(choose_tile(A.nx, A.ny, sizeof(C), A.nin + 2, &B, &smem));
+  DFT_TRY(choose_tile(A.nx, A.ny, sizeof(C), 3, &B, &smem));   // three tiles (xconv_kernel)
   A.B = B;
   A.kxh = A.nx / 2 + 1;
   A.kyh = A.ny / 2 + 1;

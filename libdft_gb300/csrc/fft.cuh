@@ -481,61 +481,95 @@ __device__ __forceinline__ typename cplx_t<T>::type apply_kernel(const XTerm<T> 
 }
 
 // grid (ny / B, nkz); one CTA = B consecutive y pencils of one kz plane.
+// One input: its spectrum is computed once into a tile and every output is
+// formed from it (3 tiles).  Several inputs: the outputs one after the other,
+// each summing its terms into an accumulator tile, the input of each term
+// transformed when the term is reached (3 tiles instead of inputs + 2, so a
+// CTA holds more pencils; the transforms are the same in number when each
+// input feeds one output).
 template <typename T>
 __global__ void __launch_bounds__(FFT_THREADS) xconv_kernel(const XConvArgs<T> A) {
   typedef typename cplx_t<T>::type C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int n = A.plan.n, B = A.B, ldb = tile_pitch(B), tile = n * ldb;   // as choose_tile
   C *bufs = reinterpret_cast<C *>(smem_raw);
-  C *scr0 = bufs + A.nin * tile, *scr1 = scr0 + tile;
   const int kz = blockIdx.y, y0 = blockIdx.x * B;
   const size_t plane = (size_t) A.nx * A.ny;
   const int l = threadIdx.x % B, e0 = threadIdx.x / B, est = blockDim.x / B;   // thread: one pencil
+  constexpr int LU = sizeof(T) == 4 ? 8 : 1;   // loads in flight per thread (FP32)
 
-  for (int in = 0; in < A.nin; in++) {   // forward transforms, each into its own tile
+  // forward transform of input `in` into tile `tin` (scratch `tsc`); returns the result's tile
+  auto forward = [&](int in, C *tin, C *tsc) -> C * {
     const C *src = A.src[in] + kz * plane + y0;
-    C *tin = bufs + in * tile;
-    batched_tile<sizeof(T) == 4 ? 8 : 1>(0, n, B, [&](int ll, int e) { return src[(size_t) e * A.ny + ll]; },
-                                         [&](int ll, int e, C v) { tin[e * ldb + ll] = v; });
+    batched_tile<LU>(0, n, B, [&](int ll, int e) { return src[(size_t) e * A.ny + ll]; },
+                     [&](int ll, int e, C v) { tin[e * ldb + ll] = v; });
     __syncthreads();
-    C *r = tile_fft<T>(tin, scr0, A.plan, B, ldb, (T) -1);
-    if (r != tin) {   // an odd number of stages ends in the scratch tile
-      for (int idx = threadIdx.x; idx < tile; idx += blockDim.x) tin[idx] = r[idx];
-      __syncthreads();
-    }
-  }
-
-  for (int o = 0; o < A.nout; o++) {
-    const XOut<T> &out = A.out[o];
-    constexpr int U = sizeof(T) == 4 ? 4 : 1;   // elements per batch (FP32): their kernel values loaded together
-    for (int eb = e0; eb < n; eb += U * est) {
-      C acc[U];
-#pragma unroll
-      for (int u = 0; u < U; u++) acc[u] = mk<T>((T) 0, (T) 0);
-      for (int t = out.t0; t < out.t0 + out.nt; t++) {
-        const XTerm<T> &tm = A.term[t];
-#pragma unroll
-        for (int u = 0; u < U; u++) {
-          const int e = eb + u * est;
-          if (e < n) acc[u] = acc[u] + apply_kernel<T>(tm, bufs[tm.in * tile + e * ldb + l], e, y0 + l, kz, A);
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < U; u++) {
-        const int e = eb + u * est;
-        if (e < n) scr0[e * ldb + l] = acc[u];
-      }
-    }
-    __syncthreads();
-    C *r = tile_fft<T>(scr0, scr1, A.plan, B, ldb, (T) 1);
+    return tile_fft<T>(tin, tsc, A.plan, B, ldb, (T) -1);
+  };
+  // inverse transform of tile `acc` (scratch `tsc`) and the store of output `out`
+  auto emit = [&](const XOut<T> &out, C *acc, C *tsc) {
+    C *r = tile_fft<T>(acc, tsc, A.plan, B, ldb, (T) 1);
     C *dst = out.dst + kz * plane + y0;
     if (out.accumulate) {
-      batched_tile<sizeof(T) == 4 ? 8 : 1>(0, n, B, [&](int ll, int e) { return dst[(size_t) e * A.ny + ll]; },
-                                           [&](int ll, int e, C v) { dst[(size_t) e * A.ny + ll] = v + r[e * ldb + ll]; });
+      batched_tile<LU>(0, n, B, [&](int ll, int e) { return dst[(size_t) e * A.ny + ll]; },
+                       [&](int ll, int e, C v) { dst[(size_t) e * A.ny + ll] = v + r[e * ldb + ll]; });
     } else {
       for (int e = e0; e < n; e += est) dst[(size_t) e * A.ny + l] = r[e * ldb + l];
     }
     __syncthreads();
+  };
+
+  if (A.nin == 1) {
+    C *X = bufs, *scr0 = bufs + tile, *scr1 = scr0 + tile;
+    C *r = forward(0, X, scr0);
+    if (r != X) {   // an odd number of stages ends in the scratch tile
+      for (int idx = threadIdx.x; idx < tile; idx += blockDim.x) X[idx] = r[idx];
+      __syncthreads();
+    }
+    for (int o = 0; o < A.nout; o++) {
+      const XOut<T> &out = A.out[o];
+      constexpr int U = sizeof(T) == 4 ? 4 : 1;   // elements per batch (FP32): their kernel values loaded together
+      for (int eb = e0; eb < n; eb += U * est) {
+        C acc[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) acc[u] = mk<T>((T) 0, (T) 0);
+        for (int t = out.t0; t < out.t0 + out.nt; t++) {
+          const XTerm<T> &tm = A.term[t];
+#pragma unroll
+          for (int u = 0; u < U; u++) {
+            const int e = eb + u * est;
+            if (e < n) acc[u] = acc[u] + apply_kernel<T>(tm, X[e * ldb + l], e, y0 + l, kz, A);
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+          const int e = eb + u * est;
+          if (e < n) scr0[e * ldb + l] = acc[u];
+        }
+      }
+      __syncthreads();
+      emit(out, scr0, scr1);
+    }
+    return;
+  }
+
+  C *X = bufs, *Y = bufs + tile, *ACC = bufs + 2 * tile;
+  for (int o = 0; o < A.nout; o++) {
+    const XOut<T> &out = A.out[o];
+    if (out.nt == 0) {   // no term: a zero output (added: no change)
+      for (int e = e0; e < n; e += est) ACC[e * ldb + l] = mk<T>((T) 0, (T) 0);
+      __syncthreads();
+    }
+    for (int t = out.t0; t < out.t0 + out.nt; t++) {
+      const XTerm<T> &tm = A.term[t];
+      const C *r = forward(tm.in, X, Y);
+      for (int e = e0; e < n; e += est) {   // each thread its own elements: no barrier before the sum
+        const C v = apply_kernel<T>(tm, r[e * ldb + l], e, y0 + l, kz, A);
+        ACC[e * ldb + l] = t == out.t0 ? v : ACC[e * ldb + l] + v;
+      }
+      __syncthreads();   // the tiles X / Y are free for the next term's input
+    }
+    emit(out, ACC, X);
   }
 }
 
