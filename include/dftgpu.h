@@ -62,6 +62,20 @@ extern "C" {
 #define DFT_OT_HD2      4
 #define DFT_OT_BACKFLOW 8
 #define DFT_OT_T0MK    16
+#define DFT_OT_T400MK  32        /* thermal models: their parameter sets (src/ot.c:1038-1222) */
+#define DFT_OT_T600MK  64        /* and the ideal Bose gas term (src/ot.c:402-407, 804-809)   */
+#define DFT_OT_T800MK  128
+#define DFT_OT_T1200MK 256
+#define DFT_OT_T1400MK 512
+#define DFT_OT_T1600MK 1024
+#define DFT_OT_T1800MK 2048
+#define DFT_OT_T2000MK 4096
+#define DFT_OT_T2100MK 8192
+#define DFT_OT_T2200MK 16384
+#define DFT_OT_T2400MK 32768
+#define DFT_OT_T2600MK 65536
+#define DFT_OT_T2800MK 131072
+#define DFT_OT_T3000MK 262144
 #define DFT_GP         524288
 #define DFT_DR         1048576
 #define DFT_ZERO       2097152

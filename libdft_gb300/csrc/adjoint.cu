@@ -27,6 +27,7 @@
 #include <vector>
 
 #include "grid_internal.cuh"
+#include "ot_thermal.cuh"
 #include "ot_work.cuh"
 
 namespace dftgpu {
@@ -589,6 +590,10 @@ bool fits_r(dft_ot_functional *otf, const rgrid *r) {
 int hd_refused(dft_ot_functional *otf, wf *gwf = nullptr) {
   if (gwf && ((WfPriv *) gwf->priv)->abs.on) {
     set_error(DFTGPU_ERR_UNSUPPORTED, "adjoint: the absorbing boundary is not differentiated");
+    return DFTGPU_ERR_UNSUPPORTED;
+  }
+  if (bose_model(otf)) {
+    set_error(DFTGPU_ERR_UNSUPPORTED, "adjoint: the thermal models' ideal Bose gas term is not differentiated");
     return DFTGPU_ERR_UNSUPPORTED;
   }
   if (!hd_model(otf)) return DFTGPU_OK;

@@ -7,6 +7,7 @@
 
 #include "grid_internal.cuh"
 #include "ot_internal.cuh"
+#include "ot_thermal.cuh"
 
 using namespace dftgpu;
 
@@ -491,6 +492,31 @@ void dft_ot_init_params(dft_ot_functional *otf, INT model) {
   otf->temp = 0.0;
   otf->rho0 = 0.0218360;
   otf->lj_params.h = 2.1903;
+  // the thermal parameter sets (src/ot.c:1038-1222): b, c2, c3 (K, Angstrom),
+  // c4, T (K), rho0, h; each selected by its bit, a later bit overriding an
+  // earlier one as in the reference
+  static const struct { INT bit; double b, c2, c3, c4, temp, rho0, h; } tset[] = {
+    { DFT_OT_T0MK, -719.2435, -24258.88, 1865257.0, 0.0, 0.0, 0.0218354, 2.19035 },
+    { DFT_OT_T400MK, -714.2174, -24566.29, 1873203.0, 0.98004, 0.4, 0.0218351, 2.18982 },
+    { DFT_OT_T600MK, -705.1319, -25124.17, 1887707.0, 0.99915, 0.6, 0.0218346, 2.18887 },
+    { DFT_OT_T800MK, -690.4745, -26027.12, 1911283.0, 0.99548, 0.8, 0.0218331, 2.18735 },
+    { DFT_OT_T1200MK, -646.5135, -28582.81, 1973737.0, 0.99666, 1.2, 0.0218298, 2.18287 },
+    { DFT_OT_T1400MK, -625.8123, -29434.03, 1984068.0, 0.99829, 1.4, 0.0218332, 2.18080 },
+    { DFT_OT_T1600MK, -605.9788, -30025.96, 1980898.0, 1.00087, 1.6, 0.0218453, 2.17885 },
+    { DFT_OT_T1800MK, -593.8289, -29807.56, 1945685.0, 1.00443, 1.8, 0.0218703, 2.17766 },
+    { DFT_OT_T2000MK, -600.8313, -27850.96, 1847407.0, 1.00919, 2.0, 0.0219153, 2.17834 },
+    { DFT_OT_T2100MK, -620.9129, -25418.15, 1747494.0, 1.01156, 2.1, 0.0219500, 2.18032 },
+    { DFT_OT_T2200MK, -619.2016, -25096.68, 1720802.0, 1.01436, 2.2, 0.0219859, 2.18015 },
+    { DFT_OT_T2400MK, -609.0757, -26009.98, 1747943.0, 1.02130, 2.4, 0.0218748, 2.17915 },
+    { DFT_OT_T2600MK, -634.0664, -23790.66, 1670707.0, 1.02770, 2.6, 0.0217135, 2.18162 },
+    { DFT_OT_T2800MK, -663.9942, -21046.37, 1574611.0, 1.03429, 2.8, 0.0215090, 2.18463 },
+    { DFT_OT_T3000MK, -673.6543, -20022.76, 1535887.0, 1.04271, 3.0, 0.0212593, 2.18562 },
+  };
+  for (const auto &t : tset)
+    if (model & t.bit) {
+      otf->b = t.b; otf->c2 = t.c2; otf->c3 = t.c3; otf->c4 = t.c4;
+      otf->temp = t.temp; otf->rho0 = t.rho0; otf->lj_params.h = t.h;
+    }
   otf->mu0 = 0.0;
   otf->xi = 1E4 / a3;
   otf->rhobf = 0.033 * a3;
@@ -520,8 +546,9 @@ void dft_ot_init_params(dft_ot_functional *otf, INT model) {
 
 dft_ot_functional *dft_ot_alloc(INT model, wf *gwf, INT min_substeps, INT max_substeps) {
   if (!gwf) { bad_arg("dft_ot_alloc: NULL wave function"); return nullptr; }
-  if (model & ~((INT) (DFT_OT_KC | DFT_OT_HD | DFT_OT_HD2 | DFT_OT_BACKFLOW))) {
-    set_error(DFTGPU_ERR_UNSUPPORTED, "dft_ot_alloc: model %ld outside {PLAIN, KC, HD, HD2, BACKFLOW}", (long) model);
+  if (model & ~((INT) (DFT_OT_KC | DFT_OT_HD | DFT_OT_HD2 | DFT_OT_BACKFLOW | (2 * DFT_OT_T3000MK - DFT_OT_T0MK)))) {
+    set_error(DFTGPU_ERR_UNSUPPORTED, "dft_ot_alloc: model %ld outside {PLAIN, KC, HD, HD2, BACKFLOW, T0MK..T3000MK}",
+              (long) model);
     return nullptr;
   }
   cgrid *c = gwf->grid;
@@ -667,13 +694,73 @@ int dftgpu_ot_kernel(dft_ot_functional *otf, int which, double *host) {
   return copy_values_out(P->prec, P->ker[which], host, P->oct_n);
 }
 
+}  // extern "C"
+
+// ------------------------------------------------------------------ ideal Bose gas (host)
+// libdft's host forms (src/common.c:253-529): lambda^3, the 256-term
+// polylogarithms, z from golden-section search to a bracket of 1e-6, and the
+// free energy / its density derivative; the bulk relations use them when
+// c4 != 0 (src/helium-ot-bulk.c:30-31, 54-55).  The device form of the same
+// term is ot_thermal.cuh.
+namespace {
+double polylog256(double z, double s) {
+  double val = 0.0, zk = 1.0;
+  for (int k = 1; k <= 256; k++) {
+    zk *= z;
+    val += zk / pow((double) k, s);
+  }
+  return val;
+}
+double golden_z(double val) {
+  const double g = (sqrt(5.0) + 1.0) / 2.0;
+  if (val >= polylog256(1.0, 1.5)) return 1.0;
+  double a = 0.0, b = 1.0, c = b - (b - a) / g, d = a + (b - a) / g;
+  while (fabs(c - d) > 1E-6) {
+    double t = val - polylog256(c, 1.5);
+    const double fc = t * t;
+    t = val - polylog256(d, 1.5);
+    const double fd = t * t;
+    if (fc < fd) b = d; else a = c;
+    c = b - (b - a) / g;
+    d = a + (b - a) / g;
+  }
+  return (b + a) / 2.0;
+}
+double bose_energy(const dft_ot_functional *o, double rho) {
+  const double l3 = dftgpu::bose_lwl3(o->mass, o->temp), z = golden_z(rho * l3);
+  return o->c4 * GRID_AUKB * o->temp * (rho * log(z) - polylog256(z, 2.5) / l3);
+}
+double bose_dEdRho(const dft_ot_functional *o, double rho) {
+  const double l3 = dftgpu::bose_lwl3(o->mass, o->temp), rl3 = rho * l3, g32_1 = polylog256(1.0, 1.5);
+  if (rl3 >= g32_1) return -o->c4 * GRID_AUKB * (o->temp / l3) * g32_1;
+  const double z0 = golden_z(rl3), g12 = polylog256(z0, 0.5), g32 = polylog256(z0, 1.5);
+  return o->c4 * GRID_AUKB * o->temp * (log(z0) + rl3 / g12 - g32 / g12);
+}
+}  // namespace
+
+namespace dftgpu {
+bool bose_model(const dft_ot_functional *otf) { return otf->model >= DFT_OT_T400MK && otf->c4 != 0.0; }
+double bose_lwl3(double mass, double temp) {
+  const double lwl = sqrt(2.0 * M_PI * HBAR * HBAR / (mass * GRID_AUKB * temp));
+  return lwl * lwl * lwl;
+}
+double bose_g32_one() { return polylog256(1.0, 1.5); }
+double bose_zmin() { return golden_z(0.0); }
+}  // namespace dftgpu
+
+extern "C" {
+
 // ------------------------------------------------------------------ bulk (host)
 // src/helium-ot-bulk.c:21-33, 45-57, 143-172, 185-258, 376-434
 REAL dft_ot_bulk_energy(dft_ot_functional *o, REAL rho) {
-  return 0.5 * o->b * rho * rho + 0.5 * o->c2 * rho * rho * rho + (1.0 / 3.0) * o->c3 * rho * rho * rho * rho;
+  double e = 0.5 * o->b * rho * rho + 0.5 * o->c2 * rho * rho * rho + (1.0 / 3.0) * o->c3 * rho * rho * rho * rho;
+  if (o->c4 != 0.0) e += bose_energy(o, rho);
+  return e;
 }
 REAL dft_ot_bulk_dEdRho(dft_ot_functional *o, REAL rho) {
-  return o->b * rho + 1.5 * o->c2 * rho * rho + (4.0 / 3.0) * o->c3 * rho * rho * rho;
+  double d = o->b * rho + 1.5 * o->c2 * rho * rho + (4.0 / 3.0) * o->c3 * rho * rho * rho;
+  if (o->c4 != 0.0) d += bose_dEdRho(o, rho);
+  return d;
 }
 REAL dft_ot_bulk_pressure(dft_ot_functional *o, REAL rho) { return rho * dft_ot_bulk_dEdRho(o, rho) - dft_ot_bulk_energy(o, rho); }
 REAL dft_ot_bulk_dPdRho(dft_ot_functional *o, REAL rho) {

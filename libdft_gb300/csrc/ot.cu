@@ -21,6 +21,7 @@
 
 #include "grid_internal.cuh"
 #include "ot_march.cuh"
+#include "ot_thermal.cuh"
 #include "ot_work.cuh"
 
 namespace dftgpu {
@@ -419,6 +420,14 @@ template <typename T> static int potential_t(dft_ot_functional *otf, cgrid *Pg, 
     }, nb * (5 + (kc ? 4 : 0) + (bf ? 9 : 0)), "ot_pointwise_1"));
   }
 
+  // ideal Bose gas of the thermal models (src/ot.c:402-407, 804-809): its own
+  // pass, so that the other models' pointwise passes carry none of its code
+  if (bose_model(otf) && (src.terms & POT_THERMAL)) {
+    const BoseGas<T> bg = bose_par<T>(otf);
+    DFT_TRY(launch_each((size_t) nx * ny * nz, [=] __device__(size_t i) { pot[i].x += bg.dEdRho(rho[i]); },
+                        3.0 * nb, "ot_thermal"));
+  }
+
   // forward transforms of the produced fields (independent: parallel branches)
   {
     const T *in[8]; C *sp[8]; int n = 0;
@@ -597,6 +606,8 @@ template <typename T> static int energy_density_t(dft_ot_functional *otf, rgrid 
   // high-density models: Barranco's energy with the plain part
   // (src/ot-energy.c:96-99), the backflow with rho G(rho) (src/ot-energy.c:221-227)
   const bool hd = hd_model(otf), hde = hd && (terms & POT_HD), bfhd = bf && hd;
+  const bool bosee = bose_model(otf) && (terms & POT_THERMAL);
+  const BoseGas<T> bg = bose_par<T>(otf);
   const HdPar<T> hp = hd_par<T>(otf);
   const Stencil3 S{nx, ny, nz};
   const C *psi = (const C *) gwf->grid->value;
@@ -656,6 +667,7 @@ template <typename T> static int energy_density_t(dft_ot_functional *otf, rgrid 
         acc += (T) 0.5 * rh * u[i] + (c2 / (T) 2) * ((b * b) * rh) + (c3 / (T) 3) * ((b * b * b) * rh);
       }
       if (hde) acc += hp.ehd(rh);   // src/ot-energy.c:96-99
+      if (bosee) acc += bg.energy(rh);   // src/ot-energy.c:101-105
       if (kc) {  // src/ot-energy.c:144-161
         const T st = rt[i] * (-irs) + (T) 1;
         rst[i] = st;

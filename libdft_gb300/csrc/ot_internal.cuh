@@ -35,7 +35,8 @@ inline void *ot_spec(OtPriv *P, int i) {
 
 // Terms of the OT potential and the sources of rho and v (default: every
 // term of the model, rho and v from the wave function).
-enum { POT_LJ = 1, POT_LOCAL = 2, POT_KC = 4, POT_BF = 8, POT_HD = 16, POT_ALL = 31 };   // POT_HD: Barranco penalty
+// POT_HD: Barranco penalty; POT_THERMAL: the ideal Bose gas of the thermal models
+enum { POT_LJ = 1, POT_LOCAL = 2, POT_KC = 4, POT_BF = 8, POT_HD = 16, POT_THERMAL = 32, POT_ALL = 63 };
 struct PotSrc {
   int terms = POT_ALL;
   const void *dens = nullptr;                      // rho grid (bulk precision) instead of |psi|^2

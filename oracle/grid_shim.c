@@ -14,6 +14,7 @@
 #include <time.h>
 #include <omp.h>
 #include "grid/grid.h"
+#include "grid/au.h"
 
 /* ------------------------------------------------------------------ */
 /* 1-D mixed-radix Stockham FFT                                         */
@@ -242,8 +243,7 @@ static void not_restated(const char *name) {
   abort();
 }
 
-void grid_func6a_operate_one(rgrid *d, rgrid *s, REAL x, REAL y, REAL z) { (void) d; (void) s; (void) x; (void) y; (void) z; not_restated("grid_func6a_operate_one"); }
-void grid_func6b_operate_one(rgrid *d, rgrid *s, REAL x, REAL y, REAL z) { (void) d; (void) s; (void) x; (void) y; (void) z; not_restated("grid_func6b_operate_one"); }
+
 void grid_spline_ypp(REAL *x, REAL *y, INT n, REAL yp1, REAL ypn, REAL *y2) { (void) x; (void) y; (void) n; (void) yp1; (void) ypn; (void) y2; not_restated("grid_spline_ypp"); }
 REAL grid_spline_interpolate(REAL *xa, REAL *ya, REAL *y2a, INT n, REAL x) { (void) xa; (void) ya; (void) y2a; (void) n; (void) x; not_restated("grid_spline_interpolate"); return 0.0; }
 REAL grid_polynomial_interpolate(REAL *xa, REAL *ya, INT n, REAL x, REAL *dy) { (void) xa; (void) ya; (void) n; (void) x; (void) dy; not_restated("grid_polynomial_interpolate"); return 0.0; }
@@ -974,3 +974,71 @@ void grid_wf_propagate_potential(wf *g, REAL complex dt, cgrid *pot, REAL cons) 
 }
 
 void grid_wf_propagate_kinetic_fft(wf *g, REAL complex dt) { apply_kinetic(g->grid, g->grid, g->mass, dt, 0); }
+
+/* ------------------------------------------------------------------ */
+/* ideal Bose gas of the thermal OT models (grid_func6a / 6b)            */
+/* ------------------------------------------------------------------ */
+/* libgrid's grid_func6a / 6b (src/ot.c:804-809, src/ot-energy.c:103) are
+ * absent; they are restated as libdft's own host forms of the same term,
+ * which its bulk relations use (src/common.c:253-529, src/helium-ot-bulk.c:
+ * 30-31, 54-55): thermal wavelength lambda^3 = (2 pi hbar^2 / (m kB T))^(3/2);
+ * the polylogarithms g_s(z) = sum_{k=1}^{256} z^k / k^s; z solving
+ * g_{3/2}(z) = rho lambda^3 by golden-section search to a bracket of 1e-6
+ * (z = 1 from g_{3/2}(1) on);
+ *   f(rho)  = c4 kB T (rho ln z - g_{5/2}(z) / lambda^3),
+ *   mu(rho) = c4 kB T (ln z + rho lambda^3 / g_{1/2}(z) - g_{3/2}(z) / g_{1/2}(z)),
+ *             and -c4 kB T g_{3/2}(1) / lambda^3 for rho lambda^3 >= g_{3/2}(1). */
+REAL oracle_lwl3(REAL mass, REAL temp) {
+  REAL lwl = sqrt(2.0 * M_PI * HBAR * HBAR / (mass * GRID_AUKB * temp));
+  return lwl * lwl * lwl;
+}
+
+static REAL oracle_polylog(REAL z, REAL s) {
+  REAL val = 0.0, zk = 1.0;
+  for (INT k = 1; k <= 256; k++) {
+    zk *= z;
+    val += zk / pow((REAL) k, s);
+  }
+  return val;
+}
+
+static REAL oracle_bose_z(REAL val) {
+  const REAL golden = (sqrt(5.0) + 1.0) / 2.0;
+  if (val >= oracle_polylog(1.0, 1.5)) return 1.0;
+  REAL a = 0.0, b = 1.0, c = b - (b - a) / golden, d = a + (b - a) / golden;
+  while (fabs(c - d) > 1E-6) {
+    REAL t = val - oracle_polylog(c, 1.5), fc = t * t;
+    t = val - oracle_polylog(d, 1.5);
+    REAL fd = t * t;
+    if (fc < fd) b = d; else a = c;
+    c = b - (b - a) / golden;
+    d = a + (b - a) / golden;
+  }
+  return (b + a) / 2.0;
+}
+
+REAL oracle_bose_energy(REAL rho, REAL mass, REAL temp, REAL c4) {
+  REAL l3 = oracle_lwl3(mass, temp), z = oracle_bose_z(rho * l3);
+  return c4 * GRID_AUKB * temp * (rho * log(z) - oracle_polylog(z, 2.5) / l3);
+}
+
+REAL oracle_bose_dEdRho(REAL rho, REAL mass, REAL temp, REAL c4) {
+  REAL l3 = oracle_lwl3(mass, temp), rl3 = rho * l3, g32_1 = oracle_polylog(1.0, 1.5);
+  if (rl3 >= g32_1) return -c4 * GRID_AUKB * (temp / l3) * g32_1;
+  REAL z0 = oracle_bose_z(rl3), g12 = oracle_polylog(z0, 0.5), g32 = oracle_polylog(z0, 1.5);
+  return c4 * GRID_AUKB * temp * (log(z0) + rl3 / g12 - g32 / g12);
+}
+
+void grid_func6a_operate_one(rgrid *d, rgrid *s, REAL mass, REAL temp, REAL c4) {
+  INT nz = s->nz;
+#pragma omp parallel for schedule(static)
+  for (INT ij = 0; ij < s->nx * s->ny; ij++)
+    for (INT k = 0; k < nz; k++) d->value[ij * d->nz2 + k] = oracle_bose_dEdRho(s->value[ij * s->nz2 + k], mass, temp, c4);
+}
+
+void grid_func6b_operate_one(rgrid *d, rgrid *s, REAL mass, REAL temp, REAL c4) {
+  INT nz = s->nz;
+#pragma omp parallel for schedule(static)
+  for (INT ij = 0; ij < s->nx * s->ny; ij++)
+    for (INT k = 0; k < nz; k++) d->value[ij * d->nz2 + k] = oracle_bose_energy(s->value[ij * s->nz2 + k], mass, temp, c4);
+}

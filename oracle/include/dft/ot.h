@@ -21,14 +21,31 @@
 #define DFT_OT_BACKFLOW 8
 #define DFT_OT_T0MK    16
 #define DFT_OT_T400MK  32
+#define DFT_OT_T600MK  64
+#define DFT_OT_T800MK  128
+#define DFT_OT_T1200MK 256
+#define DFT_OT_T1400MK 512
+#define DFT_OT_T1600MK 1024
+#define DFT_OT_T1800MK 2048
+#define DFT_OT_T2000MK 4096
+#define DFT_OT_T2100MK 8192
+#define DFT_OT_T2200MK 16384
+#define DFT_OT_T2400MK 32768
+#define DFT_OT_T2600MK 65536
+#define DFT_OT_T2800MK 131072
+#define DFT_OT_T3000MK 262144
 #define DFT_GP         524288
 #define DFT_DR         1048576
 #define DFT_ZERO       2097152
 #define DFT_GP2        4194304
 
-/* Models the oracle restates: the 0 K OT functional with optional KC, BF and
- * the high-density terms (HD, HD2). */
-#define ORACLE_SUPPORTED_MODELS (DFT_OT_KC | DFT_OT_HD | DFT_OT_HD2 | DFT_OT_BACKFLOW)
+/* Models the oracle restates: the OT functional (0 K and the thermal
+ * parameter sets with their ideal Bose gas term) with optional KC, BF and the
+ * high-density terms (HD, HD2). */
+#define ORACLE_THERMAL_MODELS (DFT_OT_T0MK | DFT_OT_T400MK | DFT_OT_T600MK | DFT_OT_T800MK | DFT_OT_T1200MK | \
+                               DFT_OT_T1400MK | DFT_OT_T1600MK | DFT_OT_T1800MK | DFT_OT_T2000MK | DFT_OT_T2100MK | \
+                               DFT_OT_T2200MK | DFT_OT_T2400MK | DFT_OT_T2600MK | DFT_OT_T2800MK | DFT_OT_T3000MK)
+#define ORACLE_SUPPORTED_MODELS (DFT_OT_KC | DFT_OT_HD | DFT_OT_HD2 | DFT_OT_BACKFLOW | ORACLE_THERMAL_MODELS)
 
 #define DFT_HELIUM_MASS (4.002602 / GRID_AUTOAMU)
 #define DFT_MIN_SUBSTEPS 4

@@ -241,6 +241,10 @@ void grid_func4_operate_one(rgrid *dst, rgrid *src, REAL beta, REAL rhom, REAL C
 void grid_func5_operate_one(rgrid *dst, rgrid *src, REAL beta, REAL rhom, REAL C);
 void grid_func6a_operate_one(rgrid *dst, rgrid *src, REAL mass, REAL temp, REAL c4);
 void grid_func6b_operate_one(rgrid *dst, rgrid *src, REAL mass, REAL temp, REAL c4);
+/* ideal Bose gas (the shim's restatement behind grid_func6a / 6b) */
+REAL oracle_lwl3(REAL mass, REAL temp);
+REAL oracle_bose_energy(REAL rho, REAL mass, REAL temp, REAL c4);
+REAL oracle_bose_dEdRho(REAL rho, REAL mass, REAL temp, REAL c4);
 void grid_spline_ypp(REAL *x, REAL *y, INT n, REAL yp1, REAL ypn, REAL *y2);
 REAL grid_spline_interpolate(REAL *xa, REAL *ya, REAL *y2a, INT n, REAL x);
 REAL grid_polynomial_interpolate(REAL *xa, REAL *ya, INT n, REAL x, REAL *dy);

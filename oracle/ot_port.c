@@ -126,6 +126,30 @@ void dft_ot_init_params(dft_ot_functional *otf, INT model) {
   otf->temp = 0.0;
   otf->rho0 = 0.0218360;
   otf->lj_params.h = 2.1903;
+  /* the thermal parameter sets (src/ot.c:1038-1222), each selected by its
+   * bit; a later bit overrides an earlier one as in the reference */
+  static const struct { INT bit; REAL b, c2, c3, c4, temp, rho0, h; } tset[] = {
+    { DFT_OT_T0MK, -719.2435, -24258.88, 1865257.0, 0.0, 0.0, 0.0218354, 2.19035 },
+    { DFT_OT_T400MK, -714.2174, -24566.29, 1873203.0, 0.98004, 0.4, 0.0218351, 2.18982 },
+    { DFT_OT_T600MK, -705.1319, -25124.17, 1887707.0, 0.99915, 0.6, 0.0218346, 2.18887 },
+    { DFT_OT_T800MK, -690.4745, -26027.12, 1911283.0, 0.99548, 0.8, 0.0218331, 2.18735 },
+    { DFT_OT_T1200MK, -646.5135, -28582.81, 1973737.0, 0.99666, 1.2, 0.0218298, 2.18287 },
+    { DFT_OT_T1400MK, -625.8123, -29434.03, 1984068.0, 0.99829, 1.4, 0.0218332, 2.18080 },
+    { DFT_OT_T1600MK, -605.9788, -30025.96, 1980898.0, 1.00087, 1.6, 0.0218453, 2.17885 },
+    { DFT_OT_T1800MK, -593.8289, -29807.56, 1945685.0, 1.00443, 1.8, 0.0218703, 2.17766 },
+    { DFT_OT_T2000MK, -600.8313, -27850.96, 1847407.0, 1.00919, 2.0, 0.0219153, 2.17834 },
+    { DFT_OT_T2100MK, -620.9129, -25418.15, 1747494.0, 1.01156, 2.1, 0.0219500, 2.18032 },
+    { DFT_OT_T2200MK, -619.2016, -25096.68, 1720802.0, 1.01436, 2.2, 0.0219859, 2.18015 },
+    { DFT_OT_T2400MK, -609.0757, -26009.98, 1747943.0, 1.02130, 2.4, 0.0218748, 2.17915 },
+    { DFT_OT_T2600MK, -634.0664, -23790.66, 1670707.0, 1.02770, 2.6, 0.0217135, 2.18162 },
+    { DFT_OT_T2800MK, -663.9942, -21046.37, 1574611.0, 1.03429, 2.8, 0.0215090, 2.18463 },
+    { DFT_OT_T3000MK, -673.6543, -20022.76, 1535887.0, 1.04271, 3.0, 0.0212593, 2.18562 },
+  };
+  for (unsigned i = 0; i < sizeof(tset) / sizeof(tset[0]); i++)
+    if (model & tset[i].bit) {
+      otf->b = tset[i].b; otf->c2 = tset[i].c2; otf->c3 = tset[i].c3; otf->c4 = tset[i].c4;
+      otf->temp = tset[i].temp; otf->rho0 = tset[i].rho0; otf->lj_params.h = tset[i].h;
+    }
   otf->mu0 = 0.0;
   otf->xi = 1E4 / a3;
   otf->rhobf = 0.033 * a3;
@@ -448,6 +472,10 @@ void dft_ot_potential(dft_ot_functional *otf, cgrid *P, wf *gwf) {
     grid_add_real_to_complex_re(P, q);
   }
   if (otf->model & DFT_OT_BACKFLOW) bf_potential(otf, P, gwf, rho, rk);
+  if (otf->model >= DFT_OT_T400MK) {                           /* ideal Bose gas  src/ot.c:402-407, 804-809 */
+    grid_func6a_operate_one(q, rho, otf->mass, otf->temp, otf->c4);
+    grid_add_real_to_complex_re(P, q);
+  }
 }
 
 /* ------------------------------------------------------------------ */
@@ -475,6 +503,10 @@ void dft_ot_energy_density(dft_ot_functional *otf, rgrid *ed, wf *gwf) {
     }
   if (otf->model & (DFT_OT_HD | DFT_OT_HD2)) {                 /* Barranco  src/ot-energy.c:96-99 */
     grid_func5_operate_one(u, rho, otf->beta, otf->rhom, otf->C);
+    rgrid_sum(ed, ed, u);
+  }
+  if (otf->model >= DFT_OT_T400MK) {                           /* ideal Bose gas  src/ot-energy.c:101-105 */
+    grid_func6b_operate_one(u, rho, otf->mass, otf->temp, otf->c4);
     rgrid_sum(ed, ed, u);
   }
 
@@ -564,14 +596,19 @@ void dft_ot_energy_density(dft_ot_functional *otf, rgrid *ed, wf *gwf) {
 /* bulk liquid (src/helium-ot-bulk.c:21-434)                            */
 /* ------------------------------------------------------------------ */
 
-/* E/V = b/2 rho^2 + c2/2 rho^3 + c3/3 rho^4  (src/helium-ot-bulk.c:21-33) */
+/* E/V = b/2 rho^2 + c2/2 rho^3 + c3/3 rho^4 (+ the ideal Bose gas when c4 != 0)
+ * (src/helium-ot-bulk.c:21-33) */
 REAL dft_ot_bulk_energy(dft_ot_functional *otf, REAL rho) {
-  return 0.5 * otf->b * rho * rho + 0.5 * otf->c2 * rho * rho * rho + (1.0 / 3.0) * otf->c3 * rho * rho * rho * rho;
+  REAL e = 0.5 * otf->b * rho * rho + 0.5 * otf->c2 * rho * rho * rho + (1.0 / 3.0) * otf->c3 * rho * rho * rho * rho;
+  if (otf->c4 != 0.0) e += oracle_bose_energy(rho, otf->mass, otf->temp, otf->c4);
+  return e;
 }
 
 /* dE/drho (src/helium-ot-bulk.c:45-57) */
 REAL dft_ot_bulk_dEdRho(dft_ot_functional *otf, REAL rho) {
-  return otf->b * rho + 1.5 * otf->c2 * rho * rho + (4.0 / 3.0) * otf->c3 * rho * rho * rho;
+  REAL d = otf->b * rho + 1.5 * otf->c2 * rho * rho + (4.0 / 3.0) * otf->c3 * rho * rho * rho;
+  if (otf->c4 != 0.0) d += oracle_bose_dEdRho(rho, otf->mass, otf->temp, otf->c4);
+  return d;
 }
 
 /* P = rho dE/drho - E (src/helium-ot-bulk.c:143-146) */

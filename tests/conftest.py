@@ -68,3 +68,14 @@ def line_psi(o, n, step, seed=5):
     z = (np.arange(n) - n // 2) * step
     rho = rho0 * (1 + 0.3 * np.cos(2 * np.pi * z / (n * step)) + 0.05 * rng.random(n))
     return (np.sqrt(rho) * np.exp(0.4j * np.sin(2 * np.pi * z / (n * step)))).reshape(1, 1, n)
+
+
+def thermal_psi(o, shape, step, seed=5):
+    """a droplet of radius 5 bohr over a 1e-4 rho0 vapour: the ideal Bose gas
+    term takes both of its branches (rho lambda^3 above and below g_{3/2}(1))"""
+    rng = np.random.default_rng(seed)
+    rho0 = 0.0218360 * o.AUTOANG ** 3
+    X = [(np.arange(n) - n // 2) * step for n in shape]
+    r = np.sqrt(X[0][:, None, None] ** 2 + X[1][None, :, None] ** 2 + X[2][None, None, :] ** 2)
+    rho = rho0 * (0.5 * (1 - np.tanh((r - 5.0) / 1.0)) + 1e-4) * (1 + 0.05 * rng.random(shape))
+    return np.sqrt(rho) * np.exp(0.2j * rng.random(shape))

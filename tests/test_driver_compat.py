@@ -65,7 +65,7 @@ def ot_params(lib, model):
 
 
 @needs_ref
-@pytest.mark.parametrize("model", [0, 1, 8, 9])
+@pytest.mark.parametrize("model", [0, 1, 8, 9, 16, 32, 32 | 9, 256 | 1, 4096, 262144 | 8])
 def test_functional_parameters_bit_identical_to_libdft(lib, ref, model):
     """dft_ot_init_params: every public parameter in atomic units equals the
     value libdft's own conversion gives (src/ot.c:1002-1270)."""
@@ -314,3 +314,26 @@ def test_grid_file_refusals(lib, tmp_path):
     open(tmp_path / "f.grd", "wb").write(b"\0" * len(raw))
     assert read(str(tmp_path / "f").encode(), 0, *shape, dp(m), dp(out)) == 6         # DFTGPU_ERR_UNSUPPORTED
     assert lib.dftgpu_last_error() == 6
+
+
+@needs_ref
+@pytest.mark.parametrize("model", [32, 1024 | 9, 262144])
+def test_thermal_bulk_relations_equal_libdft(lib, ref, model):
+    """The ideal Bose gas in the bulk relations of the thermal models
+    (src/helium-ot-bulk.c:30-31, 54-55 with src/common.c:253-529): the
+    library's host restatement against libdft's own code, at the bulk density
+    (rho lambda^3 above g_{3/2}(1)) and in the dilute z < 1 branch."""
+    p = ot_params(lib, model)
+    R = ref.lib
+    for L in (lib, R):
+        for name in ("dft_ot_bulk_energy", "dft_ot_bulk_dEdRho"):
+            getattr(L, name).restype = C.c_double
+            getattr(L, name).argtypes = [C.c_void_p, C.c_double]
+    with Grids(ref, (8, 8, 8), 1.0, 4.002602 / ref.AUTOAMU) as g:
+        w = g.wf()
+        o = g.ot(model, w)
+        for f in (1.3, 1.0, 0.2, 0.01, 1e-4, 1e-7):
+            rho = f * p.rho0
+            for name in ("dft_ot_bulk_energy", "dft_ot_bulk_dEdRho"):
+                a, b = getattr(lib, name)(C.byref(p), rho), getattr(R, name)(o, rho)
+                assert abs(a - b) <= 1e-15 * abs(b), (name, f, a, b)

@@ -383,7 +383,7 @@ def test_errors_are_reported(gpu):
     assert not L.grid_wf_alloc(16, 16, 16, 1.0, 7000.0, 1, 1, b"dirichlet")
     assert L.dftgpu_last_error() == 6
     w = gpu.Wf((16, 16, 16), 1.0)
-    assert not L.dft_ot_alloc(32, w.ptr, 4, 32)                            # DFT_OT_T400MK (thermal)
+    assert not L.dft_ot_alloc(1048576, w.ptr, 4, 32)                       # DFT_DR (Dupont-Roc)
     assert L.dftgpu_last_error() == 6
     psi = np.ones((16, 16, 16), dtype=complex)
     psi[3, 4, 5] = np.nan

@@ -10,7 +10,7 @@ common.c and helium-ot-bulk.c (golden/*.npz, see make_golden.py).
 import numpy as np
 import pytest
 
-from conftest import golden, line_psi, relerr
+from conftest import golden, line_psi, relerr, thermal_psi
 from oracle import Grids, Oracle, ref_available
 
 
@@ -264,3 +264,43 @@ def test_one_d_uniform_liquid_is_near_the_bulk_chemical_potential(port, model):
         mu = port.lib.orc_bulk_dEdRho(otf, rho0)
     assert np.ptp(P.real) < 1e-12 * abs(mu)
     assert abs(P.real.mean() / mu - 1) < 0.02
+
+
+@pytest.mark.skipif(not ref_available(), reason="reference tree not present")
+@pytest.mark.parametrize("model", [16, 32, 32 | 9, 256 | 1, 4096 | 8, 262144])
+def test_reference_build_live_vs_port_thermal(model):
+    """The thermal models (src/ot.c:1038-1222 parameter sets, the ideal Bose gas
+    term src/ot.c:402-407, 804-809 and src/ot-energy.c:101-105): the
+    restatement against libdft's own ot.c / ot-energy.c on the same shim."""
+    ref, prt = Oracle("ref"), Oracle("port")
+    shape, step = (16, 18, 20), 0.8
+    out = []
+    for o in (ref, prt):
+        with Grids(o, shape, step, 4.002602 / o.AUTOAMU) as g:
+            w = g.wf(thermal_psi(o, shape, step))
+            otf = g.ot(model, w)
+            out.append((g.potential(otf, w), g.energy_density(otf, w)))
+    assert relerr(out[0][0].real, out[1][0].real) < 1e-12
+    assert relerr(out[0][1], out[1][1]) < 1e-12
+
+
+@pytest.mark.skipif(not ref_available(), reason="reference tree not present")
+@pytest.mark.parametrize("model", [32, 4096, 262144])
+@pytest.mark.parametrize("frac", [1.0, 0.05, 1e-3])
+def test_thermal_uniform_liquid_matches_libdft_bulk(model, frac):
+    """The shim's grid_func6a / 6b (libgrid's, absent) against libdft's own host
+    forms of the ideal Bose gas (src/common.c:487-529, through the bulk
+    relations src/helium-ot-bulk.c:30-31, 54-55) on the reference build: the
+    potential and energy density of a uniform liquid at the bulk density
+    (rho lambda^3 above g_{3/2}(1)) and of dilute ones (the z < 1 branch)."""
+    o = Oracle("ref")
+    shape = (12, 10, 8)
+    with Grids(o, shape, 0.9, 4.002602 / o.AUTOAMU) as g:
+        w = g.wf(np.ones(shape))
+        otf = g.ot(model, w)
+        rho = frac * o.lib.orc_bulk_density(otf, 0.0)
+        g.set_wf(w, np.full(shape, np.sqrt(rho), dtype=complex))
+        P = g.potential(otf, w)
+        ed = g.energy_density(otf, w)
+        assert relerr(P.real, np.full(shape, o.lib.orc_bulk_dEdRho(otf, rho))) < 1e-12
+        assert relerr(ed, np.full(shape, o.lib.orc_bulk_energy(otf, rho))) < 1e-12
