@@ -313,7 +313,10 @@ int dftgpu_wf_propagate_noalloc(void *psi_out, const void *psi_in, const void *p
                                 REAL step, REAL mass, double dt_re, double dt_im, int prec, void *stream);
 
 /* ---------------------------------------------------------- OT functional */
-dft_ot_functional *dft_ot_alloc(INT model, wf *gwf, INT min_substeps, INT max_substeps);   /* src/ot.c:66 */
+/* src/ot.c:66.  Models: PLAIN, KC, HD, HD2, BACKFLOW and the thermal sets
+ * T0MK..T3000MK (combinations as in libdft); GP and DR get NULL with
+ * DFTGPU_ERR_UNSUPPORTED.  On a 1-D grid (nx = ny = 1) the 1-D effective kernels. */
+dft_ot_functional *dft_ot_alloc(INT model, wf *gwf, INT min_substeps, INT max_substeps);
 void dft_ot_free(dft_ot_functional *otf);                                                   /* src/ot.c:268 */
 void dft_ot_potential(dft_ot_functional *otf, cgrid *potential, wf *gwf);                    /* src/ot.c:314 */
 void dft_ot_energy_density(dft_ot_functional *otf, rgrid *energy_density, wf *gwf);         /* src/ot-energy.c:38 */
