@@ -111,7 +111,7 @@ def test_bulk_response_matches_libdft(lib, ref, model):
 # libgrid functions outside the time step; the design notes list them)
 DRIVERS = ["imag_time/imag_time.c", "dynamics/dynamics.c", "dispersion/dispersion.c",
            "dispersion/dispersion2.c", "dispersion/dispersion3.c", "dispersion/static-resp.c",
-           "bulk/bulk_properties.c"]
+           "bulk/bulk_properties.c", "piston/piston.c", "shock/shock.c"]
 
 
 @pytest.mark.skipif(not os.path.isdir(REF_EXAMPLES), reason="reference tree not present")
