@@ -257,7 +257,13 @@ void grid_add_real_to_complex_im(cgrid *dst, rgrid *src);
 
 /* -------------------------------------------------------- wave functions
  * libgrid wf API as called by libdft and its examples. */
-/* grid_wf_alloc (imag_time.c:197): periodic boundary + WF_2ND_ORDER_FFT only.
+/* grid_wf_alloc (imag_time.c:197): periodic boundary with WF_2ND_ORDER_FFT or
+ * WF_2ND_ORDER_CN (examples/gas-bubble/config.h:66).  The CN wave function
+ * steps its kinetic part by Crank-Nicolson on the 3-point finite-difference
+ * operator, axis by axis (x, y, z); on the periodic grid each axis factor is
+ * diagonal in k, (1 - i dt Q / 4m) / (1 + i dt Q / 4m) with
+ * Q = (2 sin((k - k0) h / 2) / h)^2, and is applied there.  grid_wf_energy of
+ * a CN wave function uses the same finite-difference kinetic operator.
  * Dimensions 2^a 3^b 5^c in [2, 1024], x and y may be odd, z even; a 1-D grid
  * (nx = ny = 1, examples/1d-bubble/bubble-1d.c:126) takes nz up to 4096 and the
  * OT functional's 1-D effective model (src/ot.c:133-217).  Other sizes return

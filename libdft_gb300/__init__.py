@@ -26,6 +26,7 @@ DFT_OT_KC = 1
 DFT_OT_BACKFLOW = 8
 WF_PERIODIC_BOUNDARY = 3
 WF_2ND_ORDER_FFT = 1
+WF_2ND_ORDER_CN = 3
 
 AUTOANG = 0.529177210903
 AUTOK = 3.1577502480407e5
@@ -273,13 +274,14 @@ class RGrid:
 
 
 class Wf:
-    """libgrid wave function on the GPU (periodic, 2nd-order FFT propagator)."""
+    """libgrid wave function on the GPU (periodic; 2nd-order FFT propagator, or
+    Crank-Nicolson with propagator=WF_2ND_ORDER_CN)."""
 
-    def __init__(self, shape, step, mass=HELIUM_MASS, ptr=None):
+    def __init__(self, shape, step, mass=HELIUM_MASS, ptr=None, propagator=WF_2ND_ORDER_FFT):
         L = lib()
         self.shape = tuple(int(s) for s in shape)
         self.step = float(step)
-        self.ptr = ptr or L.grid_wf_alloc(*self.shape, self.step, mass, WF_PERIODIC_BOUNDARY, WF_2ND_ORDER_FFT, b"wf")
+        self.ptr = ptr or L.grid_wf_alloc(*self.shape, self.step, mass, WF_PERIODIC_BOUNDARY, propagator, b"wf")
         if not self.ptr:
             check(what="grid_wf_alloc")
 

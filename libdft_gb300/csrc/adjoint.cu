@@ -401,6 +401,7 @@ static int strang_vjp_t(wf *g, cgrid *V, double dr, double di, const cgrid *psi,
   KinArgs<T> K;
   kin_args<T>(K, nx, ny, nz, V->step, make_double2(di / (2.0 * g->mass), dr / (2.0 * g->mass)),   // conj(-i dt / 2m)
               g->grid->kx0, g->grid->ky0, g->grid->kz0, spec);
+  K.cn = g->propagator == WF_2ND_ORDER_CN;   // real Q: the conjugate factor is the factor of conj(c)
   DFT_TRY(launch_xkinetic<T>(K));
   DFT_TRY(ypass<T>(spec, nx, ny, nz, (T) 1));
   SpecLoadZ<T> lz{spec, nx, ny};
@@ -444,7 +445,7 @@ static void same_momentum(wf *dst, const wf *src) {
 
 static AdjWork *work_get(OtPriv *P, wf *gwf) {
   AdjWork *W = (AdjWork *) P->adj;
-  if (W && W->wk->mass == gwf->mass) {
+  if (W && W->wk->mass == gwf->mass && W->wk->propagator == gwf->propagator) {
     same_momentum(W->wk, gwf); same_momentum(W->wp, gwf);
     return W;
   }

@@ -317,13 +317,14 @@ void grid_add_real_to_complex_im(cgrid *d, rgrid *s) { if (!rc_shape(d, s)) { ba
 
 // ------------------------------------------------------------------ wave functions
 wf *grid_wf_alloc(INT nx, INT ny, INT nz, REAL step, REAL mass, char boundary, char propagator, char *id) {
-  if (boundary != WF_PERIODIC_BOUNDARY || propagator != WF_2ND_ORDER_FFT) {
-    set_error(DFTGPU_ERR_UNSUPPORTED, "grid_wf_alloc: periodic boundary with WF_2ND_ORDER_FFT only");
+  if (boundary != WF_PERIODIC_BOUNDARY || (propagator != WF_2ND_ORDER_FFT && propagator != WF_2ND_ORDER_CN)) {
+    set_error(DFTGPU_ERR_UNSUPPORTED, "grid_wf_alloc: periodic boundary with WF_2ND_ORDER_FFT or WF_2ND_ORDER_CN only");
     return nullptr;
   }
   cgrid *c = cgrid_new(nx, ny, nz, step, rt().precision, id);
   if (!c) return nullptr;
   wf *w = (wf *) calloc(1, sizeof(wf));
+  if (!w) { cgrid_free(c); set_error(DFTGPU_ERR_NOMEM, "grid_wf_alloc"); return nullptr; }
   w->grid = c;
   w->mass = mass;
   w->norm = 1.0;

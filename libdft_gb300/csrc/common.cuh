@@ -117,6 +117,24 @@ template <typename C> __device__ __forceinline__ C cprod1p(C p, C q) {
   return r;
 }
 
+// One axis of the Crank-Nicolson kinetic step, minus one:
+//   (1 + c Q / 2) / (1 - c Q / 2) - 1 = c Q / (1 - c Q / 2),
+// Q = (2 sin(k h / 2) / h)^2 the eigenvalue of the periodic second difference
+// -(f[j+1] - 2 f[j] + f[j-1]) / h^2 at wave number k, c = -i dt / 2m.  For
+// Re c <= 0 (real or imaginary time) |1 - c Q / 2| >= 1.
+__device__ __forceinline__ float2 cn_m1(float2 c, float k, float h) {
+  const float s = 2.f * sinf(0.5f * k * h) / h, q = s * s;
+  const float nx = c.x * q, ny = c.y * q, dx = 1.f - 0.5f * nx, dy = -0.5f * ny;
+  const float id = 1.f / (dx * dx + dy * dy);
+  return make_float2((nx * dx + ny * dy) * id, (ny * dx - nx * dy) * id);
+}
+__device__ __forceinline__ double2 cn_m1(double2 c, double k, double h) {
+  const double s = 2.0 * sin(0.5 * k * h) / h, q = s * s;
+  const double nx = c.x * q, ny = c.y * q, dx = 1.0 - 0.5 * nx, dy = -0.5 * ny;
+  const double id = 1.0 / (dx * dx + dy * dy);
+  return make_double2((nx * dx + ny * dy) * id, (ny * dx - nx * dy) * id);
+}
+
 // a * exp(z).  For small |z| the factor is applied as a + a (exp(z) - 1): a
 // factor rounded as a whole has |exp(i theta)|^2 = c^2 + s^2 off 1 by the
 // rounding of c near 1, which is biased for small angles and changed the norm

@@ -774,25 +774,27 @@ __global__ void __launch_bounds__(256, MODE == 1 ? 1 : (MODE == 0 ? 3 : 2)) xcon
   }
 }
 
-// psi(k) *= exp(cdt k^2) / N between forward and inverse x transforms
-template <int N>
+// psi(k) *= exp(cdt k^2) / N between forward and inverse x transforms; CN:
+// the Crank-Nicolson factor of the finite-difference kinetic operator, one per
+// axis (cn_m1; h the grid step)
+template <int N, bool CN>
 __global__ void __launch_bounds__(256) xkinetic_kernel(const C *__restrict__ tw, C *data, int ny, int nz, float2 cdt,
                                                       float inv_n, float dkx, float dky, float dkz, float kx0,
-                                                      float ky0, float kz0) {
+                                                      float ky0, float kz0, float h) {
   constexpr int E = Shape<N>::E, TL = Shape<N>::TL, B = Shape<N>::B, LP = Shape<N>::LP;
   __shared__ C sm[B * LP];
   __shared__ C fx[N];   // exp(cdt (kx - kx0)^2) - 1
   const int kz = blockIdx.y, l = threadIdx.x % B, t = threadIdx.x / B, y = blockIdx.x * B + l;
   for (int e = threadIdx.x; e < N; e += 256) {
     const float k = (float) (e < (N + 1) / 2 ? e : e - N) * dkx - kx0;
-    fx[e] = cexpm1(make_float2(cdt.x * (k * k), cdt.y * (k * k)));
+    fx[e] = CN ? cn_m1(cdt, k, h) : cexpm1(make_float2(cdt.x * (k * k), cdt.y * (k * k)));
   }
   C fyz;                // exp(cdt ((ky - ky0)^2 + (kz - kz0)^2)) - 1 of this thread's line
   {
     const float kzv = (float) (kz < (nz + 1) / 2 ? kz : kz - nz) * dkz - kz0;
     const float kyv = (float) (y < (ny + 1) / 2 ? y : y - ny) * dky - ky0;
     const float q = kyv * kyv + kzv * kzv;
-    fyz = cexpm1(make_float2(cdt.x * q, cdt.y * q));
+    fyz = CN ? cprod1p(cn_m1(cdt, kyv, h), cn_m1(cdt, kzv, h)) : cexpm1(make_float2(cdt.x * q, cdt.y * q));
   }
   C *base = data + kz * (size_t) N * ny + y;
   C v[E];

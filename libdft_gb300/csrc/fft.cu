@@ -309,9 +309,10 @@ template <int N> int fast_xkinetic(const KinArgs<float> &A) {
   FftPlan<float> p;
   DFT_TRY(get_plan<float>(N, &p));
   ProfScope prof("fft_x_kinetic", 2.0 * A.nx * A.ny * A.nz * sizeof(float2));
-  ff::xkinetic_kernel<N><<<dim3(A.ny / B, A.nz), 256, 0, rt().stream>>>(
+  auto k = A.cn ? ff::xkinetic_kernel<N, true> : ff::xkinetic_kernel<N, false>;
+  k<<<dim3(A.ny / B, A.nz), 256, 0, rt().stream>>>(
       p.tw, A.data, A.ny, A.nz, make_float2((float) A.cdt.x, (float) A.cdt.y), (float) A.inv_n, (float) A.dkx,
-      (float) A.dky, (float) A.dkz, (float) A.kx0, (float) A.ky0, (float) A.kz0);
+      (float) A.dky, (float) A.dkz, (float) A.kx0, (float) A.ky0, (float) A.kz0, (float) A.h);
   DFT_CHECK_LAUNCH();
   return DFTGPU_OK;
 }

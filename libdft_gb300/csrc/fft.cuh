@@ -580,7 +580,9 @@ __global__ void __launch_bounds__(FFT_THREADS) xconv_kernel(const XConvArgs<T> A
 // so each CTA tabulates fx for its line length and fyz for its lines (two
 // transcendental evaluations per thread instead of one per element) and
 // applies psi + psi ((1 + fx)(1 + fyz) - 1), which keeps |factor| = 1 to the
-// rounding of the exponent in real time.
+// rounding of the exponent in real time.  With cn set the factor is the
+// Crank-Nicolson one of the finite-difference kinetic operator, one per axis
+// (cn_m1), and separates the same way: (1 + fx)(1 + fy)(1 + fz).
 template <typename T> struct KinArgs {
   FftPlan<T> plan;
   int B, nx, ny, nz;
@@ -588,6 +590,8 @@ template <typename T> struct KinArgs {
   double inv_n;
   double dkx, dky, dkz; // 2 pi / (n step)
   double kx0, ky0, kz0; // moving-background momentum
+  double h;             // grid step
+  int cn;               // Crank-Nicolson factors instead of exp(cdt |k - k0|^2)
   typename cplx_t<T>::type *data;
 };
 
@@ -602,6 +606,8 @@ inline void kin_args(KinArgs<T> &K, int nx, int ny, int nz, double step, double2
   K.dky = 2.0 * M_PI / (ny * step);
   K.dkz = 2.0 * M_PI / (nz * step);
   K.kx0 = kx0; K.ky0 = ky0; K.kz0 = kz0;
+  K.h = step;
+  K.cn = 0;
 }
 
 // shared memory of the generic kinetic kernel: two tiles + the factor tables
@@ -622,14 +628,16 @@ __global__ void __launch_bounds__(FFT_THREADS) xkinetic_kernel(const KinArgs<T> 
   const int kz = blockIdx.y, y0 = blockIdx.x * B;
   const size_t plane = (size_t) A.nx * A.ny;
   C *base = A.data + kz * plane + y0;
+  const C c = mk<T>((T) A.cdt.x, (T) A.cdt.y);
   for (int e = threadIdx.x; e < n; e += blockDim.x) {
     const double k = kfreq(e, A.nx, A.dkx) - A.kx0, q = k * k;
-    fx[e] = cexpm1(mk<T>((T) (A.cdt.x * q), (T) (A.cdt.y * q)));
+    fx[e] = A.cn ? cn_m1(c, (T) k, (T) A.h) : cexpm1(mk<T>((T) (A.cdt.x * q), (T) (A.cdt.y * q)));
   }
   const double kzv = kfreq(kz, A.nz, A.dkz) - A.kz0;
   for (int l = threadIdx.x; l < B; l += blockDim.x) {
     const double k = kfreq(y0 + l, A.ny, A.dky) - A.ky0, q = k * k + kzv * kzv;
-    fyz[l] = cexpm1(mk<T>((T) (A.cdt.x * q), (T) (A.cdt.y * q)));
+    fyz[l] = A.cn ? cprod1p(cn_m1(c, (T) k, (T) A.h), cn_m1(c, (T) kzv, (T) A.h))
+                  : cexpm1(mk<T>((T) (A.cdt.x * q), (T) (A.cdt.y * q)));
   }
   for (int idx = threadIdx.x; idx < n * B; idx += blockDim.x) {
     const int l = idx % B, e = idx / B;

@@ -351,8 +351,9 @@ static int strang_factorised(wf *g, cgrid *dst, cgrid *src, cgrid *V, double dr,
 template <typename T> int strang(wf *g, cgrid *dst, cgrid *src, cgrid *V, double dr, double di) {
   typedef typename cplx_t<T>::type C;
   const int nx = (int) src->nx, ny = (int) src->ny, nz = (int) src->nz;
+  const int cn = g->propagator == WF_2ND_ORDER_CN;
   if constexpr (std::is_same<T, float>::value) {
-    if (factorised_propagation() && kin_fits(nx, ny, nz)) return strang_factorised(g, dst, src, V, dr, di);
+    if (!cn && factorised_propagation() && kin_fits(nx, ny, nz)) return strang_factorised(g, dst, src, V, dr, di);
   }
   C *spec = (C *) wf_spec(g);
   if (!spec) return DFTGPU_ERR_NOMEM;
@@ -366,6 +367,7 @@ template <typename T> int strang(wf *g, cgrid *dst, cgrid *src, cgrid *V, double
   const cgrid *mg = g->grid;   // moving-background momentum of the wave function
   kin_args<T>(K, nx, ny, nz, src->step, make_double2(di / (2.0 * m), -dr / (2.0 * m)),   // -i dt / 2m
               mg->kx0, mg->ky0, mg->kz0, spec);
+  K.cn = cn;
   DFT_TRY(launch_xkinetic<T>(K));
   DFT_TRY(ypass<T>(spec, nx, ny, nz, (T) 1));
   SpecLoadZ<T> lz{spec, nx, ny};
@@ -454,7 +456,19 @@ template <typename T> int kinetic_energy_t(wf *g, double *out) {
   const double dv = c->step * c->step * c->step;
   const double scale = 1.0 / (2.0 * g->mass) * dv / ((double) nx * ny * nz);
   const size_t n = (size_t) nx * ny * nz;
-  // spectral layout [kz][kx][ky]
+  const double h = c->step;
+  // spectral layout [kz][kx][ky]; Crank-Nicolson wave functions: the
+  // finite-difference kinetic operator that propagator steps with,
+  // (2 sin(k h / 2) / h)^2 per axis in place of k^2
+  if (g->propagator == WF_2ND_ORDER_CN)
+    return reduce_host<1>(n, [=] __device__(size_t i, double *v) {
+      const int ky = (int) (i % ny), kx = (int) ((i / ny) % nx), kz = (int) (i / ((size_t) nx * ny));
+      const double a = 2.0 * sin(0.5 * h * (kfreq(kx, nx, dkx) - k0x)) / h;
+      const double b = 2.0 * sin(0.5 * h * (kfreq(ky, ny, dky) - k0y)) / h;
+      const double cc = 2.0 * sin(0.5 * h * (kfreq(kz, nz, dkz) - k0z)) / h;
+      const C s = spec[i];
+      v[0] = (a * a + b * b + cc * cc) * ((double) s.x * s.x + (double) s.y * s.y);
+    }, out, scale);
   return reduce_host<1>(n, [=] __device__(size_t i, double *v) {
     const int ky = (int) (i % ny), kx = (int) ((i / ny) % nx), kz = (int) (i / ((size_t) nx * ny));
     const double a = kfreq(kx, nx, dkx) - k0x, b = kfreq(ky, ny, dky) - k0y, cc = kfreq(kz, nz, dkz) - k0z;

@@ -83,6 +83,7 @@ class Oracle:
             "orc_wf_density": (None, [_vp, _vp]),
             "orc_wf_velocity": (None, [_vp, _vp, _vp, _vp, _d]),
             "orc_wf_set_momentum": (None, [_vp, _d, _d, _d]),
+            "orc_wf_set_propagator": (None, [_vp, _i]),
             "orc_wf_boundary": (None, [_vp, _vp, _d, _d, _l, _l, _l, _l, _l, _l]),
             "orc_wf_absorb_potential": (None, [_vp, _vp, _d, _d]),
             "orc_cgrid_new": (_vp, [_l, _l, _l, _d]),
@@ -166,12 +167,15 @@ class Grids:
         self.mass = float(mass)
         self._owned = []
 
-    def wf(self, psi: np.ndarray | None = None):
+    def wf(self, psi: np.ndarray | None = None, propagator: int = 1):
+        """propagator: 1 = WF_2ND_ORDER_FFT, 3 = WF_2ND_ORDER_CN"""
         nx, ny, nz = self.shape
         w = self.o.lib.orc_wf_new(nx, ny, nz, self.step, self.mass)
         if not w:
             raise RuntimeError("oracle wf alloc failed")
         self._owned.append(("wf", w))
+        if propagator != 1:
+            self.o.lib.orc_wf_set_propagator(w, propagator)
         if psi is not None:
             self.set_wf(w, psi)
         return w

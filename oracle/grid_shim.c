@@ -704,8 +704,8 @@ void grid_complex_im_to_real(rgrid *d, cgrid *s) {
 /* ------------------------------------------------------------------ */
 
 wf *grid_wf_alloc(INT nx, INT ny, INT nz, REAL step, REAL mass, char boundary, char propagator, char *id) {
-  if (boundary != WF_PERIODIC_BOUNDARY || propagator != WF_2ND_ORDER_FFT) {
-    fprintf(stderr, "oracle: only periodic boundaries with the 2nd-order FFT propagator are restated.\n");
+  if (boundary != WF_PERIODIC_BOUNDARY || (propagator != WF_2ND_ORDER_FFT && propagator != WF_2ND_ORDER_CN)) {
+    fprintf(stderr, "oracle: only periodic boundaries with the 2nd-order FFT or CN propagator are restated.\n");
     return NULL;
   }
   wf *w = (wf *) calloc(1, sizeof(wf));
@@ -784,20 +784,33 @@ static inline REAL kval(INT i, INT n, REAL step) {
   return 2.0 * M_PI * (REAL) m / ((REAL) n * step);
 }
 
+/* The kinetic operator's value along one axis at wave number k: k^2 for the
+ * FFT propagator; for WF_2ND_ORDER_CN the eigenvalue (2 sin(k h / 2) / h)^2 of
+ * the periodic second difference -(f[j+1] - 2 f[j] + f[j-1]) / h^2, the
+ * finite-difference operator that propagator steps with (libgrid's CN
+ * propagator is absent; this is the restatement both sides share). */
+static inline REAL kin_axis(REAL k, REAL h, int cn) {
+  if (!cn) return k * k;
+  REAL s = 2.0 * sin(0.5 * k * h) / h;
+  return s * s;
+}
+
 REAL grid_wf_kinetic_energy(wf *g) {
   cgrid *c = g->grid, *w = wf_workspace(g);
   INT nx = c->nx, ny = c->ny, nz = c->nz, nr = nx * ny;
+  int cn = g->propagator == WF_2ND_ORDER_CN;
+  REAL h = c->step;
   cgrid_copy(w, c);
   cgrid_fft(w);
   REAL *rs = malloc(sizeof(REAL) * (size_t) nr);
 #pragma omp parallel for schedule(static)
   for (INT ij = 0; ij < nr; ij++) {
     INT i = ij / ny, j = ij % ny;
-    REAL kx = kval(i, nx, c->step) - c->kx0, ky = kval(j, ny, c->step) - c->ky0, s = 0.0;
+    REAL qxy = kin_axis(kval(i, nx, h) - c->kx0, h, cn) + kin_axis(kval(j, ny, h) - c->ky0, h, cn), s = 0.0;
     for (INT k = 0; k < nz; k++) {
-      REAL kz = kval(k, nz, c->step) - c->kz0;
+      REAL q = qxy + kin_axis(kval(k, nz, h) - c->kz0, h, cn);
       REAL complex v = w->value[ij * nz + k];
-      s += (kx * kx + ky * ky + kz * kz) * (creal(v) * creal(v) + cimag(v) * cimag(v));
+      s += q * (creal(v) * creal(v) + cimag(v) * cimag(v));
     }
     rs[ij] = s;
   }
@@ -869,16 +882,30 @@ static void apply_potential_half(cgrid *dst, cgrid *src, cgrid *pot, REAL comple
     dst->value[ii] = src->value[ii] * cexp(-I * pot->value[ii] * dt / (2.0 * HBAR));
 }
 
-/* psi(k) *= exp(-i hbar |k - k0|^2 dt / 2m) / N, k0 = the momentum of grid m */
-static void apply_kinetic(cgrid *c, const cgrid *m, REAL mass, REAL complex dt, int normalize) {
+/* The Crank-Nicolson factor of one axis: (1 - i hbar Q dt / 4m) / (1 + i hbar Q dt / 4m),
+ * Q = kin_axis(k, h, 1).  Crank-Nicolson applied axis by axis (x, y, z) to
+ * the periodic finite-difference operator multiplies each k by the product
+ * of the three factors (every axis operator is diagonal in k). */
+static inline REAL complex cn_axis(REAL k, REAL h, REAL mass, REAL complex dt) {
+  REAL complex a = I * HBAR * kin_axis(k, h, 1) * dt / (4.0 * mass);
+  return (1.0 - a) / (1.0 + a);
+}
+
+/* psi(k) *= exp(-i hbar |k - k0|^2 dt / 2m) / N, k0 = the momentum of grid m
+ * (the Crank-Nicolson factors instead for a WF_2ND_ORDER_CN wave function) */
+static void apply_kinetic(cgrid *c, const cgrid *m, REAL mass, REAL complex dt, int normalize, int cn) {
   INT nx = c->nx, ny = c->ny, nz = c->nz;
-  REAL inv_n = normalize ? 1.0 / (REAL) (nx * ny * nz) : 1.0;
+  REAL inv_n = normalize ? 1.0 / (REAL) (nx * ny * nz) : 1.0, h = c->step;
 #pragma omp parallel for schedule(static)
   for (INT ij = 0; ij < nx * ny; ij++) {
     INT i = ij / ny, j = ij % ny;
-    REAL kx = kval(i, nx, c->step) - m->kx0, ky = kval(j, ny, c->step) - m->ky0;
+    REAL kx = kval(i, nx, h) - m->kx0, ky = kval(j, ny, h) - m->ky0;
     for (INT k = 0; k < nz; k++) {
-      REAL kz = kval(k, nz, c->step) - m->kz0;
+      REAL kz = kval(k, nz, h) - m->kz0;
+      if (cn) {
+        c->value[ij * nz + k] *= cn_axis(kx, h, mass, dt) * cn_axis(ky, h, mass, dt) * cn_axis(kz, h, mass, dt) * inv_n;
+        continue;
+      }
       REAL k2 = kx * kx + ky * ky + kz * kz;
       c->value[ij * nz + k] *= cexp(-I * HBAR * k2 * dt / (2.0 * mass)) * inv_n;
     }
@@ -889,7 +916,7 @@ static void apply_kinetic(cgrid *c, const cgrid *m, REAL mass, REAL complex dt, 
 static void strang_step(wf *g, cgrid *dst, cgrid *src, cgrid *pot, REAL complex dt) {
   apply_potential_half(dst, src, pot, dt);
   cgrid_fft(dst);
-  apply_kinetic(dst, g->grid, g->mass, dt, 1);
+  apply_kinetic(dst, g->grid, g->mass, dt, 1, g->propagator == WF_2ND_ORDER_CN);
   cgrid_inverse_fft(dst);
   apply_potential_half(dst, dst, pot, dt);
 }
@@ -973,7 +1000,7 @@ void grid_wf_propagate_potential(wf *g, REAL complex dt, cgrid *pot, REAL cons) 
     g->grid->value[ii] *= cexp(-I * (pot->value[ii] + cons) * dt / HBAR);
 }
 
-void grid_wf_propagate_kinetic_fft(wf *g, REAL complex dt) { apply_kinetic(g->grid, g->grid, g->mass, dt, 0); }
+void grid_wf_propagate_kinetic_fft(wf *g, REAL complex dt) { apply_kinetic(g->grid, g->grid, g->mass, dt, 0, 0); }
 
 /* ------------------------------------------------------------------ */
 /* ideal Bose gas of the thermal OT models (grid_func6a / 6b)            */

@@ -44,6 +44,7 @@ double orc_wf_kinetic_energy(wf *g) { return grid_wf_energy(g, NULL); }
 void orc_wf_density(wf *g, rgrid *d) { grid_wf_density(g, d); }
 void orc_wf_velocity(wf *g, rgrid *vx, rgrid *vy, rgrid *vz, double eps) { grid_wf_velocity(g, vx, vy, vz, eps); }
 void orc_wf_set_momentum(wf *g, double kx0, double ky0, double kz0) { cgrid_set_momentum(g->grid, kx0, ky0, kz0); }
+void orc_wf_set_propagator(wf *g, int propagator) { g->propagator = (char) propagator; }
 void orc_wf_boundary(wf *g, wf *gp, double amp, double rho0, long lx, long hx, long ly, long hy, long lz, long hz) {
   grid_wf_boundary(g, gp, amp, rho0, lx, hx, ly, hy, lz, hz);
 }
