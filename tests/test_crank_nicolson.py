@@ -15,9 +15,10 @@ axis in k space.
   <psi|T|psi> with T applied as the second difference; real-time steps keep
   the norm; for a smooth state and a small step it approaches the FFT
   propagator.
-* GPU against the oracle: the bare propagator (FP64 generic and FP32 register
-  kinetic passes), the kinetic energy, predict-correct steps of the full
-  functional, and the adjoint identity of the propagator.
+* GPU against the oracle: the bare propagator (generic kinetic pass in FP64
+  and FP32, register kinetic pass in FP32, a 1-D line), the kinetic energy,
+  predict-correct steps of the full functional; the adjoint identity of the
+  propagator and a trajectory gradient against finite differences.
 """
 import numpy as np
 import pytest
@@ -109,6 +110,7 @@ def test_oracle_cn_keeps_norm_and_approaches_fft_for_smooth_states(port):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("prec,shape,tol", [(0, (24, 20, 16), 1e-11), (0, (30, 18, 20), 1e-11),
+                                            (0, (1, 1, 256), 1e-11), (1, (27, 24, 20), 3e-5),
                                             (1, (64, 64, 64), 3e-5), (1, (96, 64, 64), 3e-5)])
 @pytest.mark.parametrize("dt", [41.3 + 0j, 30 - 5j])
 def test_cn_propagate_matches_oracle(gpu, port, prec, shape, tol, dt):
@@ -203,3 +205,39 @@ def test_cn_propagator_adjoint_identity(gpu, prec):
         o.free()
     gpu.set_precision(0)
     assert abs(lhs - rhs) < (1e-12 if prec == 0 else 1e-6) * scale
+
+
+@pytest.mark.gpu
+def test_cn_trajectory_gradient(gpu):
+    """dJ/dVext of 4 real-time steps of the full functional on a CN wave
+    function with momentum, against central finite differences of the GPU
+    forward map (FP64)."""
+    from conftest import coords
+    shape, h, nsteps = (24, 24, 24), 0.8, 4
+    gpu.set_precision(0)
+    rng = np.random.default_rng(21)
+    psi = liquid_psi(shape, h, 6)
+    w = gpu.Wf(shape, h, propagator=gpu.WF_2ND_ORDER_CN)
+    w.set_momentum(*off_grid_momentum(shape, h))
+    ot = gpu.OT(9, w)
+    mu0 = ot.bulk_chempot(0.0)
+    X, Y, Z = coords(shape, h)
+    vx = 5.0 / gpu.AUTOK * np.exp(-(X ** 2 + Y ** 2 + Z ** 2) / 20.0)
+    vext, rt, gv = gpu.RGrid(shape, h), gpu.RGrid(shape, h), gpu.RGrid(shape, h)
+    rt.set(np.abs(liquid_psi(shape, h, 9)) ** 2)
+    dt = 41.3
+
+    def J(v, grad=None):
+        vext.set(v)
+        w.set(psi)
+        return ot.adjoint_run(w, vext, mu0, dt, nsteps, False, rt, grad, checkpoint_every=2)
+
+    J(vx, gv)
+    g = gv.get()
+    dv = rng.standard_normal(shape) / gpu.AUTOK
+    step = 1e-2
+    fd = (J(vx + step * dv) - J(vx - step * dv)) / (2 * step)
+    an = float(np.sum(g * dv))
+    for o in (gv, rt, vext, ot, w):
+        o.free()
+    assert abs(fd / an - 1) < 1e-6
