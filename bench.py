@@ -110,9 +110,12 @@ WORKLOADS = {
 W = dict(WORKLOADS["cfg2"], name="cfg2")
 
 
-def set_workload(name, grid=None):
+PROPAGATORS = {"fft": 1, "cn": 3}   # WF_2ND_ORDER_FFT, WF_2ND_ORDER_CN
+
+
+def set_workload(name, grid=None, propagator="fft"):
     global W
-    W = dict(WORKLOADS[name], name=name)
+    W = dict(WORKLOADS[name], name=name, propagator=PROPAGATORS[propagator])
     if grid:
         W["n"] = grid if isinstance(grid, int) or len(grid) != 1 else grid[0]
 
@@ -215,7 +218,8 @@ class Setup:
     def __init__(self, G, prec, psi0, vext0, norm):
         G.set_precision(prec)
         step, shp = W["step"], shape()
-        self.w, self.wp = G.Wf(shp, step), G.Wf(shp, step)
+        self.w = G.Wf(shp, step, propagator=W["propagator"])
+        self.wp = G.Wf(shp, step, propagator=W["propagator"])
         lg = W["lg"] / AUTOANG if W["lg"] else None
         self.ot = G.OT(W["model"], self.w, lg_bohr=lg)
         self.w.set(psi0)
@@ -463,7 +467,8 @@ def model_name():
 def workload_name():
     nx, ny, nz = shape()
     g = "%d^3" % nx if nx == ny == nz else "%dx%dx%d" % (nx, ny, nz)
-    return "%s: %s, %s, step %g bohr" % (W["name"], W["what"], g, W["step"])
+    cn = ", Crank-Nicolson kinetic step" if W["propagator"] == PROPAGATORS["cn"] else ""
+    return "%s: %s%s, %s, step %g bohr" % (W["name"], W["what"], cn, g, W["step"])
 
 
 def l2_note():
@@ -484,14 +489,14 @@ def cpu_baseline(warmup=1, steps=5):
     step = W["step"]
     mass = 4.002602 / o.AUTOAMU
     with Grids(o, shape(), step, mass) as g:
-        w = g.wf(psi0)
+        w = g.wf(psi0, W["propagator"])
         vext = g.rgrid(vext0) if vext0 is not None else None
         # kernels sampled with one sub-point per cell: the step's cost does not
         # depend on the kernel values and full adaptive sampling takes minutes
         lg = W["lg"] / AUTOANG if W["lg"] else 0.0
         otf = g.ot(W["model"], w, min_ns=1, max_ns=1, lg_bohr=lg)
         mu0 = o.lib.orc_bulk_chempot(otf, 0.0)
-        wp, P = g.wf(), g.cgrid()
+        wp, P = g.wf(None, W["propagator"]), g.cgrid()
         if norm is not None:
             o.lib.orc_wf_set_norm(w, norm)
             o.lib.orc_wf_normalize(w)
@@ -542,11 +547,13 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--grid", default="", help="grid size N (cubic) or NXxNYxNZ (default: the workload's)")
     ap.add_argument("--fp32-only", action="store_true", help="skip the FP64 and accuracy phases (profiling runs)")
+    ap.add_argument("--propagator", default="fft", choices=sorted(PROPAGATORS),
+                    help="kinetic step of the wave functions: FFT (default) or Crank-Nicolson")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     grid = tuple(int(v) for v in args.grid.lower().split("x")) if args.grid else None
-    set_workload(args.workload, grid)
+    set_workload(args.workload, grid, args.propagator)
     line = run_reference(args) if args.impl == "reference" else run_gpu(args)
     if line is not None:
         print(json.dumps(finite_or_null(line)))
