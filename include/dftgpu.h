@@ -309,7 +309,8 @@ void grid_wf_absorb_potential(wf *gwf, cgrid *potential, REAL amp, REAL rho0);
  * start-up.  The caller passes device pointers it owns: psi_in and potential
  * (nx*ny*nz interleaved complex values of precision prec, [x][y][z] order) and
  * psi_out (same size; may equal psi_in); one step psi_out = S(V, dt) psi_in on
- * `stream` (NULL = legacy default stream).  Work memory is a static 32 MiB
+ * `stream` (NULL = legacy default stream), with the FFT propagator's kinetic
+ * step and no moving background.  Work memory is a static 32 MiB
  * device array plus twiddle tables, held by every GPU that loads the library
  * until exit: grids up to 2,097,152 points in FP64 or 4,194,304 in FP32;
  * larger ones are rejected with DFTGPU_ERR_SIZE.  All calls share that array
