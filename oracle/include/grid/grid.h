@@ -31,7 +31,13 @@
  *  - propagation (WF_2ND_ORDER_FFT, periodic): one step
  *    S(V,dt) = exp(-i V dt/2) F^-1 exp(-i hbar k^2 dt / 2m) F exp(-i V dt/2),
  *    complex dt allowed; predict: psi_p = S(V,dt) psi, correct:
- *    psi = S(V,dt) psi with the caller's averaged V.
+ *    psi = S(V,dt) psi with the caller's averaged V;
+ *  - WF_2ND_ORDER_CN (periodic): the same S with the kinetic factor replaced
+ *    by Crank-Nicolson on the 3-point finite-difference operator, axis by
+ *    axis, prod_a (1 - i hbar Q_a dt / 4m) / (1 + i hbar Q_a dt / 4m) with
+ *    Q_a = (2 sin((k_a - k0_a) step / 2) / step)^2 (each axis operator is
+ *    diagonal in k); the kinetic energy of such a wave function uses Q_a in
+ *    place of (k_a - k0_a)^2.
  */
 #ifndef ORACLE_GRID_GRID_H
 #define ORACLE_GRID_GRID_H
