@@ -32,7 +32,11 @@ namespace dftgpu {
 namespace {
 
 constexpr size_t NOALLOC_SCRATCH_BYTES = (size_t) 32 << 20;   // spectral scratch, 32 MiB
-constexpr size_t NOALLOC_TW_BYTES = (size_t) 64 << 10;        // 3 tables of <= 1024 complex doubles
+// the z, y and x twiddle tables one after the other, each starting on a
+// 256-byte boundary: nz + ny + nx complex values plus padding, at most
+// 4096 + 32 + 1 (a 1-D grid) or 3 * 1024 (a 3-D grid) complex doubles
+constexpr size_t NOALLOC_TW_BYTES = (size_t) 128 << 10;
+constexpr int TW_ALIGN = 32;   // table offsets in complex values (256 bytes in FP64)
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES + NOALLOC_TW_BYTES];
 
@@ -155,10 +159,17 @@ int propagate_noalloc_t(void *out, const void *in, const void *pot, int nx, int 
   typedef typename cplx_t<T>::type C;
   C *spec = (C *) base;
   C *tw = (C *) (base + NOALLOC_SCRATCH_BYTES);
+  // tables placed by the lengths they hold (a 1-D grid's z line is up to 4096 long)
+  const size_t oy = (size_t) (nz + TW_ALIGN - 1) / TW_ALIGN * TW_ALIGN;
+  const size_t ox = oy + (size_t) (ny + TW_ALIGN - 1) / TW_ALIGN * TW_ALIGN;
+  if ((ox + nx) * sizeof(C) > NOALLOC_TW_BYTES) {
+    set_error(DFTGPU_ERR_SIZE, "noalloc: twiddle tables for %dx%dx%d exceed %zu bytes", nx, ny, nz, NOALLOC_TW_BYTES);
+    return DFTGPU_ERR_SIZE;
+  }
   FftPlan<T> pz, py, px;
   DFT_TRY(make_plan<T>(nz, tw, s, &pz));
-  DFT_TRY(make_plan<T>(ny, tw + 1024, s, &py));
-  DFT_TRY(make_plan<T>(nx, tw + 2048, s, &px));
+  DFT_TRY(make_plan<T>(ny, tw + oy, s, &py));
+  DFT_TRY(make_plan<T>(nx, tw + ox, s, &px));
   const T hr = (T) (0.5 * dr), hi = (T) (0.5 * di);
   HalfStepLoad<T> ld{(const C *) in, (const C *) pot, ny, nz, hr, hi};
   SpecStoreZ<T> sz{spec, nx, ny};

@@ -31,8 +31,10 @@ def _psi_and_potential(shape, step, seed):
 
 
 @pytest.mark.parametrize("prec", [0, 1], ids=["fp64", "fp32"])
-@pytest.mark.parametrize("shape", [(32, 48, 40), (64, 64, 128)])
+@pytest.mark.parametrize("shape", [(32, 48, 40), (64, 64, 128), (1, 1, 2048)])
 def test_noalloc_propagate_matches_allocating_entry_point(prec, shape):
+    """(1, 1, 2048) is a 1-D grid whose z twiddle table is longer than 1024
+    entries: the y and x tables must start after it, not inside it."""
     import torch
     import libdft_gb300 as G
 
