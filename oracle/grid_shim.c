@@ -17,17 +17,29 @@
 #include "grid/au.h"
 
 /* ------------------------------------------------------------------ */
-/* 1-D mixed-radix Stockham FFT                                         */
+/* 1-D mixed-radix Stockham FFT, batched over lines                     */
 /* ------------------------------------------------------------------ */
+/*
+ * A batch holds V lines of length n in split form, re[i * V + v] and
+ * im[i * V + v] for element i of line v, so each butterfly applies one set of
+ * twiddles to V contiguous values.  Stage s has radix r and p = the product
+ * of the earlier radices: it reads elements i + q n / r (q < r), multiplies
+ * element q by exp(-+2 pi i q k / (p r)) with k = i mod p, takes the r-point
+ * DFT and writes element (i - k) r + k + q p of the other buffer (Stockham
+ * autosort: no bit reversal).  The stage twiddles are copied from the
+ * length-n table, whose angles are reduced to [-pi, pi] before cos / sin.
+ */
 
 #define MAXFAC 48
 #define MAXRADIX 64
+#define FFT_BATCH 8   /* lines per batch */
 
 typedef struct {
   INT n;
   int nf;
   int fac[MAXFAC];
-  REAL complex *tw;           /* tw[t] = exp(-2 pi i t / n) */
+  REAL complex *tw;        /* tw[t] = exp(-2 pi i t / n) */
+  REAL *stw[MAXFAC];       /* stage s: (re, im) of tw[q k n / (p r)] at [2 (k (r - 1) + q - 1)], k < p, 1 <= q < r */
 } fft_plan;
 
 #define NPLANS 512   /* distinct lengths in one process (a test session visits many) */
@@ -54,6 +66,20 @@ static void plan_init(fft_plan *p, INT n) {
     REAL a = -2.0 * M_PI * (REAL) tt / (REAL) n;
     p->tw[t] = cos(a) + I * sin(a);
   }
+  INT pp = 1;
+  for (int s = 0; s < p->nf; s++) {
+    const int r = p->fac[s];
+    const INT twstep = n / (pp * r);
+    REAL *t = (REAL *) malloc(sizeof(REAL) * 2 * (size_t) (pp * (r - 1)));
+    for (INT k = 0; k < pp; k++)
+      for (int q = 1; q < r; q++) {
+        const REAL complex w = p->tw[(q * k * twstep) % n];
+        t[2 * (k * (r - 1) + q - 1)] = creal(w);
+        t[2 * (k * (r - 1) + q - 1) + 1] = cimag(w);
+      }
+    p->stw[s] = t;
+    pp *= r;
+  }
 }
 
 static const fft_plan *get_plan(INT n) {
@@ -72,129 +98,226 @@ static const fft_plan *get_plan(INT n) {
   return res;
 }
 
-/* In-place small DFT of length r with sign = -1 (forward) or +1 (inverse). */
-static void small_dft(REAL complex *u, int r, int sign, const fft_plan *pl) {
-  REAL complex a, b, c, d, e;
-  REAL s = (REAL) sign;
-  switch (r) {
-  case 2:
-    a = u[0]; b = u[1];
-    u[0] = a + b; u[1] = a - b;
-    return;
-  case 3: {
-    const REAL s3 = 0.86602540378443864676;
-    a = u[0]; b = u[1]; c = u[2];
-    REAL complex m = a - 0.5 * (b + c);
-    REAL complex n = s3 * (b - c);
-    u[0] = a + b + c;
-    u[1] = m + I * s * n;
-    u[2] = m - I * s * n;
-    return;
-  }
-  case 4: {
-    a = u[0]; b = u[1]; c = u[2]; d = u[3];
-    REAL complex t0 = a + c, t1 = a - c, t2 = b + d, t3 = b - d;
-    u[0] = t0 + t2;
-    u[1] = t1 + I * s * t3;
-    u[2] = t0 - t2;
-    u[3] = t1 - I * s * t3;
-    return;
-  }
-  case 5: {
-    const REAL c1 = 0.30901699437494742410, c2 = -0.80901699437494742410;
-    const REAL s1 = 0.95105651629515357212, s2 = 0.58778525229247312917;
-    a = u[0]; b = u[1]; c = u[2]; d = u[3]; e = u[4];
-    REAL complex t1 = b + e, t2 = c + d, t3 = b - e, t4 = c - d;
-    REAL complex m1 = a + c1 * t1 + c2 * t2;
-    REAL complex m2 = a + c2 * t1 + c1 * t2;
-    REAL complex n1 = s1 * t3 + s2 * t4;
-    REAL complex n2 = s2 * t3 - s1 * t4;
-    u[0] = a + t1 + t2;
-    u[1] = m1 + I * s * n1;
-    u[4] = m1 - I * s * n1;
-    u[2] = m2 + I * s * n2;
-    u[3] = m2 - I * s * n2;
-    return;
-  }
-  default: {
-    REAL complex v[MAXRADIX];
-    INT step = pl->n / r;
-    for (int q = 0; q < r; q++) {
-      REAL complex acc = 0.0;
-      for (int m = 0; m < r; m++) {
-        REAL complex w = pl->tw[((INT) ((q * m) % r)) * step];
-        if (sign > 0) w = conj(w);
-        acc += u[m] * w;
-      }
-      v[q] = acc;
-    }
-    for (int q = 0; q < r; q++) u[q] = v[q];
-    return;
-  }
+/* One stage's butterflies at input index i, output index j, for the V lines
+ * of a batch.  tw: the stage twiddles of this k; sg = sign (-1 forward, +1
+ * inverse): the inverse uses the conjugate twiddles. */
+static void bfly2(const REAL *ir, const REAL *ii, REAL *orr, REAL *oi, INT i, INT j, INT nr, INT p, int V,
+                  const REAL *tw, REAL sg) {
+  const REAL wr = tw[0], wi = -sg * tw[1];
+  const REAL *ar = ir + i * V, *ai = ii + i * V, *br = ir + (i + nr) * V, *bi = ii + (i + nr) * V;
+  REAL *o0r = orr + j * V, *o0i = oi + j * V, *o1r = orr + (j + p) * V, *o1i = oi + (j + p) * V;
+  for (int v = 0; v < V; v++) {
+    const REAL xr = br[v] * wr - bi[v] * wi, xi = br[v] * wi + bi[v] * wr;
+    o0r[v] = ar[v] + xr; o0i[v] = ai[v] + xi;
+    o1r[v] = ar[v] - xr; o1i[v] = ai[v] - xi;
   }
 }
 
-/* x: n contiguous values; w: n scratch. sign -1 forward, +1 inverse. */
-static void fft_contig(const fft_plan *pl, REAL complex *x, REAL complex *w, int sign) {
-  INT n = pl->n, p = 1;
-  REAL complex *in = x, *out = w, *tmp;
+static void bfly3(const REAL *ir, const REAL *ii, REAL *orr, REAL *oi, INT i, INT j, INT nr, INT p, int V,
+                  const REAL *tw, REAL sg) {
+  const REAL s3 = 0.86602540378443864676;
+  const REAL w1r = tw[0], w1i = -sg * tw[1], w2r = tw[2], w2i = -sg * tw[3];
+  const REAL *ar = ir + i * V, *ai = ii + i * V, *br = ir + (i + nr) * V, *bi = ii + (i + nr) * V;
+  const REAL *cr = ir + (i + 2 * nr) * V, *ci = ii + (i + 2 * nr) * V;
+  REAL *o0r = orr + j * V, *o0i = oi + j * V, *o1r = orr + (j + p) * V, *o1i = oi + (j + p) * V;
+  REAL *o2r = orr + (j + 2 * p) * V, *o2i = oi + (j + 2 * p) * V;
+  for (int v = 0; v < V; v++) {
+    const REAL xr = br[v] * w1r - bi[v] * w1i, xi = br[v] * w1i + bi[v] * w1r;
+    const REAL yr = cr[v] * w2r - ci[v] * w2i, yi = cr[v] * w2i + ci[v] * w2r;
+    const REAL mr = ar[v] - 0.5 * (xr + yr), mi = ai[v] - 0.5 * (xi + yi);
+    const REAL nr_ = s3 * (xr - yr), ni = s3 * (xi - yi);
+    o0r[v] = ar[v] + xr + yr; o0i[v] = ai[v] + xi + yi;
+    o1r[v] = mr - sg * ni; o1i[v] = mi + sg * nr_;     /* m + i sg n */
+    o2r[v] = mr + sg * ni; o2i[v] = mi - sg * nr_;     /* m - i sg n */
+  }
+}
+
+static void bfly4(const REAL *ir, const REAL *ii, REAL *orr, REAL *oi, INT i, INT j, INT nr, INT p, int V,
+                  const REAL *tw, REAL sg) {
+  const REAL w1r = tw[0], w1i = -sg * tw[1], w2r = tw[2], w2i = -sg * tw[3], w3r = tw[4], w3i = -sg * tw[5];
+  const REAL *ar = ir + i * V, *ai = ii + i * V, *br = ir + (i + nr) * V, *bi = ii + (i + nr) * V;
+  const REAL *cr = ir + (i + 2 * nr) * V, *ci = ii + (i + 2 * nr) * V;
+  const REAL *dr = ir + (i + 3 * nr) * V, *di = ii + (i + 3 * nr) * V;
+  REAL *o0r = orr + j * V, *o0i = oi + j * V, *o1r = orr + (j + p) * V, *o1i = oi + (j + p) * V;
+  REAL *o2r = orr + (j + 2 * p) * V, *o2i = oi + (j + 2 * p) * V, *o3r = orr + (j + 3 * p) * V, *o3i = oi + (j + 3 * p) * V;
+  for (int v = 0; v < V; v++) {
+    const REAL xr = br[v] * w1r - bi[v] * w1i, xi = br[v] * w1i + bi[v] * w1r;
+    const REAL yr = cr[v] * w2r - ci[v] * w2i, yi = cr[v] * w2i + ci[v] * w2r;
+    const REAL zr = dr[v] * w3r - di[v] * w3i, zi = dr[v] * w3i + di[v] * w3r;
+    const REAL t0r = ar[v] + yr, t0i = ai[v] + yi, t1r = ar[v] - yr, t1i = ai[v] - yi;
+    const REAL t2r = xr + zr, t2i = xi + zi, t3r = xr - zr, t3i = xi - zi;
+    o0r[v] = t0r + t2r; o0i[v] = t0i + t2i;
+    o1r[v] = t1r - sg * t3i; o1i[v] = t1i + sg * t3r;  /* t1 + i sg t3 */
+    o2r[v] = t0r - t2r; o2i[v] = t0i - t2i;
+    o3r[v] = t1r + sg * t3i; o3i[v] = t1i - sg * t3r;  /* t1 - i sg t3 */
+  }
+}
+
+static void bfly5(const REAL *ir, const REAL *ii, REAL *orr, REAL *oi, INT i, INT j, INT nr, INT p, int V,
+                  const REAL *tw, REAL sg) {
+  const REAL c1 = 0.30901699437494742410, c2 = -0.80901699437494742410;
+  const REAL s1 = 0.95105651629515357212, s2 = 0.58778525229247312917;
+  REAL wr[4], wi[4];
+  for (int q = 0; q < 4; q++) { wr[q] = tw[2 * q]; wi[q] = -sg * tw[2 * q + 1]; }
+  const REAL *ar = ir + i * V, *ai = ii + i * V;
+  REAL *o0r = orr + j * V, *o0i = oi + j * V, *o1r = orr + (j + p) * V, *o1i = oi + (j + p) * V;
+  REAL *o2r = orr + (j + 2 * p) * V, *o2i = oi + (j + 2 * p) * V, *o3r = orr + (j + 3 * p) * V, *o3i = oi + (j + 3 * p) * V;
+  REAL *o4r = orr + (j + 4 * p) * V, *o4i = oi + (j + 4 * p) * V;
+  for (int v = 0; v < V; v++) {
+    REAL ur[4], ui[4];
+    for (int q = 0; q < 4; q++) {
+      const REAL xr = ir[(i + (q + 1) * nr) * V + v], xi = ii[(i + (q + 1) * nr) * V + v];
+      ur[q] = xr * wr[q] - xi * wi[q];
+      ui[q] = xr * wi[q] + xi * wr[q];
+    }
+    const REAL t1r = ur[0] + ur[3], t1i = ui[0] + ui[3], t2r = ur[1] + ur[2], t2i = ui[1] + ui[2];
+    const REAL t3r = ur[0] - ur[3], t3i = ui[0] - ui[3], t4r = ur[1] - ur[2], t4i = ui[1] - ui[2];
+    const REAL m1r = ar[v] + c1 * t1r + c2 * t2r, m1i = ai[v] + c1 * t1i + c2 * t2i;
+    const REAL m2r = ar[v] + c2 * t1r + c1 * t2r, m2i = ai[v] + c2 * t1i + c1 * t2i;
+    const REAL n1r = s1 * t3r + s2 * t4r, n1i = s1 * t3i + s2 * t4i;
+    const REAL n2r = s2 * t3r - s1 * t4r, n2i = s2 * t3i - s1 * t4i;
+    o0r[v] = ar[v] + t1r + t2r; o0i[v] = ai[v] + t1i + t2i;
+    o1r[v] = m1r - sg * n1i; o1i[v] = m1i + sg * n1r;  /* m1 + i sg n1 */
+    o4r[v] = m1r + sg * n1i; o4i[v] = m1i - sg * n1r;
+    o2r[v] = m2r - sg * n2i; o2i[v] = m2i + sg * n2r;  /* m2 + i sg n2 */
+    o3r[v] = m2r + sg * n2i; o3i[v] = m2i - sg * n2r;
+  }
+}
+
+/* any radix r <= MAXRADIX: the r-point DFT as a sum, roots of unity from the
+ * length-n table */
+static void bfly_any(const fft_plan *pl, int r, const REAL *ir, const REAL *ii, REAL *orr, REAL *oi, INT i, INT j,
+                     INT nr, INT p, int V, const REAL *tw, REAL sg) {
+  const INT step = pl->n / r;
+  for (int v = 0; v < V; v++) {
+    REAL ur[MAXRADIX], ui[MAXRADIX];
+    ur[0] = ir[i * V + v]; ui[0] = ii[i * V + v];
+    for (int q = 1; q < r; q++) {
+      const REAL xr = ir[(i + q * nr) * V + v], xi = ii[(i + q * nr) * V + v];
+      const REAL wr = tw[2 * (q - 1)], wi = -sg * tw[2 * (q - 1) + 1];
+      ur[q] = xr * wr - xi * wi;
+      ui[q] = xr * wi + xi * wr;
+    }
+    for (int q = 0; q < r; q++) {
+      REAL accr = 0.0, acci = 0.0;
+      for (int m = 0; m < r; m++) {
+        const REAL complex w = pl->tw[((INT) ((q * m) % r)) * step];
+        const REAL wr = creal(w), wi = -sg * cimag(w);
+        accr += ur[m] * wr - ui[m] * wi;
+        acci += ur[m] * wi + ui[m] * wr;
+      }
+      orr[(j + q * p) * V + v] = accr;
+      oi[(j + q * p) * V + v] = acci;
+    }
+  }
+}
+
+/* V lines in (xr, xi), scratch (wr, wi) of the same size; the result ends in
+ * (xr, xi).  sign -1 forward, +1 inverse (unnormalised). */
+static void fft_batch(const fft_plan *pl, REAL *xr, REAL *xi, REAL *wr, REAL *wi, int V, int sign) {
+  const INT n = pl->n;
+  const REAL sg = (REAL) sign;
+  REAL *ir = xr, *ii = xi, *orr = wr, *oi = wi, *t;
+  INT p = 1;
   if (n == 1) return;
   for (int s = 0; s < pl->nf; s++) {
-    int r = pl->fac[s];
-    INT nr = n / r, twstep = n / (p * r);
-    for (INT i = 0; i < nr; i++) {
-      INT k = i % p;
-      REAL complex u[MAXRADIX];
-      for (int q = 0; q < r; q++) {
-        REAL complex v = in[i + q * nr];
-        if (q && k) {
-          REAL complex t = pl->tw[(q * k * twstep) % n];
-          if (sign > 0) t = conj(t);
-          v *= t;
+    const int r = pl->fac[s];
+    const INT nr = n / r;
+    const REAL *st = pl->stw[s];
+    for (INT m = 0; m < nr / p; m++)
+      for (INT k = 0; k < p; k++) {
+        const INT i = m * p + k, j = m * p * r + k;
+        const REAL *tw = st + 2 * k * (r - 1);
+        switch (r) {
+        case 2: bfly2(ir, ii, orr, oi, i, j, nr, p, V, tw, sg); break;
+        case 3: bfly3(ir, ii, orr, oi, i, j, nr, p, V, tw, sg); break;
+        case 4: bfly4(ir, ii, orr, oi, i, j, nr, p, V, tw, sg); break;
+        case 5: bfly5(ir, ii, orr, oi, i, j, nr, p, V, tw, sg); break;
+        default: bfly_any(pl, r, ir, ii, orr, oi, i, j, nr, p, V, tw, sg); break;
         }
-        u[q] = v;
       }
-      small_dft(u, r, sign, pl);
-      INT j = (i - k) * r + k;
-      for (int q = 0; q < r; q++) out[j + q * p] = u[q];
-    }
     p *= r;
-    tmp = in; in = out; out = tmp;
+    t = ir; ir = orr; orr = t;
+    t = ii; ii = oi; oi = t;
   }
-  if (in != x) memcpy(x, in, sizeof(REAL complex) * (size_t) n);
+  if (ir != xr) {
+    memcpy(xr, ir, sizeof(REAL) * (size_t) (n * V));
+    memcpy(xi, ii, sizeof(REAL) * (size_t) (n * V));
+  }
+}
+
+/* work space of one thread for batches of V lines of length n */
+typedef struct { REAL *xr, *xi, *wr, *wi; } fft_work;
+
+static fft_work work_alloc(INT n, int V) {
+  fft_work w;
+  w.xr = (REAL *) malloc(sizeof(REAL) * 4 * (size_t) (n * V));
+  w.xi = w.xr + n * V;
+  w.wr = w.xi + n * V;
+  w.wi = w.wr + n * V;
+  return w;
 }
 
 void oracle_fft1d(REAL complex *data, INT n, INT stride, int sign) {
   const fft_plan *pl = get_plan(n);
-  REAL complex *buf = malloc(sizeof(REAL complex) * 2 * (size_t) n);
-  for (INT i = 0; i < n; i++) buf[i] = data[i * stride];
-  fft_contig(pl, buf, buf + n, sign);
-  for (INT i = 0; i < n; i++) data[i * stride] = buf[i];
-  free(buf);
+  fft_work w = work_alloc(n, 1);
+  for (INT i = 0; i < n; i++) { w.xr[i] = creal(data[i * stride]); w.xi[i] = cimag(data[i * stride]); }
+  fft_batch(pl, w.xr, w.xi, w.wr, w.wi, 1, sign);
+  for (INT i = 0; i < n; i++) data[i * stride] = w.xr[i] + I * w.xi[i];
+  free(w.xr);
 }
 
-/* Transform along one axis of a [n0][n1][n2] complex array. */
+/* Transform along one axis of a [n0][n1][n2] complex array, FFT_BATCH lines
+ * at a time: along x and y the batch is FFT_BATCH neighbouring lines (adjacent
+ * in z, so each element index reads one contiguous run); along z it is
+ * FFT_BATCH consecutive rows. */
 static void fft_axis(REAL complex *data, INT n0, INT n1, INT n2, int axis, int sign) {
-  INT n = (axis == 0) ? n0 : (axis == 1) ? n1 : n2;
+  const INT n = (axis == 0) ? n0 : (axis == 1) ? n1 : n2;
   if (n == 1) return;
   const fft_plan *pl = get_plan(n);
-  INT stride = (axis == 0) ? n1 * n2 : (axis == 1) ? n2 : 1;
-  INT nlines = n0 * n1 * n2 / n;
+  REAL *d = (REAL *) data;
+  const INT stride = (axis == 0) ? n1 * n2 : (axis == 1) ? n2 : 1;
+  /* lines come in runs of `inner` neighbours (consecutive line starts one
+   * complex value apart for x / y, one row apart for z), `outer` runs */
+  const INT outer = (axis == 1) ? n0 : 1;
+  const INT inner = (axis == 0) ? n1 * n2 : (axis == 1) ? n2 : n0 * n1;
+  const INT nbat = (inner + FFT_BATCH - 1) / FFT_BATCH;
 #pragma omp parallel
   {
-    REAL complex *buf = malloc(sizeof(REAL complex) * 2 * (size_t) n);
+    fft_work w = work_alloc(n, FFT_BATCH);
 #pragma omp for schedule(static)
-    for (INT l = 0; l < nlines; l++) {
-      INT base;
-      if (axis == 2) base = l * n2;
-      else if (axis == 1) base = (l / n2) * n1 * n2 + (l % n2);
-      else base = l;
-      REAL complex *p = data + base;
-      for (INT i = 0; i < n; i++) buf[i] = p[i * stride];
-      fft_contig(pl, buf, buf + n, sign);
-      for (INT i = 0; i < n; i++) p[i * stride] = buf[i];
+    for (INT b = 0; b < outer * nbat; b++) {
+      const INT o = b / nbat, c0 = (b % nbat) * FFT_BATCH;
+      const int V = (int) ((inner - c0 < FFT_BATCH) ? inner - c0 : FFT_BATCH);
+      if (axis == 2) {
+        for (int v = 0; v < V; v++) {
+          const REAL *row = d + 2 * (c0 + v) * n2;
+          for (INT i = 0; i < n; i++) { w.xr[i * V + v] = row[2 * i]; w.xi[i * V + v] = row[2 * i + 1]; }
+        }
+      } else {
+        const REAL *base = d + 2 * (o * n1 * n2 + c0);
+        for (INT i = 0; i < n; i++)
+          for (int v = 0; v < V; v++) {
+            w.xr[i * V + v] = base[2 * (i * stride + v)];
+            w.xi[i * V + v] = base[2 * (i * stride + v) + 1];
+          }
+      }
+      fft_batch(pl, w.xr, w.xi, w.wr, w.wi, V, sign);
+      if (axis == 2) {
+        for (int v = 0; v < V; v++) {
+          REAL *row = d + 2 * (c0 + v) * n2;
+          for (INT i = 0; i < n; i++) { row[2 * i] = w.xr[i * V + v]; row[2 * i + 1] = w.xi[i * V + v]; }
+        }
+      } else {
+        REAL *base = d + 2 * (o * n1 * n2 + c0);
+        for (INT i = 0; i < n; i++)
+          for (int v = 0; v < V; v++) {
+            base[2 * (i * stride + v)] = w.xr[i * V + v];
+            base[2 * (i * stride + v) + 1] = w.xi[i * V + v];
+          }
+      }
     }
-    free(buf);
+    free(w.xr);
   }
 }
 
@@ -476,45 +599,111 @@ void rgrid_gradient_y(rgrid *s, rgrid *d) { if (s->ny == 1) rgrid_zero(d); else 
 void rgrid_gradient_z(rgrid *s, rgrid *d) { if (s->nz == 1) rgrid_zero(d); else rgrid_fd(s, d, 2); }
 void rgrid_gradient(rgrid *s, rgrid *dx, rgrid *dy, rgrid *dz) { rgrid_gradient_x(s, dx); rgrid_gradient_y(s, dy); rgrid_gradient_z(s, dz); }
 
-/* r2c along z in place, then c2c along y and x on the half spectrum. */
+/* r2c along z in place, then c2c along y and x on the half spectrum.  An even
+ * nz = 2h takes a length-h complex transform of z[m] = x[2m] + i x[2m+1]:
+ * with Z its transform, E[k] = (Z[k] + conj Z[h-k]) / 2 and
+ * O[k] = (Z[k] - conj Z[h-k]) / (2i) are the transforms of the even and odd
+ * samples, and X[k] = E[k] + w^k O[k], w = exp(-2 pi i / nz), for k <= h
+ * (X[0] and X[h] real).  An odd nz is transformed as a complex line. */
 void rgrid_fft(rgrid *g) {
-  INT nx = g->nx, ny = g->ny, nz = g->nz, nzh = nz / 2 + 1;
-  const fft_plan *pl = get_plan(nz);
+  const INT nx = g->nx, ny = g->ny, nz = g->nz, nzh = nz / 2 + 1, rows = nx * ny;
+  const int half = !(nz & 1);
+  const INT nl = half ? nz / 2 : nz;
+  const fft_plan *pl = get_plan(nl);
+  const fft_plan *pw = get_plan(nz);   /* w^k = pw->tw[k] */
+  const INT nbat = (rows + FFT_BATCH - 1) / FFT_BATCH;
 #pragma omp parallel
   {
-    REAL complex *buf = malloc(sizeof(REAL complex) * 2 * (size_t) nz);
+    fft_work w = work_alloc(nl, FFT_BATCH);
 #pragma omp for schedule(static)
-    for (INT ij = 0; ij < nx * ny; ij++) {
-      REAL *row = g->value + ij * g->nz2;
-      for (INT k = 0; k < nz; k++) buf[k] = row[k];
-      fft_contig(pl, buf, buf + nz, -1);
-      REAL complex *crow = (REAL complex *) row;
-      for (INT k = 0; k < nzh; k++) crow[k] = buf[k];
+    for (INT b = 0; b < nbat; b++) {
+      const INT r0 = b * FFT_BATCH;
+      const int V = (int) ((rows - r0 < FFT_BATCH) ? rows - r0 : FFT_BATCH);
+      for (int v = 0; v < V; v++) {
+        const REAL *row = g->value + (r0 + v) * g->nz2;
+        if (half)
+          for (INT m = 0; m < nl; m++) { w.xr[m * V + v] = row[2 * m]; w.xi[m * V + v] = row[2 * m + 1]; }
+        else
+          for (INT m = 0; m < nl; m++) { w.xr[m * V + v] = row[m]; w.xi[m * V + v] = 0.0; }
+      }
+      fft_batch(pl, w.xr, w.xi, w.wr, w.wi, V, -1);
+      for (int v = 0; v < V; v++) {
+        REAL *row = g->value + (r0 + v) * g->nz2;
+        if (!half) {
+          for (INT k = 0; k < nzh; k++) { row[2 * k] = w.xr[k * V + v]; row[2 * k + 1] = w.xi[k * V + v]; }
+          continue;
+        }
+        const INT h = nl;
+        const REAL z0r = w.xr[v], z0i = w.xi[v];
+        for (INT k = 1; k < h; k++) {
+          const REAL zr = w.xr[k * V + v], zi = w.xi[k * V + v];
+          const REAL cr = w.xr[(h - k) * V + v], ci = -w.xi[(h - k) * V + v];   /* conj Z[h-k] */
+          const REAL er = 0.5 * (zr + cr), ei = 0.5 * (zi + ci);
+          const REAL or_ = 0.5 * (zi - ci), oi = -0.5 * (zr - cr);
+          const REAL wr = creal(pw->tw[k]), wi = cimag(pw->tw[k]);
+          row[2 * k] = er + (wr * or_ - wi * oi);
+          row[2 * k + 1] = ei + (wr * oi + wi * or_);
+        }
+        row[0] = z0r + z0i; row[1] = 0.0;
+        row[2 * h] = z0r - z0i; row[2 * h + 1] = 0.0;
+      }
     }
-    free(buf);
+    free(w.xr);
   }
   fft_axis((REAL complex *) g->value, nx, ny, nzh, 1, -1);
   fft_axis((REAL complex *) g->value, nx, ny, nzh, 0, -1);
 }
 
+/* Inverse of rgrid_fft (unnormalised): c2c along x and y, then c2r along z.
+ * An even nz = 2h forms Z[k] = A[k] + i B[k] (k < h) with
+ * A[k] = X[k] + conj X[h-k] and B[k] = (X[k] - conj X[h-k]) conj(w^k), whose
+ * length-h inverse is nz (x[2m] + i x[2m+1]).  The imaginary parts of X[0]
+ * and X[h], which a real field's spectrum does not have, are dropped. */
 void rgrid_inverse_fft(rgrid *g) {
-  INT nx = g->nx, ny = g->ny, nz = g->nz, nzh = nz / 2 + 1;
+  const INT nx = g->nx, ny = g->ny, nz = g->nz, nzh = nz / 2 + 1, rows = nx * ny;
   fft_axis((REAL complex *) g->value, nx, ny, nzh, 0, +1);
   fft_axis((REAL complex *) g->value, nx, ny, nzh, 1, +1);
-  const fft_plan *pl = get_plan(nz);
+  const int half = !(nz & 1);
+  const INT nl = half ? nz / 2 : nz;
+  const fft_plan *pl = get_plan(nl);
+  const fft_plan *pw = get_plan(nz);
+  const INT nbat = (rows + FFT_BATCH - 1) / FFT_BATCH;
 #pragma omp parallel
   {
-    REAL complex *buf = malloc(sizeof(REAL complex) * 2 * (size_t) nz);
+    fft_work w = work_alloc(nl, FFT_BATCH);
 #pragma omp for schedule(static)
-    for (INT ij = 0; ij < nx * ny; ij++) {
-      REAL complex *crow = (REAL complex *) (g->value + ij * g->nz2);
-      for (INT k = 0; k < nzh; k++) buf[k] = crow[k];
-      for (INT k = nzh; k < nz; k++) buf[k] = conj(buf[nz - k]);
-      fft_contig(pl, buf, buf + nz, +1);
-      REAL *row = (REAL *) crow;
-      for (INT k = 0; k < nz; k++) row[k] = creal(buf[k]);
+    for (INT b = 0; b < nbat; b++) {
+      const INT r0 = b * FFT_BATCH;
+      const int V = (int) ((rows - r0 < FFT_BATCH) ? rows - r0 : FFT_BATCH);
+      for (int v = 0; v < V; v++) {
+        const REAL *row = g->value + (r0 + v) * g->nz2;
+        if (!half) {
+          for (INT k = 0; k < nzh; k++) { w.xr[k * V + v] = row[2 * k]; w.xi[k * V + v] = row[2 * k + 1]; }
+          for (INT k = nzh; k < nz; k++) { w.xr[k * V + v] = row[2 * (nz - k)]; w.xi[k * V + v] = -row[2 * (nz - k) + 1]; }
+          continue;
+        }
+        const INT h = nl;
+        for (INT k = 0; k < h; k++) {
+          const REAL xr = row[2 * k], xi = k ? row[2 * k + 1] : 0.0;
+          const REAL cr = row[2 * (h - k)], ci = k ? -row[2 * (h - k) + 1] : 0.0;   /* conj X[h-k] */
+          const REAL ar = xr + cr, ai = xi + ci;
+          const REAL dr = xr - cr, di = xi - ci;
+          const REAL wr = creal(pw->tw[k]), wi = -cimag(pw->tw[k]);                 /* conj w^k */
+          const REAL br = dr * wr - di * wi, bi = dr * wi + di * wr;
+          w.xr[k * V + v] = ar - bi;
+          w.xi[k * V + v] = ai + br;
+        }
+      }
+      fft_batch(pl, w.xr, w.xi, w.wr, w.wi, V, +1);
+      for (int v = 0; v < V; v++) {
+        REAL *row = g->value + (r0 + v) * g->nz2;
+        if (half)
+          for (INT m = 0; m < nl; m++) { row[2 * m] = w.xr[m * V + v]; row[2 * m + 1] = w.xi[m * V + v]; }
+        else
+          for (INT m = 0; m < nl; m++) row[m] = w.xr[m * V + v];
+      }
     }
-    free(buf);
+    free(w.xr);
   }
 }
 

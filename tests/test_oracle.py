@@ -108,17 +108,30 @@ def test_oracle_fft_vs_numpy(port, n):
     assert relerr(port.fft1d(x, +1), np.fft.ifft(x) * n) < 1e-13
 
 
-def test_oracle_3d_fft_vs_numpy(port):
-    shape = (12, 10, 8)
+# even and odd z (half-length packing / complex line), odd x and y, row counts
+# that are not a multiple of the transform batch, a radix-7 factor, 1-D grids
+FFT_SHAPES = [(12, 10, 8), (9, 15, 10), (5, 7, 9), (3, 4, 14), (7, 6, 2), (1, 1, 64), (1, 1, 45), (16, 16, 16)]
+
+
+@pytest.mark.parametrize("shape", FFT_SHAPES, ids=lambda s: "x".join(map(str, s)))
+def test_oracle_3d_fft_vs_numpy(port, shape):
+    import ctypes
     rng = np.random.default_rng(3)
     f = rng.standard_normal(shape)
+    c = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
     with Grids(port, shape, 1.0, 1.0) as g:
         r = g.rgrid(f)
         port.lib.orc_rgrid_fft(r)
-        spec = np.empty((12, 10, 5), dtype=np.complex128)
-        port.lib.orc_rgrid_get_spectrum(r, spec.view(np.float64).ctypes.data_as(
-            __import__("ctypes").POINTER(__import__("ctypes").c_double)))
+        spec = np.empty(shape[:2] + (shape[2] // 2 + 1,), dtype=np.complex128)
+        port.lib.orc_rgrid_get_spectrum(r, spec.view(np.float64).ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
         assert relerr(spec, np.fft.rfftn(f)) < 1e-13
+        port.lib.orc_rgrid_inverse_fft_norm(r)
+        assert relerr(g.get_r(r), f) < 1e-13
+        cg = g.cgrid(c)
+        port.lib.orc_cgrid_fft(cg)
+        assert relerr(g.get_c(cg), np.fft.fftn(c)) < 1e-13
+        port.lib.orc_cgrid_inverse_fft_norm(cg)
+        assert relerr(g.get_c(cg), c) < 1e-13
 
 
 @pytest.mark.skipif(not ref_available(), reason="reference tree not present")
