@@ -475,22 +475,26 @@ REAL dft_common_vortex_z(void *param, REAL x, REAL y, REAL z);             /* sr
  * (examples/imag_time/imag_time.c:248-250, examples/imag_time/Makefile:16);
  * the .grd layout is this library's own, written out below, because
  * libgrid's is not part of libdft -- files written by libgrid are refused
- * (DFTGPU_ERR_UNSUPPORTED).  Reading requires the grid's shape
- * (DFTGPU_ERR_SIZE otherwise) and sets its values, origin and momentum; an
- * FP32 grid receives the values rounded to FP32.
+ * (DFTGPU_ERR_UNSUPPORTED).  Writers take a base name and add the
+ * extensions; readers take the file's whole name, as libdft's drivers pass it
+ * (argv[1] = "bubble-100.grd", examples/gas-bubble/bubble.c:143; a renamed
+ * copy, "restart.chk", examples/electron/electron.c:163): a name that is an
+ * existing regular file is read as it is, any other as <name>.grd.  Reading
+ * requires the grid's shape (DFTGPU_ERR_SIZE otherwise) and sets its values,
+ * origin and momentum; an FP32 grid receives the values rounded to FP32.
  *   .grd layout, little-endian: char magic[8] = "DFTGPUG1"; int64 kind
  *   (0 real, 1 complex); int64 nx, ny, nz; double step, x0, y0, z0, kx0,
  *   ky0, kz0; then nx*ny*nz doubles (complex: re, im pairs) in [x][y][z]
  *   order. */
 void rgrid_write_grid(char *base, rgrid *grid);            /* examples/imag_time/imag_time.c:248 */
 void cgrid_write_grid(char *base, cgrid *grid);            /* examples/imag_time/imag_time.c:250 */
-void rgrid_read_grid(rgrid *grid, char *base);             /* examples/added_mass_viscosity/added_mass2.c:368 */
-void cgrid_read_grid(cgrid *grid, char *base);             /* examples/added_mass/added_mass.c:111 */
+void rgrid_read_grid(rgrid *grid, char *file);             /* examples/added_mass_viscosity/added_mass2.c:368 */
+void cgrid_read_grid(cgrid *grid, char *file);             /* examples/added_mass/added_mass.c:111 */
 /* The same on host buffers (nx*ny*nz FP64 values, complex interleaved):
  * meta = { step, x0, y0, z0, kx0, ky0, kz0 }.  Return a DFTGPU_* code. */
 int dftgpu_grid_file_write(const char *base, int is_complex, INT nx, INT ny, INT nz, const double *meta,
                            const double *values);
-int dftgpu_grid_file_read(const char *base, int is_complex, INT nx, INT ny, INT nz, double *meta, double *values);
+int dftgpu_grid_file_read(const char *name, int is_complex, INT nx, INT ny, INT nz, double *meta, double *values);
 /* one value of a complex grid (cgrid_value_at_index; indices wrap periodically) */
 int cgrid_value_at_index_re_im(cgrid *grid, INT i, INT j, INT k, REAL *re, REAL *im);
 

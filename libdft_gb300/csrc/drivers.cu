@@ -8,6 +8,7 @@
 #include <stdint.h>
 #include <stdio.h>
 #include <string.h>
+#include <sys/stat.h>
 
 #include <string>
 #include <vector>
@@ -26,6 +27,18 @@ struct File {
   ~File() { if (f) fclose(f); }
   int close() { int rc = f ? fclose(f) : 0; f = nullptr; return rc; }
 };
+
+// The file a read takes: libdft's drivers write with a base name (the
+// writer adds .grd, examples/gas-bubble/bubble.c:182) and read with the
+// file's whole name, often renamed ("restart.chk", examples/electron/electron.c:163;
+// "liquid_input", examples/added_mass/added_mass.c:111 and its README).  A
+// name that is an existing regular file is read as it is, any other as
+// <name>.grd.
+std::string read_path(const char *name) {
+  struct stat st;
+  if (stat(name, &st) == 0 && S_ISREG(st.st_mode)) return std::string(name);
+  return std::string(name) + ".grd";
+}
 
 // "coordinate value" lines along each axis through (nx/2, ny/2, nz/2)
 int write_cuts(const std::string &base, int cplx, const INT n[3], const double *meta, const double *v) {
@@ -82,32 +95,34 @@ int dftgpu_grid_file_write(const char *base, int is_complex, INT nx, INT ny, INT
   return write_cuts(base, is_complex, n, meta, values);
 }
 
-int dftgpu_grid_file_read(const char *base, int is_complex, INT nx, INT ny, INT nz, double *meta, double *values) {
-  if (!base || !meta || !values || !dims_ok(nx, ny, nz)) {
+int dftgpu_grid_file_read(const char *name, int is_complex, INT nx, INT ny, INT nz, double *meta, double *values) {
+  if (!name || !meta || !values || !dims_ok(nx, ny, nz)) {
     set_error(DFTGPU_ERR_ARG, "dftgpu_grid_file_read: argument");
     return DFTGPU_ERR_ARG;
   }
-  File in(std::string(base) + ".grd", "rb");
-  if (!in.f) { set_error(DFTGPU_ERR_IO, "grid file: cannot open %s.grd", base); return DFTGPU_ERR_IO; }
+  const std::string path = read_path(name);
+  const char *pn = path.c_str();
+  File in(path, "rb");
+  if (!in.f) { set_error(DFTGPU_ERR_IO, "grid file: cannot open %s", pn); return DFTGPU_ERR_IO; }
   char magic[8];
   int64_t head[4];
   if (fread(magic, 1, 8, in.f) != 8 || memcmp(magic, kMagic, 8) != 0) {
-    set_error(DFTGPU_ERR_UNSUPPORTED, "grid file: %s.grd is not in this library's grid layout", base);
+    set_error(DFTGPU_ERR_UNSUPPORTED, "grid file: %s is not in this library's grid layout", pn);
     return DFTGPU_ERR_UNSUPPORTED;
   }
-  if (fread(head, sizeof(int64_t), 4, in.f) != 4) { set_error(DFTGPU_ERR_IO, "grid file: %s.grd truncated", base); return DFTGPU_ERR_IO; }
+  if (fread(head, sizeof(int64_t), 4, in.f) != 4) { set_error(DFTGPU_ERR_IO, "grid file: %s truncated", pn); return DFTGPU_ERR_IO; }
   if (head[0] != (is_complex ? 1 : 0)) {
-    set_error(DFTGPU_ERR_ARG, "grid file: %s.grd holds a %s grid", base, head[0] ? "complex" : "real");
+    set_error(DFTGPU_ERR_ARG, "grid file: %s holds a %s grid", pn, head[0] ? "complex" : "real");
     return DFTGPU_ERR_ARG;
   }
   if (head[1] != nx || head[2] != ny || head[3] != nz) {
-    set_error(DFTGPU_ERR_SIZE, "grid file: %s.grd is %lldx%lldx%lld, the grid %ldx%ldx%ld", base, (long long) head[1],
+    set_error(DFTGPU_ERR_SIZE, "grid file: %s is %lldx%lldx%lld, the grid %ldx%ldx%ld", pn, (long long) head[1],
               (long long) head[2], (long long) head[3], (long) nx, (long) ny, (long) nz);
     return DFTGPU_ERR_SIZE;
   }
   const size_t count = (size_t) nx * ny * nz * (is_complex ? 2 : 1);
   if (fread(meta, sizeof(double), 7, in.f) != 7 || fread(values, sizeof(double), count, in.f) != count) {
-    set_error(DFTGPU_ERR_IO, "grid file: %s.grd truncated", base);
+    set_error(DFTGPU_ERR_IO, "grid file: %s truncated", pn);
     return DFTGPU_ERR_IO;
   }
   return DFTGPU_OK;
@@ -129,20 +144,20 @@ void cgrid_write_grid(char *base, cgrid *g) {
   dftgpu_grid_file_write(base, 1, g->nx, g->ny, g->nz, meta, h.data());
 }
 
-void rgrid_read_grid(rgrid *g, char *base) {
+void rgrid_read_grid(rgrid *g, char *file) {
   if (!g) { set_error(DFTGPU_ERR_ARG, "rgrid_read_grid: NULL grid"); return; }
   std::vector<double> h(gsize(g));
   double meta[7];
-  if (dftgpu_grid_file_read(base, 0, g->nx, g->ny, g->nz, meta, h.data()) != DFTGPU_OK) return;
+  if (dftgpu_grid_file_read(file, 0, g->nx, g->ny, g->nz, meta, h.data()) != DFTGPU_OK) return;
   if (rgrid_copy_from_host(g, h.data()) != DFTGPU_OK) return;
   rgrid_set_origin(g, meta[1], meta[2], meta[3]);
 }
 
-void cgrid_read_grid(cgrid *g, char *base) {
+void cgrid_read_grid(cgrid *g, char *file) {
   if (!g) { set_error(DFTGPU_ERR_ARG, "cgrid_read_grid: NULL grid"); return; }
   std::vector<double> h(2 * gsize(g));
   double meta[7];
-  if (dftgpu_grid_file_read(base, 1, g->nx, g->ny, g->nz, meta, h.data()) != DFTGPU_OK) return;
+  if (dftgpu_grid_file_read(file, 1, g->nx, g->ny, g->nz, meta, h.data()) != DFTGPU_OK) return;
   if (cgrid_copy_from_host(g, h.data()) != DFTGPU_OK) return;
   g->x0 = meta[1]; g->y0 = meta[2]; g->z0 = meta[3];
   cgrid_set_momentum(g, meta[4], meta[5], meta[6]);

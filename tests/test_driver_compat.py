@@ -297,6 +297,28 @@ def test_grid_file_round_trip_and_cuts(lib, tmp_path, is_complex):
         assert np.allclose(rows[:, 1:], want, rtol=1e-6, atol=1e-12)
 
 
+def test_grid_file_read_takes_the_whole_name(lib, tmp_path):
+    """libdft's drivers write with a base name and read with the file's whole
+    name: `bubble-100.grd` from the command line (examples/gas-bubble/bubble.c:143)
+    or a renamed copy (`restart.chk`, examples/electron/electron.c:163).  A base
+    whose .grd exists still reads."""
+    import shutil
+    write, read = file_api(lib)
+    shape = (4, 6, 8)
+    v = np.random.default_rng(9).standard_normal(shape + (2,))
+    meta = np.array([0.8, 0.0, 0.0, 0.0, 0.0, 0.0, 0.1])
+    base = tmp_path / "bubble-100"
+    assert write(str(base).encode(), 1, *shape, dp(meta), dp(v)) == 0
+    shutil.copy(tmp_path / "bubble-100.grd", tmp_path / "restart.chk")
+    for name in ("bubble-100.grd", "restart.chk", "bubble-100"):
+        got, gmeta = np.zeros_like(v), np.zeros(7)
+        assert read(str(tmp_path / name).encode(), 1, *shape, dp(gmeta), dp(got)) == 0, name
+        assert np.array_equal(got, v) and np.array_equal(gmeta, meta), name
+    # a directory of that name is not a file: <name>.grd is read instead
+    (tmp_path / "bubble-200").mkdir()
+    assert read(str(tmp_path / "bubble-200").encode(), 1, *shape, dp(np.zeros(7)), dp(np.zeros_like(v))) == 8
+
+
 def test_grid_file_refusals(lib, tmp_path):
     write, read = file_api(lib)
     lib.dftgpu_last_error.restype = C.c_int
