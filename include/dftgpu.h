@@ -25,6 +25,7 @@
 
 #include <stddef.h>
 #include <stdint.h>
+#include <stdio.h>
 
 #ifdef __cplusplus
 extern "C" {
@@ -217,6 +218,9 @@ void rgrid_sum(rgrid *dst, rgrid *a, rgrid *b);
 void rgrid_product(rgrid *dst, rgrid *a, rgrid *b);
 void rgrid_add_scaled(rgrid *dst, REAL c, rgrid *src);
 void rgrid_add_scaled_product(rgrid *dst, REAL c, rgrid *a, rgrid *b);
+/* dst = src^exponent at every point (pow; examples/soliton/soliton.c:96,
+ * examples/1d-soliton/soliton-1d.c:105: the amplitude sqrt(rho)) */
+void rgrid_power(rgrid *dst, rgrid *src, REAL exponent);
 REAL rgrid_integral(rgrid *grid);
 /* Host callback evaluated in FP64 on the host at every grid point, then copied
  * to the device (setup only; examples/imag_time/imag_time.c:218). */
@@ -495,6 +499,16 @@ void cgrid_read_grid(cgrid *grid, char *file);             /* examples/added_mas
 int dftgpu_grid_file_write(const char *base, int is_complex, INT nx, INT ny, INT nz, const double *meta,
                            const double *values);
 int dftgpu_grid_file_read(const char *name, int is_complex, INT nx, INT ny, INT nz, double *meta, double *values);
+/* The .grd layout on a stream the caller opened and closes (a checkpoint read
+ * as libdft's 1-D drivers do: fopen(argv[1]); cgrid_read(gwf->grid, fp),
+ * examples/1d-bubble/bubble-1d.c:164-170, examples/1d-soliton/soliton-1d.c:93-99).
+ * A NULL grid is allocated with the file's shape and step (in the current
+ * precision); a given grid must have the file's shape.  The read functions
+ * return the grid, or NULL with the error recorded. */
+cgrid *cgrid_read(cgrid *grid, FILE *in);
+rgrid *rgrid_read(rgrid *grid, FILE *in);
+void cgrid_write(cgrid *grid, FILE *out);
+void rgrid_write(rgrid *grid, FILE *out);
 /* one value of a complex grid (cgrid_value_at_index; indices wrap periodically) */
 int cgrid_value_at_index_re_im(cgrid *grid, INT i, INT j, INT k, REAL *re, REAL *im);
 

@@ -159,6 +159,11 @@ SIGNATURES = {
     "cgrid_read_grid": (None, [_vp, C.c_char_p]),
     "dftgpu_grid_file_write": (_i, [C.c_char_p, _i, _l, _l, _l, _dp, _dp]),
     "dftgpu_grid_file_read": (_i, [C.c_char_p, _i, _l, _l, _l, _dp, _dp]),
+    "cgrid_read": (_vp, [_vp, _vp]),
+    "rgrid_read": (_vp, [_vp, _vp]),
+    "cgrid_write": (None, [_vp, _vp]),
+    "rgrid_write": (None, [_vp, _vp]),
+    "rgrid_power": (None, [_vp, _vp, _d]),
 }
 
 OPTIONAL = set()   # entry points allowed to be absent (none)

@@ -177,6 +177,10 @@ void rgrid_add_scaled_product(rgrid *d, REAL c, rgrid *a, rgrid *b) {
   if (!same_shape(d, a) || !same_shape(d, b)) { bad_arg("rgrid_add_scaled_product: shape mismatch"); return; }
   rbinary(d, a, b, c, 3);
 }
+void rgrid_power(rgrid *d, rgrid *s, REAL exponent) {
+  if (!same_shape(d, s)) { bad_arg("rgrid_power: shape mismatch"); return; }
+  rpower(d, s, exponent);
+}
 REAL rgrid_integral(rgrid *g) {
   NEED(g, "rgrid_integral", NAN);
   double v = NAN;

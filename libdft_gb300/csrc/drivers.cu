@@ -61,6 +61,58 @@ int write_cuts(const std::string &base, int cplx, const INT n[3], const double *
 
 bool dims_ok(INT nx, INT ny, INT nz) { return nx > 0 && ny > 0 && nz > 0; }
 
+// The .grd body on an open stream: magic, kind, shape, the 7 meta values
+// (step, origin, momentum), then the values.
+bool write_body(FILE *f, int is_complex, INT nx, INT ny, INT nz, const double *meta, const double *values) {
+  const size_t count = (size_t) nx * ny * nz * (is_complex ? 2 : 1);
+  const int64_t head[4] = { is_complex ? 1 : 0, (int64_t) nx, (int64_t) ny, (int64_t) nz };
+  return fwrite(kMagic, 1, 8, f) == 8 && fwrite(head, sizeof(int64_t), 4, f) == 4 &&
+         fwrite(meta, sizeof(double), 7, f) == 7 && fwrite(values, sizeof(double), count, f) == count;
+}
+
+struct GrdHead {
+  int64_t kind, nx, ny, nz;
+  double meta[7];
+};
+
+// magic, kind, shape and meta of a .grd body; `what` names the source in messages
+int read_head(FILE *f, const char *what, GrdHead *h) {
+  char magic[8];
+  int64_t head[4];
+  if (fread(magic, 1, 8, f) != 8 || memcmp(magic, kMagic, 8) != 0) {
+    set_error(DFTGPU_ERR_UNSUPPORTED, "grid file: %s is not in this library's grid layout", what);
+    return DFTGPU_ERR_UNSUPPORTED;
+  }
+  if (fread(head, sizeof(int64_t), 4, f) != 4 || fread(h->meta, sizeof(double), 7, f) != 7) {
+    set_error(DFTGPU_ERR_IO, "grid file: %s truncated", what);
+    return DFTGPU_ERR_IO;
+  }
+  h->kind = head[0]; h->nx = head[1]; h->ny = head[2]; h->nz = head[3];
+  return DFTGPU_OK;
+}
+
+// the body's kind and shape against the grid it is read into
+int check_head(const GrdHead &h, const char *what, int is_complex, INT nx, INT ny, INT nz) {
+  if (h.kind != (is_complex ? 1 : 0)) {
+    set_error(DFTGPU_ERR_ARG, "grid file: %s holds a %s grid", what, h.kind ? "complex" : "real");
+    return DFTGPU_ERR_ARG;
+  }
+  if (h.nx != nx || h.ny != ny || h.nz != nz) {
+    set_error(DFTGPU_ERR_SIZE, "grid file: %s is %lldx%lldx%lld, the grid %ldx%ldx%ld", what, (long long) h.nx,
+              (long long) h.ny, (long long) h.nz, (long) nx, (long) ny, (long) nz);
+    return DFTGPU_ERR_SIZE;
+  }
+  return DFTGPU_OK;
+}
+
+int read_vals(FILE *f, const char *what, size_t count, double *values) {
+  if (fread(values, sizeof(double), count, f) != count) {
+    set_error(DFTGPU_ERR_IO, "grid file: %s truncated", what);
+    return DFTGPU_ERR_IO;
+  }
+  return DFTGPU_OK;
+}
+
 // A driver checks the error state of the void entry points it calls: it
 // sets a pending error aside on entry and puts it back on exit if the driver
 // itself recorded none.
@@ -82,13 +134,10 @@ int dftgpu_grid_file_write(const char *base, int is_complex, INT nx, INT ny, INT
     return DFTGPU_ERR_ARG;
   }
   const INT n[3] = { nx, ny, nz };
-  const size_t count = (size_t) nx * ny * nz * (is_complex ? 2 : 1);
   {
     File out(std::string(base) + ".grd", "wb");
     if (!out.f) { set_error(DFTGPU_ERR_IO, "grid file: cannot open %s.grd", base); return DFTGPU_ERR_IO; }
-    const int64_t head[4] = { is_complex ? 1 : 0, (int64_t) nx, (int64_t) ny, (int64_t) nz };
-    bool ok = fwrite(kMagic, 1, 8, out.f) == 8 && fwrite(head, sizeof(int64_t), 4, out.f) == 4 &&
-              fwrite(meta, sizeof(double), 7, out.f) == 7 && fwrite(values, sizeof(double), count, out.f) == count;
+    bool ok = write_body(out.f, is_complex, nx, ny, nz, meta, values);
     ok = (out.close() == 0) && ok;
     if (!ok) { set_error(DFTGPU_ERR_IO, "grid file: write error on %s.grd", base); return DFTGPU_ERR_IO; }
   }
@@ -104,27 +153,11 @@ int dftgpu_grid_file_read(const char *name, int is_complex, INT nx, INT ny, INT 
   const char *pn = path.c_str();
   File in(path, "rb");
   if (!in.f) { set_error(DFTGPU_ERR_IO, "grid file: cannot open %s", pn); return DFTGPU_ERR_IO; }
-  char magic[8];
-  int64_t head[4];
-  if (fread(magic, 1, 8, in.f) != 8 || memcmp(magic, kMagic, 8) != 0) {
-    set_error(DFTGPU_ERR_UNSUPPORTED, "grid file: %s is not in this library's grid layout", pn);
-    return DFTGPU_ERR_UNSUPPORTED;
-  }
-  if (fread(head, sizeof(int64_t), 4, in.f) != 4) { set_error(DFTGPU_ERR_IO, "grid file: %s truncated", pn); return DFTGPU_ERR_IO; }
-  if (head[0] != (is_complex ? 1 : 0)) {
-    set_error(DFTGPU_ERR_ARG, "grid file: %s holds a %s grid", pn, head[0] ? "complex" : "real");
-    return DFTGPU_ERR_ARG;
-  }
-  if (head[1] != nx || head[2] != ny || head[3] != nz) {
-    set_error(DFTGPU_ERR_SIZE, "grid file: %s is %lldx%lldx%lld, the grid %ldx%ldx%ld", pn, (long long) head[1],
-              (long long) head[2], (long long) head[3], (long) nx, (long) ny, (long) nz);
-    return DFTGPU_ERR_SIZE;
-  }
-  const size_t count = (size_t) nx * ny * nz * (is_complex ? 2 : 1);
-  if (fread(meta, sizeof(double), 7, in.f) != 7 || fread(values, sizeof(double), count, in.f) != count) {
-    set_error(DFTGPU_ERR_IO, "grid file: %s truncated", pn);
-    return DFTGPU_ERR_IO;
-  }
+  GrdHead h;
+  DFT_TRY(read_head(in.f, pn, &h));
+  DFT_TRY(check_head(h, pn, is_complex, nx, ny, nz));
+  memcpy(meta, h.meta, sizeof(h.meta));
+  DFT_TRY(read_vals(in.f, pn, (size_t) nx * ny * nz * (is_complex ? 2 : 1), values));
   return DFTGPU_OK;
 }
 
@@ -161,6 +194,69 @@ void cgrid_read_grid(cgrid *g, char *file) {
   if (cgrid_copy_from_host(g, h.data()) != DFTGPU_OK) return;
   g->x0 = meta[1]; g->y0 = meta[2]; g->z0 = meta[3];
   cgrid_set_momentum(g, meta[4], meta[5], meta[6]);
+}
+
+cgrid *cgrid_read(cgrid *g, FILE *in) {
+  const char *what = "cgrid_read stream";
+  if (!in) { set_error(DFTGPU_ERR_ARG, "cgrid_read: NULL stream"); return nullptr; }
+  GrdHead h;
+  if (read_head(in, what, &h) != DFTGPU_OK) return nullptr;
+  cgrid *made = nullptr;
+  if (!g) {
+    if (h.kind != 1) { set_error(DFTGPU_ERR_ARG, "grid file: %s holds a real grid", what); return nullptr; }
+    made = g = cgrid_alloc((INT) h.nx, (INT) h.ny, (INT) h.nz, h.meta[0], nullptr, nullptr, (char *) "cgrid_read");
+    if (!g) return nullptr;
+  }
+  std::vector<double> v;
+  if (check_head(h, what, 1, g->nx, g->ny, g->nz) == DFTGPU_OK) {
+    v.resize(2 * gsize(g));
+    if (read_vals(in, what, v.size(), v.data()) == DFTGPU_OK && cgrid_copy_from_host(g, v.data()) == DFTGPU_OK) {
+      g->x0 = h.meta[1]; g->y0 = h.meta[2]; g->z0 = h.meta[3];
+      cgrid_set_momentum(g, h.meta[4], h.meta[5], h.meta[6]);
+      return g;
+    }
+  }
+  cgrid_free(made);
+  return nullptr;
+}
+
+rgrid *rgrid_read(rgrid *g, FILE *in) {
+  const char *what = "rgrid_read stream";
+  if (!in) { set_error(DFTGPU_ERR_ARG, "rgrid_read: NULL stream"); return nullptr; }
+  GrdHead h;
+  if (read_head(in, what, &h) != DFTGPU_OK) return nullptr;
+  rgrid *made = nullptr;
+  if (!g) {
+    if (h.kind != 0) { set_error(DFTGPU_ERR_ARG, "grid file: %s holds a complex grid", what); return nullptr; }
+    made = g = rgrid_alloc((INT) h.nx, (INT) h.ny, (INT) h.nz, h.meta[0], nullptr, nullptr, (char *) "rgrid_read");
+    if (!g) return nullptr;
+  }
+  std::vector<double> v;
+  if (check_head(h, what, 0, g->nx, g->ny, g->nz) == DFTGPU_OK) {
+    v.resize(gsize(g));
+    if (read_vals(in, what, v.size(), v.data()) == DFTGPU_OK && rgrid_copy_from_host(g, v.data()) == DFTGPU_OK) {
+      rgrid_set_origin(g, h.meta[1], h.meta[2], h.meta[3]);
+      return g;
+    }
+  }
+  rgrid_free(made);
+  return nullptr;
+}
+
+void cgrid_write(cgrid *g, FILE *out) {
+  if (!g || !out) { set_error(DFTGPU_ERR_ARG, "cgrid_write: NULL argument"); return; }
+  std::vector<double> v(2 * gsize(g));
+  if (cgrid_copy_to_host(g, v.data()) != DFTGPU_OK) return;
+  const double meta[7] = { g->step, g->x0, g->y0, g->z0, g->kx0, g->ky0, g->kz0 };
+  if (!write_body(out, 1, g->nx, g->ny, g->nz, meta, v.data())) set_error(DFTGPU_ERR_IO, "cgrid_write: write error");
+}
+
+void rgrid_write(rgrid *g, FILE *out) {
+  if (!g || !out) { set_error(DFTGPU_ERR_ARG, "rgrid_write: NULL argument"); return; }
+  std::vector<double> v(gsize(g));
+  if (rgrid_copy_to_host(g, v.data()) != DFTGPU_OK) return;
+  const double meta[7] = { g->step, g->x0, g->y0, g->z0, 0.0, 0.0, 0.0 };
+  if (!write_body(out, 0, g->nx, g->ny, g->nz, meta, v.data())) set_error(DFTGPU_ERR_IO, "rgrid_write: write error");
 }
 
 // ------------------------------------------------------------ potentials from files

@@ -682,6 +682,18 @@ int rbinary(rgrid *d, rgrid *a, rgrid *b, double c, int op) {
   return d->prec == DFTGPU_FP32 ? rbin_t<float>(d, a, b, c, op) : rbin_t<double>(d, a, b, c, op);
 }
 
+// d = s^e (pow of the grid's precision)
+template <typename T> static int rpow_t(rgrid *d, rgrid *s, double e) {
+  T *pd = (T *) d->value;
+  const T *ps = (const T *) s->value;
+  const T ee = (T) e;
+  return launch_each(gsize(d), [=] __device__(size_t i) { pd[i] = pow(ps[i], ee); }, 2.0 * gsize(d) * sizeof(T),
+                     "rgrid_power");
+}
+int rpower(rgrid *d, rgrid *s, double e) {
+  return d->prec == DFTGPU_FP32 ? rpow_t<float>(d, s, e) : rpow_t<double>(d, s, e);
+}
+
 template <typename T> static int rsum_t(rgrid *g, double *out) {
   const T *p = (const T *) g->value;
   const double dv = g->step * g->step * g->step;

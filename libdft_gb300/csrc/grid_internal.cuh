@@ -65,6 +65,7 @@ int cfill(cgrid *g, double re, double im);
 int cmuladd(cgrid *g, double mr, double mi, double ar, double ai);
 int real_to_complex(cgrid *d, rgrid *s, int mode);
 int rbinary(rgrid *d, rgrid *a, rgrid *b, double c, int op);
+int rpower(rgrid *d, rgrid *s, double e);
 int rintegral(rgrid *g, double *out);
 int density(cgrid *c, rgrid *d);
 int rspectrum(rgrid *g, double *host);

@@ -111,7 +111,8 @@ def test_bulk_response_matches_libdft(lib, ref, model):
 # libgrid functions outside the time step; the design notes list them)
 DRIVERS = ["imag_time/imag_time.c", "dynamics/dynamics.c", "dispersion/dispersion.c",
            "dispersion/dispersion2.c", "dispersion/dispersion3.c", "dispersion/static-resp.c",
-           "bulk/bulk_properties.c", "piston/piston.c", "shock/shock.c"]
+           "bulk/bulk_properties.c", "piston/piston.c", "shock/shock.c", "1d-bubble/bubble-1d.c",
+           "1d-soliton/soliton-1d.c", "soliton/soliton.c", "added_mass_viscosity/analyze4.c"]
 
 
 @pytest.mark.skipif(not os.path.isdir(REF_EXAMPLES), reason="reference tree not present")
