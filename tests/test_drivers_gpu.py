@@ -98,6 +98,7 @@ def test_stream_grid_io_and_power(gpu, tmp_path, prec):
     against numpy, also in place as the drivers call it."""
     L = gpu.lib()
     gpu.set_precision(prec)
+    L.dftgpu_last_error()                 # start from a clear error state
     libc = C.CDLL(None)
     libc.fopen.restype = C.c_void_p
     libc.fopen.argtypes = [C.c_char_p, C.c_char_p]
