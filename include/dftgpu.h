@@ -503,7 +503,8 @@ int dftgpu_grid_file_read(const char *name, int is_complex, INT nx, INT ny, INT 
  * as libdft's 1-D drivers do: fopen(argv[1]); cgrid_read(gwf->grid, fp),
  * examples/1d-bubble/bubble-1d.c:164-170, examples/1d-soliton/soliton-1d.c:93-99).
  * A NULL grid is allocated with the file's shape and step (in the current
- * precision); a given grid must have the file's shape.  A body of the other
+ * precision; tmp = cgrid_read(NULL, fp), examples/vortex-trace/trace.c:155);
+ * a given grid must have the file's shape.  A body of the other
  * kind (a real grid's body read by cgrid_read) is refused with DFTGPU_ERR_ARG:
  * how libgrid would turn a density into a wave function is not in the
  * reference tree.  The read functions return the grid, or NULL with the error
